@@ -1,0 +1,163 @@
+/*
+ * gfm_gb300.h -- C ABI of the GB300 two-fluid ghost-fluid Euler step.
+ *
+ * Every entry point takes plain pointers and sizes; device memory is owned by
+ * the context.  All calls are ordered on the context's CUDA stream (settable
+ * with gfm_set_stream).  Each returns a gfm_status_t.
+ *
+ * Host layout of one fluid grid: 4 planes (rho, rho u, rho v, E), each
+ * (Ny + 2 numGC) rows x (Nx + 2 numGC) columns, row i = y index, column
+ * j = x index, row-major -- the reference's grid[i][j](k) with k the plane.
+ *
+ * Reference interfaces replaced (paths within murraycutforth/PhD-2D-GFM):
+ *   sim_info / binarySGparams        -> gfm_grid_desc
+ *   GFM_settingsfile keys FS, GFM, ITM, CFL -> gfm_method_desc
+ *                                       (headers/GFM_settingsfile.hpp:24-59)
+ *   FS_base::pure_fluid_update       -> gfm_fs_update      (headers/FS_base.hpp:23-32)
+ *   GFM_base::set_ghost_states       -> gfm_set_ghost_states (headers/GFM_base.hpp:37-47)
+ *   apply_BCs_euler                  -> gfm_apply_bcs      (headers/euler_bc.hpp:5)
+ *   sim_twofluid::compute_dt         -> gfm_compute_dt     (sourcecode/sim_twofluid.cpp:108-157)
+ *   sim_onefluid::compute_dt         -> gfm_compute_dt     (sourcecode/sim_onefluid.cpp:68-91)
+ *   ls->update_interface_coupled     -> gfm_ls_update      (sourcecode/sim_twofluid.cpp:72)
+ *   the while (t < T) loop body      -> gfm_step           (sourcecode/sim_twofluid.cpp:64-88,
+ *                                                           sourcecode/sim_onefluid.cpp:40-54)
+ *   pure_RS_base::solve_RP           -> gfm_rs_pure_batch  (headers/pure_RS_base.hpp:13-20)
+ *   mixed_RS_base::solve_mixed_RP    -> gfm_rs_mixed_batch (headers/mixed_RS_base.hpp:12-24)
+ *   sim_twofluid::fluid_mass         -> gfm_fluid_mass     (sourcecode/sim_twofluid.cpp:1803-1827)
+ */
+#ifndef GFM_GB300_H
+#define GFM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int gfm_status_t;
+/* return codes */
+#define GFM_OK 0
+#define GFM_ERR_ARG 1        /* invalid argument (null pointer, bad size, bad enum) */
+#define GFM_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define GFM_ERR_NUMERIC 3    /* the device status word holds a numeric fault */
+#define GFM_ERR_UNSUPPORTED 4
+
+/* boundary conditions (sim_info BC_L/R/B/T strings) */
+#define GFM_BC_TRANSMISSIVE 0
+#define GFM_BC_REFLECTIVE 1
+#define GFM_BC_PERIODIC 2
+
+/* flux solvers (settings key FS) */
+#define GFM_FS_GODUNOV 0
+#define GFM_FS_MUSCL 1
+
+/* ghost-fluid methods (settings key GFM) */
+#define GFM_OGFM 0
+#define GFM_RIEMANN 1
+#define GFM_REAL 2
+#define GFM_MODIFIED 3
+
+/* device status bits (gfm_get_device_status) */
+#define GFM_ST_UNPHYSICAL (1u << 0)
+#define GFM_ST_NEWTON_NO_CONVERGE (1u << 1)
+#define GFM_ST_VACUUM (1u << 2)
+#define GFM_ST_NAN (1u << 3)
+#define GFM_ST_DT_NONPOSITIVE (1u << 4)
+#define GFM_ST_SCHEDULE_LIMIT (1u << 5)
+
+/* sim_info + binarySGparams */
+typedef struct {
+  int Nx, Ny, numGC;
+  double x0, y0, dx, dy;
+  int BC_L, BC_R, BC_B, BC_T;
+  double gamma1, pinf1, gamma2, pinf2;
+} gfm_grid_desc;
+
+/* the strategy choices of sim_twofluid::set_sim_methods */
+typedef struct {
+  int fs;                    /* GFM_FS_* */
+  int gfm;                   /* GFM_* (two-fluid only) */
+  int ls_order;              /* level-set advection order: 1 (upwind) or 5 (HOUC5 + RK3) */
+  int reinit_every;          /* reinitialise phi every k steps; 0 = never */
+  int reinit_iters;          /* pseudo-time iterations per reinitialisation */
+  int use_extension_vfield;  /* GFM_base::use_extension_vfield */
+  int use_slip_BCs;          /* GFM_base::use_slip_BCs */
+  double CFL;                /* settings key CFL */
+  double T;                  /* end time */
+} gfm_method_desc;
+
+typedef struct gfm_ctx gfm_ctx;
+
+/* Context: device grids for one (two_fluid = 0) or two fluids plus phi. */
+gfm_status_t gfm_ctx_create(const gfm_grid_desc* grid, int two_fluid, gfm_ctx** out);
+gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx);
+gfm_status_t gfm_set_stream(gfm_ctx* ctx, void* cuda_stream);
+
+/* host <-> device copies of a fluid grid (fluid 1 or 2) and of phi */
+gfm_status_t gfm_upload(gfm_ctx* ctx, int fluid, const double* U);
+gfm_status_t gfm_download(gfm_ctx* ctx, int fluid, double* U);
+gfm_status_t gfm_upload_phi(gfm_ctx* ctx, const double* phi);
+gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi);
+
+/* interfacial-cell mask of the last ghost fill (Levelset::is_interfacial_cell
+ * over real cells; 1 byte per padded cell, same layout as phi) */
+gfm_status_t gfm_download_mask(gfm_ctx* ctx, uint8_t* mask);
+
+/* time state kept on the device: t, step count, last dt */
+gfm_status_t gfm_set_time(gfm_ctx* ctx, double t, int numsteps);
+gfm_status_t gfm_get_time(gfm_ctx* ctx, double* t, int* numsteps, double* dt);
+
+/* One sub-step each, stream-ordered, dt kept on the device. */
+gfm_status_t gfm_compute_dt(gfm_ctx* ctx, double CFL, double T);
+gfm_status_t gfm_set_ghost_states(gfm_ctx* ctx, const gfm_method_desc* m);
+gfm_status_t gfm_fs_update(gfm_ctx* ctx, int fs, int fluid);
+gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
+gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid);
+
+/* nsteps iterations of the reference's time loop body (CFL ramp, dt, ghost
+ * fill, two flux updates, level set, BCs, t += dt).  Steps after t reaches
+ * T do nothing, as the reference's loop would have stopped. */
+gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps);
+
+/* Status word OR-ed by kernels since the last clear (GFM_ST_* bits). */
+gfm_status_t gfm_get_device_status(gfm_ctx* ctx, uint32_t* status);
+gfm_status_t gfm_clear_device_status(gfm_ctx* ctx);
+
+/* Statistics of the last step: interfacial cells, schedule rounds, Newton
+ * iterations summed over all exact Riemann solves. */
+gfm_status_t gfm_get_stats(gfm_ctx* ctx, int64_t* n_interfacial, int64_t* n_rounds, int64_t* newton_iters);
+
+/* mass of fluid 1 (interiorsign = -1, phi < 0) or 2 (+1, phi > 0) */
+gfm_status_t gfm_fluid_mass(gfm_ctx* ctx, double interiorsign, double* mass);
+
+/* Batched exact Riemann solves on DEVICE arrays (n states of 4 doubles, AoS).
+ * pure: flux at x/t = 0 (pure_RS_exact::solve_RP).
+ * mixed: out[4*k..] = (p_star, u_star, rho_star_L, rho_star_R). */
+gfm_status_t gfm_rs_pure_batch(int n, int paralleltox, double gamma, double pinf, const double* UL,
+                               const double* UR, double* flux, uint32_t* status, void* cuda_stream);
+gfm_status_t gfm_rs_mixed_batch(int n, double gammaL, double pinfL, double gammaR, double pinfR,
+                                const double* UL, const double* UR, double* out, uint32_t* status,
+                                void* cuda_stream);
+
+/* Named test cases: sim_type "onefluid" or "twofluid"; test_case one of the
+ * reference's (circularexplosion, TTC1_x .. TTC5_y, ST1_x, ST2_y, GDA,
+ * shocked_helium_bubble, shocked_R22_bubble) or shock_bubble,
+ * underwater_explosion_sg.
+ * gfm_case_params: sim_*::set_sim_parameters (sourcecode/sim_twofluid.cpp:336-490,
+ *                  sourcecode/sim_onefluid.cpp:96-146); T is the end time.
+ * gfm_case_init:   sim_*::set_sim_ICs + apply_BCs_euler (sourcecode/sim_twofluid.cpp:599-1799,
+ *                  sourcecode/sim_onefluid.cpp:196-449) into HOST arrays in the
+ *                  layout above (U2 and phi unused for one fluid). */
+gfm_status_t gfm_case_params(const char* sim_type, const char* test_case, int Nx, int Ny, gfm_grid_desc* grid,
+                             double* T);
+gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gfm_grid_desc* grid, double* U1,
+                           double* U2, double* phi);
+
+/* library version string */
+const char* gfm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,1174 @@
+// TEST INFRASTRUCTURE: the CPU oracle of the two-fluid ghost-fluid Euler step.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may load
+// this library, and only as the checker / CPU baseline.  It is never on the
+// product path.
+//
+// A single-threaded C++ restatement of murraycutforth/PhD-2D-GFM's hot path,
+// following the reference's loops, loop bounds, branch structure and quirks
+// one for one (file:line cited per function).  Grids are the reference's
+// nested std::vector<std::vector<vec4>> indexed grid[i][j] (row i = y).
+//
+// PARITY UNPINNED: the reference cannot be compiled here (it needs Eigen,
+// blitz++, PhD-Common, PhD-Interface-tracking-methods, the exact stiffened-gas
+// solver and NLopt, none of which are available), and it ships no golden
+// vectors.  The parts it takes from absent dependencies (EOS, exact Riemann
+// solver, level set, bilinear interpolation, cell-centre coordinates) are
+// restated from published methods in oracle_math.hpp and below.
+//
+// Arithmetic order is fixed (Eigen expressions are evaluated coefficient by
+// coefficient, left to right; the 4x4 quasilinear matrix products as
+// sum_k (s A_ik) d_k), and the build uses -ffp-contract=off.
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/gfm_gb300.h"
+#include "oracle_math.hpp"
+
+typedef std::array<double, 4> vec4type;
+typedef std::array<double, 2> vec2;
+typedef std::vector<std::vector<vec4type>> grideuler2type;
+typedef std::vector<std::vector<vec2>> gridVector2dtype;
+typedef std::vector<std::vector<double>> griddoubletype;
+
+namespace {
+
+uint32_t g_status = 0;     // OR of GFM_ST_* raised where the reference asserts
+int64_t g_newton_iters = 0;
+
+inline vec4type add(const vec4type& a, const vec4type& b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2], a[3] + b[3]}; }
+inline vec4type sub(const vec4type& a, const vec4type& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2], a[3] - b[3]}; }
+inline vec4type scale(double s, const vec4type& a) { return {s * a[0], s * a[1], s * a[2], s * a[3]}; }
+
+// sim_info (PhD-Common): grid geometry, boundary conditions.
+struct sim_info {
+  int Nx, Ny, numGC;
+  double x0, y0, dx, dy;
+  int BC_L, BC_R, BC_B, BC_T;
+  // cell centre of grid[i][j]
+  vec2 cellcentre_coord(int i, int j) const {
+    return {x0 + (static_cast<double>(j - numGC) + 0.5) * dx, y0 + (static_cast<double>(i - numGC) + 0.5) * dy};
+  }
+};
+
+struct binarySGparams {
+  double gamma1, pinf1, gamma2, pinf2;
+};
+
+struct BBrange {
+  int imin, imax, jmin, jmax;
+};
+
+sim_info make_params(const gfm_grid_desc* d) {
+  sim_info p;
+  p.Nx = d->Nx; p.Ny = d->Ny; p.numGC = d->numGC;
+  p.x0 = d->x0; p.y0 = d->y0; p.dx = d->dx; p.dy = d->dy;
+  p.BC_L = d->BC_L; p.BC_R = d->BC_R; p.BC_B = d->BC_B; p.BC_T = d->BC_T;
+  return p;
+}
+
+// ----------------------------------------------------------------------------
+// misc:: (headers/euler_misc.hpp)
+// ----------------------------------------------------------------------------
+namespace misc {
+
+// euler_misc.hpp:23-29
+inline double specific_ie(const vec4type& U) {
+  double rho = U[0];
+  double u = U[1] / rho;
+  double v = U[2] / rho;
+  return (U[3] / rho) - 0.5 * (u * u + v * v);
+}
+// euler_misc.hpp:32-41
+inline bool is_physical_state(double, double, const vec4type& U) {
+  double rho = U[0];
+  double u = U[1] / rho;
+  double v = U[2] / rho;
+  double e = (U[3] / rho) - 0.5 * (u * u + v * v);
+  return rho >= 0.0 && e >= 0.0;
+}
+// euler_misc.hpp:44-49
+inline bool is_physical_primitives(double gamma, double pinf, const vec4type& W) {
+  double e = eos::specific_ie(gamma, pinf, W[3], W[0]);
+  return e >= 0.0 && W[0] >= 0.0;
+}
+// euler_misc.hpp:52-67
+inline vec4type conserved_to_primitives(double gamma, double pinf, const vec4type& U) {
+  double rho = U[0];
+  double u = U[1] / rho;
+  double v = U[2] / rho;
+  double e = (U[3] / rho) - 0.5 * (u * u + v * v);
+  double p = eos::pressure(gamma, pinf, e, rho);
+  return {rho, u, v, p};
+}
+// euler_misc.hpp:70-86
+inline vec4type flux_primitive_var(double gamma, double pinf, const vec4type& W) {
+  double rho = W[0], u = W[1], v = W[2], p = W[3];
+  double e = eos::specific_ie(gamma, pinf, p, rho);
+  double E = rho * e + 0.5 * rho * (u * u + v * v);
+  return {rho * u, rho * u * u + p, rho * u * v, u * (E + p)};
+}
+// euler_misc.hpp:89-108 (assert -> status bit)
+inline vec4type primitives_to_conserved(double gamma, double pinf, const vec4type& W) {
+  double rho = W[0], u = W[1], v = W[2], p = W[3];
+  double e = eos::specific_ie(gamma, pinf, p, rho);
+  if (!(rho >= 0.0) || !(e >= 0.0)) g_status |= GFM_ST_UNPHYSICAL;
+  return {rho, rho * u, rho * v, rho * e + 0.5 * rho * (u * u + v * v)};
+}
+
+// (s M) d for the sparse quasilinear matrices: row sums left to right over
+// the non-zero entries (adding an exact zero never changes a sum's value).
+// quasilinear_form_A, euler_misc.hpp:149-163
+inline vec4type A_times(double s, double gamma, double pinf, const vec4type& W, const vec4type& d) {
+  double rho = W[0], u = W[1], p = W[3];
+  double c = eos::soundspeed(gamma, pinf, p, rho);
+  double a01 = rho, a13 = 1.0 / rho, a31 = rho * c * c;
+  double su = s * u;
+  return {su * d[0] + (s * a01) * d[1], su * d[1] + (s * a13) * d[3], su * d[2], (s * a31) * d[1] + su * d[3]};
+}
+// quasilinear_form_B, euler_misc.hpp:166-180
+inline vec4type B_times(double s, double gamma, double pinf, const vec4type& W, const vec4type& d) {
+  double rho = W[0], v = W[2], p = W[3];
+  double c = eos::soundspeed(gamma, pinf, p, rho);
+  double b02 = rho, b23 = 1.0 / rho, b32 = rho * c * c;
+  double sv = s * v;
+  return {sv * d[0] + (s * b02) * d[2], sv * d[1], sv * d[2] + (s * b23) * d[3], (s * b32) * d[2] + sv * d[3]};
+}
+
+}  // namespace misc
+
+// ----------------------------------------------------------------------------
+// pure_RS_exact::solve_RP (sourcecode/pure_RS_exact.cpp:9-73)
+// ----------------------------------------------------------------------------
+void pure_RS_solve_RP(bool paralleltox, double gamma, double pinf, const vec4type& Lstate, const vec4type& Rstate,
+                      vec4type& flux) {
+  if (!misc::is_physical_state(gamma, pinf, Lstate) || !misc::is_physical_state(gamma, pinf, Rstate))
+    g_status |= GFM_ST_UNPHYSICAL;
+  vec4type Lprims = misc::conserved_to_primitives(gamma, pinf, Lstate);
+  vec4type Rprims = misc::conserved_to_primitives(gamma, pinf, Rstate);
+  vec4type soln;
+  double Lb[3], Rb[3], sb[3];
+  exact_rs_stiffenedgas RS(gamma, gamma, pinf, pinf);
+  if (paralleltox) {
+    Lb[0] = Lprims[0]; Lb[1] = Lprims[1]; Lb[2] = Lprims[3];
+    Rb[0] = Rprims[0]; Rb[1] = Rprims[1]; Rb[2] = Rprims[3];
+    RS.solve_RP(Lb, Rb);
+    RS.sample_solution(Lb, Rb, 0.0, sb);
+    soln = {sb[0], sb[1], RS.S_STAR <= 0.0 ? Rprims[2] : Lprims[2], sb[2]};
+    flux = misc::flux_primitive_var(gamma, pinf, soln);
+  } else {
+    Lb[0] = Lprims[0]; Lb[1] = Lprims[2]; Lb[2] = Lprims[3];
+    Rb[0] = Rprims[0]; Rb[1] = Rprims[2]; Rb[2] = Rprims[3];
+    RS.solve_RP(Lb, Rb);
+    RS.sample_solution(Lb, Rb, 0.0, sb);
+    soln = {sb[0], sb[1], RS.S_STAR <= 0.0 ? Rprims[1] : Lprims[1], sb[2]};
+    flux = misc::flux_primitive_var(gamma, pinf, soln);
+    std::swap(flux[1], flux[2]);
+  }
+  if (RS.vacuum) g_status |= GFM_ST_VACUUM;
+  if (!RS.converged) g_status |= GFM_ST_NEWTON_NO_CONVERGE;
+  g_newton_iters += RS.iterations;
+}
+
+// mixed_RS_exact::solve_mixed_RP (sourcecode/mixed_RS_exact.cpp:8-48)
+void mixed_RS_solve(double gammaL, double pinfL, double gammaR, double pinfR, const vec4type& Lstate,
+                    const vec4type& Rstate, double& p_star, double& u_star, double& rho_star_L, double& rho_star_R) {
+  if (!misc::is_physical_state(gammaL, pinfL, Lstate) || !misc::is_physical_state(gammaR, pinfR, Rstate))
+    g_status |= GFM_ST_UNPHYSICAL;
+  vec4type Lprims = misc::conserved_to_primitives(gammaL, pinfL, Lstate);
+  vec4type Rprims = misc::conserved_to_primitives(gammaR, pinfR, Rstate);
+  double Lb[3] = {Lprims[0], Lprims[1], Lprims[3]};
+  double Rb[3] = {Rprims[0], Rprims[1], Rprims[3]};
+  exact_rs_stiffenedgas RS(gammaL, gammaR, pinfL, pinfR);
+  RS.solve_RP(Lb, Rb);
+  p_star = RS.P_STAR;
+  u_star = RS.S_STAR;
+  rho_star_L = RS.rho_star_L;
+  rho_star_R = RS.rho_star_R;
+  if (RS.vacuum) g_status |= GFM_ST_VACUUM;
+  if (!RS.converged) g_status |= GFM_ST_NEWTON_NO_CONVERGE;
+  if (p_star != p_star) g_status |= GFM_ST_NAN;
+  g_newton_iters += RS.iterations;
+}
+
+// ----------------------------------------------------------------------------
+// apply_BCs_euler (headers/euler_bc.hpp:5-103), including its quirk: the right
+// boundary negates u when BC_L (not BC_R) is reflective (:51).  Periodic
+// follows :7-20; it is defined for Nx == Ny only (the loop bounds there swap
+// Nx and Ny), which the library enforces.
+// ----------------------------------------------------------------------------
+template <typename G>
+void apply_BCs_euler(const sim_info& params, G& grid) {
+  const int g = params.numGC, Nx = params.Nx, Ny = params.Ny;
+  if (params.BC_T == GFM_BC_PERIODIC && params.BC_L == GFM_BC_PERIODIC && params.BC_B == GFM_BC_PERIODIC &&
+      params.BC_R == GFM_BC_PERIODIC) {
+    for (int i = 0; i < Nx + 2 * g; i++)
+      for (int j = 0; j < Ny + 2 * g; j++)
+        grid[i][j] = grid[(i - g + Ny) % Ny + g][(j - g + Nx) % Nx + g];
+    return;
+  }
+  for (int i = g; i < Ny + g; i++)
+    for (int j = 0; j < g; j++) {
+      grid[i][j] = grid[i][2 * g - j - 1];
+      if (params.BC_L == GFM_BC_REFLECTIVE) grid[i][j][1] = -grid[i][j][1];
+    }
+  for (int i = g; i < Ny + g; i++)
+    for (int j = 0; j < g; j++) {
+      grid[i][j + Nx + g] = grid[i][Nx + g - 1 - j];
+      if (params.BC_L == GFM_BC_REFLECTIVE) grid[i][j + Nx + g][1] = -grid[i][j + Nx + g][1];
+    }
+  for (int j = 0; j < Nx + 2 * g; j++)
+    for (int i = 0; i < g; i++) {
+      grid[i][j] = grid[2 * g - i - 1][j];
+      if (params.BC_B == GFM_BC_REFLECTIVE) grid[i][j][2] = -grid[i][j][2];
+    }
+  for (int j = 0; j < Nx + 2 * g; j++)
+    for (int i = 0; i < g; i++) {
+      grid[i + Ny + g][j] = grid[Ny + g - 1 - i][j];
+      if (params.BC_T == GFM_BC_REFLECTIVE) grid[i + Ny + g][j][2] = -grid[i + Ny + g][j][2];
+    }
+}
+
+// Scalar-field BCs for phi (the level set's own boundary handling, which the
+// reference takes from its absent ITM library): mirror copy, or wrap.
+void apply_BCs_scalar(const sim_info& params, griddoubletype& f) {
+  const int g = params.numGC, Nx = params.Nx, Ny = params.Ny;
+  if (params.BC_T == GFM_BC_PERIODIC && params.BC_L == GFM_BC_PERIODIC && params.BC_B == GFM_BC_PERIODIC &&
+      params.BC_R == GFM_BC_PERIODIC) {
+    for (int i = 0; i < Ny + 2 * g; i++)
+      for (int j = 0; j < Nx + 2 * g; j++)
+        f[i][j] = f[(i - g + Ny) % Ny + g][(j - g + Nx) % Nx + g];
+    return;
+  }
+  for (int i = g; i < Ny + g; i++)
+    for (int j = 0; j < g; j++) {
+      f[i][j] = f[i][2 * g - j - 1];
+      f[i][j + Nx + g] = f[i][Nx + g - 1 - j];
+    }
+  for (int j = 0; j < Nx + 2 * g; j++)
+    for (int i = 0; i < g; i++) {
+      f[i][j] = f[2 * g - i - 1][j];
+      f[i + Ny + g][j] = f[Ny + g - 1 - i][j];
+    }
+}
+
+// ----------------------------------------------------------------------------
+// FS_MUSCL::pure_fluid_update (sourcecode/FS_MUSCL.cpp:148-304) and
+// minmod_limited_slope (:310-327)
+// ----------------------------------------------------------------------------
+vec4type minmod_limited_slope(const vec4type& diff_L, const vec4type& diff_R) {
+  vec4type slope;
+  for (int k = 0; k < 4; k++) {
+    if (diff_R[k] > 0.0)
+      slope[k] = std::max(0.0, std::min(diff_L[k], diff_R[k]));
+    else
+      slope[k] = std::min(0.0, std::max(diff_L[k], diff_R[k]));
+  }
+  return slope;
+}
+
+void FS_MUSCL_update(const sim_info& params, double gamma, double pinf, double dt, const BBrange& realcells,
+                     grideuler2type& grid, grideuler2type& future_grid) {
+  using namespace misc;
+  const double dtodx = dt / params.dx;
+  const double dtody = dt / params.dy;
+  for (int i = realcells.imin; i < realcells.imax; i++)
+    for (int j = realcells.jmin; j < realcells.jmax; j++) {
+      future_grid[i][j] = grid[i][j];
+      if (!is_physical_state(gamma, pinf, grid[i][j])) g_status |= GFM_ST_UNPHYSICAL;
+    }
+  const double sx = 0.5 * dtodx, sy = 0.5 * dtody;
+  for (int i = realcells.imin; i < realcells.imax + 1; i++) {
+    for (int j = realcells.jmin; j < realcells.jmax + 1; j++) {
+      vec4type W_i_j = conserved_to_primitives(gamma, pinf, grid[i][j]);
+      vec4type W_ip_j = conserved_to_primitives(gamma, pinf, grid[i + 1][j]);
+      vec4type W_im_j = conserved_to_primitives(gamma, pinf, grid[i - 1][j]);
+      vec4type W_imm_j = conserved_to_primitives(gamma, pinf, grid[i - 2][j]);
+      vec4type W_i_jp = conserved_to_primitives(gamma, pinf, grid[i][j + 1]);
+      vec4type W_i_jm = conserved_to_primitives(gamma, pinf, grid[i][j - 1]);
+      vec4type W_i_jmm = conserved_to_primitives(gamma, pinf, grid[i][j - 2]);
+      vec4type W_im_jm = conserved_to_primitives(gamma, pinf, grid[i - 1][j - 1]);
+
+      vec4type slope_C_x = minmod_limited_slope(sub(W_i_j, W_i_jm), sub(W_i_jp, W_i_j));
+      vec4type slope_C_y = minmod_limited_slope(sub(W_i_j, W_im_j), sub(W_ip_j, W_i_j));
+      vec4type slope_L_x = minmod_limited_slope(sub(W_i_jm, W_i_jmm), sub(W_i_j, W_i_jm));
+      vec4type slope_L_y = minmod_limited_slope(
+          sub(W_i_jm, W_im_jm), sub(conserved_to_primitives(gamma, pinf, grid[i + 1][j - 1]), W_i_jm));
+      vec4type slope_B_x = minmod_limited_slope(
+          sub(W_im_j, W_im_jm), sub(conserved_to_primitives(gamma, pinf, grid[i - 1][j + 1]), W_im_j));
+      vec4type slope_B_y = minmod_limited_slope(sub(W_im_j, W_imm_j), sub(W_i_j, W_im_j));
+
+      vec4type C_BEV_L = sub(W_i_j, scale(0.5, slope_C_x));
+      vec4type C_BEV_R = add(W_i_j, scale(0.5, slope_C_x));
+      vec4type C_BEV_B = sub(W_i_j, scale(0.5, slope_C_y));
+      vec4type C_BEV_T = add(W_i_j, scale(0.5, slope_C_y));
+      vec4type B_BEV_L = sub(W_im_j, scale(0.5, slope_B_x));
+      vec4type B_BEV_R = add(W_im_j, scale(0.5, slope_B_x));
+      vec4type B_BEV_B = sub(W_im_j, scale(0.5, slope_B_y));
+      vec4type B_BEV_T = add(W_im_j, scale(0.5, slope_B_y));
+      vec4type L_BEV_L = sub(W_i_jm, scale(0.5, slope_L_x));
+      vec4type L_BEV_R = add(W_i_jm, scale(0.5, slope_L_x));
+      vec4type L_BEV_B = sub(W_i_jm, scale(0.5, slope_L_y));
+      vec4type L_BEV_T = add(W_i_jm, scale(0.5, slope_L_y));
+
+      if (!is_physical_primitives(gamma, pinf, C_BEV_L) || !is_physical_primitives(gamma, pinf, C_BEV_R)) {
+        C_BEV_L = W_i_j; C_BEV_R = W_i_j;
+      }
+      if (!is_physical_primitives(gamma, pinf, C_BEV_B) || !is_physical_primitives(gamma, pinf, C_BEV_T)) {
+        C_BEV_B = W_i_j; C_BEV_T = W_i_j;
+      }
+      if (!is_physical_primitives(gamma, pinf, B_BEV_L) || !is_physical_primitives(gamma, pinf, B_BEV_R)) {
+        B_BEV_L = W_im_j; B_BEV_R = W_im_j;
+      }
+      if (!is_physical_primitives(gamma, pinf, B_BEV_B) || !is_physical_primitives(gamma, pinf, B_BEV_T)) {
+        B_BEV_B = W_im_j; B_BEV_T = W_im_j;
+      }
+      if (!is_physical_primitives(gamma, pinf, L_BEV_L) || !is_physical_primitives(gamma, pinf, L_BEV_R)) {
+        L_BEV_L = W_i_jm; L_BEV_R = W_i_jm;
+      }
+      if (!is_physical_primitives(gamma, pinf, L_BEV_B) || !is_physical_primitives(gamma, pinf, L_BEV_T)) {
+        L_BEV_B = W_i_jm; L_BEV_T = W_i_jm;
+      }
+
+      // C_BEV + 0.5 dt/dx A (L - R) + 0.5 dt/dy B (B - T)   (:258-272)
+      vec4type XC = A_times(sx, gamma, pinf, W_i_j, sub(C_BEV_L, C_BEV_R));
+      vec4type YC = B_times(sy, gamma, pinf, W_i_j, sub(C_BEV_B, C_BEV_T));
+      vec4type XL = A_times(sx, gamma, pinf, W_i_jm, sub(L_BEV_L, L_BEV_R));
+      vec4type YL = B_times(sy, gamma, pinf, W_i_jm, sub(L_BEV_B, L_BEV_T));
+      vec4type XB = A_times(sx, gamma, pinf, W_im_j, sub(B_BEV_L, B_BEV_R));
+      vec4type YB = B_times(sy, gamma, pinf, W_im_j, sub(B_BEV_B, B_BEV_T));
+      vec4type C_BEV_L_evolved = add(add(C_BEV_L, XC), YC);
+      vec4type C_BEV_B_evolved = add(add(C_BEV_B, XC), YC);
+      vec4type L_BEV_R_evolved = add(add(L_BEV_R, XL), YL);
+      vec4type B_BEV_T_evolved = add(add(B_BEV_T, XB), YB);
+
+      if (!is_physical_primitives(gamma, pinf, C_BEV_L_evolved) ||
+          !is_physical_primitives(gamma, pinf, L_BEV_R_evolved)) {
+        C_BEV_L_evolved = W_i_j;
+        L_BEV_R_evolved = W_i_jm;
+      }
+      if (!is_physical_primitives(gamma, pinf, C_BEV_B_evolved) ||
+          !is_physical_primitives(gamma, pinf, B_BEV_T_evolved)) {
+        C_BEV_B_evolved = W_i_j;
+        B_BEV_T_evolved = W_im_j;
+      }
+
+      vec4type flux_x, flux_y;
+      pure_RS_solve_RP(true, gamma, pinf, primitives_to_conserved(gamma, pinf, L_BEV_R_evolved),
+                       primitives_to_conserved(gamma, pinf, C_BEV_L_evolved), flux_x);
+      pure_RS_solve_RP(false, gamma, pinf, primitives_to_conserved(gamma, pinf, B_BEV_T_evolved),
+                       primitives_to_conserved(gamma, pinf, C_BEV_B_evolved), flux_y);
+
+      future_grid[i][j] = add(future_grid[i][j], add(scale(dtodx, flux_x), scale(dtody, flux_y)));
+      future_grid[i][j - 1] = sub(future_grid[i][j - 1], scale(dtodx, flux_x));
+      future_grid[i - 1][j] = sub(future_grid[i - 1][j], scale(dtody, flux_y));
+    }
+  }
+  for (int i = realcells.imin; i < realcells.imax; i++)
+    for (int j = realcells.jmin; j < realcells.jmax; j++) grid[i][j] = future_grid[i][j];
+}
+
+// FS_godunov::pure_fluid_update (sourcecode/FS_godunov.cpp:5-50)
+void FS_godunov_update(const sim_info& params, double gamma, double pinf, double dt, const BBrange& realcells,
+                       grideuler2type& grid, grideuler2type& future_grid) {
+  const double dtodx = dt / params.dx;
+  const double dtody = dt / params.dy;
+  vec4type flux_x, flux_y;
+  for (int i = realcells.imin; i < realcells.imax; i++)
+    for (int j = realcells.jmin; j < realcells.jmax; j++) {
+      future_grid[i][j] = grid[i][j];
+      if (!misc::is_physical_state(gamma, pinf, grid[i][j])) g_status |= GFM_ST_UNPHYSICAL;
+    }
+  for (int i = realcells.imin; i < realcells.imax + 1; i++)
+    for (int j = realcells.jmin; j < realcells.jmax + 1; j++) {
+      pure_RS_solve_RP(true, gamma, pinf, grid[i][j - 1], grid[i][j], flux_x);
+      pure_RS_solve_RP(false, gamma, pinf, grid[i - 1][j], grid[i][j], flux_y);
+      future_grid[i][j] = add(future_grid[i][j], add(scale(dtodx, flux_x), scale(dtody, flux_y)));
+      future_grid[i][j - 1] = sub(future_grid[i][j - 1], scale(dtodx, flux_x));
+      future_grid[i - 1][j] = sub(future_grid[i - 1][j], scale(dtody, flux_y));
+    }
+  for (int i = realcells.imin; i < realcells.imax; i++)
+    for (int j = realcells.jmin; j < realcells.jmax; j++) grid[i][j] = future_grid[i][j];
+}
+
+void FS_update(int fs, const sim_info& params, double gamma, double pinf, double dt, const BBrange& rc,
+               grideuler2type& grid, grideuler2type& future_grid) {
+  if (fs == GFM_FS_MUSCL)
+    FS_MUSCL_update(params, gamma, pinf, dt, rc, grid, future_grid);
+  else
+    FS_godunov_update(params, gamma, pinf, dt, rc, grid, future_grid);
+}
+
+// ----------------------------------------------------------------------------
+// Level set (the reference's Levelset class lives in the absent
+// PhD-Interface-tracking-methods library; this is the project's own
+// definition, call sites sourcecode/sim_twofluid.cpp:47,72,555-570).
+//   normal at a cell centre: central-difference gradient of phi
+//   interfacial cell: phi <= 0 differs from a 4-neighbour's phi <= 0
+//   advection: order 1 = first-order upwind, forward Euler;
+//              order 5 = HOUC5 with 3-stage TVD Runge-Kutta, frozen velocity
+//   reinitialisation: Sussman-Smereka-Osher PDE, Godunov upwinding,
+//              dtau = 0.5 min(dx, dy), S(phi0) = phi0 / sqrt(phi0^2 + h^2)
+// ----------------------------------------------------------------------------
+struct Levelset {
+  sim_info params;
+  griddoubletype phi;
+  int order = 5, reinit_every = 1, reinit_iters = 5;
+  int updates = 0;
+
+  double get_sdf(int i, int j) const { return phi[i][j]; }
+  vec2 get_normal(int i, int j) const {
+    return {(phi[i][j + 1] - phi[i][j - 1]) / (2.0 * params.dx), (phi[i + 1][j] - phi[i - 1][j]) / (2.0 * params.dy)};
+  }
+  bool is_interfacial_cell(int i, int j) const {
+    bool s = phi[i][j] <= 0.0;
+    return (phi[i][j - 1] <= 0.0) != s || (phi[i][j + 1] <= 0.0) != s || (phi[i - 1][j] <= 0.0) != s ||
+           (phi[i + 1][j] <= 0.0) != s;
+  }
+
+  // HOUC5 one-sided derivative in x for velocity sign a
+  static double houc5(double a, double fm3, double fm2, double fm1, double f0, double fp1, double fp2, double fp3,
+                      double h) {
+    if (a >= 0.0)
+      return (-2.0 * fm3 + 15.0 * fm2 - 60.0 * fm1 + 20.0 * f0 + 30.0 * fp1 - 3.0 * fp2) / (60.0 * h);
+    return (3.0 * fm2 - 30.0 * fm1 - 20.0 * f0 + 60.0 * fp1 - 15.0 * fp2 + 2.0 * fp3) / (60.0 * h);
+  }
+
+  // rate L(f) = -(u f_x + v f_y) on real cells
+  void rate(const griddoubletype& f, const gridVector2dtype& vel, griddoubletype& out) const {
+    const int g = params.numGC;
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++) {
+        double u = vel[i][j][0], v = vel[i][j][1];
+        double fx, fy;
+        if (order == 1) {
+          fx = (u >= 0.0) ? (f[i][j] - f[i][j - 1]) / params.dx : (f[i][j + 1] - f[i][j]) / params.dx;
+          fy = (v >= 0.0) ? (f[i][j] - f[i - 1][j]) / params.dy : (f[i + 1][j] - f[i][j]) / params.dy;
+        } else {
+          fx = houc5(u, f[i][j - 3], f[i][j - 2], f[i][j - 1], f[i][j], f[i][j + 1], f[i][j + 2], f[i][j + 3],
+                     params.dx);
+          fy = houc5(v, f[i - 3][j], f[i - 2][j], f[i - 1][j], f[i][j], f[i + 1][j], f[i + 2][j], f[i + 3][j],
+                     params.dy);
+        }
+        out[i][j] = -(u * fx + v * fy);
+      }
+  }
+
+  void advect(const gridVector2dtype& vel, double dt) {
+    const int g = params.numGC;
+    griddoubletype L(phi.size(), std::vector<double>(phi[0].size(), 0.0));
+    if (order == 1) {
+      rate(phi, vel, L);
+      for (int i = g; i < params.Ny + g; i++)
+        for (int j = g; j < params.Nx + g; j++) phi[i][j] = phi[i][j] + dt * L[i][j];
+      apply_BCs_scalar(params, phi);
+      return;
+    }
+    griddoubletype p1 = phi, p2 = phi;
+    rate(phi, vel, L);
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++) p1[i][j] = phi[i][j] + dt * L[i][j];
+    apply_BCs_scalar(params, p1);
+    rate(p1, vel, L);
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++) p2[i][j] = 0.75 * phi[i][j] + 0.25 * (p1[i][j] + dt * L[i][j]);
+    apply_BCs_scalar(params, p2);
+    rate(p2, vel, L);
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++)
+        phi[i][j] = (1.0 / 3.0) * phi[i][j] + (2.0 / 3.0) * (p2[i][j] + dt * L[i][j]);
+    apply_BCs_scalar(params, phi);
+  }
+
+  void reinitialise() {
+    const int g = params.numGC;
+    const double h = std::min(params.dx, params.dy);
+    const double dtau = 0.5 * h;
+    griddoubletype phi0 = phi, next = phi;
+    for (int it = 0; it < reinit_iters; it++) {
+      for (int i = g; i < params.Ny + g; i++)
+        for (int j = g; j < params.Nx + g; j++) {
+          double p0 = phi0[i][j];
+          double S = p0 / std::sqrt(p0 * p0 + h * h);
+          double a = (phi[i][j] - phi[i][j - 1]) / params.dx;
+          double b = (phi[i][j + 1] - phi[i][j]) / params.dx;
+          double c = (phi[i][j] - phi[i - 1][j]) / params.dy;
+          double d = (phi[i + 1][j] - phi[i][j]) / params.dy;
+          double gx, gy;
+          if (p0 > 0.0) {
+            double ap = std::max(a, 0.0), bm = std::min(b, 0.0), cp = std::max(c, 0.0), dm = std::min(d, 0.0);
+            gx = std::max(ap * ap, bm * bm);
+            gy = std::max(cp * cp, dm * dm);
+          } else {
+            double am = std::min(a, 0.0), bp = std::max(b, 0.0), cm = std::min(c, 0.0), dp = std::max(d, 0.0);
+            gx = std::max(am * am, bp * bp);
+            gy = std::max(cm * cm, dp * dp);
+          }
+          double G = std::sqrt(gx + gy) - 1.0;
+          next[i][j] = phi[i][j] - dtau * S * G;
+        }
+      apply_BCs_scalar(params, next);
+      phi = next;
+    }
+  }
+
+  // update_interface_coupled(vfield, t, dt)
+  void update_interface_coupled(const gridVector2dtype& vel, double dt) {
+    advect(vel, dt);
+    updates++;
+    if (reinit_every > 0 && updates % reinit_every == 0) reinitialise();
+  }
+};
+
+// unit normal with the reference's fallback (e.g. sourcecode/GFM_riemann.cpp:58-68)
+inline vec2 unit_normal(const Levelset& ls, int i, int j) {
+  vec2 n = ls.get_normal(i, j);
+  double nn = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+  if (nn < 1e-12) return {1.0, 0.0};
+  return {n[0] / nn, n[1] / nn};
+}
+
+// grid_bilinear_interpolate (PhD-Common; absent): bilinear in the four cell
+// centres surrounding x.
+vec4type grid_bilinear_interpolate(const sim_info& params, const grideuler2type& grid, const vec2& x) {
+  double s = (x[0] - params.x0) / params.dx + static_cast<double>(params.numGC) - 0.5;
+  double t = (x[1] - params.y0) / params.dy + static_cast<double>(params.numGC) - 0.5;
+  int j0 = static_cast<int>(std::floor(s));
+  int i0 = static_cast<int>(std::floor(t));
+  const int nrow = params.Ny + 2 * params.numGC, ncol = params.Nx + 2 * params.numGC;
+  j0 = std::min(std::max(j0, 0), ncol - 2);
+  i0 = std::min(std::max(i0, 0), nrow - 2);
+  double a = s - static_cast<double>(j0);
+  double b = t - static_cast<double>(i0);
+  vec4type out;
+  for (int k = 0; k < 4; k++)
+    out[k] = ((1.0 - a) * (1.0 - b)) * grid[i0][j0][k] + (a * (1.0 - b)) * grid[i0][j0 + 1][k] +
+             ((1.0 - a) * b) * grid[i0 + 1][j0][k] + (a * b) * grid[i0 + 1][j0 + 1][k];
+  return out;
+}
+
+// GFM_base::get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33)
+void get_interpolated_mixedRPstates(const sim_info& params, const grideuler2type& prims1,
+                                    const grideuler2type& prims2, const Levelset& ls, int i, int j, double ds,
+                                    vec4type& Lprims, vec4type& Rprims) {
+  vec2 CC = params.cellcentre_coord(i, j);
+  double lsval = ls.get_sdf(i, j);
+  vec2 normal = ls.get_normal(i, j);
+  double normmag = std::sqrt(normal[0] * normal[0] + normal[1] * normal[1]);
+  if (std::fabs(lsval) > ds) lsval = std::copysign(ds, lsval);
+  vec2 nh = {normal[0] / normmag, normal[1] / normmag};
+  vec2 interfacelocation = {CC[0] - lsval * nh[0], CC[1] - lsval * nh[1]};
+  vec2 sampleposL = {interfacelocation[0] + ds * nh[0], interfacelocation[1] + ds * nh[1]};
+  vec2 sampleposR = {interfacelocation[0] - ds * nh[0], interfacelocation[1] - ds * nh[1]};
+  Lprims = grid_bilinear_interpolate(params, prims2, sampleposL);
+  Rprims = grid_bilinear_interpolate(params, prims1, sampleposR);
+}
+
+// ----------------------------------------------------------------------------
+// extrapolate_vector / extrapolate_vector_mgfm (sourcecode/extrapolate_vector.cpp:5-141, 150-288)
+// ----------------------------------------------------------------------------
+void extrapolate_vector_impl(const sim_info& params, const Levelset& ls, int N, grideuler2type& grid1,
+                             grideuler2type& grid2, bool skip_interfacial) {
+  const int g = params.numGC;
+  grideuler2type updated_grid1 = grid1, updated_grid2 = grid2;
+  const double dt = 0.5 * std::min(params.dx, params.dy);
+  for (int num = 0; num < N; num++) {
+    grid1 = updated_grid1;
+    grid2 = updated_grid2;
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++) {
+        double lsval = ls.get_sdf(i, j);
+        vec2 normal = unit_normal(ls, i, j);
+        if (skip_interfacial && ls.is_interfacial_cell(i, j)) continue;
+        vec4type del_vec_x, del_vec_y;
+        if (lsval <= 0.0) {
+          del_vec_x = (normal[0] > 0.0) ? sub(grid2[i][j + 1], grid2[i][j]) : sub(grid2[i][j], grid2[i][j - 1]);
+          del_vec_y = (normal[1] > 0.0) ? sub(grid2[i + 1][j], grid2[i][j]) : sub(grid2[i][j], grid2[i - 1][j]);
+          updated_grid2[i][j] = add(add(grid2[i][j], scale((dt / params.dx) * normal[0], del_vec_x)),
+                                    scale((dt / params.dy) * normal[1], del_vec_y));
+        } else {
+          del_vec_x = (normal[0] > 0.0) ? sub(grid1[i][j], grid1[i][j - 1]) : sub(grid1[i][j + 1], grid1[i][j]);
+          del_vec_y = (normal[1] > 0.0) ? sub(grid1[i][j], grid1[i - 1][j]) : sub(grid1[i + 1][j], grid1[i][j]);
+          updated_grid1[i][j] = sub(sub(grid1[i][j], scale((dt / params.dx) * normal[0], del_vec_x)),
+                                    scale((dt / params.dy) * normal[1], del_vec_y));
+        }
+      }
+    apply_BCs_euler(params, updated_grid1);
+    apply_BCs_euler(params, updated_grid2);
+  }
+  grid1 = updated_grid1;
+  grid2 = updated_grid2;
+}
+
+// extrapolate_extension_vfield (sourcecode/extrapolate_extension_vfield.cpp:4-122);
+// BCs by the vector analogue of the Euler mirror (velocity components copied).
+void extrapolate_extension_vfield(const sim_info& params, const Levelset& ls, int N, gridVector2dtype& vel) {
+  const int g = params.numGC;
+  gridVector2dtype updated = vel;
+  const double dt = 0.5 * std::min(params.dx, params.dy);
+  for (int num = 0; num < N; num++) {
+    vel = updated;
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++) {
+        if (ls.is_interfacial_cell(i, j)) continue;
+        double lsval = ls.get_sdf(i, j);
+        vec2 n = ls.get_normal(i, j);
+        double nn = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+        if (!(nn > 1e-12)) continue;
+        vec2 normal = {n[0] / nn, n[1] / nn};
+        vec2 dvx, dvy;
+        if (lsval <= 0.0) {
+          for (int k = 0; k < 2; k++) {
+            dvx[k] = (normal[0] > 0.0) ? vel[i][j + 1][k] - vel[i][j][k] : vel[i][j][k] - vel[i][j - 1][k];
+            dvy[k] = (normal[1] > 0.0) ? vel[i + 1][j][k] - vel[i][j][k] : vel[i][j][k] - vel[i - 1][j][k];
+          }
+          for (int k = 0; k < 2; k++)
+            updated[i][j][k] = (vel[i][j][k] + ((dt / params.dx) * normal[0]) * dvx[k]) +
+                               ((dt / params.dy) * normal[1]) * dvy[k];
+        } else {
+          for (int k = 0; k < 2; k++) {
+            dvx[k] = (normal[0] > 0.0) ? vel[i][j][k] - vel[i][j - 1][k] : vel[i][j + 1][k] - vel[i][j][k];
+            dvy[k] = (normal[1] > 0.0) ? vel[i][j][k] - vel[i - 1][j][k] : vel[i + 1][j][k] - vel[i][j][k];
+          }
+          for (int k = 0; k < 2; k++)
+            updated[i][j][k] = (vel[i][j][k] - ((dt / params.dx) * normal[0]) * dvx[k]) -
+                               ((dt / params.dy) * normal[1]) * dvy[k];
+        }
+      }
+    // vector mirror BCs
+    const int Nx = params.Nx, Ny = params.Ny;
+    for (int i = g; i < Ny + g; i++)
+      for (int j = 0; j < g; j++) {
+        updated[i][j] = updated[i][2 * g - j - 1];
+        updated[i][j + Nx + g] = updated[i][Nx + g - 1 - j];
+      }
+    for (int j = 0; j < Nx + 2 * g; j++)
+      for (int i = 0; i < g; i++) {
+        updated[i][j] = updated[2 * g - i - 1][j];
+        updated[i + Ny + g][j] = updated[Ny + g - 1 - i][j];
+      }
+  }
+  vel = updated;
+}
+
+// composite velocity field: the real fluid's velocity in every cell
+void real_fluid_velocities(const sim_info& params, const Levelset& ls, const grideuler2type& prims1,
+                           const grideuler2type& prims2, gridVector2dtype& vel) {
+  for (int i = 0; i < params.Ny + 2 * params.numGC; i++)
+    for (int j = 0; j < params.Nx + 2 * params.numGC; j++) {
+      if (ls.get_sdf(i, j) <= 0.0)
+        vel[i][j] = {prims1[i][j][1], prims1[i][j][2]};
+      else
+        vel[i][j] = {prims2[i][j][1], prims2[i][j][2]};
+    }
+}
+
+// ----------------------------------------------------------------------------
+// GFM variants: set_ghost_states.  Scratch grids are locals (the reference's
+// function-static scratch, e.g. sourcecode/GFM_riemann.cpp:20-30, is only a
+// reuse of storage).
+// ----------------------------------------------------------------------------
+struct GFMState {
+  gridVector2dtype newvelocities;  // vfield handed to the level set
+  int64_t n_interfacial = 0;
+};
+
+void gfm_convert_all(const sim_info& params, const binarySGparams& eos, const grideuler2type& grid1,
+                     const grideuler2type& grid2, grideuler2type& prims1, grideuler2type& prims2) {
+  for (int i = 0; i < params.Ny + 2 * params.numGC; i++)
+    for (int j = 0; j < params.Nx + 2 * params.numGC; j++) {
+      prims1[i][j] = misc::conserved_to_primitives(eos.gamma1, eos.pinf1, grid1[i][j]);
+      prims2[i][j] = misc::conserved_to_primitives(eos.gamma2, eos.pinf2, grid2[i][j]);
+    }
+}
+
+void gfm_back_to_conserved(const sim_info& params, const binarySGparams& eos, const grideuler2type& prims1,
+                           const grideuler2type& prims2, grideuler2type& grid1, grideuler2type& grid2) {
+  for (int i = 0; i < params.Ny + 2 * params.numGC; i++)
+    for (int j = 0; j < params.Nx + 2 * params.numGC; j++) {
+      grid1[i][j] = misc::primitives_to_conserved(eos.gamma1, eos.pinf1, prims1[i][j]);
+      grid2[i][j] = misc::primitives_to_conserved(eos.gamma2, eos.pinf2, prims2[i][j]);
+    }
+}
+
+// The mixed Riemann problem in the interface-normal frame, shared by the
+// Riemann, real and modified GFM (e.g. sourcecode/GFM_riemann.cpp:76-122).
+struct MRPResult {
+  double p_star, u_star, rho_star_L, rho_star_R;
+  vec2 u1_tang, u2_tang;
+};
+MRPResult solve_interface_RP(const binarySGparams& eos, const vec4type& interfaceprims1,
+                             const vec4type& interfaceprims2, const vec2& normal) {
+  vec2 u1 = {interfaceprims1[1], interfaceprims1[2]};
+  vec2 u2 = {interfaceprims2[1], interfaceprims2[2]};
+  double u1n = u1[0] * normal[0] + u1[1] * normal[1];
+  double u2n = u2[0] * normal[0] + u2[1] * normal[1];
+  vec2 u1_normal = {u1n * normal[0], u1n * normal[1]};
+  vec2 u2_normal = {u2n * normal[0], u2n * normal[1]};
+  MRPResult r;
+  r.u1_tang = {u1[0] - u1_normal[0], u1[1] - u1_normal[1]};
+  r.u2_tang = {u2[0] - u2_normal[0], u2[1] - u2_normal[1]};
+  vec4type Lprims = {interfaceprims1[0], u1n, 0.0, std::max(1e-6, interfaceprims1[3])};
+  vec4type Rprims = {interfaceprims2[0], u2n, 0.0, std::max(1e-6, interfaceprims2[3])};
+  vec4type Lstate = misc::primitives_to_conserved(eos.gamma1, eos.pinf1, Lprims);
+  vec4type Rstate = misc::primitives_to_conserved(eos.gamma2, eos.pinf2, Rprims);
+  mixed_RS_solve(eos.gamma1, eos.pinf1, eos.gamma2, eos.pinf2, Lstate, Rstate, r.p_star, r.u_star, r.rho_star_L,
+                 r.rho_star_R);
+  return r;
+}
+
+// GFM_riemann::set_ghost_states (sourcecode/GFM_riemann.cpp:8-188)
+void GFM_riemann_set_ghost_states(const sim_info& params, const Levelset& ls, const binarySGparams& eos,
+                                  const gfm_method_desc& m, grideuler2type& grid1, grideuler2type& grid2,
+                                  GFMState& st) {
+  const int g = params.numGC;
+  const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+  grideuler2type prims1(nr, std::vector<vec4type>(nc)), prims2(nr, std::vector<vec4type>(nc));
+  st.newvelocities.assign(nr, std::vector<vec2>(nc, vec2{0.0, 0.0}));
+  const double ds = 1.0 * std::min(params.dx, params.dy);
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      if (!misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j]) ||
+          !misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]))
+        g_status |= GFM_ST_UNPHYSICAL;
+    }
+  gfm_convert_all(params, eos, grid1, grid2, prims1, prims2);
+  extrapolate_vector_impl(params, ls, 2, prims1, prims2, false);
+  st.n_interfacial = 0;
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      if (!ls.is_interfacial_cell(i, j)) continue;
+      st.n_interfacial++;
+      double lsval = ls.get_sdf(i, j);
+      vec2 normal = unit_normal(ls, i, j);
+      vec4type interfaceprims1, interfaceprims2;
+      get_interpolated_mixedRPstates(params, prims1, prims2, ls, i, j, ds, interfaceprims2, interfaceprims1);
+      MRPResult r = solve_interface_RP(eos, interfaceprims1, interfaceprims2, normal);
+      vec2 u1_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+      vec2 u2_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+      if (lsval <= 0.0)
+        prims1[i][j] = {r.rho_star_L, u1_star[0], u1_star[1], r.p_star};
+      else
+        prims2[i][j] = {r.rho_star_R, u2_star[0], u2_star[1], r.p_star};
+      st.newvelocities[i][j] = {r.u_star * normal[0], r.u_star * normal[1]};
+    }
+  extrapolate_vector_impl(params, ls, 6, prims1, prims2, false);
+  if (m.use_extension_vfield)
+    extrapolate_extension_vfield(params, ls, 20, st.newvelocities);
+  else
+    real_fluid_velocities(params, ls, prims1, prims2, st.newvelocities);
+  gfm_back_to_conserved(params, eos, prims1, prims2, grid1, grid2);
+}
+
+// GFM_real::set_ghost_states (sourcecode/GFM_real.cpp:8-248)
+void GFM_real_set_ghost_states(const sim_info& params, const Levelset& ls, const binarySGparams& eos,
+                               const gfm_method_desc& m, grideuler2type& grid1, grideuler2type& grid2,
+                               GFMState& st) {
+  const int g = params.numGC;
+  const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+  grideuler2type prims1(nr, std::vector<vec4type>(nc)), prims2(nr, std::vector<vec4type>(nc));
+  st.newvelocities.assign(nr, std::vector<vec2>(nc, vec2{0.0, 0.0}));
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      double lsval = ls.get_sdf(i, j);
+      prims1[i][j] = misc::conserved_to_primitives(eos.gamma1, eos.pinf1, grid1[i][j]);
+      prims2[i][j] = misc::conserved_to_primitives(eos.gamma2, eos.pinf2, grid2[i][j]);
+      bool ok = (lsval <= 0.0) ? misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j])
+                               : misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]);
+      if (!ok) g_status |= GFM_ST_UNPHYSICAL;
+    }
+  st.n_interfacial = 0;
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      if (!ls.is_interfacial_cell(i, j)) continue;
+      st.n_interfacial++;
+      double lsval = ls.get_sdf(i, j);
+      vec2 normal = unit_normal(ls, i, j);
+      // :77-117 neighbour with opposite phi sign and the closest normal direction
+      double mindiff = 1e100;
+      int i_opp = -1000, j_opp = -1000;
+      for (int xinc = -1; xinc <= 1; xinc++)
+        for (int yinc = -1; yinc <= 1; yinc++) {
+          double otherlsval = ls.get_sdf(i + yinc, j + xinc);
+          if (lsval * otherlsval <= 0.0) {
+            vec2 othernormal = unit_normal(ls, i + yinc, j + xinc);
+            double dotprod = normal[0] * othernormal[0] + normal[1] * othernormal[1];
+            dotprod = std::max(dotprod, -1.0);
+            dotprod = std::min(dotprod, 1.0);
+            double anglediff = omath::acos(dotprod);
+            if (anglediff < mindiff) {
+              i_opp = i + yinc;
+              j_opp = j + xinc;
+              mindiff = anglediff;
+            }
+          }
+        }
+      vec4type interfaceprims1, interfaceprims2;
+      if (lsval <= 0.0) {
+        interfaceprims1 = prims1[i][j];
+        interfaceprims2 = prims2[i_opp][j_opp];
+      } else {
+        interfaceprims2 = prims2[i][j];
+        interfaceprims1 = prims1[i_opp][j_opp];
+      }
+      MRPResult r = solve_interface_RP(eos, interfaceprims1, interfaceprims2, normal);
+      vec2 u1_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+      vec2 u2_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+      if (lsval <= 0.0)
+        prims1[i][j] = {r.rho_star_L, u1_star[0], u1_star[1], r.p_star};
+      else
+        prims2[i][j] = {r.rho_star_R, u2_star[0], u2_star[1], r.p_star};
+      st.newvelocities[i][j] = {r.u_star * normal[0], r.u_star * normal[1]};
+    }
+  extrapolate_vector_impl(params, ls, 6, prims1, prims2, false);
+  if (m.use_extension_vfield)
+    extrapolate_extension_vfield(params, ls, 20, st.newvelocities);
+  else
+    real_fluid_velocities(params, ls, prims1, prims2, st.newvelocities);
+  gfm_back_to_conserved(params, eos, prims1, prims2, grid1, grid2);
+}
+
+// GFM_modified::set_ghost_states (sourcecode/GFM_modified.cpp:8-240), with
+// its quirk: the grids are rebuilt from new_prims (:234-235), so the
+// extrapolation of prims (:202) only reaches the velocity field.
+void GFM_modified_set_ghost_states(const sim_info& params, const Levelset& ls, const binarySGparams& eos,
+                                   const gfm_method_desc& m, grideuler2type& grid1, grideuler2type& grid2,
+                                   GFMState& st) {
+  const int g = params.numGC;
+  const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+  grideuler2type prims1(nr, std::vector<vec4type>(nc)), prims2(nr, std::vector<vec4type>(nc));
+  st.newvelocities.assign(nr, std::vector<vec2>(nc, vec2{0.0, 0.0}));
+  const double ds = 1.0 * std::min(params.dx, params.dy);
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      double lsval = ls.get_sdf(i, j);
+      prims1[i][j] = misc::conserved_to_primitives(eos.gamma1, eos.pinf1, grid1[i][j]);
+      prims2[i][j] = misc::conserved_to_primitives(eos.gamma2, eos.pinf2, grid2[i][j]);
+      bool ok = (lsval <= 0.0) ? misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j])
+                               : misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]);
+      if (!ok) g_status |= GFM_ST_UNPHYSICAL;
+    }
+  grideuler2type new_prims1 = prims1, new_prims2 = prims2;
+  extrapolate_vector_impl(params, ls, 2, prims1, prims2, false);
+  st.n_interfacial = 0;
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      double lsval = ls.get_sdf(i, j);
+      if (!ls.is_interfacial_cell(i, j)) continue;
+      st.n_interfacial++;
+      vec2 normal = unit_normal(ls, i, j);
+      vec4type interfaceprims1, interfaceprims2;
+      get_interpolated_mixedRPstates(params, prims1, prims2, ls, i, j, ds, interfaceprims2, interfaceprims1);
+      MRPResult r = solve_interface_RP(eos, interfaceprims1, interfaceprims2, normal);
+      vec2 u1_star, u2_star;
+      if (m.use_slip_BCs) {
+        u1_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+        u2_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+      } else if (lsval <= 0.0) {
+        u1_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+        u2_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+      } else {
+        u1_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+        u2_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+      }
+      if (lsval <= 0.0) {
+        new_prims1[i][j][0] = eos::isentropic_extrapolation(eos.gamma1, eos.pinf1, r.rho_star_L, r.p_star,
+                                                            prims1[i][j][3]);
+        new_prims2[i][j] = {r.rho_star_R, u2_star[0], u2_star[1], r.p_star};
+      } else {
+        new_prims2[i][j][0] = eos::isentropic_extrapolation(eos.gamma2, eos.pinf2, r.rho_star_R, r.p_star,
+                                                            prims2[i][j][3]);
+        new_prims1[i][j] = {r.rho_star_L, u1_star[0], u1_star[1], r.p_star};
+      }
+      st.newvelocities[i][j] = {r.u_star * normal[0], r.u_star * normal[1]};
+    }
+  extrapolate_vector_impl(params, ls, 6, prims1, prims2, true);
+  if (m.use_extension_vfield)
+    extrapolate_extension_vfield(params, ls, 20, st.newvelocities);
+  else
+    real_fluid_velocities(params, ls, prims1, prims2, st.newvelocities);
+  gfm_back_to_conserved(params, eos, new_prims1, new_prims2, grid1, grid2);
+}
+
+// GFM_original::set_ghost_states (sourcecode/GFM_original.cpp:8-166)
+void GFM_original_set_ghost_states(const sim_info& params, const Levelset& ls, const binarySGparams& eos,
+                                   const gfm_method_desc& m, grideuler2type& grid1, grideuler2type& grid2,
+                                   BBrange& realcells1, BBrange& realcells2, GFMState& st) {
+  const int g = params.numGC;
+  const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+  grideuler2type prims1(nr, std::vector<vec4type>(nc)), prims2(nr, std::vector<vec4type>(nc));
+  st.newvelocities.assign(nr, std::vector<vec2>(nc, vec2{0.0, 0.0}));
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      if (!misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j]) ||
+          !misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]))
+        g_status |= GFM_ST_UNPHYSICAL;
+    }
+  gfm_convert_all(params, eos, grid1, grid2, prims1, prims2);
+  realcells1 = {g + params.Ny, g, g + params.Nx, g};
+  realcells2 = {g + params.Ny, g, g + params.Nx, g};
+  extrapolate_vector_impl(params, ls, 6, prims1, prims2, false);
+  st.n_interfacial = 0;
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      double lsval = ls.get_sdf(i, j);
+      if (ls.is_interfacial_cell(i, j)) st.n_interfacial++;
+      if (lsval <= 0.0) {
+        if (ls.is_interfacial_cell(i, j)) st.newvelocities[i][j] = {prims1[i][j][1], prims1[i][j][2]};
+        double u_new = prims1[i][j][1], v_new = prims1[i][j][2], p_new = prims1[i][j][3];
+        double rho_new = eos::isentropic_extrapolation(eos.gamma2, eos.pinf2, prims2[i][j][0], prims2[i][j][3], p_new);
+        if (!(rho_new >= 0.0)) g_status |= GFM_ST_UNPHYSICAL;
+        prims2[i][j] = {rho_new, u_new, v_new, p_new};
+        realcells1.imin = std::min(realcells1.imin, i - 2);
+        realcells1.imax = std::max(realcells1.imax, i + 2);
+        realcells1.jmin = std::min(realcells1.jmin, j - 2);
+        realcells1.jmax = std::max(realcells1.jmax, j + 2);
+      } else {
+        if (ls.is_interfacial_cell(i, j)) st.newvelocities[i][j] = {prims2[i][j][1], prims2[i][j][2]};
+        double u_new = prims2[i][j][1], v_new = prims2[i][j][2], p_new = prims2[i][j][3];
+        double rho_new = eos::isentropic_extrapolation(eos.gamma1, eos.pinf1, prims1[i][j][0], prims1[i][j][3], p_new);
+        if (!(rho_new >= 0.0)) g_status |= GFM_ST_UNPHYSICAL;
+        prims1[i][j] = {rho_new, u_new, v_new, p_new};
+        realcells2.imin = std::min(realcells2.imin, i - 2);
+        realcells2.imax = std::max(realcells2.imax, i + 2);
+        realcells2.jmin = std::min(realcells2.jmin, j - 2);
+        realcells2.jmax = std::max(realcells2.jmax, j + 2);
+      }
+    }
+  realcells1.imin = std::max(realcells1.imin, g);
+  realcells1.imax = std::min(realcells1.imax, g + params.Ny);
+  realcells1.jmin = std::max(realcells1.jmin, g);
+  realcells1.jmax = std::min(realcells1.jmax, g + params.Nx);
+  realcells2.imin = std::max(realcells2.imin, g);
+  realcells2.imax = std::min(realcells2.imax, g + params.Ny);
+  realcells2.jmin = std::max(realcells2.jmin, g);
+  realcells2.jmax = std::min(realcells2.jmax, g + params.Nx);
+  gfm_back_to_conserved(params, eos, prims1, prims2, grid1, grid2);
+  if (m.use_extension_vfield)
+    extrapolate_extension_vfield(params, ls, 20, st.newvelocities);
+  else
+    real_fluid_velocities(params, ls, prims1, prims2, st.newvelocities);
+}
+
+// ----------------------------------------------------------------------------
+// compute_dt (sourcecode/sim_twofluid.cpp:108-157, sim_onefluid.cpp:68-91)
+// ----------------------------------------------------------------------------
+double compute_dt_twofluid(double CFL, const sim_info& params, const grideuler2type& grid1,
+                           const grideuler2type& grid2, const Levelset& ls, const binarySGparams& eos, double T,
+                           double t) {
+  double maxu = 0.0, maxv = 0.0;
+  for (int i = params.numGC; i < params.Ny + params.numGC; i++)
+    for (int j = params.numGC; j < params.Nx + params.numGC; j++) {
+      double phi = ls.get_sdf(i, j);
+      const vec4type& U = (phi < 0.0) ? grid1[i][j] : grid2[i][j];
+      double gamma = (phi < 0.0) ? eos.gamma1 : eos.gamma2;
+      double pinf = (phi < 0.0) ? eos.pinf1 : eos.pinf2;
+      double rho = U[0];
+      double e = misc::specific_ie(U);
+      double p = eos::pressure(gamma, pinf, e, rho);
+      double c = eos::soundspeed(gamma, pinf, p, rho);
+      maxu = std::max(maxu, std::fabs(U[1]) / rho + c);
+      maxv = std::max(maxv, std::fabs(U[2]) / rho + c);
+    }
+  double dt = CFL * std::min(params.dx / maxu, params.dy / maxv);
+  if (t + dt > T) dt = T - t;
+  if (!(dt > 0.0)) g_status |= GFM_ST_DT_NONPOSITIVE;
+  return dt;
+}
+
+double compute_dt_onefluid(double CFL, const sim_info& params, const grideuler2type& grid, const binarySGparams& eos,
+                           double T, double t) {
+  double maxu = 0.0, maxv = 0.0;
+  for (int i = params.numGC; i < params.Ny + params.numGC; i++)
+    for (int j = params.numGC; j < params.Nx + params.numGC; j++) {
+      double rho = grid[i][j][0];
+      double e = misc::specific_ie(grid[i][j]);
+      double p = eos::pressure(eos.gamma1, eos.pinf1, e, rho);
+      double c = eos::soundspeed(eos.gamma1, eos.pinf1, p, rho);
+      maxu = std::max(maxu, std::fabs(grid[i][j][1]) / rho + c);
+      maxv = std::max(maxv, std::fabs(grid[i][j][2]) / rho + c);
+    }
+  double dt = CFL * std::min(params.dx / maxu, params.dy / maxv);
+  if (t + dt > T) dt = T - t;
+  return dt;
+}
+
+// SoA planes <-> nested grid
+grideuler2type from_soa(const sim_info& p, const double* U) {
+  const int nr = p.Ny + 2 * p.numGC, nc = p.Nx + 2 * p.numGC;
+  const size_t plane = static_cast<size_t>(nr) * nc;
+  grideuler2type g(nr, std::vector<vec4type>(nc));
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++)
+      for (int k = 0; k < 4; k++) g[i][j][k] = U[k * plane + static_cast<size_t>(i) * nc + j];
+  return g;
+}
+void to_soa(const sim_info& p, const grideuler2type& g, double* U) {
+  const int nr = p.Ny + 2 * p.numGC, nc = p.Nx + 2 * p.numGC;
+  const size_t plane = static_cast<size_t>(nr) * nc;
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++)
+      for (int k = 0; k < 4; k++) U[k * plane + static_cast<size_t>(i) * nc + j] = g[i][j][k];
+}
+griddoubletype phi_from(const sim_info& p, const double* f) {
+  const int nr = p.Ny + 2 * p.numGC, nc = p.Nx + 2 * p.numGC;
+  griddoubletype g(nr, std::vector<double>(nc));
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) g[i][j] = f[static_cast<size_t>(i) * nc + j];
+  return g;
+}
+void phi_to(const sim_info& p, const griddoubletype& g, double* f) {
+  const int nr = p.Ny + 2 * p.numGC, nc = p.Nx + 2 * p.numGC;
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) f[static_cast<size_t>(i) * nc + j] = g[i][j];
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI of the oracle (loaded with ctypes by the tests)
+// ============================================================================
+extern "C" {
+
+uint32_t oracle_status(void) { return g_status; }
+void oracle_clear_status(void) { g_status = 0; g_newton_iters = 0; }
+int64_t oracle_newton_iters(void) { return g_newton_iters; }
+
+double oracle_exp(double x) { return omath::exp(x); }
+double oracle_log(double x) { return omath::log(x); }
+double oracle_pow(double x, double y) { return omath::pow(x, y); }
+double oracle_acos(double x) { return omath::acos(x); }
+
+void oracle_rs_pure_batch(int n, int paralleltox, double gamma, double pinf, const double* UL, const double* UR,
+                          double* flux) {
+  for (int k = 0; k < n; k++) {
+    vec4type L = {UL[4 * k], UL[4 * k + 1], UL[4 * k + 2], UL[4 * k + 3]};
+    vec4type R = {UR[4 * k], UR[4 * k + 1], UR[4 * k + 2], UR[4 * k + 3]};
+    vec4type f;
+    pure_RS_solve_RP(paralleltox != 0, gamma, pinf, L, R, f);
+    for (int c = 0; c < 4; c++) flux[4 * k + c] = f[c];
+  }
+}
+
+void oracle_rs_mixed_batch(int n, double gL, double pinfL, double gR, double pinfR, const double* UL,
+                           const double* UR, double* out) {
+  for (int k = 0; k < n; k++) {
+    vec4type L = {UL[4 * k], UL[4 * k + 1], UL[4 * k + 2], UL[4 * k + 3]};
+    vec4type R = {UR[4 * k], UR[4 * k + 1], UR[4 * k + 2], UR[4 * k + 3]};
+    mixed_RS_solve(gL, pinfL, gR, pinfR, L, R, out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+  }
+}
+
+// One-fluid run (sim_onefluid::run_sim loop, sourcecode/sim_onefluid.cpp:40-54):
+// advances U (SoA planes) by nsteps steps or until t >= T.  t and numsteps are
+// in/out.  Returns the number of steps taken.
+int oracle_onefluid_run(const gfm_grid_desc* d, const gfm_method_desc* m, double* U, int nsteps, double* t,
+                        int* numsteps) {
+  sim_info params = make_params(d);
+  binarySGparams eos = {d->gamma1, d->pinf1, d->gamma2, d->pinf2};
+  grideuler2type grid = from_soa(params, U);
+  grideuler2type future_grid = grid;
+  BBrange realcells = {params.numGC, params.Ny + params.numGC, params.numGC, params.Nx + params.numGC};
+  int taken = 0;
+  while (*t < m->T && taken < nsteps) {
+    double CFL = (*numsteps < 5) ? std::min(m->CFL, 0.2) : m->CFL;
+    double dt = compute_dt_onefluid(CFL, params, grid, eos, m->T, *t);
+    FS_update(m->fs, params, eos.gamma1, eos.pinf1, dt, realcells, grid, future_grid);
+    apply_BCs_euler(params, grid);
+    (*numsteps)++;
+    *t += dt;
+    taken++;
+  }
+  to_soa(params, grid, U);
+  return taken;
+}
+
+// Two-fluid run (sim_twofluid::run_sim loop, sourcecode/sim_twofluid.cpp:64-88).
+// U1, U2: SoA planes; phi: one plane; vel (optional, 2 planes): the velocity
+// field of the last ghost fill.  Returns the number of steps taken.
+int oracle_twofluid_run(const gfm_grid_desc* d, const gfm_method_desc* m, double* U1, double* U2, double* phi,
+                        int nsteps, double* t, int* numsteps, double* vel, int64_t* n_interfacial) {
+  sim_info params = make_params(d);
+  binarySGparams eos = {d->gamma1, d->pinf1, d->gamma2, d->pinf2};
+  grideuler2type grid1 = from_soa(params, U1), grid2 = from_soa(params, U2);
+  grideuler2type future_grid1 = grid1, future_grid2 = grid2;
+  Levelset ls;
+  ls.params = params;
+  ls.phi = phi_from(params, phi);
+  ls.order = m->ls_order;
+  ls.reinit_every = m->reinit_every;
+  ls.reinit_iters = m->reinit_iters;
+  ls.updates = *numsteps;
+  const int g = params.numGC;
+  GFMState st;
+  int taken = 0;
+  while (*t < m->T && taken < nsteps) {
+    BBrange realcells1 = {g, params.Ny + g, g, params.Nx + g};
+    BBrange realcells2 = realcells1;
+    double CFL = (*numsteps < 5) ? std::min(m->CFL, 0.2) : m->CFL;
+    double dt = compute_dt_twofluid(CFL, params, grid1, grid2, ls, eos, m->T, *t);
+    switch (m->gfm) {
+      case GFM_RIEMANN: GFM_riemann_set_ghost_states(params, ls, eos, *m, grid1, grid2, st); break;
+      case GFM_REAL: GFM_real_set_ghost_states(params, ls, eos, *m, grid1, grid2, st); break;
+      case GFM_MODIFIED: GFM_modified_set_ghost_states(params, ls, eos, *m, grid1, grid2, st); break;
+      default:
+        GFM_original_set_ghost_states(params, ls, eos, *m, grid1, grid2, realcells1, realcells2, st);
+        break;
+    }
+    FS_update(m->fs, params, eos.gamma1, eos.pinf1, dt, realcells1, grid1, future_grid1);
+    FS_update(m->fs, params, eos.gamma2, eos.pinf2, dt, realcells2, grid2, future_grid2);
+    ls.update_interface_coupled(st.newvelocities, dt);
+    apply_BCs_euler(params, grid1);
+    apply_BCs_euler(params, grid2);
+    (*numsteps)++;
+    *t += dt;
+    taken++;
+  }
+  to_soa(params, grid1, U1);
+  to_soa(params, grid2, U2);
+  phi_to(params, ls.phi, phi);
+  if (vel && !st.newvelocities.empty()) {
+    const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+    const size_t plane = static_cast<size_t>(nr) * nc;
+    for (int i = 0; i < nr; i++)
+      for (int j = 0; j < nc; j++) {
+        vel[static_cast<size_t>(i) * nc + j] = st.newvelocities[i][j][0];
+        vel[plane + static_cast<size_t>(i) * nc + j] = st.newvelocities[i][j][1];
+      }
+  }
+  if (n_interfacial) *n_interfacial = st.n_interfacial;
+  return taken;
+}
+
+// Interfacial-cell mask of phi (Levelset::is_interfacial_cell over real cells).
+void oracle_interfacial_mask(const gfm_grid_desc* d, const double* phi, uint8_t* mask) {
+  sim_info params = make_params(d);
+  Levelset ls;
+  ls.params = params;
+  ls.phi = phi_from(params, phi);
+  const int g = params.numGC, nc = params.Nx + 2 * g;
+  for (int i = 0; i < params.Ny + 2 * g; i++)
+    for (int j = 0; j < nc; j++) {
+      bool inner = i >= g && i < params.Ny + g && j >= g && j < params.Nx + g;
+      mask[static_cast<size_t>(i) * nc + j] = inner && ls.is_interfacial_cell(i, j) ? 1 : 0;
+    }
+}
+
+double oracle_fluid_mass(const gfm_grid_desc* d, double interiorsign, const double* U, const double* phi) {
+  sim_info params = make_params(d);
+  const int g = params.numGC, nc = params.Nx + 2 * g;
+  double total = 0.0;
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      double lsval = phi[static_cast<size_t>(i) * nc + j];
+      if (interiorsign * lsval > 0.0) total += U[static_cast<size_t>(i) * nc + j] * params.dx * params.dy;
+    }
+  return total;
+}
+
+}  // extern "C"

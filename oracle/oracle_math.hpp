@@ -1,0 +1,271 @@
+// TEST INFRASTRUCTURE -- part of the CPU oracle.  Only tests/, the smoke check
+// and bench.py's cpu_baseline leg may load it.
+//
+// Scalar arithmetic of the oracle, written independently of the CUDA kernels
+// from the same specification (same operations in the same order, so a
+// -ffp-contract=off build agrees bit for bit with --fmad=false kernels):
+//   * Tang's table-driven exp and log (ACM TOMS 15(2) 1989, 16(4) 1990), pow
+//     as exp(y log x), and acos by the asin Taylor series with half-angle
+//     reduction.  The table data come from the generated gfm_tables.h.
+//   * the stiffened-gas EOS that the reference takes from its absent
+//     PhD-Common dependency (call sites headers/euler_misc.hpp:46,59,77,96).
+//   * exact_rs_stiffenedgas, the absent exact solver called at
+//     sourcecode/pure_RS_exact.cpp:29-45 and sourcecode/mixed_RS_exact.cpp:33-47,
+//     restated from Toro, "Riemann Solvers and Numerical Methods for Fluid
+//     Dynamics", ch. 4 (STARPU, PREFUN, SAMPLE) with p -> p + p_inf.
+// Parity with the reference is unpinned for these parts: the reference's own
+// implementations are not in its repository.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include "../phd-2d-gfm_gb300/csrc/gfm_tables.h"
+
+namespace omath {
+
+static const double EXP2T[64] = GFM_EXP2_TABLE;
+static const double LOGFT[97] = GFM_LOGF_TABLE;
+static const double INVFT[97] = GFM_INVF_TABLE;
+static const double ASINC[28] = GFM_ASIN_COEFFS;
+
+inline int64_t bits_of(double x) { int64_t b; std::memcpy(&b, &x, 8); return b; }
+inline double double_of(int64_t b) { double x; std::memcpy(&x, &b, 8); return x; }
+
+inline double exp(double x) {
+  if (std::isnan(x)) return x;
+  if (x > 709.78) return HUGE_VAL;
+  if (x < -745.2) return 0.0;
+  const double kd = std::rint(x * GFM_INV_LN2_64);
+  const int k = static_cast<int>(kd);
+  const double r = (x - kd * GFM_LN2_64_HI) - kd * GFM_LN2_64_LO;
+  const int j = k & 63;
+  const int m = (k - j) / 64;
+  // expm1(r) to degree 6: r + r^2 (1/2 + r (1/6 + r (1/24 + r (1/120 + r/720))))
+  const double c6 = 0x1.6c16c16c16c17p-10, c5 = 0x1.1111111111111p-7, c4 = 0x1.5555555555555p-5,
+               c3 = 0x1.5555555555555p-3;
+  const double q = r + (r * r) * (0.5 + r * (c3 + r * (c4 + r * (c5 + r * c6))));
+  double y = EXP2T[j] + EXP2T[j] * q;
+  if (m < -1020) {
+    y = y * double_of(static_cast<int64_t>(m + 1023 + 200) << 52);
+    return y * double_of(static_cast<int64_t>(1023 - 200) << 52);
+  }
+  return y * double_of(static_cast<int64_t>(m + 1023) << 52);
+}
+
+inline double log(double x) {
+  if (!(x > 0.0)) return (x == 0.0) ? -HUGE_VAL : std::nan("");
+  if (std::isinf(x)) return x;
+  int64_t b = bits_of(x);
+  int expo = static_cast<int>((b >> 52) & 0x7ff);
+  if (expo == 0) {
+    x = x * 0x1p54;
+    b = bits_of(x);
+    expo = static_cast<int>((b >> 52) & 0x7ff) - 54;
+  }
+  expo -= 1023;
+  double mant = double_of((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  if (mant >= 1.5) {  // mantissa in [0.75, 1.5): no cancellation near x = 1
+    mant = mant * 0.5;
+    expo += 1;
+  }
+  const double jd = std::rint((mant - 1.0) * 128.0);
+  const double F = 1.0 + jd * 0x1p-7;
+  const double r = (mant - F) * INVFT[static_cast<int>(jd) + 32];
+  // log1p(r) - r to degree 7
+  const double c3 = 0x1.5555555555555p-2, c5 = 0x1.999999999999ap-3, c6 = -0x1.5555555555555p-3,
+               c7 = 0x1.2492492492492p-3;
+  const double poly = (r * r) * (-0.5 + r * (c3 + r * (-0.25 + r * (c5 + r * (c6 + r * c7)))));
+  const double e = static_cast<double>(expo);
+  const double hi = e * GFM_LN2_HI + LOGFT[static_cast<int>(jd) + 32];
+  const double lo = e * GFM_LN2_LO + poly;
+  return hi + (r + lo);
+}
+
+inline double pow(double x, double y) {
+  if (x == 0.0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : HUGE_VAL);
+  return omath::exp(y * omath::log(x));
+}
+
+inline double asin_series(double x) {
+  const double s = x * x;
+  double acc = ASINC[27];
+  for (int n = 26; n >= 1; n--) acc = ASINC[n] + s * acc;
+  return x + x * (s * acc);
+}
+
+inline double acos(double x) {
+  if (x > 0.5) return 2.0 * asin_series(std::sqrt((1.0 - x) * 0.5));
+  if (x < -0.5) return GFM_PI - 2.0 * asin_series(std::sqrt((1.0 + x) * 0.5));
+  return GFM_PI_2 - asin_series(x);
+}
+
+}  // namespace omath
+
+// Stiffened-gas equation of state, p = (gamma - 1) rho e - gamma pinf.
+namespace eos {
+inline double pressure(double gamma, double pinf, double e, double rho) {
+  return (gamma - 1.0) * rho * e - gamma * pinf;
+}
+inline double specific_ie(double gamma, double pinf, double p, double rho) {
+  return (p + gamma * pinf) / ((gamma - 1.0) * rho);
+}
+inline double soundspeed(double gamma, double pinf, double p, double rho) {
+  return std::sqrt(gamma * (p + pinf) / rho);
+}
+inline double isentropic_extrapolation(double gamma, double pinf, double rho1, double p1, double p2) {
+  return rho1 * omath::pow((p2 + pinf) / (p1 + pinf), 1.0 / gamma);
+}
+}  // namespace eos
+
+// The exact stiffened-gas Riemann solver with the interface the reference
+// uses: constructor (gammaL, gammaR, pinfL, pinfR), solve_RP(L, R) with
+// 1D primitive states (rho, u, p), members P_STAR, S_STAR, rho_star_L,
+// rho_star_R, and sample_solution(L, R, S).
+//
+// Operation order (shared with the kernels): gamma constants
+// G1 = (g-1)/(2g), G2 = (g+1)/(2g), G3 = 2g/(g-1), G4 = 2/(g-1), G5 = 2/(g+1),
+// G6 = (g-1)/(g+1), G7 = (g-1)/2, IG = 1/g; per side pb = p + pinf,
+// c = sqrt(g pb / rho), A = G5/rho, B = G6 pb, 1/pb, G4 c, 1/(rho c);
+// Newton stops when 2|p - p_old| <= 1e-12 (p + p_old + 2 min(pinf)).
+class exact_rs_stiffenedgas {
+ public:
+  struct Gas {
+    double g, pinf, G1, G2, G3, G4, G5, G6, G7, IG;
+    Gas(double gamma, double pinf_) : g(gamma), pinf(pinf_) {
+      G1 = (g - 1.0) / (2.0 * g);
+      G2 = (g + 1.0) / (2.0 * g);
+      G3 = 2.0 * g / (g - 1.0);
+      G4 = 2.0 / (g - 1.0);
+      G5 = 2.0 / (g + 1.0);
+      G6 = (g - 1.0) / (g + 1.0);
+      G7 = (g - 1.0) / 2.0;
+      IG = 1.0 / g;
+    }
+  };
+  struct Side {
+    double rho, u, p, pb, c, A, B, ipb, G4c, irc;
+    Side(const double W[3], const Gas& k) : rho(W[0]), u(W[1]), p(W[2]) {
+      pb = p + k.pinf;
+      c = std::sqrt(k.g * pb / rho);
+      A = k.G5 / rho;
+      B = k.G6 * pb;
+      ipb = 1.0 / pb;
+      G4c = k.G4 * c;
+      irc = 1.0 / (rho * c);
+    }
+  };
+
+  Gas KL, KR;
+  double P_STAR = 0.0, S_STAR = 0.0, rho_star_L = 0.0, rho_star_R = 0.0;
+  int iterations = 0;
+  bool vacuum = false, converged = true;
+
+  exact_rs_stiffenedgas(double gammaL, double gammaR, double pinf_L, double pinf_R)
+      : KL(gammaL, pinf_L), KR(gammaR, pinf_R) {}
+
+  static const int MAXIT = 60;
+
+  // Toro's PREFUN for one side.
+  static void prefun(double p, const Side& K, const Gas& k, double& f, double& fd) {
+    const double pb = p + k.pinf;
+    if (p > K.p) {
+      const double r = 1.0 / (pb + K.B);
+      const double qrt = std::sqrt(K.A * r);
+      f = (p - K.p) * qrt;
+      fd = (1.0 - 0.5 * ((p - K.p) * r)) * qrt;
+    } else {
+      const double prat = pb * K.ipb;
+      const double pw = omath::pow(prat, k.G1);
+      f = K.G4c * (pw - 1.0);
+      fd = K.irc * (pw / prat);
+    }
+  }
+
+  static double star_density(double pstar, const Side& K, const Gas& k) {
+    const double pr = (pstar + k.pinf) * K.ipb;
+    if (pstar > K.p) return K.rho * ((pr + k.G6) / (pr * k.G6 + 1.0));
+    return K.rho * omath::pow(pr, k.IG);
+  }
+
+  void solve_RP(const double L[3], const double R[3]) {
+    const Side SL(L, KL), SR(R, KR);
+    vacuum = false;
+    converged = true;
+    if (SL.u == SR.u && SL.p == SR.p) {
+      // No pressure or velocity jump: a contact at most.
+      P_STAR = SL.p;
+      S_STAR = SL.u;
+      iterations = 0;
+    } else {
+      const double udiff = SR.u - SL.u;
+      if (SL.G4c + SR.G4c <= udiff) vacuum = true;
+      const double pinfmin = KL.pinf < KR.pinf ? KL.pinf : KR.pinf;
+      const double pbmin = SL.pb < SR.pb ? SL.pb : SR.pb;
+      const double pfloor = 1e-6 * pbmin - pinfmin;
+      // PVRS initial guess (Toro eq. 4.47)
+      const double ppv = 0.5 * (SL.p + SR.p) - 0.125 * (SR.u - SL.u) * (SL.rho + SR.rho) * (SL.c + SR.c);
+      double pold = ppv > pfloor ? ppv : pfloor;
+      double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0, p = pold;
+      int it = 0;
+      while (true) {
+        prefun(pold, SL, KL, fL, fLd);
+        prefun(pold, SR, KR, fR, fRd);
+        p = pold - (fL + fR + udiff) / (fLd + fRd);
+        if (p < pfloor) p = pfloor;
+        it++;
+        const bool conv = 2.0 * std::fabs(p - pold) <= 1e-12 * (p + pold + 2.0 * pinfmin);
+        pold = p;
+        if (conv) break;
+        if (it >= MAXIT) { converged = false; break; }
+      }
+      P_STAR = p;
+      S_STAR = 0.5 * (SL.u + SR.u + fR - fL);
+      iterations = it;
+    }
+    rho_star_L = star_density(P_STAR, SL, KL);
+    rho_star_R = star_density(P_STAR, SR, KR);
+  }
+
+  // Toro's SAMPLE at wave speed S = x/t, after solve_RP.
+  void sample_solution(const double L[3], const double R[3], double S, double out[3]) const {
+    const Side SL(L, KL), SR(R, KR);
+    if (S <= S_STAR) {
+      if (P_STAR <= SL.p) {
+        const double shl = SL.u - SL.c;
+        if (S <= shl) { out[0] = SL.rho; out[1] = SL.u; out[2] = SL.p; return; }
+        const double cml = SL.c * omath::pow((P_STAR + KL.pinf) * SL.ipb, KL.G1);
+        const double stl = S_STAR - cml;
+        if (S > stl) { out[0] = rho_star_L; out[1] = S_STAR; out[2] = P_STAR; return; }
+        const double c = KL.G5 * (SL.c + KL.G7 * (SL.u - S));
+        const double cr = c / SL.c;
+        out[0] = SL.rho * omath::pow(cr, KL.G4);
+        out[1] = KL.G5 * (SL.c + KL.G7 * SL.u + S);
+        out[2] = SL.pb * omath::pow(cr, KL.G3) - KL.pinf;
+        return;
+      }
+      const double pml = (P_STAR + KL.pinf) * SL.ipb;
+      const double sl = SL.u - SL.c * std::sqrt(KL.G2 * pml + KL.G1);
+      if (S <= sl) { out[0] = SL.rho; out[1] = SL.u; out[2] = SL.p; return; }
+      out[0] = rho_star_L; out[1] = S_STAR; out[2] = P_STAR;
+      return;
+    }
+    if (P_STAR > SR.p) {
+      const double pmr = (P_STAR + KR.pinf) * SR.ipb;
+      const double sr = SR.u + SR.c * std::sqrt(KR.G2 * pmr + KR.G1);
+      if (S >= sr) { out[0] = SR.rho; out[1] = SR.u; out[2] = SR.p; return; }
+      out[0] = rho_star_R; out[1] = S_STAR; out[2] = P_STAR;
+      return;
+    }
+    const double shr = SR.u + SR.c;
+    if (S >= shr) { out[0] = SR.rho; out[1] = SR.u; out[2] = SR.p; return; }
+    const double cmr = SR.c * omath::pow((P_STAR + KR.pinf) * SR.ipb, KR.G1);
+    const double str = S_STAR + cmr;
+    if (S <= str) { out[0] = rho_star_R; out[1] = S_STAR; out[2] = P_STAR; return; }
+    const double c = KR.G5 * (SR.c - KR.G7 * (SR.u - S));
+    const double cr = c / SR.c;
+    out[0] = SR.rho * omath::pow(cr, KR.G4);
+    out[1] = KR.G5 * (-SR.c + KR.G7 * SR.u + S);
+    out[2] = SR.pb * omath::pow(cr, KR.G3) - KR.pinf;
+  }
+};

@@ -1,0 +1,395 @@
+// C ABI of the library (include/gfm_gb300.h): context lifetime, host <-> device
+// copies, the time-loop body, batched Riemann solves, status and statistics.
+#include "gfm_internal.cuh"
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+namespace gfm {
+void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter);
+void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m);
+void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out);
+}  // namespace gfm
+
+using namespace gfm;
+
+namespace {
+
+struct CtxExtra {
+  unsigned int* counters;   // [0] CFL last-block counter, [1] interface ticket
+  double* mass_part;        // 256 partial sums + 1 result
+};
+
+// the extra buffers live right after the context allocation
+CtxExtra& extra(gfm_ctx* ctx) { return *reinterpret_cast<CtxExtra*>(ctx + 1); }
+
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t e_ = (x);                       \
+    if (e_ != cudaSuccess) {                    \
+      fprintf(stderr, "gfm: %s failed: %s\n", #x, cudaGetErrorString(e_)); \
+      return GFM_ERR_CUDA;                      \
+    }                                           \
+  } while (0)
+
+bool valid_bc(int b) { return b == GFM_BC_TRANSMISSIVE || b == GFM_BC_REFLECTIVE || b == GFM_BC_PERIODIC; }
+
+gfm_status_t check_method(const gfm_ctx* ctx, const gfm_method_desc* m) {
+  if (!m) return GFM_ERR_ARG;
+  if (m->fs != GFM_FS_GODUNOV && m->fs != GFM_FS_MUSCL) return GFM_ERR_ARG;
+  if (ctx->two_fluid) {
+    if (m->gfm < GFM_OGFM || m->gfm > GFM_MODIFIED) return GFM_ERR_ARG;
+    if (m->ls_order != 1 && m->ls_order != 5) return GFM_ERR_ARG;
+    if (m->reinit_every < 0 || m->reinit_iters < 0) return GFM_ERR_ARG;
+  }
+  if (!(m->CFL > 0.0)) return GFM_ERR_ARG;
+  return GFM_OK;
+}
+
+gfm_status_t last_error() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gfm: kernel launch failed: %s\n", cudaGetErrorString(e));
+    return GFM_ERR_CUDA;
+  }
+  return GFM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gfm_version(void) { return "gfm_gb300 1.0 (sm_103a, FP64)"; }
+
+gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out) {
+  if (!d || !out) return GFM_ERR_ARG;
+  *out = nullptr;
+  if (d->Nx < 1 || d->Ny < 1 || d->numGC < 2 || d->numGC > 64) return GFM_ERR_ARG;
+  if (d->Nx < d->numGC || d->Ny < d->numGC) return GFM_ERR_ARG;   // BC sources must be real cells
+  if (two_fluid && d->numGC < 4) return GFM_ERR_ARG;                 // HOUC5 stencil reach 3 (+1 gradient)
+  if (!(d->dx > 0.0) || !(d->dy > 0.0)) return GFM_ERR_ARG;
+  if (!valid_bc(d->BC_L) || !valid_bc(d->BC_R) || !valid_bc(d->BC_B) || !valid_bc(d->BC_T)) return GFM_ERR_ARG;
+  bool periodic = d->BC_L == GFM_BC_PERIODIC && d->BC_R == GFM_BC_PERIODIC && d->BC_B == GFM_BC_PERIODIC &&
+                  d->BC_T == GFM_BC_PERIODIC;
+  bool anyper = d->BC_L == GFM_BC_PERIODIC || d->BC_R == GFM_BC_PERIODIC || d->BC_B == GFM_BC_PERIODIC ||
+                d->BC_T == GFM_BC_PERIODIC;
+  if (anyper && !periodic) return GFM_ERR_UNSUPPORTED;   // the reference has no mixed periodic case
+  if (periodic && d->Nx != d->Ny) return GFM_ERR_UNSUPPORTED;   // its periodic loop is defined for Nx == Ny
+  if (!(d->gamma1 > 1.0) || (two_fluid && !(d->gamma2 > 1.0))) return GFM_ERR_ARG;
+
+  void* mem = calloc(1, sizeof(gfm_ctx) + sizeof(CtxExtra));
+  if (!mem) return GFM_ERR_ARG;
+  gfm_ctx* ctx = static_cast<gfm_ctx*>(mem);
+  GridP& P = ctx->P;
+  P.Nx = d->Nx; P.Ny = d->Ny; P.g = d->numGC;
+  P.nr = P.Ny + 2 * P.g; P.nc = P.Nx + 2 * P.g;
+  P.pitch = (P.nc + 31) / 32 * 32;
+  P.plane = (int64_t)P.nr * P.pitch;
+  P.x0 = d->x0; P.y0 = d->y0; P.dx = d->dx; P.dy = d->dy;
+  P.bcL = d->BC_L; P.bcR = d->BC_R; P.bcB = d->BC_B; P.bcT = d->BC_T;
+  P.g1 = d->gamma1; P.p1 = d->pinf1;
+  P.g2 = two_fluid ? d->gamma2 : d->gamma1;
+  P.p2 = two_fluid ? d->pinf2 : d->pinf1;
+  P.gas1 = make_gas(P.g1, P.p1);
+  P.gas2 = make_gas(P.g2, P.p2);
+  P.periodic = periodic;
+  ctx->two_fluid = two_fluid ? 1 : 0;
+  ctx->stream = 0;
+
+  size_t plane_b = sizeof(double) * (size_t)P.plane;
+  int nf = ctx->two_fluid ? 2 : 1;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t b) {
+    if (e == cudaSuccess) e = cudaMalloc(p, b);
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, b);
+  };
+  for (int f = 0; f < nf; f++) {
+    alloc((void**)&ctx->U[f], 4 * plane_b);
+    alloc((void**)&ctx->Unew[f], 4 * plane_b);
+  }
+  alloc((void**)&ctx->dtime, sizeof(DevTime));
+  CtxExtra& X = extra(ctx);
+  alloc((void**)&X.counters, 64);
+  alloc((void**)&X.mass_part, sizeof(double) * 260);
+  if (ctx->two_fluid) {
+    for (int f = 0; f < 2; f++) {
+      alloc((void**)&ctx->W[f], 4 * plane_b);
+      alloc((void**)&ctx->Wt[f], 4 * plane_b);
+      alloc((void**)&ctx->Wc[f], 4 * plane_b);
+    }
+    alloc((void**)&ctx->phi, plane_b);
+    alloc((void**)&ctx->phi_a, plane_b);
+    alloc((void**)&ctx->phi_b, plane_b);
+    alloc((void**)&ctx->phi0, plane_b);
+    alloc((void**)&ctx->nrm, 2 * plane_b);
+    alloc((void**)&ctx->vel, 2 * plane_b);
+    alloc((void**)&ctx->vel_t, 2 * plane_b);
+    alloc((void**)&ctx->mask, (size_t)P.plane);
+    alloc((void**)&ctx->ifc_map, sizeof(int) * (size_t)P.plane);
+    size_t cap = (size_t)P.Nx * P.Ny;
+    alloc((void**)&ctx->ifc_list, sizeof(int) * cap);
+    alloc((void**)&ctx->ifc_done, sizeof(int) * cap);
+    alloc((void**)&ctx->ifc_out, sizeof(double) * 8 * cap);
+    ctx->n_chunks = (int)(((int64_t)P.nr * P.nc + 2047) / 2048);
+    alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)ctx->n_chunks);
+  }
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_dtime, sizeof(DevTime));
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gfm: allocation failed: %s\n", cudaGetErrorString(e));
+    gfm_ctx_destroy(ctx);
+    return GFM_ERR_CUDA;
+  }
+  memset(ctx->h_dtime, 0, sizeof(DevTime));
+  *out = ctx;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
+  if (!ctx) return GFM_OK;
+  cudaStreamSynchronize(ctx->stream);
+  for (int f = 0; f < 2; f++) {
+    cudaFree(ctx->U[f]); cudaFree(ctx->Unew[f]);
+    cudaFree(ctx->W[f]); cudaFree(ctx->Wt[f]); cudaFree(ctx->Wc[f]);
+  }
+  cudaFree(ctx->phi); cudaFree(ctx->phi_a); cudaFree(ctx->phi_b); cudaFree(ctx->phi0);
+  cudaFree(ctx->nrm); cudaFree(ctx->vel); cudaFree(ctx->vel_t);
+  cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
+  cudaFree(ctx->ifc_out); cudaFree(ctx->chunk_count);
+  cudaFree(ctx->dtime);
+  cudaFree(extra(ctx).counters);
+  cudaFree(extra(ctx).mass_part);
+  if (ctx->h_dtime) cudaFreeHost(ctx->h_dtime);
+  free(ctx);
+  return GFM_OK;
+}
+
+gfm_status_t gfm_set_stream(gfm_ctx* ctx, void* s) {
+  if (!ctx) return GFM_ERR_ARG;
+  ctx->stream = static_cast<cudaStream_t>(s);
+  return GFM_OK;
+}
+
+static gfm_status_t copy_grid(gfm_ctx* ctx, double* dev, const double* host_src, double* host_dst, int planes) {
+  const GridP& P = ctx->P;
+  size_t wb = sizeof(double) * (size_t)P.nc;
+  for (int k = 0; k < planes; k++) {
+    if (host_src)
+      CK(cudaMemcpy2DAsync(dev + k * P.plane, sizeof(double) * P.pitch, host_src + (size_t)k * P.nr * P.nc, wb, wb,
+                           P.nr, cudaMemcpyHostToDevice, ctx->stream));
+    else
+      CK(cudaMemcpy2DAsync(host_dst + (size_t)k * P.nr * P.nc, wb, dev + k * P.plane, sizeof(double) * P.pitch, wb,
+                           P.nr, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFM_OK;
+}
+
+gfm_status_t gfm_upload(gfm_ctx* ctx, int fluid, const double* U) {
+  if (!ctx || !U || fluid < 1 || fluid > (ctx->two_fluid ? 2 : 1)) return GFM_ERR_ARG;
+  return copy_grid(ctx, ctx->U[fluid - 1], U, nullptr, 4);
+}
+gfm_status_t gfm_download(gfm_ctx* ctx, int fluid, double* U) {
+  if (!ctx || !U || fluid < 1 || fluid > (ctx->two_fluid ? 2 : 1)) return GFM_ERR_ARG;
+  return copy_grid(ctx, ctx->U[fluid - 1], nullptr, U, 4);
+}
+gfm_status_t gfm_upload_phi(gfm_ctx* ctx, const double* phi) {
+  if (!ctx || !phi || !ctx->two_fluid) return GFM_ERR_ARG;
+  return copy_grid(ctx, ctx->phi, phi, nullptr, 1);
+}
+gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi) {
+  if (!ctx || !phi || !ctx->two_fluid) return GFM_ERR_ARG;
+  return copy_grid(ctx, ctx->phi, nullptr, phi, 1);
+}
+
+gfm_status_t gfm_download_mask(gfm_ctx* ctx, uint8_t* mask) {
+  if (!ctx || !mask || !ctx->two_fluid) return GFM_ERR_ARG;
+  const GridP& P = ctx->P;
+  CK(cudaMemcpy2DAsync(mask, (size_t)P.nc, ctx->mask, (size_t)P.pitch, (size_t)P.nc, P.nr, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFM_OK;
+}
+
+gfm_status_t gfm_set_time(gfm_ctx* ctx, double t, int numsteps) {
+  if (!ctx) return GFM_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost));
+  ctx->h_dtime->t = t;
+  ctx->h_dtime->numsteps = numsteps;
+  ctx->h_dtime->active = 0;
+  const GridP& P = ctx->P;
+  int full[4] = {P.g, P.g + P.Ny, P.g, P.g + P.Nx};
+  for (int f = 0; f < 2; f++)
+    for (int q = 0; q < 4; q++) ctx->h_dtime->rc[4 * f + q] = full[q];
+  CK(cudaMemcpy(ctx->dtime, ctx->h_dtime, sizeof(DevTime), cudaMemcpyHostToDevice));
+  ctx->steps_done_host = numsteps;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_get_time(gfm_ctx* ctx, double* t, int* numsteps, double* dt) {
+  if (!ctx) return GFM_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (t) *t = ctx->h_dtime->t;
+  if (numsteps) *numsteps = ctx->h_dtime->numsteps;
+  if (dt) *dt = ctx->h_dtime->dt;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_compute_dt(gfm_ctx* ctx, double CFL, double T) {
+  if (!ctx || !(CFL > 0.0)) return GFM_ERR_ARG;
+  launch_cfl_impl(ctx, CFL, T, false, extra(ctx).counters);
+  return last_error();
+}
+
+gfm_status_t gfm_set_ghost_states(gfm_ctx* ctx, const gfm_method_desc* m) {
+  if (!ctx || !ctx->two_fluid) return GFM_ERR_ARG;
+  gfm_status_t r = check_method(ctx, m);
+  if (r != GFM_OK) return r;
+  // the ticket of the interface solve
+  ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
+  launch_ghost_fill(ctx, m);
+  return last_error();
+}
+
+gfm_status_t gfm_fs_update(gfm_ctx* ctx, int fs, int fluid) {
+  if (!ctx || (fs != GFM_FS_GODUNOV && fs != GFM_FS_MUSCL)) return GFM_ERR_ARG;
+  if (fluid < 1 || fluid > (ctx->two_fluid ? 2 : 1)) return GFM_ERR_ARG;
+  launch_fs_update(ctx, fs, 1 << (fluid - 1));
+  return last_error();
+}
+
+gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
+  if (!ctx || !ctx->two_fluid) return GFM_ERR_ARG;
+  gfm_status_t r = check_method(ctx, m);
+  if (r != GFM_OK) return r;
+  launch_ls_update(ctx, m);
+  return last_error();
+}
+
+gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid) {
+  if (!ctx || fluid < 1 || fluid > (ctx->two_fluid ? 2 : 1)) return GFM_ERR_ARG;
+  launch_bcs(ctx, 1 << (fluid - 1));
+  return last_error();
+}
+
+gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps) {
+  if (!ctx || nsteps < 0) return GFM_ERR_ARG;
+  gfm_status_t r = check_method(ctx, m);
+  if (r != GFM_OK) return r;
+  ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
+  for (int s = 0; s < nsteps; s++) {
+    bool ogfm = ctx->two_fluid && m->gfm == GFM_OGFM;
+    launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
+    if (ctx->two_fluid) {
+      launch_ghost_fill(ctx, m);
+      launch_fs_update(ctx, m->fs, 3);
+      launch_ls_update(ctx, m);
+      int upd = ctx->steps_done_host + 1;
+      if (m->reinit_every > 0 && upd % m->reinit_every == 0 && m->reinit_iters > 0) launch_reinit(ctx, m);
+      launch_bcs(ctx, 3);
+    } else {
+      launch_fs_update(ctx, m->fs, 1);
+      launch_bcs(ctx, 1);
+    }
+    launch_end_step(ctx);
+    ctx->steps_done_host++;
+    r = last_error();
+    if (r != GFM_OK) return r;
+  }
+  return GFM_OK;
+}
+
+gfm_status_t gfm_get_device_status(gfm_ctx* ctx, uint32_t* status) {
+  if (!ctx || !status) return GFM_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *status = ctx->h_dtime->status;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_clear_device_status(gfm_ctx* ctx) {
+  if (!ctx) return GFM_ERR_ARG;
+  CK(cudaMemsetAsync(&ctx->dtime->status, 0, sizeof(uint32_t), ctx->stream));
+  return GFM_OK;
+}
+
+gfm_status_t gfm_get_stats(gfm_ctx* ctx, int64_t* n_interfacial, int64_t* n_rounds, int64_t* newton_iters) {
+  if (!ctx) return GFM_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (n_interfacial) *n_interfacial = ctx->h_dtime->n_ifc;
+  if (n_rounds) *n_rounds = ctx->h_dtime->n_rounds;
+  if (newton_iters) *newton_iters = (int64_t)ctx->h_dtime->newton_iters;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_fluid_mass(gfm_ctx* ctx, double interiorsign, double* mass) {
+  if (!ctx || !mass) return GFM_ERR_ARG;
+  double* part = extra(ctx).mass_part;
+  launch_mass(ctx, interiorsign, part, part + 256);
+  CK(cudaMemcpyAsync(mass, part + 256, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFM_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batched Riemann solves (unit tests and the pure/mixed solver classes)
+// ---------------------------------------------------------------------------
+namespace gfm {
+
+__global__ void k_rs_pure(int n, int xdir, Gas k, const double* UL, const double* UR, double* flux,
+                          uint32_t* status) {
+  uint32_t st = 0;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    V4 L = V4{UL[4 * q], UL[4 * q + 1], UL[4 * q + 2], UL[4 * q + 3]};
+    V4 R = V4{UR[4 * q], UR[4 * q + 1], UR[4 * q + 2], UR[4 * q + 3]};
+    int it = 0;
+    V4 f = pure_rs_flux(xdir != 0, k, L, R, &st, &it);
+    flux[4 * q] = f.a; flux[4 * q + 1] = f.b; flux[4 * q + 2] = f.c; flux[4 * q + 3] = f.d;
+  }
+  if (status && st) atomicOr(status, st);
+}
+
+__global__ void k_rs_mixed(int n, Gas kL, Gas kR, const double* UL, const double* UR, double* out,
+                           uint32_t* status) {
+  uint32_t st = 0;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    V4 L = V4{UL[4 * q], UL[4 * q + 1], UL[4 * q + 2], UL[4 * q + 3]};
+    V4 R = V4{UR[4 * q], UR[4 * q + 1], UR[4 * q + 2], UR[4 * q + 3]};
+    int it = 0;
+    MixedStar m = mixed_rs(kL, kR, L, R, &st, &it);
+    out[4 * q] = m.p_star; out[4 * q + 1] = m.u_star; out[4 * q + 2] = m.rho_star_L; out[4 * q + 3] = m.rho_star_R;
+  }
+  if (status && st) atomicOr(status, st);
+}
+
+}  // namespace gfm
+
+extern "C" {
+
+gfm_status_t gfm_rs_pure_batch(int n, int paralleltox, double gamma, double pinf, const double* UL, const double* UR,
+                               double* flux, uint32_t* status, void* stream) {
+  if (n < 0 || (n > 0 && (!UL || !UR || !flux)) || !(gamma > 1.0)) return GFM_ERR_ARG;
+  if (n == 0) return GFM_OK;
+  int blocks = (n + 127) / 128;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_rs_pure<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(n, paralleltox, make_gas(gamma, pinf), UL, UR,
+                                                                   flux, status);
+  return last_error();
+}
+
+gfm_status_t gfm_rs_mixed_batch(int n, double gammaL, double pinfL, double gammaR, double pinfR, const double* UL,
+                                const double* UR, double* out, uint32_t* status, void* stream) {
+  if (n < 0 || (n > 0 && (!UL || !UR || !out)) || !(gammaL > 1.0) || !(gammaR > 1.0)) return GFM_ERR_ARG;
+  if (n == 0) return GFM_OK;
+  int blocks = (n + 127) / 128;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_rs_mixed<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(n, make_gas(gammaL, pinfL),
+                                                                    make_gas(gammaR, pinfR), UL, UR, out, status);
+  return last_error();
+}
+
+}  // extern "C"

@@ -1,0 +1,253 @@
+// Fused flux update of one fluid over its realcells box:
+// FS_MUSCL::pure_fluid_update (sourcecode/FS_MUSCL.cpp:148-304) and
+// FS_godunov::pure_fluid_update (sourcecode/FS_godunov.cpp:5-50).
+//
+// One CTA owns a TX x TY tile of real cells.
+//   phase 1  conserved -> primitive once per cell of the tile + 2-cell halo,
+//            into shared memory (the reference converts each neighbour again
+//            for every face it touches; the values are identical).
+//   phase 2  per cell: minmod slopes, boundary-extrapolated values, the
+//            physicality fallback and the half-step evolution, giving the
+//            four evolved face states of the cell (shared memory).  The
+//            reference recomputes these per face (as cell C, L or B); each
+//            cell's values do not depend on which face asks for them.
+//   phase 3  per face: the second fallback, primitives -> conserved, and the
+//            exact Riemann flux (pure_RS_exact::solve_RP).
+//   phase 4  per cell: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn, the
+//            accumulation order of the reference's face loop (:290-292).
+#include "gfm_internal.cuh"
+
+namespace gfm {
+
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NT = 256;
+constexpr int WR = TY + 4;   // primitive region rows   (i0-2 .. i0+TY+1)
+constexpr int WC = TX + 4;   // primitive region columns (j0-2 .. j0+TX+1)
+constexpr int SR = TY + 2;   // face-state cells rows    (i0-1 .. i0+TY)
+constexpr int SC = TX + 2;   // face-state cells columns (j0-1 .. j0+TX)
+constexpr int NXF = TY * (TX + 1);
+constexpr int NYF = (TY + 1) * TX;
+
+struct FluxSmem {
+  double w[4][WR][WC];          // primitives (MUSCL) or conserved (Godunov)
+  double fs[4][4][SR][SC];      // [face L,R,B,T][component][r][c]
+  double fx[4][TY][TX + 1];
+  double fy[4][TY + 1][TX];
+};
+
+struct FluxArgs {
+  GridP P;
+  const double* U[2];
+  double* Unew[2];
+  const DevTime* dtime;
+  DevTime* dtime_w;
+  int fluid_base;
+};
+
+__device__ __forceinline__ V4 sW(const FluxSmem& s, int r, int c) {
+  return V4{s.w[0][r][c], s.w[1][r][c], s.w[2][r][c], s.w[3][r][c]};
+}
+__device__ __forceinline__ V4 sFS(const FluxSmem& s, int f, int r, int c) {
+  return V4{s.fs[f][0][r][c], s.fs[f][1][r][c], s.fs[f][2][r][c], s.fs[f][3][r][c]};
+}
+__device__ __forceinline__ void putFS(FluxSmem& s, int f, int r, int c, const V4& v) {
+  s.fs[f][0][r][c] = v.a; s.fs[f][1][r][c] = v.b; s.fs[f][2][r][c] = v.c; s.fs[f][3][r][c] = v.d;
+}
+__device__ __forceinline__ V4 v4sub(const V4& x, const V4& y) { return V4{x.a - y.a, x.b - y.b, x.c - y.c, x.d - y.d}; }
+
+// (s A(W)) d, quasilinear_form_A (headers/euler_misc.hpp:149-163), non-zero
+// terms; irho = 1/rho and rcc = rho c c are the matrix entries A(1,3), A(3,1).
+__device__ __forceinline__ V4 A_times(double s, const V4& W, double irho, double rcc, const V4& d) {
+  double su = s * W.b;
+  return V4{su * d.a + (s * W.a) * d.b, su * d.b + (s * irho) * d.d, su * d.c, (s * rcc) * d.b + su * d.d};
+}
+// (s B(W)) d, quasilinear_form_B (headers/euler_misc.hpp:166-180)
+__device__ __forceinline__ V4 B_times(double s, const V4& W, double irho, double rcc, const V4& d) {
+  double sv = s * W.c;
+  return V4{sv * d.a + (s * W.a) * d.c, sv * d.b, sv * d.c + (s * irho) * d.d, (s * rcc) * d.c + sv * d.d};
+}
+
+template <bool MUSCL>
+__global__ void __launch_bounds__(NT) k_flux_update(FluxArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FluxSmem& s = *reinterpret_cast<FluxSmem*>(smem_raw);
+  const GridP& P = a.P;
+  const int fluid = a.fluid_base + blockIdx.z;
+  const double* __restrict__ U = a.U[blockIdx.z];
+  double* __restrict__ Unew = a.Unew[blockIdx.z];
+  const Gas& gas = fluid == 0 ? P.gas1 : P.gas2;
+  const double gam = gas.g;
+  const double pinf = gas.pinf;
+  const int i0 = P.g + blockIdx.y * TY;
+  const int j0 = P.g + blockIdx.x * TX;
+  const int tid = threadIdx.x;
+  const bool active = a.dtime->active != 0;
+  const int* rc = &a.dtime->rc[4 * fluid];
+  const int imin = rc[0], imax = rc[1], jmin = rc[2], jmax = rc[3];
+
+  // tile outside the realcells box (or step inactive): copy
+  const bool tile_live = active && !(i0 + TY <= imin || i0 >= imax || j0 + TX <= jmin || j0 >= jmax);
+  if (!tile_live) {
+    for (int k = tid; k < TX * TY; k += NT) {
+      int i = i0 + k / TX, j = j0 + k % TX;
+      if (i < P.Ny + P.g && j < P.Nx + P.g) {
+        int64_t c = cidx(P, i, j);
+        for (int q = 0; q < 4; q++) Unew[c + q * P.plane] = U[c + q * P.plane];
+      }
+    }
+    return;
+  }
+  const double dt = a.dtime->dt;
+  const double dtodx = dt / P.dx;
+  const double dtody = dt / P.dy;
+  uint32_t st = 0;
+  int iters = 0;
+
+  // phase 1
+  for (int k = tid; k < WR * WC; k += NT) {
+    int r = k / WC, c = k % WC;
+    int i = min(max(i0 - 2 + r, 0), P.nr - 1);
+    int j = min(max(j0 - 2 + c, 0), P.nc - 1);
+    V4 u = load4(U, P, cidx(P, i, j));
+    V4 w = MUSCL ? cons_to_prims(gam, pinf, u) : u;
+    s.w[0][r][c] = w.a; s.w[1][r][c] = w.b; s.w[2][r][c] = w.c; s.w[3][r][c] = w.d;
+  }
+  __syncthreads();
+
+  // phase 2: evolved face states of cells (i0-1 .. i0+TY) x (j0-1 .. j0+TX)
+  if (MUSCL) {
+    const double sx = 0.5 * dtodx, sy = 0.5 * dtody;
+    for (int k = tid; k < SR * SC; k += NT) {
+      int r = k / SC, c = k % SC;       // cell (i0-1+r, j0-1+c) = w[r+1][c+1]
+      V4 W = sW(s, r + 1, c + 1);
+      V4 Ww = sW(s, r + 1, c), We = sW(s, r + 1, c + 2);
+      V4 Ws = sW(s, r, c + 1), Wn = sW(s, r + 2, c + 1);
+      V4 dxL = v4sub(W, Ww), dxR = v4sub(We, W);
+      V4 dyL = v4sub(W, Ws), dyR = v4sub(Wn, W);
+      V4 sxv = V4{minmod(dxL.a, dxR.a), minmod(dxL.b, dxR.b), minmod(dxL.c, dxR.c), minmod(dxL.d, dxR.d)};
+      V4 syv = V4{minmod(dyL.a, dyR.a), minmod(dyL.b, dyR.b), minmod(dyL.c, dyR.c), minmod(dyL.d, dyR.d)};
+      V4 L = V4{W.a - 0.5 * sxv.a, W.b - 0.5 * sxv.b, W.c - 0.5 * sxv.c, W.d - 0.5 * sxv.d};
+      V4 R = V4{W.a + 0.5 * sxv.a, W.b + 0.5 * sxv.b, W.c + 0.5 * sxv.c, W.d + 0.5 * sxv.d};
+      V4 B = V4{W.a - 0.5 * syv.a, W.b - 0.5 * syv.b, W.c - 0.5 * syv.c, W.d - 0.5 * syv.d};
+      V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
+      if (!is_physical_primitives(gam, pinf, L) || !is_physical_primitives(gam, pinf, R)) { L = W; R = W; }
+      if (!is_physical_primitives(gam, pinf, B) || !is_physical_primitives(gam, pinf, T)) { B = W; T = W; }
+      double cs = eos_soundspeed(gam, pinf, W.d, W.a);
+      double irho = 1.0 / W.a, rcc = W.a * cs * cs;
+      V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
+      V4 Y = B_times(sy, W, irho, rcc, v4sub(B, T));
+      putFS(s, 0, r, c, V4{(L.a + X.a) + Y.a, (L.b + X.b) + Y.b, (L.c + X.c) + Y.c, (L.d + X.d) + Y.d});
+      putFS(s, 1, r, c, V4{(R.a + X.a) + Y.a, (R.b + X.b) + Y.b, (R.c + X.c) + Y.c, (R.d + X.d) + Y.d});
+      putFS(s, 2, r, c, V4{(B.a + X.a) + Y.a, (B.b + X.b) + Y.b, (B.c + X.c) + Y.c, (B.d + X.d) + Y.d});
+      putFS(s, 3, r, c, V4{(T.a + X.a) + Y.a, (T.b + X.b) + Y.b, (T.c + X.c) + Y.c, (T.d + X.d) + Y.d});
+    }
+    __syncthreads();
+  }
+
+  // phase 3: x faces (TY rows x TX+1) then y faces (TY+1 rows x TX)
+  for (int k = tid; k < NXF + NYF; k += NT) {
+    V4 UL, UR;
+    bool xdir = k < NXF;
+    int fr, fc;
+    if (xdir) { fr = k / (TX + 1); fc = k % (TX + 1); }
+    else { int q = k - NXF; fr = q / TX; fc = q % TX; }
+    if (MUSCL) {
+      bool ok1 = true, ok2 = true;
+      if (xdir) {
+        // face between cell (i0+fr, j0+fc-1) [left, its R face] and (i0+fr, j0+fc) [right, its L face]
+        V4 Cl = sFS(s, 0, fr + 1, fc + 1);
+        V4 Lr = sFS(s, 1, fr + 1, fc);
+        if (!is_physical_primitives(gam, pinf, Cl) || !is_physical_primitives(gam, pinf, Lr)) {
+          Cl = sW(s, fr + 2, fc + 2);
+          Lr = sW(s, fr + 2, fc + 1);
+        }
+        UL = prims_to_cons(gam, pinf, Lr, &ok1);
+        UR = prims_to_cons(gam, pinf, Cl, &ok2);
+      } else {
+        // face between cell (i0+fr-1, j0+fc) [below, its T face] and (i0+fr, j0+fc) [above, its B face]
+        V4 Cb = sFS(s, 2, fr + 1, fc + 1);
+        V4 Bt = sFS(s, 3, fr, fc + 1);
+        if (!is_physical_primitives(gam, pinf, Cb) || !is_physical_primitives(gam, pinf, Bt)) {
+          Cb = sW(s, fr + 2, fc + 2);
+          Bt = sW(s, fr + 1, fc + 2);
+        }
+        UL = prims_to_cons(gam, pinf, Bt, &ok1);
+        UR = prims_to_cons(gam, pinf, Cb, &ok2);
+      }
+      if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
+    } else {
+      if (xdir) { UL = sW(s, fr + 2, fc + 1); UR = sW(s, fr + 2, fc + 2); }
+      else { UL = sW(s, fr + 1, fc + 2); UR = sW(s, fr + 2, fc + 2); }
+    }
+    V4 f = pure_rs_flux(xdir, gas, UL, UR, &st, &iters);
+    if (xdir) { s.fx[0][fr][fc] = f.a; s.fx[1][fr][fc] = f.b; s.fx[2][fr][fc] = f.c; s.fx[3][fr][fc] = f.d; }
+    else { s.fy[0][fr][fc] = f.a; s.fy[1][fr][fc] = f.b; s.fy[2][fr][fc] = f.c; s.fy[3][fr][fc] = f.d; }
+  }
+  __syncthreads();
+
+  // phase 4
+  for (int k = tid; k < TX * TY; k += NT) {
+    int r = k / TX, c = k % TX;
+    int i = i0 + r, j = j0 + c;
+    if (i >= P.Ny + P.g || j >= P.Nx + P.g) continue;
+    int64_t ci = cidx(P, i, j);
+    V4 u = load4(U, P, ci);
+    if (i >= imin && i < imax && j >= jmin && j < jmax) {
+      if (!is_physical_state(u)) st |= ST_UNPHYSICAL;
+      double o[4] = {u.a, u.b, u.c, u.d};
+      for (int q = 0; q < 4; q++) {
+        double v = o[q] + (dtodx * s.fx[q][r][c] + dtody * s.fy[q][r][c]);
+        v = v - dtodx * s.fx[q][r][c + 1];
+        v = v - dtody * s.fy[q][r + 1][c];
+        o[q] = v;
+      }
+      u = V4{o[0], o[1], o[2], o[3]};
+    }
+    store4(Unew, P, ci, u);
+  }
+
+  // status and Newton statistics, one atomic per warp
+  uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+  unsigned wit = __reduce_add_sync(0xffffffffu, (unsigned)iters);
+  if ((tid & 31) == 0) {
+    if (wst) atomicOr(&a.dtime_w->status, wst);
+    if (wit) atomicAdd(&a.dtime_w->newton_iters, (unsigned long long)wit);
+  }
+}
+
+static size_t flux_smem() { return sizeof(FluxSmem); }
+
+void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
+  const GridP& P = ctx->P;
+  FluxArgs a;
+  a.P = P;
+  a.dtime = ctx->dtime;
+  a.dtime_w = ctx->dtime;
+  int nz = 0;
+  a.fluid_base = (fluid_mask & 1) ? 0 : 1;
+  for (int f = 0; f < 2; f++) {
+    if (!(fluid_mask & (1 << f))) continue;
+    a.U[nz] = ctx->U[f];
+    a.Unew[nz] = ctx->Unew[f];
+    nz++;
+  }
+  dim3 grid((P.Nx + TX - 1) / TX, (P.Ny + TY - 1) / TY, nz);
+  size_t sm = flux_smem();
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_flux_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_flux_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr_set = true;
+  }
+  if (fs == GFM_FS_MUSCL)
+    k_flux_update<true><<<grid, NT, sm, ctx->stream>>>(a);
+  else
+    k_flux_update<false><<<grid, NT, sm, ctx->stream>>>(a);
+  for (int f = 0; f < 2; f++) {
+    if (!(fluid_mask & (1 << f))) continue;
+    double* t = ctx->U[f]; ctx->U[f] = ctx->Unew[f]; ctx->Unew[f] = t;
+  }
+}
+
+}  // namespace gfm

@@ -1,0 +1,122 @@
+// Internal declarations shared by the CUDA translation units: the context
+// (device-resident grids of one instance), the padded SoA layout, and the
+// boundary-condition index mapping used by kernels that fuse apply_BCs_euler.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "gfm_math.cuh"
+#include "../../include/gfm_gb300.h"
+
+namespace gfm {
+
+// Geometry + EOS of one instance, passed by value to kernels.
+struct GridP {
+  int Nx, Ny, g;        // real cells, ghost width
+  int nr, nc;           // padded rows / columns = Ny + 2g, Nx + 2g
+  int pitch;            // doubles per row in device planes (>= nc)
+  int64_t plane;        // doubles per plane = nr * pitch
+  double x0, y0, dx, dy;
+  int bcL, bcR, bcB, bcT;
+  double g1, p1, g2, p2;  // gamma1, pinf1, gamma2, pinf2
+  Gas gas1, gas2;         // gamma-derived constants of each material
+  bool periodic;
+};
+
+// Device time/step state, one per instance (written by kernels only).
+struct DevTime {
+  double t, dt, T, CFL;
+  int numsteps;
+  int active;              // t < T at the start of the step
+  unsigned long long maxu_bits, maxv_bits;   // CFL reduction (positive doubles)
+  uint32_t status;
+  int n_ifc;               // interfacial cells of the last ghost fill
+  int n_rounds;            // schedule rounds of the last interface solve
+  unsigned long long newton_iters;
+  int rc[8];               // realcells1 (imin,imax,jmin,jmax), realcells2
+};
+
+}  // namespace gfm
+
+struct gfm_ctx {
+  gfm::GridP P;
+  int two_fluid;
+  cudaStream_t stream;
+  // conserved grids: U[f] current, Unew[f] flux-update output (swapped)
+  double* U[2];
+  double* Unew[2];
+  // primitive work planes
+  double* W[2];      // conversion / extrapolation ping
+  double* Wt[2];     // extrapolation pong
+  double* Wc[2];     // copy of the first conversion (modified GFM)
+  double* phi;
+  double* phi_a;     // level-set stage buffers
+  double* phi_b;
+  double* phi0;      // reinitialisation reference
+  double* nrm;       // 2 planes: raw central-difference gradient of phi
+  double* vel;       // 2 planes: velocity field handed to the level set
+  double* vel_t;     // 2 planes: extension-velocity pong
+  uint8_t* mask;     // interfacial-cell mask (real cells only)
+  int* ifc_map;      // cell -> interface list index, -1 elsewhere
+  int* ifc_list;     // interfacial cells in row-major order
+  int* chunk_count;  // per-CTA counts of the compaction
+  int n_chunks;
+  // per-interface work arrays (capacity = Nx*Ny)
+  int* ifc_done;
+  int* ifc_pred;     // 8 per interface
+  double* ifc_out;   // 8 per interface: star state (4), extension velocity (2), rho* other side, spare
+  int* ifc_opp;      // real GFM: opposite cell
+  gfm::DevTime* dtime;
+  gfm::DevTime* h_dtime;  // pinned host mirror
+  int steps_done_host;
+};
+
+namespace gfm {
+
+// Source of a padded cell under apply_BCs_euler (headers/euler_bc.hpp:5-103):
+// every ghost cell equals one real cell, with u negated (flipu) and/or v
+// negated (flipv).  Requires Nx >= g and Ny >= g, so sources are real cells.
+struct BCSrc { int i, j; bool flipu, flipv; };
+
+__host__ __device__ inline BCSrc bc_source(const GridP& P, int i, int j) {
+  BCSrc s;
+  s.flipu = false; s.flipv = false;
+  if (P.periodic) {
+    s.i = (i - P.g + P.Ny) % P.Ny + P.g;
+    s.j = (j - P.g + P.Nx) % P.Nx + P.g;
+    return s;
+  }
+  s.i = i; s.j = j;
+  if (j < P.g) { s.j = 2 * P.g - j - 1; s.flipu = (P.bcL == GFM_BC_REFLECTIVE); }
+  else if (j >= P.Nx + P.g) { s.j = 2 * (P.Nx + P.g) - 1 - j; s.flipu = (P.bcL == GFM_BC_REFLECTIVE); }
+  if (i < P.g) { s.i = 2 * P.g - i - 1; s.flipv = (P.bcB == GFM_BC_REFLECTIVE); }
+  else if (i >= P.Ny + P.g) { s.i = 2 * (P.Ny + P.g) - 1 - i; s.flipv = (P.bcT == GFM_BC_REFLECTIVE); }
+  return s;
+}
+
+__host__ __device__ inline bool is_real(const GridP& P, int i, int j) {
+  return i >= P.g && i < P.Ny + P.g && j >= P.g && j < P.Nx + P.g;
+}
+
+__device__ __forceinline__ int64_t cidx(const GridP& P, int i, int j) { return (int64_t)i * P.pitch + j; }
+
+__device__ __forceinline__ V4 load4(const double* A, const GridP& P, int64_t c) {
+  return V4{A[c], A[c + P.plane], A[c + 2 * P.plane], A[c + 3 * P.plane]};
+}
+__device__ __forceinline__ void store4(double* A, const GridP& P, int64_t c, const V4& v) {
+  A[c] = v.a; A[c + P.plane] = v.b; A[c + 2 * P.plane] = v.c; A[c + 3 * P.plane] = v.d;
+}
+
+__device__ __forceinline__ void raise_status(DevTime* dt, uint32_t bits) {
+  if (bits) atomicOr(&dt->status, bits);
+}
+
+// kernel launch helpers (defined in the .cu files)
+void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask);
+void launch_bcs(gfm_ctx* ctx, int fluid_mask);
+void launch_cfl(gfm_ctx* ctx, double CFL, double T);
+void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
+void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
+void launch_end_step(gfm_ctx* ctx);
+
+}  // namespace gfm

@@ -1,0 +1,487 @@
+// Scalar FP64 arithmetic of the two-fluid ghost-fluid Euler step, shared by
+// every kernel (and compiled for the host by the unit tests).
+//
+// Every function here fixes its operation order so that a CPU restatement
+// compiled with -ffp-contract=off and these kernels compiled with
+// --fmad=false produce bit-identical doubles.  The elementary functions
+// (exp, log, pow, acos) are this project's own, so neither libm nor CUDA's
+// math library decides a single bit of the result.
+//
+// Contents, with the reference code each part follows:
+//   * stiffened-gas EOS (pressure, specific_ie, soundspeed,
+//     isentropic_extrapolation).  The reference calls these from its absent
+//     PhD-Common dependency (headers/euler_misc.hpp:46,59,77,96,156,173,
+//     sourcecode/GFM_original.cpp:76); the standard stiffened-gas forms are used.
+//   * misc:: state algebra, headers/euler_misc.hpp:23-180.
+//   * exact stiffened-gas Riemann solver: Toro, "Riemann Solvers and Numerical
+//     Methods for Fluid Dynamics", ch. 4 (pressure functions, Newton-Raphson
+//     from the PVRS guess, sampling), with p -> p + p_inf.  It replaces the
+//     absent exact_rs_stiffenedgas used at sourcecode/pure_RS_exact.cpp:29-45
+//     and sourcecode/mixed_RS_exact.cpp:33-47.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+#include "gfm_tables.h"
+
+#if defined(__CUDACC__)
+#define GFM_HD __host__ __device__ __forceinline__
+#else
+#define GFM_HD inline
+#endif
+
+namespace gfm {
+
+// ---------------------------------------------------------------------------
+// Status bits written by kernels (never __trap or assert on the device).
+// ---------------------------------------------------------------------------
+enum : uint32_t {
+  ST_OK = 0,
+  ST_UNPHYSICAL = 1u << 0,       // rho < 0 or e < 0 where the reference asserts
+  ST_NEWTON_NO_CONVERGE = 1u << 1,
+  ST_VACUUM = 1u << 2,           // Riemann data generate vacuum
+  ST_NAN = 1u << 3,              // NaN p* from the mixed solver (GFM_real.cpp:173)
+  ST_DT_NONPOSITIVE = 1u << 4,   // sim_twofluid.cpp:155
+  ST_SCHEDULE_LIMIT = 1u << 5,   // interface schedule exceeded its round limit
+  ST_BAD_ARGUMENT = 1u << 6,
+};
+
+// ---------------------------------------------------------------------------
+// Bit casts and constant tables
+// ---------------------------------------------------------------------------
+GFM_HD int64_t as_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return __double_as_longlong(x);
+#else
+  int64_t b; memcpy(&b, &x, 8); return b;
+#endif
+}
+GFM_HD double from_bits(int64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double(b);
+#else
+  double x; memcpy(&x, &b, 8); return x;
+#endif
+}
+
+#if defined(__CUDACC__)
+__device__ static const double d_exp2_tab[64] = GFM_EXP2_TABLE;
+__device__ static const double d_logf_tab[97] = GFM_LOGF_TABLE;
+__device__ static const double d_invf_tab[97] = GFM_INVF_TABLE;
+#endif
+static const double h_exp2_tab[64] = GFM_EXP2_TABLE;
+static const double h_logf_tab[97] = GFM_LOGF_TABLE;
+static const double h_invf_tab[97] = GFM_INVF_TABLE;
+static const double h_asin_c[28] = GFM_ASIN_COEFFS;
+#if defined(__CUDACC__)
+__device__ static const double d_asin_c[28] = GFM_ASIN_COEFFS;
+#endif
+
+GFM_HD double tab_exp2(int j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&d_exp2_tab[j]);
+#else
+  return h_exp2_tab[j];
+#endif
+}
+GFM_HD double tab_logf(int j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&d_logf_tab[j]);
+#else
+  return h_logf_tab[j];
+#endif
+}
+GFM_HD double tab_invf(int j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&d_invf_tab[j]);
+#else
+  return h_invf_tab[j];
+#endif
+}
+GFM_HD double tab_asin(int j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&d_asin_c[j]);
+#else
+  return h_asin_c[j];
+#endif
+}
+
+GFM_HD double gfm_inf() { return from_bits(0x7ff0000000000000LL); }
+GFM_HD double gfm_nan() { return from_bits(0x7ff8000000000000LL); }
+
+// ---------------------------------------------------------------------------
+// exp: Tang (ACM TOMS 15(2), 1989) with a 64-entry table.
+//   x = (64 m + j) ln2/64 + r,  |r| <= ln2/128
+//   exp(x) = 2^m * 2^(j/64) * (1 + q(r)),  q = r + r^2 (1/2 + r (1/6 + ...))
+// exp(0) == 1 exactly.
+// ---------------------------------------------------------------------------
+GFM_HD double gfm_exp(double x) {
+  if (x != x) return x;
+  if (x > 709.78) return gfm_inf();
+  if (x < -745.2) return 0.0;
+  double kd = rint(x * GFM_INV_LN2_64);
+  int k = (int)kd;
+  double r = (x - kd * GFM_LN2_64_HI) - kd * GFM_LN2_64_LO;
+  int j = k & 63;
+  int m = (k - j) / 64;
+  double q = r + (r * r) * (0.5 + r * (0x1.5555555555555p-3 + r * (0x1.5555555555555p-5 +
+                 r * (0x1.1111111111111p-7 + r * 0x1.6c16c16c16c17p-10))));
+  double t = tab_exp2(j);
+  double y = t + t * q;
+  if (m < -1020) {  // result near or below the normal range: scale in two steps
+    y = y * from_bits((int64_t)(m + 1023 + 200) << 52);
+    return y * from_bits((int64_t)(1023 - 200) << 52);
+  }
+  return y * from_bits((int64_t)(m + 1023) << 52);
+}
+
+// ---------------------------------------------------------------------------
+// log: Tang (ACM TOMS 16(4), 1990) with a 97-entry table.
+//   x = 2^e * m, m in [0.75, 1.5) (so x near 1 has e = 0 and no cancellation)
+//   F = 1 + j/128 nearest to m (j = -32..64);  f = m - F (exact)
+//   log(x) = e ln2 + log(F) + log1p(r),  r = f * (1/F),  |r| <= 2^-8 / 0.75
+// log(1) == 0 exactly.
+// ---------------------------------------------------------------------------
+GFM_HD double gfm_log(double x) {
+  if (!(x > 0.0)) return (x == 0.0) ? -gfm_inf() : gfm_nan();
+  if (x == gfm_inf()) return x;
+  int64_t b = as_bits(x);
+  int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) {  // subnormal
+    x = x * 0x1p54;
+    b = as_bits(x);
+    e = (int)((b >> 52) & 0x7ff) - 54;
+  }
+  e -= 1023;
+  double m = from_bits((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  if (m >= 1.5) { m = m * 0.5; e += 1; }
+  double jd = rint((m - 1.0) * 128.0);
+  int j = (int)jd + 32;
+  double F = 1.0 + jd * 0x1p-7;
+  double f = m - F;
+  double r = f * tab_invf(j);
+  double p = (r * r) * (-0.5 + r * (0x1.5555555555555p-2 + r * (-0.25 + r * (0x1.999999999999ap-3 +
+                 r * (-0x1.5555555555555p-3 + r * 0x1.2492492492492p-3)))));
+  double ed = (double)e;
+  double hi = ed * GFM_LN2_HI + tab_logf(j);
+  double lo = ed * GFM_LN2_LO + p;
+  return hi + (r + lo);
+}
+
+// pow for x >= 0 (all uses have a positive base): exp(y log x); pow(1,y) == 1.
+GFM_HD double gfm_pow(double x, double y) {
+  if (x == 0.0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : gfm_inf());
+  return gfm_exp(y * gfm_log(x));
+}
+
+// asin on [-0.5, 0.5] by its Taylor series (28 terms), in Horner form in x^2.
+GFM_HD double gfm_asin_small(double x) {
+  double s = x * x;
+  double acc = tab_asin(27);
+  for (int n = 26; n >= 1; n--) acc = tab_asin(n) + s * acc;
+  return x + x * (s * acc);
+}
+
+// acos on [-1, 1]: series for |x| <= 0.5, half-angle reduction otherwise.
+GFM_HD double gfm_acos(double x) {
+  if (x > 0.5) return 2.0 * gfm_asin_small(sqrt((1.0 - x) * 0.5));
+  if (x < -0.5) return GFM_PI - 2.0 * gfm_asin_small(sqrt((1.0 + x) * 0.5));
+  return GFM_PI_2 - gfm_asin_small(x);
+}
+
+// ---------------------------------------------------------------------------
+// Stiffened-gas EOS: p = (g-1) rho e - g pinf
+// ---------------------------------------------------------------------------
+GFM_HD double eos_pressure(double g, double pinf, double e, double rho) {
+  return (g - 1.0) * rho * e - g * pinf;
+}
+GFM_HD double eos_specific_ie(double g, double pinf, double p, double rho) {
+  return (p + g * pinf) / ((g - 1.0) * rho);
+}
+GFM_HD double eos_soundspeed(double g, double pinf, double p, double rho) {
+  return sqrt(g * (p + pinf) / rho);
+}
+GFM_HD double eos_isentropic_extrapolation(double g, double pinf, double rho1, double p1, double p2) {
+  return rho1 * gfm_pow((p2 + pinf) / (p1 + pinf), 1.0 / g);
+}
+
+// ---------------------------------------------------------------------------
+// misc:: state algebra (headers/euler_misc.hpp:23-180).  States are 4 doubles:
+// conserved U = (rho, rho u, rho v, E), primitive W = (rho, u, v, p).
+// ---------------------------------------------------------------------------
+struct V4 { double a, b, c, d; };
+
+// euler_misc.hpp:23-29
+GFM_HD double misc_specific_ie(const V4& U) {
+  double rho = U.a;
+  double u = U.b / rho;
+  double v = U.c / rho;
+  return (U.d / rho) - 0.5 * (u * u + v * v);
+}
+// euler_misc.hpp:32-41
+GFM_HD bool is_physical_state(const V4& U) {
+  double rho = U.a;
+  double u = U.b / rho;
+  double v = U.c / rho;
+  double e = (U.d / rho) - 0.5 * (u * u + v * v);
+  return rho >= 0.0 && e >= 0.0;
+}
+// euler_misc.hpp:44-49
+GFM_HD bool is_physical_primitives(double g, double pinf, const V4& W) {
+  double e = eos_specific_ie(g, pinf, W.d, W.a);
+  return e >= 0.0 && W.a >= 0.0;
+}
+// euler_misc.hpp:52-67
+GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
+  double rho = U.a;
+  double u = U.b / rho;
+  double v = U.c / rho;
+  double e = (U.d / rho) - 0.5 * (u * u + v * v);
+  double p = eos_pressure(g, pinf, e, rho);
+  return V4{rho, u, v, p};
+}
+// euler_misc.hpp:70-86
+GFM_HD V4 flux_primitive_var(double g, double pinf, const V4& W) {
+  double rho = W.a, u = W.b, v = W.c, p = W.d;
+  double e = eos_specific_ie(g, pinf, p, rho);
+  double E = rho * e + 0.5 * rho * (u * u + v * v);
+  return V4{rho * u, rho * u * u + p, rho * u * v, u * (E + p)};
+}
+// euler_misc.hpp:89-108 (the asserts become a returned flag)
+GFM_HD V4 prims_to_cons(double g, double pinf, const V4& W, bool* ok) {
+  double rho = W.a, u = W.b, v = W.c, p = W.d;
+  double e = eos_specific_ie(g, pinf, p, rho);
+  if (ok) *ok = (rho >= 0.0) && (e >= 0.0);
+  return V4{rho, rho * u, rho * v, rho * e + 0.5 * rho * (u * u + v * v)};
+}
+
+// ---------------------------------------------------------------------------
+// Exact Riemann solver for the stiffened gas (Toro ch. 4, p -> p + pinf).
+//
+// Arithmetic is arranged for GB300, where an FP64 division or square root
+// costs about ten multiplies: every gamma-derived constant is computed once
+// per material (Gas), every per-side reciprocal once per solve (RSSide), and
+// Newton's stopping test is 2|p - p_old| <= TOL (p + p_old + 2 pinf_min).
+// ---------------------------------------------------------------------------
+struct Gas {
+  double g, pinf;
+  double G1, G2, G3, G4, G5, G6, G7, IG;
+};
+
+GFM_HD Gas make_gas(double g, double pinf) {
+  Gas k;
+  k.g = g; k.pinf = pinf;
+  k.G1 = (g - 1.0) / (2.0 * g);
+  k.G2 = (g + 1.0) / (2.0 * g);
+  k.G3 = 2.0 * g / (g - 1.0);
+  k.G4 = 2.0 / (g - 1.0);
+  k.G5 = 2.0 / (g + 1.0);
+  k.G6 = (g - 1.0) / (g + 1.0);
+  k.G7 = (g - 1.0) / 2.0;
+  k.IG = 1.0 / g;
+  return k;
+}
+
+struct RSSide {
+  double rho, u, p;   // primitive 1D state
+  double pb;          // p + pinf
+  double c;           // sound speed sqrt(g pb / rho)
+  double AK, BK;      // shock constants G5/rho, G6 pb
+  double ipb;         // 1 / pb
+  double G4c;         // G4 c
+  double irc;         // 1 / (rho c)
+};
+
+GFM_HD RSSide rs_side(double rho, double u, double p, const Gas& k) {
+  RSSide s;
+  s.rho = rho; s.u = u; s.p = p;
+  s.pb = p + k.pinf;
+  s.c = sqrt(k.g * s.pb / rho);
+  s.AK = k.G5 / rho;
+  s.BK = k.G6 * s.pb;
+  s.ipb = 1.0 / s.pb;
+  s.G4c = k.G4 * s.c;
+  s.irc = 1.0 / (rho * s.c);
+  return s;
+}
+
+// Toro's PREFUN: pressure function f_K and its derivative at pressure p.
+GFM_HD void rs_prefun(const RSSide& K, const Gas& k, double p, double* f, double* fd) {
+  double pb = p + k.pinf;
+  if (p > K.p) {  // shock
+    double r = 1.0 / (pb + K.BK);
+    double qrt = sqrt(K.AK * r);
+    *f = (p - K.p) * qrt;
+    *fd = (1.0 - 0.5 * ((p - K.p) * r)) * qrt;
+  } else {        // rarefaction
+    double prat = pb * K.ipb;
+    double pw = gfm_pow(prat, k.G1);
+    *f = K.G4c * (pw - 1.0);
+    *fd = K.irc * (pw / prat);
+  }
+}
+
+struct RSStar {
+  double p, u;        // P_STAR, S_STAR
+  int iters;
+  uint32_t status;
+};
+
+#define GFM_RS_TOL 1e-12
+#define GFM_RS_MAXIT 60
+
+// Newton-Raphson on p* (Toro's STARPU) from the initial guess p0, then u*
+// from the last pressure-function evaluation.
+GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, double p0) {
+  RSStar s;
+  s.status = ST_OK;
+  double udiff = R.u - L.u;
+  if (L.G4c + R.G4c <= udiff) s.status |= ST_VACUUM;
+  double pinf_min = kL.pinf < kR.pinf ? kL.pinf : kR.pinf;
+  double pbmin = L.pb < R.pb ? L.pb : R.pb;
+  double pfl = 1e-6 * pbmin - pinf_min;
+  double pold = p0 > pfl ? p0 : pfl;
+  double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0;
+  double p = pold;
+  int it = 0;
+  for (;;) {
+    rs_prefun(L, kL, pold, &fL, &fLd);
+    rs_prefun(R, kR, pold, &fR, &fRd);
+    p = pold - (fL + fR + udiff) / (fLd + fRd);
+    if (p < pfl) p = pfl;
+    it++;
+    bool conv = 2.0 * fabs(p - pold) <= GFM_RS_TOL * (p + pold + 2.0 * pinf_min);
+    pold = p;
+    if (conv) break;
+    if (it >= GFM_RS_MAXIT) { s.status |= ST_NEWTON_NO_CONVERGE; break; }
+  }
+  s.p = p;
+  s.u = 0.5 * (L.u + R.u + fR - fL);
+  s.iters = it;
+  return s;
+}
+
+// PVRS guess (Toro eq. 4.47)
+GFM_HD double rs_guess_pvrs(const RSSide& L, const RSSide& R) {
+  return 0.5 * (L.p + R.p) - 0.125 * (R.u - L.u) * (L.rho + R.rho) * (L.c + R.c);
+}
+
+// Whole solve.  When u and p agree on both sides the data hold at most a
+// contact and the exact answer p* = p, u* = u is returned without iterating.
+GFM_HD RSStar rs_solve(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR) {
+  if (L.u == R.u && L.p == R.p) {
+    RSStar s;
+    s.p = L.p;
+    s.u = L.u;
+    s.iters = 0;
+    s.status = ST_OK;
+    return s;
+  }
+  return rs_star(L, kL, R, kR, rs_guess_pvrs(L, R));
+}
+
+// Star density behind the K wave (shock or rarefaction).
+GFM_HD double rs_rho_star(const RSSide& K, const Gas& k, double pstar) {
+  double pr = (pstar + k.pinf) * K.ipb;
+  if (pstar > K.p) return K.rho * ((pr + k.G6) / (pr * k.G6 + 1.0));
+  return K.rho * gfm_pow(pr, k.IG);
+}
+
+// Toro's SAMPLE at speed S; returns (rho, u, p).
+struct RS1D { double rho, u, p; };
+GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, const RSStar& st,
+                      double S) {
+  RS1D w;
+  if (S <= st.u) {  // left of contact
+    if (st.p <= L.p) {  // left rarefaction
+      double shl = L.u - L.c;
+      if (S <= shl) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
+      double cml = L.c * gfm_pow((st.p + kL.pinf) * L.ipb, kL.G1);
+      double stl = st.u - cml;
+      if (S > stl) { w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w; }
+      double c = kL.G5 * (L.c + kL.G7 * (L.u - S));
+      double cr = c / L.c;
+      w.rho = L.rho * gfm_pow(cr, kL.G4);
+      w.u = kL.G5 * (L.c + kL.G7 * L.u + S);
+      w.p = L.pb * gfm_pow(cr, kL.G3) - kL.pinf;
+      return w;
+    } else {  // left shock
+      double pml = (st.p + kL.pinf) * L.ipb;
+      double sl = L.u - L.c * sqrt(kL.G2 * pml + kL.G1);
+      if (S <= sl) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
+      w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w;
+    }
+  } else {  // right of contact
+    if (st.p > R.p) {  // right shock
+      double pmr = (st.p + kR.pinf) * R.ipb;
+      double sr = R.u + R.c * sqrt(kR.G2 * pmr + kR.G1);
+      if (S >= sr) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
+      w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w;
+    } else {  // right rarefaction
+      double shr = R.u + R.c;
+      if (S >= shr) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
+      double cmr = R.c * gfm_pow((st.p + kR.pinf) * R.ipb, kR.G1);
+      double str = st.u + cmr;
+      if (S <= str) { w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w; }
+      double c = kR.G5 * (R.c - kR.G7 * (R.u - S));
+      double cr = c / R.c;
+      w.rho = R.rho * gfm_pow(cr, kR.G4);
+      w.u = kR.G5 * (-R.c + kR.G7 * R.u + S);
+      w.p = R.pb * gfm_pow(cr, kR.G3) - kR.pinf;
+      return w;
+    }
+  }
+}
+
+// pure_RS_exact::solve_RP (sourcecode/pure_RS_exact.cpp:9-73): flux of the
+// exact solution at x/t = 0 between conserved states UL and UR, one material.
+GFM_HD V4 pure_rs_flux(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
+  if (!is_physical_state(UL) || !is_physical_state(UR)) *status |= ST_UNPHYSICAL;
+  V4 Lp = cons_to_prims(k.g, k.pinf, UL);
+  V4 Rp = cons_to_prims(k.g, k.pinf, UR);
+  double uLn = paralleltox ? Lp.b : Lp.c;
+  double uRn = paralleltox ? Rp.b : Rp.c;
+  RSSide L = rs_side(Lp.a, uLn, Lp.d, k);
+  RSSide R = rs_side(Rp.a, uRn, Rp.d, k);
+  RSStar st = rs_solve(L, k, R, k);
+  *status |= st.status;
+  *iters += st.iters;
+  RS1D w = rs_sample(L, k, R, k, st, 0.0);
+  double ut = paralleltox ? (st.u <= 0.0 ? Rp.c : Lp.c) : (st.u <= 0.0 ? Rp.b : Lp.b);
+  V4 f = flux_primitive_var(k.g, k.pinf, V4{w.rho, w.u, ut, w.p});
+  if (!paralleltox) { double t = f.b; f.b = f.c; f.c = t; }
+  return f;
+}
+
+// mixed_RS_exact::solve_mixed_RP (sourcecode/mixed_RS_exact.cpp:8-48).
+struct MixedStar { double p_star, u_star, rho_star_L, rho_star_R; };
+GFM_HD MixedStar mixed_rs(const Gas& kL, const Gas& kR, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
+  if (!is_physical_state(UL) || !is_physical_state(UR)) *status |= ST_UNPHYSICAL;
+  V4 Lp = cons_to_prims(kL.g, kL.pinf, UL);
+  V4 Rp = cons_to_prims(kR.g, kR.pinf, UR);
+  RSSide L = rs_side(Lp.a, Lp.b, Lp.d, kL);
+  RSSide R = rs_side(Rp.a, Rp.b, Rp.d, kR);
+  RSStar st = rs_solve(L, kL, R, kR);
+  *status |= st.status;
+  *iters += st.iters;
+  MixedStar m;
+  m.p_star = st.p;
+  m.u_star = st.u;
+  m.rho_star_L = rs_rho_star(L, kL, st.p);
+  m.rho_star_R = rs_rho_star(R, kR, st.p);
+  if (m.p_star != m.p_star) *status |= ST_NAN;
+  return m;
+}
+
+// minmod slope, one component (sourcecode/FS_MUSCL.cpp:310-327)
+GFM_HD double minmod(double dL, double dR) {
+  if (dR > 0.0) {
+    double m = (dR < dL) ? dR : dL;     // std::min(dL, dR)
+    return (0.0 < m) ? m : 0.0;         // std::max(0.0, m)
+  }
+  double m = (dL < dR) ? dR : dL;       // std::max(dL, dR)
+  return (m < 0.0) ? m : 0.0;           // std::min(0.0, m)
+}
+
+}  // namespace gfm

@@ -1,0 +1,1014 @@
+// Kernels of the two-fluid time step other than the flux update:
+//   CFL time step             sim_twofluid::compute_dt   (sourcecode/sim_twofluid.cpp:108-157)
+//                             sim_onefluid::compute_dt   (sourcecode/sim_onefluid.cpp:68-91)
+//   boundary conditions       apply_BCs_euler            (headers/euler_bc.hpp:5-103)
+//   ghost-fluid fill          GFM_{original,riemann,real,modified}::set_ghost_states
+//   narrow-band extrapolation extrapolate_vector(_mgfm)  (sourcecode/extrapolate_vector.cpp:5-288)
+//   extension velocity        extrapolate_extension_vfield (sourcecode/extrapolate_extension_vfield.cpp:4-122)
+//   level set                 advection + reinitialisation (the project's own Levelset)
+//
+// Every kernel that the reference follows with apply_BCs_euler computes the
+// ghost-layer cells itself: a ghost cell is a mirrored real cell, so its
+// thread evaluates that real cell's update and applies the reflective signs.
+#include "gfm_internal.cuh"
+#include <climits>
+
+namespace gfm {
+
+constexpr int CHUNK = 2048;      // cells per CTA in the 1D full-grid kernels
+constexpr int CHUNK_T = 512;
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dmax_std(double a, double b) { return (a < b) ? b : a; }  // std::max
+__device__ __forceinline__ double dmin_std(double a, double b) { return (b < a) ? b : a; }  // std::min
+
+// unit normal with the reference's fallback (sourcecode/GFM_riemann.cpp:58-68)
+__device__ __forceinline__ void unit_normal(const double* nrm, const GridP& P, int64_t c, double& nx, double& ny) {
+  double gx = nrm[c], gy = nrm[c + P.plane];
+  double nn = sqrt(gx * gx + gy * gy);
+  if (nn < 1e-12) { nx = 1.0; ny = 0.0; return; }
+  nx = gx / nn; ny = gy / nn;
+}
+
+__device__ __forceinline__ V4 v4d(const V4& x, const V4& y) { return V4{x.a - y.a, x.b - y.b, x.c - y.c, x.d - y.d}; }
+
+__device__ __forceinline__ void linear_to_ij(const GridP& P, int64_t lin, int& i, int& j) {
+  i = (int)(lin / P.nc);
+  j = (int)(lin - (int64_t)i * P.nc);
+}
+
+// ---------------------------------------------------------------------------
+// CFL reduction + dt (last-block pattern); also the start-of-step flags
+// ---------------------------------------------------------------------------
+struct CflArgs {
+  GridP P;
+  const double* U1;
+  const double* U2;
+  const double* phi;   // null for one fluid
+  DevTime* dt;
+  unsigned int* counter;
+  double CFL, T;
+  int ogfm;            // realcells boxes start empty (GFM_original.cpp:47-55)
+};
+
+__global__ void __launch_bounds__(256) k_cfl(CflArgs a) {
+  const GridP& P = a.P;
+  __shared__ double s_u[8], s_v[8];
+  __shared__ bool s_last;
+  DevTime* D = a.dt;
+  const bool active = D->t < a.T;
+  if (!active) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) D->active = 0;
+    return;
+  }
+  double mu = 0.0, mv = 0.0;
+  const int64_t n = (int64_t)P.Nx * P.Ny;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.Nx) + P.g, j = (int)(k % P.Nx) + P.g;
+    int64_t c = cidx(P, i, j);
+    bool f1 = (a.phi == nullptr) || (a.phi[c] < 0.0);
+    const double* U = f1 ? a.U1 : a.U2;
+    double gm = f1 ? P.g1 : P.g2, pinf = f1 ? P.p1 : P.p2;
+    V4 u = load4(U, P, c);
+    double rho = u.a;
+    double e = misc_specific_ie(u);
+    double p = eos_pressure(gm, pinf, e, rho);
+    double cs = eos_soundspeed(gm, pinf, p, rho);
+    double xu = fabs(u.b) / rho + cs;
+    double xv = fabs(u.c) / rho + cs;
+    mu = dmax_std(mu, xu);   // NaN never replaces the running max (std::max semantics)
+    mv = dmax_std(mv, xv);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mu = dmax_std(mu, __shfl_xor_sync(0xffffffffu, mu, o));
+    mv = dmax_std(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+  }
+  int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { s_u[w] = mu; s_v[w] = mv; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < (int)(blockDim.x >> 5); q++) { mu = dmax_std(mu, s_u[q]); mv = dmax_std(mv, s_v[q]); }
+    // positive doubles order as their bit patterns
+    atomicMax(&D->maxu_bits, (unsigned long long)__double_as_longlong(mu));
+    atomicMax(&D->maxv_bits, (unsigned long long)__double_as_longlong(mv));
+    __threadfence();
+    unsigned int prev = atomicAdd(a.counter, 1u);
+    s_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    double maxu = __longlong_as_double((long long)atomicAdd(&D->maxu_bits, 0ull));
+    double maxv = __longlong_as_double((long long)atomicAdd(&D->maxv_bits, 0ull));
+    double cfl = (D->numsteps < 5) ? ((0.2 < a.CFL) ? 0.2 : a.CFL) : a.CFL;   // std::min(CFL, 0.2)
+    double dx_u = P.dx / maxu, dy_v = P.dy / maxv;
+    double dt = cfl * ((dy_v < dx_u) ? dy_v : dx_u);
+    if (D->t + dt > a.T) dt = a.T - D->t;
+    if (!(dt > 0.0)) D->status |= ST_DT_NONPOSITIVE;
+    D->dt = dt;
+    D->T = a.T;
+    D->CFL = cfl;
+    D->active = 1;
+    D->maxu_bits = 0ull;
+    D->maxv_bits = 0ull;
+    int g = P.g;
+    for (int f = 0; f < 2; f++) {
+      if (a.ogfm) {
+        D->rc[4 * f + 0] = g + P.Ny; D->rc[4 * f + 1] = g; D->rc[4 * f + 2] = g + P.Nx; D->rc[4 * f + 3] = g;
+      } else {
+        D->rc[4 * f + 0] = g; D->rc[4 * f + 1] = g + P.Ny; D->rc[4 * f + 2] = g; D->rc[4 * f + 3] = g + P.Nx;
+      }
+    }
+    D->newton_iters = 0ull;
+    *a.counter = 0u;
+  }
+}
+
+__global__ void k_end_step(DevTime* D) {
+  if (D->active) {
+    D->t += D->dt;
+    D->numsteps += 1;
+  }
+}
+
+void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter) {
+  CflArgs a;
+  a.P = ctx->P;
+  a.U1 = ctx->U[0];
+  a.U2 = ctx->two_fluid ? ctx->U[1] : ctx->U[0];
+  a.phi = ctx->two_fluid ? ctx->phi : nullptr;
+  a.dt = ctx->dtime;
+  a.counter = counter;
+  a.CFL = CFL;
+  a.T = T;
+  a.ogfm = ogfm ? 1 : 0;
+  int64_t n = (int64_t)ctx->P.Nx * ctx->P.Ny;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_cfl<<<blocks, 256, 0, ctx->stream>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// apply_BCs_euler on conserved grids (ghost cells only)
+// ---------------------------------------------------------------------------
+__global__ void k_bc_u(GridP P, double* U, const DevTime* D) {
+  if (!D->active) return;
+  int64_t n = (int64_t)P.nr * P.nc;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    if (is_real(P, i, j) && !P.periodic) continue;
+    BCSrc s = bc_source(P, i, j);
+    if (s.i == i && s.j == j) continue;
+    V4 v = load4(U, P, cidx(P, s.i, s.j));
+    if (s.flipu) v.b = -v.b;
+    if (s.flipv) v.c = -v.c;
+    store4(U, P, cidx(P, i, j), v);
+  }
+}
+
+void launch_bcs(gfm_ctx* ctx, int fluid_mask) {
+  int64_t n = (int64_t)ctx->P.nr * ctx->P.nc;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  for (int f = 0; f < 2; f++)
+    if (fluid_mask & (1 << f)) k_bc_u<<<blocks, 256, 0, ctx->stream>>>(ctx->P, ctx->U[f], ctx->dtime);
+}
+
+// ---------------------------------------------------------------------------
+// Ghost fill stage 1: conversion of both grids, phi gradient, interfacial
+// mask, per-chunk interfacial counts.
+// ---------------------------------------------------------------------------
+struct PrimArgs {
+  GridP P;
+  const double* U1; const double* U2;
+  double* W1; double* W2;
+  double* Wc1; double* Wc2;   // optional copies (modified GFM)
+  const double* phi;
+  double* nrm;
+  uint8_t* mask;
+  int* ifc_map;
+  int* chunk_count;
+  DevTime* D;
+  int check_both;             // 1: assert both grids (OGFM, RGFM); 0: the phi-selected one
+};
+
+__global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  __shared__ int s_cnt;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  uint32_t st = 0;
+  int cnt = 0;
+  for (int q = threadIdx.x; q < CHUNK; q += CHUNK_T) {
+    int64_t lin = base + q;
+    if (lin >= n) break;
+    int i, j;
+    linear_to_ij(P, lin, i, j);
+    int64_t c = cidx(P, i, j);
+    V4 u1 = load4(a.U1, P, c), u2 = load4(a.U2, P, c);
+    double ph = a.phi[c];
+    if (a.check_both) {
+      if (!is_physical_state(u1) || !is_physical_state(u2)) st |= ST_UNPHYSICAL;
+    } else {
+      if (!is_physical_state(ph <= 0.0 ? u1 : u2)) st |= ST_UNPHYSICAL;
+    }
+    V4 w1 = cons_to_prims(P.g1, P.p1, u1);
+    V4 w2 = cons_to_prims(P.g2, P.p2, u2);
+    store4(a.W1, P, c, w1);
+    store4(a.W2, P, c, w2);
+    if (a.Wc1) { store4(a.Wc1, P, c, w1); store4(a.Wc2, P, c, w2); }
+    double gx = 0.0, gy = 0.0;
+    if (i >= 1 && i < P.nr - 1 && j >= 1 && j < P.nc - 1) {
+      gx = (a.phi[c + 1] - a.phi[c - 1]) / (2.0 * P.dx);
+      gy = (a.phi[c + P.pitch] - a.phi[c - P.pitch]) / (2.0 * P.dy);
+    }
+    a.nrm[c] = gx;
+    a.nrm[c + P.plane] = gy;
+    uint8_t m = 0;
+    if (is_real(P, i, j)) {
+      bool s = ph <= 0.0;
+      m = ((a.phi[c - 1] <= 0.0) != s || (a.phi[c + 1] <= 0.0) != s || (a.phi[c - P.pitch] <= 0.0) != s ||
+           (a.phi[c + P.pitch] <= 0.0) != s) ? 1 : 0;
+    }
+    a.mask[c] = m;
+    a.ifc_map[c] = -1;
+    cnt += m;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_cnt, cnt);
+  uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+  if ((threadIdx.x & 31) == 0 && wst) atomicOr(&a.D->status, wst);
+  __syncthreads();
+  if (threadIdx.x == 0) a.chunk_count[blockIdx.x] = s_cnt;
+}
+
+// Stage 2: ordered compaction of the interfacial cells (row-major order).
+__global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mask, const int* chunk_count,
+                                                     int n_chunks, int* list, int* ifc_map, DevTime* D) {
+  if (!D->active) return;
+  __shared__ int s_off;
+  __shared__ int s_warp[CHUNK_T / 32];
+  if (threadIdx.x == 0) s_off = 0;
+  __syncthreads();
+  int part = 0;
+  for (int b = threadIdx.x; b < (int)blockIdx.x; b += CHUNK_T) part += chunk_count[b];
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0 && part) atomicAdd(&s_off, part);
+  __syncthreads();
+  int off = s_off;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) D->n_ifc = off + chunk_count[blockIdx.x];
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // cells base + it*CHUNK_T + tid, in order of it then tid
+  for (int it = 0; it < CHUNK / CHUNK_T; it++) {
+    int64_t lin = base + (int64_t)it * CHUNK_T + threadIdx.x;
+    int m = 0;
+    int i = 0, j = 0;
+    if (lin < n) {
+      linear_to_ij(P, lin, i, j);
+      m = mask[cidx(P, i, j)];
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, m);
+    if (lane == 0) s_warp[w] = __popc(bal);
+    __syncthreads();
+    int wofs = 0, tot = 0;
+    for (int q = 0; q < CHUNK_T / 32; q++) { if (q < w) wofs += s_warp[q]; tot += s_warp[q]; }
+    if (m) {
+      int k = off + wofs + __popc(bal & ((1u << lane) - 1u));
+      list[k] = (int)lin;
+      ifc_map[cidx(P, i, j)] = k;
+    }
+    off += tot;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// extrapolate_vector sweep (+ apply_BCs_euler on the updated grids), one
+// launch per iteration.  mode 1 = extrapolate_vector_mgfm (interfacial cells
+// are left unchanged).
+// ---------------------------------------------------------------------------
+struct ExtrapArgs {
+  GridP P;
+  const double* S1; const double* S2;   // grid1/grid2 of this iteration
+  double* D1; double* D2;               // updated_grid1/2
+  const double* phi;
+  const double* nrm;
+  const uint8_t* mask;
+  const DevTime* D;
+  int mgfm;
+};
+
+__global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const double dt = 0.5 * dmin_std(P.dx, P.dy);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    BCSrc s = bc_source(P, i, j);
+    int64_t c = cidx(P, s.i, s.j);
+    V4 v1 = load4(a.S1, P, c), v2 = load4(a.S2, P, c);
+    bool skip = a.mgfm && a.mask[c];
+    if (!skip) {
+      double nx, ny;
+      unit_normal(a.nrm, P, c, nx, ny);
+      double cx = (dt / P.dx) * nx, cy = (dt / P.dy) * ny;
+      if (a.phi[c] <= 0.0) {
+        // fluid 2 is ghost: information flows along -normal
+        V4 dxv = (nx > 0.0) ? v4d(load4(a.S2, P, c + 1), v2) : v4d(v2, load4(a.S2, P, c - 1));
+        V4 dyv = (ny > 0.0) ? v4d(load4(a.S2, P, c + P.pitch), v2) : v4d(v2, load4(a.S2, P, c - P.pitch));
+        v2 = V4{(v2.a + cx * dxv.a) + cy * dyv.a, (v2.b + cx * dxv.b) + cy * dyv.b,
+                (v2.c + cx * dxv.c) + cy * dyv.c, (v2.d + cx * dxv.d) + cy * dyv.d};
+      } else {
+        V4 dxv = (nx > 0.0) ? v4d(v1, load4(a.S1, P, c - 1)) : v4d(load4(a.S1, P, c + 1), v1);
+        V4 dyv = (ny > 0.0) ? v4d(v1, load4(a.S1, P, c - P.pitch)) : v4d(load4(a.S1, P, c + P.pitch), v1);
+        v1 = V4{(v1.a - cx * dxv.a) - cy * dyv.a, (v1.b - cx * dxv.b) - cy * dyv.b,
+                (v1.c - cx * dxv.c) - cy * dyv.c, (v1.d - cx * dxv.d) - cy * dyv.d};
+      }
+    }
+    if (s.flipu) { v1.b = -v1.b; v2.b = -v2.b; }
+    if (s.flipv) { v1.c = -v1.c; v2.c = -v2.c; }
+    int64_t o = cidx(P, i, j);
+    store4(a.D1, P, o, v1);
+    store4(a.D2, P, o, v2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interface solve: the loop over interfacial cells of GFM_riemann
+// (sourcecode/GFM_riemann.cpp:51-148), GFM_real (sourcecode/GFM_real.cpp:52-208)
+// and GFM_modified (sourcecode/GFM_modified.cpp:65-200).
+//
+// The reference visits interfacial cells in row-major order and, for the
+// Riemann and real GFM, overwrites prims of the visited cell's real fluid
+// while later cells still read prims (bilinear samples, or the opposite
+// cell).  A later cell therefore reads the star state of an earlier
+// interfacial cell when that cell lies in its read set and has the read
+// fluid as its real fluid, and the original value otherwise.  Each cell here
+// resolves its reads by exactly that rule and waits only for those earlier
+// cells (its predecessors), so the result is the sequential one while
+// independent cells run in parallel.
+//
+// Cells are claimed in list (row-major) order through a ticket counter, so
+// every predecessor was claimed before its dependant by a running thread: the
+// lowest unfinished cell can always proceed.  Waits are bounded; a wait that
+// runs out sets ST_SCHEDULE_LIMIT and the thread abandons its cell.
+// ---------------------------------------------------------------------------
+enum { IFC_RIEMANN = 0, IFC_REAL = 1, IFC_MODIFIED = 2 };
+constexpr int IFC_OUT = 8;
+constexpr long long IFC_SPIN_LIMIT = 1ll << 24;
+
+struct IfcArgs {
+  GridP P;
+  const double* W1; const double* W2;
+  const double* phi; const double* nrm; const uint8_t* mask;
+  const int* list; const int* ifc_map;
+  int* done;            // per cell of the list: 0 pending, 1 finished, 2 abandoned
+  double* out;          // IFC_OUT doubles per cell
+  unsigned int* ticket;
+  DevTime* D;
+  int slip;             // GFM_base::use_slip_BCs
+};
+
+__device__ __forceinline__ bool ifc_wait(const IfcArgs& a, int p) {
+  volatile int* d = a.done;
+  long long spins = 0;
+  while (d[p] == 0) {
+    if (++spins > IFC_SPIN_LIMIT) return false;
+    __nanosleep(64);
+  }
+  __threadfence();
+  return d[p] == 1;
+}
+
+__device__ __forceinline__ V4 ifc_out4(const IfcArgs& a, int p) {
+  const double* o = a.out + (int64_t)p * IFC_OUT;
+  return V4{__ldcg(o), __ldcg(o + 1), __ldcg(o + 2), __ldcg(o + 3)};
+}
+
+// Value of fluid f's primitives at cell (i,j) as the sequential loop of cell
+// `lin` sees it; waits for the writer if it is an earlier interfacial cell.
+__device__ V4 ifc_read(const IfcArgs& a, int f, int i, int j, int64_t lin, bool& ok) {
+  const GridP& P = a.P;
+  int64_t c = cidx(P, i, j);
+  int64_t l2 = (int64_t)i * P.nc + j;
+  if (a.mask[c] && ((a.phi[c] <= 0.0) == (f == 0)) && l2 < lin) {
+    int p = a.ifc_map[c];
+    if (!ifc_wait(a, p)) { ok = false; return V4{0.0, 0.0, 0.0, 0.0}; }
+    return ifc_out4(a, p);
+  }
+  return load4(f == 0 ? a.W1 : a.W2, P, c);
+}
+
+// grid_bilinear_interpolate at x (the project's definition, shared with the oracle)
+__device__ V4 ifc_bilinear(const IfcArgs& a, int f, double x, double y, int64_t lin, bool resolve, bool& ok) {
+  const GridP& P = a.P;
+  double s = (x - P.x0) / P.dx + (double)P.g - 0.5;
+  double t = (y - P.y0) / P.dy + (double)P.g - 0.5;
+  int j0 = (int)floor(s), i0 = (int)floor(t);
+  j0 = min(max(j0, 0), P.nc - 2);
+  i0 = min(max(i0, 0), P.nr - 2);
+  double wa = s - (double)j0, wb = t - (double)i0;
+  V4 g00, g01, g10, g11;
+  if (resolve) {
+    g00 = ifc_read(a, f, i0, j0, lin, ok);
+    g01 = ifc_read(a, f, i0, j0 + 1, lin, ok);
+    g10 = ifc_read(a, f, i0 + 1, j0, lin, ok);
+    g11 = ifc_read(a, f, i0 + 1, j0 + 1, lin, ok);
+  } else {
+    const double* G = f == 0 ? a.W1 : a.W2;
+    g00 = load4(G, P, cidx(P, i0, j0));
+    g01 = load4(G, P, cidx(P, i0, j0 + 1));
+    g10 = load4(G, P, cidx(P, i0 + 1, j0));
+    g11 = load4(G, P, cidx(P, i0 + 1, j0 + 1));
+  }
+  double w00 = (1.0 - wa) * (1.0 - wb), w01 = wa * (1.0 - wb), w10 = (1.0 - wa) * wb, w11 = wa * wb;
+  return V4{w00 * g00.a + w01 * g01.a + w10 * g10.a + w11 * g11.a,
+            w00 * g00.b + w01 * g01.b + w10 * g10.b + w11 * g11.b,
+            w00 * g00.c + w01 * g01.c + w10 * g10.c + w11 * g11.c,
+            w00 * g00.d + w01 * g01.d + w10 * g10.d + w11 * g11.d};
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int n = a.D->n_ifc;
+  uint32_t st = 0;
+  int iters = 0;
+  for (;;) {
+    int k = (int)atomicAdd(a.ticket, 1u);
+    if (k >= n) break;
+    int64_t lin = a.list[k];
+    int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
+    int64_t c = cidx(P, i, j);
+    double lsval = a.phi[c];
+    double nx, ny;
+    unit_normal(a.nrm, P, c, nx, ny);
+    bool ok = true;
+    V4 ip1, ip2;   // interfaceprims1, interfaceprims2
+    if (MODE == IFC_REAL) {
+      // neighbour with opposite phi sign and the closest normal (GFM_real.cpp:77-117)
+      double mindiff = 1e100;
+      int iopp = -1000, jopp = -1000;
+      for (int xinc = -1; xinc <= 1; xinc++)
+        for (int yinc = -1; yinc <= 1; yinc++) {
+          int64_t c2 = cidx(P, i + yinc, j + xinc);
+          double other = a.phi[c2];
+          if (lsval * other <= 0.0) {
+            double ox, oy;
+            unit_normal(a.nrm, P, c2, ox, oy);
+            double dp = nx * ox + ny * oy;
+            dp = (dp < -1.0) ? -1.0 : dp;
+            dp = (1.0 < dp) ? 1.0 : dp;
+            double ang = gfm_acos(dp);
+            if (ang < mindiff) { iopp = i + yinc; jopp = j + xinc; mindiff = ang; }
+          }
+        }
+      if (iopp == -1000) { st |= ST_BAD_ARGUMENT; iopp = i; jopp = j; }
+      if (lsval <= 0.0) {
+        ip1 = load4(a.W1, P, c);
+        ip2 = ifc_read(a, 1, iopp, jopp, lin, ok);
+      } else {
+        ip2 = load4(a.W2, P, c);
+        ip1 = ifc_read(a, 0, iopp, jopp, lin, ok);
+      }
+    } else {
+      // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33)
+      double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
+      double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
+      double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
+      double gx = a.nrm[c], gy = a.nrm[c + P.plane];
+      double nm = sqrt(gx * gx + gy * gy);
+      double lv = lsval;
+      if (fabs(lv) > ds) lv = copysign(ds, lv);
+      double hx = gx / nm, hy = gy / nm;
+      double ilx = ccx - lv * hx, ily = ccy - lv * hy;
+      bool resolve = (MODE == IFC_RIEMANN);
+      ip2 = ifc_bilinear(a, 1, ilx + ds * hx, ily + ds * hy, lin, resolve, ok);
+      ip1 = ifc_bilinear(a, 0, ilx - ds * hx, ily - ds * hy, lin, resolve, ok);
+    }
+    double* o = a.out + (int64_t)k * IFC_OUT;
+    if (!ok) {
+      st |= ST_SCHEDULE_LIMIT;
+      __threadfence();
+      ((volatile int*)a.done)[k] = 2;
+      continue;
+    }
+    // mixed Riemann problem in the normal frame (e.g. GFM_riemann.cpp:76-122)
+    double u1n = ip1.b * nx + ip1.c * ny;
+    double u2n = ip2.b * nx + ip2.c * ny;
+    double t1x = ip1.b - u1n * nx, t1y = ip1.c - u1n * ny;
+    double t2x = ip2.b - u2n * nx, t2y = ip2.c - u2n * ny;
+    V4 Lp = V4{ip1.a, u1n, 0.0, (1e-6 < ip1.d) ? ip1.d : 1e-6};
+    V4 Rp = V4{ip2.a, u2n, 0.0, (1e-6 < ip2.d) ? ip2.d : 1e-6};
+    bool ok1 = true, ok2 = true;
+    V4 Ls = prims_to_cons(P.g1, P.p1, Lp, &ok1);
+    V4 Rs = prims_to_cons(P.g2, P.p2, Rp, &ok2);
+    if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
+    MixedStar m = mixed_rs(P.gas1, P.gas2, Ls, Rs, &st, &iters);
+    double snx = m.u_star * nx, sny = m.u_star * ny;
+    if (MODE == IFC_MODIFIED) {
+      double u1x, u1y, u2x, u2y;
+      if (a.slip) { u1x = snx + t1x; u1y = sny + t1y; u2x = snx + t2x; u2y = sny + t2y; }
+      else if (lsval <= 0.0) { u1x = snx + t1x; u1y = sny + t1y; u2x = snx + t1x; u2y = sny + t1y; }
+      else { u1x = snx + t2x; u1y = sny + t2y; u2x = snx + t2x; u2y = sny + t2y; }
+      if (lsval <= 0.0) {
+        o[0] = eos_isentropic_extrapolation(P.g1, P.p1, m.rho_star_L, m.p_star, load4(a.W1, P, c).d);
+        o[1] = m.rho_star_R; o[2] = u2x; o[3] = u2y; o[4] = m.p_star;
+      } else {
+        o[0] = eos_isentropic_extrapolation(P.g2, P.p2, m.rho_star_R, m.p_star, load4(a.W2, P, c).d);
+        o[1] = m.rho_star_L; o[2] = u1x; o[3] = u1y; o[4] = m.p_star;
+      }
+      o[5] = snx; o[6] = sny;
+    } else {
+      if (lsval <= 0.0) { o[0] = m.rho_star_L; o[1] = snx + t1x; o[2] = sny + t1y; o[3] = m.p_star; }
+      else { o[0] = m.rho_star_R; o[1] = snx + t2x; o[2] = sny + t2y; o[3] = m.p_star; }
+      o[4] = snx; o[5] = sny;
+    }
+    __threadfence();
+    ((volatile int*)a.done)[k] = 1;
+  }
+  uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+  unsigned wit = __reduce_add_sync(0xffffffffu, (unsigned)iters);
+  if ((threadIdx.x & 31) == 0) {
+    if (wst) atomicOr(&a.D->status, wst);
+    if (wit) atomicAdd(&a.D->newton_iters, (unsigned long long)wit);
+  }
+}
+
+// Reset of the per-step interface bookkeeping.
+__global__ void k_ifc_reset(int* done, int cap, unsigned int* ticket, const DevTime* D) {
+  if (!D->active) return;
+  int n = D->n_ifc;
+  if (n > cap) n = cap;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) done[k] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ticket = 0u;
+}
+
+// Scatter of the interface results into the primitive grids.
+//   Riemann / real GFM: prims of the real fluid := star state
+//   modified GFM: new_prims (Wc) real density and ghost state
+struct ScatterArgs {
+  GridP P;
+  double* W1; double* W2;    // written grids
+  const double* phi;
+  const int* list;
+  const double* out;
+  double* vel;               // extension velocity seeds (or null)
+  DevTime* D;
+  int modified;
+};
+
+__global__ void k_ifc_scatter(ScatterArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int n = a.D->n_ifc;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int64_t lin = a.list[k];
+    int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
+    int64_t c = cidx(P, i, j);
+    const double* o = a.out + (int64_t)k * IFC_OUT;
+    bool f1 = a.phi[c] <= 0.0;
+    if (a.modified) {
+      double* Wr = f1 ? a.W1 : a.W2;
+      double* Wg = f1 ? a.W2 : a.W1;
+      Wr[c] = o[0];
+      store4(Wg, P, c, V4{o[1], o[2], o[3], o[4]});
+      if (a.vel) { a.vel[c] = o[5]; a.vel[c + P.plane] = o[6]; }
+    } else {
+      store4(f1 ? a.W1 : a.W2, P, c, V4{o[0], o[1], o[2], o[3]});
+      if (a.vel) { a.vel[c] = o[4]; a.vel[c + P.plane] = o[5]; }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// End of the ghost fill: primitives -> conserved on the whole padded grid,
+// velocity field (real fluid's velocity per cell), and for the original GFM
+// the ghost assignment of sourcecode/GFM_original.cpp:59-118 with the
+// realcells boxes.
+// ---------------------------------------------------------------------------
+struct FinalArgs {
+  GridP P;
+  double* W1; double* W2;        // final primitives (modified in place by OGFM)
+  const double* C1; const double* C2;   // grids converted to conserved (== W unless modified GFM)
+  const double* V1; const double* V2;   // source of the velocity field
+  const uint8_t* mask;
+  const double* phi;
+  double* U1; double* U2;
+  double* vel;
+  DevTime* D;
+  int ogfm;
+  int vel_mode;   // 0: real-fluid velocity, 1: extension seeds (OGFM interfacial), 2: leave vel alone
+};
+
+__global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  uint32_t st = 0;
+  int bb[8] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    int64_t c = cidx(P, i, j);
+    bool f1 = a.phi[c] <= 0.0;
+    if (a.ogfm) {
+      V4 w1 = load4(a.W1, P, c), w2 = load4(a.W2, P, c);
+      if (is_real(P, i, j)) {
+        if (f1) {
+          double rho_new = eos_isentropic_extrapolation(P.g2, P.p2, w2.a, w2.d, w1.d);
+          if (!(rho_new >= 0.0)) st |= ST_UNPHYSICAL;
+          w2 = V4{rho_new, w1.b, w1.c, w1.d};
+          store4(a.W2, P, c, w2);
+          bb[0] = min(bb[0], i - 2); bb[1] = max(bb[1], i + 2); bb[2] = min(bb[2], j - 2); bb[3] = max(bb[3], j + 2);
+        } else {
+          double rho_new = eos_isentropic_extrapolation(P.g1, P.p1, w1.a, w1.d, w2.d);
+          if (!(rho_new >= 0.0)) st |= ST_UNPHYSICAL;
+          w1 = V4{rho_new, w2.b, w2.c, w2.d};
+          store4(a.W1, P, c, w1);
+          bb[4] = min(bb[4], i - 2); bb[5] = max(bb[5], i + 2); bb[6] = min(bb[6], j - 2); bb[7] = max(bb[7], j + 2);
+        }
+      }
+    }
+    bool ok1 = true, ok2 = true;
+    V4 u1 = prims_to_cons(P.g1, P.p1, load4(a.C1, P, c), &ok1);
+    V4 u2 = prims_to_cons(P.g2, P.p2, load4(a.C2, P, c), &ok2);
+    if (!ok1 || !ok2 || !is_physical_state(u1) || !is_physical_state(u2)) st |= ST_UNPHYSICAL;
+    store4(a.U1, P, c, u1);
+    store4(a.U2, P, c, u2);
+    if (a.vel_mode == 0) {
+      const double* V = f1 ? a.V1 : a.V2;
+      a.vel[c] = V[c + P.plane];
+      a.vel[c + P.plane] = V[c + 2 * P.plane];
+    } else if (a.vel_mode == 1) {
+      double vx = 0.0, vy = 0.0;
+      if (a.mask[c]) { const double* V = f1 ? a.V1 : a.V2; vx = V[c + P.plane]; vy = V[c + 2 * P.plane]; }
+      a.vel[c] = vx;
+      a.vel[c + P.plane] = vy;
+    }
+  }
+  uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+  if ((threadIdx.x & 31) == 0 && wst) atomicOr(&a.D->status, wst);
+  if (a.ogfm) {
+    for (int q = 0; q < 8; q++) {
+      int v = bb[q];
+      if (q & 1) { for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o)); }
+      else { for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o)); }
+      if ((threadIdx.x & 31) == 0) {
+        if (q & 1) { if (v != INT_MIN) atomicMax(&a.D->rc[q], v); }
+        else { if (v != INT_MAX) atomicMin(&a.D->rc[q], v); }
+      }
+    }
+  }
+}
+
+// realcells clamp of sourcecode/GFM_original.cpp:120-128
+__global__ void k_rc_clamp(GridP P, DevTime* D) {
+  if (!D->active) return;
+  for (int f = 0; f < 2; f++) {
+    int* r = &D->rc[4 * f];
+    r[0] = max(r[0], P.g);
+    r[1] = min(r[1], P.g + P.Ny);
+    r[2] = max(r[2], P.g);
+    r[3] = min(r[3], P.g + P.Nx);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// extrapolate_extension_vfield sweep (sourcecode/extrapolate_extension_vfield.cpp:4-122)
+// with the mirror BCs of the vector field, one launch per iteration.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_ext_vel(GridP P, const double* S, double* Dd, const double* phi,
+                                                const double* nrm, const uint8_t* mask, const DevTime* D) {
+  if (!D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const double dt = 0.5 * dmin_std(P.dx, P.dy);
+  GridP Q = P;
+  Q.bcL = Q.bcR = Q.bcB = Q.bcT = GFM_BC_TRANSMISSIVE;
+  Q.periodic = false;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    BCSrc s = bc_source(Q, i, j);
+    int64_t c = cidx(P, s.i, s.j);
+    double vx = S[c], vy = S[c + P.plane];
+    double gx = nrm[c], gy = nrm[c + P.plane];
+    double nn = sqrt(gx * gx + gy * gy);
+    if (!mask[c] && nn > 1e-12) {
+      double nx = gx / nn, ny = gy / nn;
+      double cx = (dt / P.dx) * nx, cy = (dt / P.dy) * ny;
+      double dxx, dxy, dyx, dyy;
+      if (phi[c] <= 0.0) {
+        if (nx > 0.0) { dxx = S[c + 1] - vx; dxy = S[c + 1 + P.plane] - vy; }
+        else { dxx = vx - S[c - 1]; dxy = vy - S[c - 1 + P.plane]; }
+        if (ny > 0.0) { dyx = S[c + P.pitch] - vx; dyy = S[c + P.pitch + P.plane] - vy; }
+        else { dyx = vx - S[c - P.pitch]; dyy = vy - S[c - P.pitch + P.plane]; }
+        vx = (vx + cx * dxx) + cy * dyx;
+        vy = (vy + cx * dxy) + cy * dyy;
+      } else {
+        if (nx > 0.0) { dxx = vx - S[c - 1]; dxy = vy - S[c - 1 + P.plane]; }
+        else { dxx = S[c + 1] - vx; dxy = S[c + 1 + P.plane] - vy; }
+        if (ny > 0.0) { dyx = vx - S[c - P.pitch]; dyy = vy - S[c - P.pitch + P.plane]; }
+        else { dyx = S[c + P.pitch] - vx; dyy = S[c + P.pitch + P.plane] - vy; }
+        vx = (vx - cx * dxx) - cy * dyx;
+        vy = (vy - cx * dxy) - cy * dyy;
+      }
+    }
+    int64_t o = cidx(P, i, j);
+    Dd[o] = vx;
+    Dd[o + P.plane] = vy;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Level set (the project's Levelset; see the oracle for the same definition)
+//   order 1: phi + dt L(phi), first-order upwind
+//   order 5: HOUC5 in space, 3-stage TVD Runge-Kutta (Shu-Osher) in time
+//   L(f) = -(u f_x + v f_y) with the cell-centred velocity field
+// Ghost cells: mirror (or periodic) copies, computed by their own threads.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double houc5(double a, const double* f, int64_t c, int64_t st, double inv60h) {
+  if (a >= 0.0)
+    return (-2.0 * f[c - 3 * st] + 15.0 * f[c - 2 * st] - 60.0 * f[c - st] + 20.0 * f[c] + 30.0 * f[c + st] -
+            3.0 * f[c + 2 * st]) * inv60h;
+  return (3.0 * f[c - 2 * st] - 30.0 * f[c - st] - 20.0 * f[c] + 60.0 * f[c + st] - 15.0 * f[c + 2 * st] +
+          2.0 * f[c + 3 * st]) * inv60h;
+}
+
+template <int ORDER, int STAGE>
+__global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, const double* phi, double* out,
+                                                  const double* vel, const DevTime* D) {
+  if (!D->active) return;
+  const double dt = D->dt;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  GridP Q = P;
+  if (!P.periodic) { Q.bcL = Q.bcR = Q.bcB = Q.bcT = GFM_BC_TRANSMISSIVE; }
+  const double idx = 1.0 / P.dx, idy = 1.0 / P.dy;
+  const double i60x = 1.0 / (60.0 * P.dx), i60y = 1.0 / (60.0 * P.dy);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    BCSrc s = bc_source(Q, i, j);
+    int64_t c = cidx(P, s.i, s.j);
+    double u = vel[c], v = vel[c + P.plane];
+    double fx, fy;
+    if (ORDER == 1) {
+      fx = (u >= 0.0) ? (X[c] - X[c - 1]) * idx : (X[c + 1] - X[c]) * idx;
+      fy = (v >= 0.0) ? (X[c] - X[c - P.pitch]) * idy : (X[c + P.pitch] - X[c]) * idy;
+    } else {
+      fx = houc5(u, X, c, 1, i60x);
+      fy = houc5(v, X, c, P.pitch, i60y);
+    }
+    double L = -(u * fx + v * fy);
+    double r;
+    if (ORDER == 1 || STAGE == 1) r = X[c] + dt * L;
+    else if (STAGE == 2) r = 0.75 * phi[c] + 0.25 * (X[c] + dt * L);
+    else r = (1.0 / 3.0) * phi[c] + (2.0 / 3.0) * (X[c] + dt * L);
+    out[cidx(P, i, j)] = r;
+  }
+}
+
+// S(phi0) = phi0 / sqrt(phi0^2 + h^2), cached for the reinitialisation
+__global__ void k_reinit_sign(GridP P, const double* phi, double* S, const DevTime* D) {
+  if (!D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const double h = dmin_std(P.dx, P.dy);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    int64_t c = cidx(P, i, j);
+    double p0 = phi[c];
+    S[c] = p0 / sqrt(p0 * p0 + h * h);
+  }
+}
+
+// one Sussman-Smereka-Osher iteration with Godunov upwinding
+__global__ void __launch_bounds__(256) k_reinit_iter(GridP P, const double* cur, const double* S, double* out,
+                                                     const DevTime* D) {
+  if (!D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  GridP Q = P;
+  if (!P.periodic) { Q.bcL = Q.bcR = Q.bcB = Q.bcT = GFM_BC_TRANSMISSIVE; }
+  const double h = dmin_std(P.dx, P.dy);
+  const double dtau = 0.5 * h;
+  const double idx = 1.0 / P.dx, idy = 1.0 / P.dy;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    BCSrc s = bc_source(Q, i, j);
+    int64_t c = cidx(P, s.i, s.j);
+    double f = cur[c];
+    double sg = S[c];
+    double a = (f - cur[c - 1]) * idx;
+    double b = (cur[c + 1] - f) * idx;
+    double cc = (f - cur[c - P.pitch]) * idy;
+    double d = (cur[c + P.pitch] - f) * idy;
+    double gx, gy;
+    if (sg > 0.0) {
+      double ap = dmax_std(a, 0.0), bm = dmin_std(b, 0.0), cp = dmax_std(cc, 0.0), dm = dmin_std(d, 0.0);
+      gx = dmax_std(ap * ap, bm * bm);
+      gy = dmax_std(cp * cp, dm * dm);
+    } else {
+      double am = dmin_std(a, 0.0), bp = dmax_std(b, 0.0), cm = dmin_std(cc, 0.0), dp = dmax_std(d, 0.0);
+      gx = dmax_std(am * am, bp * bp);
+      gy = dmax_std(cm * cm, dp * dp);
+    }
+    double G = sqrt(gx + gy) - 1.0;
+    out[cidx(P, i, j)] = f - dtau * sg * G;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fluid mass (sim_twofluid::fluid_mass, sourcecode/sim_twofluid.cpp:1803-1827):
+// fixed-order two-pass sum
+// ---------------------------------------------------------------------------
+__global__ void k_mass_partial(GridP P, const double* U, const double* phi, double sign, double* part) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  const int64_t n = (int64_t)P.Nx * P.Ny;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.Nx) + P.g, j = (int)(k % P.Nx) + P.g;
+    int64_t c = cidx(P, i, j);
+    double ls = phi ? phi[c] : -1.0;
+    if (sign * ls > 0.0) acc += U[c] * P.dx * P.dy;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_mass_final(const double* part, int nb, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += part[b];
+    *out = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+static int grid_blocks(int64_t n, int per) {
+  int64_t b = (n + per - 1) / per;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
+  const GridP& P = ctx->P;
+  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  for (int it = 0; it < N; it++) {
+    ExtrapArgs e;
+    e.P = P;
+    e.S1 = ctx->W[0]; e.S2 = ctx->W[1];
+    e.D1 = ctx->Wt[0]; e.D2 = ctx->Wt[1];
+    e.phi = ctx->phi; e.nrm = ctx->nrm; e.mask = ctx->mask; e.D = ctx->dtime;
+    e.mgfm = mgfm ? 1 : 0;
+    k_extrap<<<blocks, 256, 0, ctx->stream>>>(e);
+    for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
+  }
+}
+
+static void run_ext_vfield(gfm_ctx* ctx, int N) {
+  const GridP& P = ctx->P;
+  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  for (int it = 0; it < N; it++) {
+    k_ext_vel<<<blocks, 256, 0, ctx->stream>>>(P, ctx->vel, ctx->vel_t, ctx->phi, ctx->nrm, ctx->mask, ctx->dtime);
+    double* t = ctx->vel; ctx->vel = ctx->vel_t; ctx->vel_t = t;
+  }
+}
+
+void launch_cfl(gfm_ctx* ctx, double CFL, double T) { (void)ctx; (void)CFL; (void)T; }
+
+void launch_cfl_ogfm(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter) {
+  launch_cfl_impl(ctx, CFL, T, ogfm, counter);
+}
+
+void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
+  const GridP& P = ctx->P;
+  cudaStream_t s = ctx->stream;
+  const int variant = m->gfm;
+  const bool modified = variant == GFM_MODIFIED;
+  // 1. conversion, gradient of phi, interfacial mask, chunk counts
+  PrimArgs pa;
+  pa.P = P;
+  pa.U1 = ctx->U[0]; pa.U2 = ctx->U[1];
+  pa.W1 = ctx->W[0]; pa.W2 = ctx->W[1];
+  pa.Wc1 = modified ? ctx->Wc[0] : nullptr;
+  pa.Wc2 = modified ? ctx->Wc[1] : nullptr;
+  pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
+  pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
+  pa.check_both = (variant == GFM_OGFM || variant == GFM_RIEMANN) ? 1 : 0;
+  k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa);
+  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
+                                              ctx->ifc_map, ctx->dtime);
+  const bool ext = m->use_extension_vfield != 0;
+  int fblocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  if (variant == GFM_OGFM) {
+    run_extrap(ctx, 6, false);
+    FinalArgs f;
+    f.P = P;
+    f.W1 = ctx->W[0]; f.W2 = ctx->W[1];
+    f.C1 = ctx->W[0]; f.C2 = ctx->W[1];
+    f.V1 = ctx->W[0]; f.V2 = ctx->W[1];
+    f.mask = ctx->mask; f.phi = ctx->phi;
+    f.U1 = ctx->U[0]; f.U2 = ctx->U[1];
+    f.vel = ctx->vel; f.D = ctx->dtime;
+    f.ogfm = 1;
+    f.vel_mode = ext ? 1 : 0;
+    k_finalize<<<fblocks, 256, 0, s>>>(f);
+    k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime);
+    if (ext) run_ext_vfield(ctx, 20);
+    return;
+  }
+  // 2. extrapolate_vector(2) before the interface loop (Riemann, modified)
+  if (variant != GFM_REAL) run_extrap(ctx, 2, false);
+  // 3. interface loop
+  int cap = P.Nx * P.Ny;
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime);
+  IfcArgs ia;
+  ia.P = P;
+  ia.W1 = ctx->W[0]; ia.W2 = ctx->W[1];
+  ia.phi = ctx->phi; ia.nrm = ctx->nrm; ia.mask = ctx->mask;
+  ia.list = ctx->ifc_list; ia.ifc_map = ctx->ifc_map;
+  ia.done = ctx->ifc_done; ia.out = ctx->ifc_out;
+  ia.ticket = (unsigned int*)(ctx->ifc_opp);
+  ia.D = ctx->dtime;
+  ia.slip = m->use_slip_BCs;
+  int iblocks = 152 * 4;
+  if (variant == GFM_RIEMANN) k_interface<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
+  else if (variant == GFM_REAL) k_interface<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
+  else k_interface<IFC_MODIFIED><<<iblocks, 128, 0, s>>>(ia);
+  if (ext) cudaMemsetAsync(ctx->vel, 0, sizeof(double) * 2 * P.plane, s);
+  ScatterArgs sa;
+  sa.P = P;
+  sa.W1 = modified ? ctx->Wc[0] : ctx->W[0];
+  sa.W2 = modified ? ctx->Wc[1] : ctx->W[1];
+  sa.phi = ctx->phi; sa.list = ctx->ifc_list; sa.out = ctx->ifc_out;
+  sa.vel = ext ? ctx->vel : nullptr;
+  sa.D = ctx->dtime;
+  sa.modified = modified ? 1 : 0;
+  k_ifc_scatter<<<grid_blocks(cap, 256), 256, 0, s>>>(sa);
+  // 4. extrapolate_vector(6) / extrapolate_vector_mgfm(6)
+  run_extrap(ctx, 6, modified);
+  // 5. conserved grids and velocity field
+  FinalArgs f;
+  f.P = P;
+  f.W1 = ctx->W[0]; f.W2 = ctx->W[1];
+  f.C1 = modified ? ctx->Wc[0] : ctx->W[0];
+  f.C2 = modified ? ctx->Wc[1] : ctx->W[1];
+  f.V1 = ctx->W[0]; f.V2 = ctx->W[1];
+  f.mask = ctx->mask; f.phi = ctx->phi;
+  f.U1 = ctx->U[0]; f.U2 = ctx->U[1];
+  f.vel = ctx->vel; f.D = ctx->dtime;
+  f.ogfm = 0;
+  f.vel_mode = ext ? 2 : 0;
+  k_finalize<<<fblocks, 256, 0, s>>>(f);
+  if (ext) run_ext_vfield(ctx, 20);
+}
+
+void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
+  const GridP& P = ctx->P;
+  cudaStream_t s = ctx->stream;
+  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  if (m->ls_order == 1) {
+    k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime);
+  } else {
+    k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime);
+    k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime);
+    k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime);
+  }
+  { double* t = ctx->phi; ctx->phi = ctx->phi_a; ctx->phi_a = t; }
+}
+
+void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m) {
+  const GridP& P = ctx->P;
+  cudaStream_t s = ctx->stream;
+  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime);
+  for (int it = 0; it < m->reinit_iters; it++) {
+    k_reinit_iter<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->phi_a, ctx->dtime);
+    double* t = ctx->phi; ctx->phi = ctx->phi_a; ctx->phi_a = t;
+  }
+}
+
+void launch_end_step(gfm_ctx* ctx) { k_end_step<<<1, 1, 0, ctx->stream>>>(ctx->dtime); }
+
+void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out) {
+  const GridP& P = ctx->P;
+  int nb = 256;
+  k_mass_partial<<<nb, 256, 0, ctx->stream>>>(P, sign < 0.0 ? ctx->U[0] : ctx->U[ctx->two_fluid ? 1 : 0],
+                                               ctx->two_fluid ? ctx->phi : nullptr, sign, part);
+  k_mass_final<<<1, 32, 0, ctx->stream>>>(part, nb, out);
+}
+
+}  // namespace gfm

@@ -1,0 +1,342 @@
+"""Python host side of the GB300 two-fluid ghost-fluid Euler step.
+
+A thin ctypes layer over the C ABI in include/gfm_gb300.h (libgfm_gb300.so),
+mirroring the reference's host objects:
+
+    GFM_settingsfile   headers/GFM_settingsfile.hpp:9-60 (same keys, plus
+                       nsteps / reinit_every / reinit_iters / ls_order)
+    sim_onefluid       sourcecode/sim_onefluid.cpp:12-64  (run_sim)
+    sim_twofluid       sourcecode/sim_twofluid.cpp:27-103 (run_sim)
+    Context            the device-resident grids behind both
+
+The library is the only compute path: if libgfm_gb300.so cannot be loaded,
+every entry point raises.  There is no CPU fallback.
+"""
+import ctypes
+import os
+import platform
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", platform.machine(), "libgfm_gb300.so")
+
+BC = {"transmissive": 0, "reflective": 1, "periodic": 2}
+FS = {"Godunov": 0, "MUSCL": 1}
+GFM = {"OGFM": 0, "riemannGFM": 1, "realGFM": 2, "MGFM": 3}
+ITM = {"LS1": (1, 1), "LS5": (5, 1)}   # (advection order, reinitialise every k steps)
+
+ST_BITS = {
+    1 << 0: "UNPHYSICAL_STATE",
+    1 << 1: "NEWTON_NO_CONVERGE",
+    1 << 2: "VACUUM",
+    1 << 3: "NAN_DETECTED",
+    1 << 4: "DT_NONPOSITIVE",
+    1 << 5: "SCHEDULE_LIMIT",
+}
+
+
+class GridDesc(ctypes.Structure):
+    """sim_info + binarySGparams (gfm_grid_desc)."""
+    _fields_ = [("Nx", ctypes.c_int), ("Ny", ctypes.c_int), ("numGC", ctypes.c_int),
+                ("x0", ctypes.c_double), ("y0", ctypes.c_double), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("BC_L", ctypes.c_int), ("BC_R", ctypes.c_int), ("BC_B", ctypes.c_int), ("BC_T", ctypes.c_int),
+                ("gamma1", ctypes.c_double), ("pinf1", ctypes.c_double),
+                ("gamma2", ctypes.c_double), ("pinf2", ctypes.c_double)]
+
+    @property
+    def shape(self):
+        return (self.Ny + 2 * self.numGC, self.Nx + 2 * self.numGC)
+
+
+class MethodDesc(ctypes.Structure):
+    """Strategy choices of set_sim_methods (gfm_method_desc)."""
+    _fields_ = [("fs", ctypes.c_int), ("gfm", ctypes.c_int), ("ls_order", ctypes.c_int),
+                ("reinit_every", ctypes.c_int), ("reinit_iters", ctypes.c_int),
+                ("use_extension_vfield", ctypes.c_int), ("use_slip_BCs", ctypes.c_int),
+                ("CFL", ctypes.c_double), ("T", ctypes.c_double)]
+
+
+class GFMError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load libgfm_gb300.so once (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GFMError("libgfm_gb300.so is not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, D, V = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    pd = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "gfm_ctx_create": [ctypes.POINTER(GridDesc), I, ctypes.POINTER(P)],
+        "gfm_ctx_destroy": [P],
+        "gfm_set_stream": [P, V],
+        "gfm_upload": [P, I, pd], "gfm_download": [P, I, pd],
+        "gfm_upload_phi": [P, pd], "gfm_download_phi": [P, pd],
+        "gfm_set_time": [P, D, I],
+        "gfm_download_mask": [P, ctypes.POINTER(ctypes.c_uint8)],
+        "gfm_get_time": [P, pd, ctypes.POINTER(I), pd],
+        "gfm_compute_dt": [P, D, D],
+        "gfm_set_ghost_states": [P, ctypes.POINTER(MethodDesc)],
+        "gfm_fs_update": [P, I, I],
+        "gfm_ls_update": [P, ctypes.POINTER(MethodDesc)],
+        "gfm_apply_bcs": [P, I],
+        "gfm_step": [P, ctypes.POINTER(MethodDesc), I],
+        "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
+        "gfm_clear_device_status": [P],
+        "gfm_get_stats": [P, ctypes.POINTER(ctypes.c_int64)] * 1 + [ctypes.POINTER(ctypes.c_int64)] * 2,
+        "gfm_fluid_mass": [P, D, pd],
+        "gfm_rs_pure_batch": [I, I, D, D, V, V, V, V, V],
+        "gfm_rs_mixed_batch": [I, D, D, D, D, V, V, V, V, V],
+        "gfm_case_params": [ctypes.c_char_p, ctypes.c_char_p, I, I, ctypes.POINTER(GridDesc), pd],
+        "gfm_case_init": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(GridDesc), pd, pd, pd],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    L.gfm_version.restype = ctypes.c_char_p
+    L.gfm_version.argtypes = []
+    _lib = L
+    return L
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise GFMError("%s failed with gfm_status_t %d" % (what, rc))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def status_names(bits):
+    return [n for b, n in ST_BITS.items() if bits & b]
+
+
+# ---------------------------------------------------------------------------
+# test cases (set_sim_parameters + set_sim_ICs)
+# ---------------------------------------------------------------------------
+def case_params(sim_type, test_case, Nx, Ny):
+    """Returns (GridDesc, T) of a named test case."""
+    d = GridDesc()
+    T = ctypes.c_double(0.0)
+    _check(lib().gfm_case_params(sim_type.encode(), test_case.encode(), Nx, Ny, ctypes.byref(d), ctypes.byref(T)),
+           "gfm_case_params(%s, %s)" % (sim_type, test_case))
+    return d, T.value
+
+
+def case_init(sim_type, test_case, desc):
+    """Initial conditions as host arrays: U1 (4,nr,nc), U2 (4,nr,nc) or None, phi (nr,nc) or None."""
+    nr, nc = desc.shape
+    two = sim_type == "twofluid"
+    U1 = np.zeros((4, nr, nc))
+    U2 = np.zeros((4, nr, nc)) if two else None
+    phi = np.zeros((nr, nc)) if two else None
+    _check(lib().gfm_case_init(sim_type.encode(), test_case.encode(), ctypes.byref(desc), _dptr(U1),
+                               _dptr(U2) if two else None, _dptr(phi) if two else None),
+           "gfm_case_init(%s, %s)" % (sim_type, test_case))
+    return U1, U2, phi
+
+
+def method(fs="MUSCL", gfm="riemannGFM", itm="LS5", CFL=0.6, T=1.0, reinit_every=None, reinit_iters=5,
+           use_extension_vfield=False, use_slip_BCs=False):
+    order, every = ITM[itm]
+    m = MethodDesc()
+    m.fs = FS[fs]
+    m.gfm = GFM[gfm]
+    m.ls_order = order
+    m.reinit_every = every if reinit_every is None else reinit_every
+    m.reinit_iters = reinit_iters
+    m.use_extension_vfield = int(bool(use_extension_vfield))
+    m.use_slip_BCs = int(bool(use_slip_BCs))
+    m.CFL = CFL
+    m.T = T
+    return m
+
+
+# ---------------------------------------------------------------------------
+# device context
+# ---------------------------------------------------------------------------
+class Context:
+    """Device-resident grids of one instance (gfm_ctx)."""
+
+    def __init__(self, desc, two_fluid=True, stream=None):
+        self.desc = desc
+        self.two_fluid = bool(two_fluid)
+        self._p = ctypes.c_void_p()
+        _check(lib().gfm_ctx_create(ctypes.byref(desc), int(self.two_fluid), ctypes.byref(self._p)),
+               "gfm_ctx_create")
+        if stream is not None:
+            _check(lib().gfm_set_stream(self._p, ctypes.c_void_p(stream)), "gfm_set_stream")
+
+    def close(self):
+        if self._p:
+            lib().gfm_ctx_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        _check(lib().gfm_set_stream(self._p, ctypes.c_void_p(stream)), "gfm_set_stream")
+
+    def upload(self, U1, U2=None, phi=None, t=0.0, numsteps=0):
+        U1 = np.ascontiguousarray(U1, dtype=np.float64)
+        _check(lib().gfm_upload(self._p, 1, _dptr(U1)), "gfm_upload(1)")
+        if self.two_fluid:
+            U2 = np.ascontiguousarray(U2, dtype=np.float64)
+            phi = np.ascontiguousarray(phi, dtype=np.float64)
+            _check(lib().gfm_upload(self._p, 2, _dptr(U2)), "gfm_upload(2)")
+            _check(lib().gfm_upload_phi(self._p, _dptr(phi)), "gfm_upload_phi")
+        _check(lib().gfm_set_time(self._p, t, numsteps), "gfm_set_time")
+
+    def download(self):
+        nr, nc = self.desc.shape
+        U1 = np.empty((4, nr, nc))
+        _check(lib().gfm_download(self._p, 1, _dptr(U1)), "gfm_download(1)")
+        if not self.two_fluid:
+            return U1, None, None
+        U2 = np.empty((4, nr, nc))
+        phi = np.empty((nr, nc))
+        _check(lib().gfm_download(self._p, 2, _dptr(U2)), "gfm_download(2)")
+        _check(lib().gfm_download_phi(self._p, _dptr(phi)), "gfm_download_phi")
+        return U1, U2, phi
+
+    def mask(self):
+        nr, nc = self.desc.shape
+        out = np.zeros((nr, nc), dtype=np.uint8)
+        _check(lib().gfm_download_mask(self._p, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
+               "gfm_download_mask")
+        return out
+
+    def step(self, m, nsteps=1):
+        _check(lib().gfm_step(self._p, ctypes.byref(m), nsteps), "gfm_step")
+
+    def time(self):
+        t = ctypes.c_double()
+        n = ctypes.c_int()
+        dt = ctypes.c_double()
+        _check(lib().gfm_get_time(self._p, ctypes.byref(t), ctypes.byref(n), ctypes.byref(dt)), "gfm_get_time")
+        return t.value, n.value, dt.value
+
+    def status(self):
+        s = ctypes.c_uint32()
+        _check(lib().gfm_get_device_status(self._p, ctypes.byref(s)), "gfm_get_device_status")
+        return s.value
+
+    def clear_status(self):
+        _check(lib().gfm_clear_device_status(self._p), "gfm_clear_device_status")
+
+    def stats(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().gfm_get_stats(self._p, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "gfm_get_stats")
+        return {"n_interfacial": a.value, "rounds": b.value, "newton_iters": c.value}
+
+    def fluid_mass(self, interiorsign):
+        m = ctypes.c_double()
+        _check(lib().gfm_fluid_mass(self._p, interiorsign, ctypes.byref(m)), "gfm_fluid_mass")
+        return m.value
+
+
+# ---------------------------------------------------------------------------
+# GFM_settingsfile and the simulation drivers
+# ---------------------------------------------------------------------------
+class GFM_settingsfile:
+    """Whitespace 'key value' lines; unknown keys are ignored (headers/GFM_settingsfile.hpp:24-59)."""
+
+    def __init__(self):
+        self.Nx = 0
+        self.Ny = 0
+        self.CFL = 0.0
+        self.sim_type = ""
+        self.FS = ""
+        self.ITM = ""
+        self.GFM = ""
+        self.test_case = ""
+        self.outputpath = ""
+        self.basename = ""
+        self.nsteps = 0          # 0: run to the test case's end time T
+        self.reinit_every = None
+        self.reinit_iters = 5
+
+    def read_settings_file(self, filename):
+        conv = {"Nx": int, "Ny": int, "CFL": float, "nsteps": int, "reinit_every": int, "reinit_iters": int}
+        with open(filename) as f:
+            for line in f:
+                parts = line.split()
+                if not parts:
+                    continue
+                key = parts[0]
+                if len(parts) < 2:
+                    continue
+                if key in ("Nx", "Ny", "CFL", "sim_type", "FS", "test_case", "ITM", "GFM", "outputpath", "nsteps",
+                           "reinit_every", "reinit_iters"):
+                    setattr(self, key, conv.get(key, str)(parts[1]))
+        if self.sim_type == "onefluid":
+            self.basename = "%s%s-%s-%s-%d-%d" % (self.outputpath, self.sim_type, self.test_case, self.FS, self.Nx,
+                                                 self.Ny)
+        else:
+            self.basename = "%s%s-%s-%s-%s-%d-%d" % (self.outputpath, self.GFM, self.ITM, self.test_case, self.FS,
+                                                    self.Nx, self.Ny)
+        return self
+
+
+class sim_base:
+    def run_sim(self, SF):
+        raise NotImplementedError
+
+
+class sim_onefluid(sim_base):
+    """sourcecode/sim_onefluid.cpp:12-64 on the GPU."""
+
+    def run_sim(self, SF, stream=None):
+        desc, T = case_params("onefluid", SF.test_case, SF.Nx, SF.Ny)
+        U1, _, _ = case_init("onefluid", SF.test_case, desc)
+        ctx = Context(desc, two_fluid=False, stream=stream)
+        ctx.upload(U1)
+        m = method(fs=SF.FS, CFL=SF.CFL, T=T)
+        nsteps = SF.nsteps if SF.nsteps > 0 else 10 ** 9
+        done = 0
+        while done < nsteps:
+            chunk = min(256, nsteps - done)
+            ctx.step(m, chunk)
+            done += chunk
+            t, n, _ = ctx.time()
+            if t >= T:
+                break
+        self.ctx = ctx
+        return ctx
+
+
+class sim_twofluid(sim_base):
+    """sourcecode/sim_twofluid.cpp:27-103 on the GPU."""
+
+    def run_sim(self, SF, stream=None):
+        desc, T = case_params("twofluid", SF.test_case, SF.Nx, SF.Ny)
+        U1, U2, phi = case_init("twofluid", SF.test_case, desc)
+        ctx = Context(desc, two_fluid=True, stream=stream)
+        ctx.upload(U1, U2, phi)
+        m = method(fs=SF.FS, gfm=SF.GFM, itm=SF.ITM, CFL=SF.CFL, T=T, reinit_every=SF.reinit_every,
+                   reinit_iters=SF.reinit_iters)
+        nsteps = SF.nsteps if SF.nsteps > 0 else 10 ** 9
+        done = 0
+        while done < nsteps:
+            chunk = min(256, nsteps - done)
+            ctx.step(m, chunk)
+            done += chunk
+            t, n, _ = ctx.time()
+            if t >= T:
+                break
+        self.ctx = ctx
+        return ctx

@@ -1,0 +1,133 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Both follow the same operation order with no contracted multiply-adds, so
+the expected difference is zero; the bar written into the asserts is the
+spec tolerance, relative L1 <= 1e-10 per conserved field over real
+cells (and for phi), with interfacial masks bit-exact.
+"""
+import numpy as np
+import pytest
+
+import gfm_gb300 as g
+import oracle_binding as orc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+def rel_l1(a, b):
+    den = np.abs(b).sum()
+    return np.abs(a - b).sum() / (den if den > 0 else 1.0)
+
+
+def real(desc, a):
+    gc = desc.numGC
+    return a[..., gc:gc + desc.Ny, gc:gc + desc.Nx]
+
+
+ONEFLUID = [
+    ("TTC1_x", 64, 8, "MUSCL"), ("TTC1_y", 8, 64, "MUSCL"), ("TTC2_x", 64, 8, "MUSCL"),
+    ("TTC3_x", 64, 8, "MUSCL"), ("TTC4_y", 8, 64, "MUSCL"), ("TTC5_x", 64, 8, "MUSCL"),
+    ("TTC1_x", 64, 8, "Godunov"), ("TTC3_y", 8, 64, "Godunov"),
+    ("circularexplosion", 40, 40, "MUSCL"), ("circularexplosion", 36, 28, "Godunov"),
+]
+
+
+@pytest.mark.parametrize("case,Nx,Ny,fs", ONEFLUID)
+def test_onefluid_parity(case, Nx, Ny, fs):
+    desc, T = g.case_params("onefluid", case, Nx, Ny)
+    U, _, _ = g.case_init("onefluid", case, desc)
+    m = g.method(fs=fs, CFL=0.8, T=T)
+    nsteps = 25
+    ctx = g.Context(desc, two_fluid=False)
+    ctx.upload(U)
+    ctx.step(m, nsteps)
+    G, _, _ = ctx.download()
+    t, n, _ = ctx.time()
+    st = ctx.status()
+    ctx.close()
+    orc.clear_status()
+    R, tr, nr_, _ = orc.onefluid_run(desc, m, U, nsteps)
+    assert n == nr_ and t == tr
+    for k in range(4):
+        assert rel_l1(real(desc, G[k]), real(desc, R[k])) <= TOL
+    assert np.array_equal(G, R), "expected bit-identical fields"
+    assert st == 0 and orc.status() == 0
+
+
+TWOFLUID = [
+    # case, Nx, Ny, GFM, FS, ITM, reinit_every, steps, extension vfield
+    ("shock_bubble", 80, 32, "riemannGFM", "MUSCL", "LS5", 1, 12, False),
+    ("shock_bubble", 80, 32, "realGFM", "MUSCL", "LS5", 5, 12, False),
+    ("shock_bubble", 80, 32, "MGFM", "MUSCL", "LS5", 1, 12, False),
+    ("shock_bubble", 80, 32, "OGFM", "MUSCL", "LS5", 1, 12, False),
+    ("shock_bubble", 80, 32, "riemannGFM", "Godunov", "LS1", 1, 12, False),
+    ("shock_bubble", 64, 24, "riemannGFM", "MUSCL", "LS5", 1, 8, True),
+    ("shock_bubble", 64, 24, "MGFM", "MUSCL", "LS1", 0, 8, True),
+    ("underwater_explosion_sg", 48, 48, "realGFM", "MUSCL", "LS5", 5, 10, False),
+    ("underwater_explosion_sg", 40, 40, "riemannGFM", "MUSCL", "LS5", 1, 8, False),
+    ("ST1_x", 64, 12, "riemannGFM", "MUSCL", "LS5", 1, 15, False),
+    ("ST2_y", 12, 64, "MGFM", "MUSCL", "LS5", 1, 15, False),
+    ("GDA", 24, 24, "OGFM", "MUSCL", "LS5", 1, 10, False),
+    ("shocked_helium_bubble", 64, 20, "riemannGFM", "MUSCL", "LS5", 1, 10, False),
+    ("circularexplosion", 32, 32, "realGFM", "Godunov", "LS1", 1, 10, False),
+]
+
+
+@pytest.mark.parametrize("case,Nx,Ny,gfm,fs,itm,reinit,nsteps,ext", TWOFLUID)
+def test_twofluid_parity(case, Nx, Ny, gfm, fs, itm, reinit, nsteps, ext):
+    desc, T = g.case_params("twofluid", case, Nx, Ny)
+    U1, U2, phi = g.case_init("twofluid", case, desc)
+    m = g.method(fs=fs, gfm=gfm, itm=itm, CFL=0.6, T=T, reinit_every=reinit, use_extension_vfield=ext)
+    ctx = g.Context(desc, two_fluid=True)
+    ctx.upload(U1, U2, phi)
+    ctx.step(m, nsteps)
+    G1, G2, Gphi = ctx.download()
+    mask = ctx.mask()
+    stats = ctx.stats()
+    t, n, _ = ctx.time()
+    st = ctx.status()
+    ctx.close()
+    orc.clear_status()
+    ref = orc.twofluid_run(desc, m, U1, U2, phi, nsteps)
+    assert n == ref["numsteps"] and t == ref["t"]
+    sgn = real(desc, Gphi) <= 0.0
+    for k in range(4):
+        comp_gpu = np.where(sgn, real(desc, G1[k]), real(desc, G2[k]))
+        comp_ref = np.where(real(desc, ref["phi"]) <= 0.0, real(desc, ref["U1"][k]), real(desc, ref["U2"][k]))
+        assert rel_l1(comp_gpu, comp_ref) <= TOL
+    assert rel_l1(real(desc, Gphi), real(desc, ref["phi"])) <= TOL
+    # bit-exact integer work: the interfacial mask of the last ghost fill
+    # (computed from phi before the last level-set update) and its count
+    assert stats["n_interfacial"] == ref["n_interfacial"]
+    assert int(mask.sum()) == ref["n_interfacial"]
+    assert np.array_equal(G1, ref["U1"]) and np.array_equal(G2, ref["U2"]), "expected bit-identical grids"
+    assert np.array_equal(Gphi, ref["phi"])
+    assert st == 0 and orc.status() == 0
+
+
+def test_mask_matches_oracle_definition():
+    desc, T = g.case_params("twofluid", "shock_bubble", 96, 40)
+    U1, U2, phi = g.case_init("twofluid", "shock_bubble", desc)
+    m = g.method(T=T)
+    ctx = g.Context(desc, two_fluid=True)
+    ctx.upload(U1, U2, phi)
+    ctx.step(m, 1)
+    mask = ctx.mask()
+    ctx.close()
+    assert np.array_equal(mask, orc.interfacial_mask(desc, phi))
+
+
+def test_determinism():
+    desc, T = g.case_params("twofluid", "shock_bubble", 120, 48)
+    U1, U2, phi = g.case_init("twofluid", "shock_bubble", desc)
+    m = g.method(T=T)
+    outs = []
+    for _ in range(2):
+        ctx = g.Context(desc, two_fluid=True)
+        ctx.upload(U1, U2, phi)
+        ctx.step(m, 20)
+        outs.append(ctx.download())
+        ctx.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
