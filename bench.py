@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Benchmark of the two-fluid ghost-fluid Euler step on GB300.
+
+Workload: the 1000x400 shock-bubble (light gas gamma=1.648, rho=0.182 bubble
+of radius 0.025 at (0.175, 0.0445) in air; Mach 1.22 shock from x=0.225;
+reflective top/bottom, transmissive ends), Riemann GFM with the HOUC5 level
+set, MUSCL-Hancock + exact Riemann fluxes, CFL 0.6, FP64.  One step is one
+iteration of the reference's time loop (sourcecode/sim_twofluid.cpp:64-88):
+CFL dt, ghost fill, both flux updates, level set, BCs.  Metric: cell-updates
+per second (real cells x steps / device time).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gfm|reference]
+
+Timed region: W untimed steps from the initial condition, then K steps, each
+timed with CUDA events on the library's stream, with a 512 MiB write between
+steps to flush the 129 MB L2.  Multi-GPU: independent replicas per rank
+(torchrun), barrier + max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "phd-2d-gfm_gb300"))
+
+WORKLOAD = {"workload": "shock_bubble_1000x400_riemannGFM_MUSCL_LS5", "test_case": "shock_bubble", "Nx": 1000,
+            "Ny": 400, "GFM": "riemannGFM", "FS": "MUSCL", "ITM": "LS5", "CFL": 0.6, "run_steps": 2000}
+METRIC = "cell-updates/s/GB300 FP64 (1000x400 shock-bubble, Riemann GFM, plain Newton)"
+UNIT = "cell-updates/s"
+FLUX_BYTES_PER_CELL = 128   # both fluids: 32 B read + 32 B write of U each
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gfm", choices=["gfm", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """dram read+write bytes per flux-update launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "flux_update_shock_bubble.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_full_size"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", "gfm_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_gfm(args):
+    import ctypes
+    import numpy as np
+    import torch
+    import gfm_gb300 as g
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    W = WORKLOAD
+    desc, T = g.case_params("twofluid", W["test_case"], W["Nx"], W["Ny"])
+    U1, U2, phi = g.case_init("twofluid", W["test_case"], desc)
+    m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T)
+    stream = torch.cuda.current_stream()
+    ctx = g.Context(desc, two_fluid=True, stream=stream.cuda_stream)
+    ctx.upload(U1, U2, phi)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ctx.step(m, args.warmup)
+    torch.cuda.synchronize()
+    ctx.clear_status()
+    cells = desc.Nx * desc.Ny
+    phases = np.zeros(5)
+    ph = np.zeros(5)
+    L = g.lib()
+    L.gfm_step_timed.argtypes = [ctypes.c_void_p, ctypes.POINTER(g.MethodDesc), ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_double)]
+    L.gfm_launch_count.restype = ctypes.c_int64
+    launches0 = L.gfm_launch_count()
+    newton = 0
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.time()
+    with ClockSampler(local) as clk:
+        for s in range(args.steps):
+            flush.zero_()
+            ph[:] = 0.0
+            rc = L.gfm_step_timed(ctx._p, ctypes.byref(m), 1, ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            if rc != 0:
+                raise RuntimeError("gfm_step_timed failed: %d" % rc)
+            phases += ph
+            if s % 50 == 0:
+                newton += ctx.stats()["newton_iters"] * 0   # statistics read below
+        torch.cuda.synchronize()
+    wall = time.time() - t_wall
+    launches = L.gfm_launch_count() - launches0
+    step_ms = float(phases.sum())
+    if world > 1:
+        import torch.distributed as tdist
+        tt = torch.tensor([step_ms], device="cuda", dtype=torch.float64)
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        step_ms = float(tt.item())
+        tdist.barrier()
+    status = ctx.status()
+    stats = ctx.stats()
+    t_sim, nsteps_done, _ = ctx.time()
+    value = cells * args.steps * world / (step_ms * 1e-3)
+
+    # roofline of the dominant kernel (flux update: both fluids in one launch)
+    flux_ms = phases[2] / args.steps
+    achieved = FLUX_BYTES_PER_CELL * cells / (flux_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 5), "traffic": ncu_traffic(), "kernel": "k_flux_update<MUSCL>",
+            "peak_source": peak_kind,
+            "phase_ms_per_step": {n: round(v / args.steps, 5) for n, v in
+                                  zip(["cfl", "ghost_fill", "flux_update", "level_set", "bcs"], phases)}}
+
+    # end to end through the C ABI: pinned host state -> device -> step -> host
+    e2e = None
+    if args.e2e_steps > 0:
+        shp = desc.shape
+        hU1 = torch.empty((4,) + shp, dtype=torch.float64, pin_memory=True).numpy()
+        hU2 = torch.empty((4,) + shp, dtype=torch.float64, pin_memory=True).numpy()
+        hphi = torch.empty(shp, dtype=torch.float64, pin_memory=True).numpy()
+        G1, G2, Gp = ctx.download()
+        hU1[...] = G1
+        hU2[...] = G2
+        hphi[...] = Gp
+        pd = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(args.e2e_steps):
+            L.gfm_upload(ctx._p, 1, pd(hU1))
+            L.gfm_upload(ctx._p, 2, pd(hU2))
+            L.gfm_upload_phi(ctx._p, pd(hphi))
+            L.gfm_step(ctx._p, ctypes.byref(m), 1)
+            L.gfm_download(ctx._p, 1, pd(hU1))
+            L.gfm_download(ctx._p, 2, pd(hU2))
+            L.gfm_download_phi(ctx._p, pd(hphi))
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        nbytes = (hU1.nbytes + hU2.nbytes + hphi.nbytes)
+        e2e = {"value": cells * args.e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD["workload"], "Nx": desc.Nx, "Ny": desc.Ny, "GFM": W["GFM"],
+                       "FS": W["FS"], "ITM": W["ITM"], "CFL": W["CFL"], "parallelism": "replicas%d" % world,
+                       "l2": "512 MiB flush between timed steps", "steps_from": args.warmup},
+            "roofline": roof, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk.summary(), "device_status": g.status_names(status),
+            "stats_last_step": stats, "sim_time": t_sim, "wall_s": wall}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(desc, m, ctx, args.cpu_seconds)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+def _oracle_steps(desc_fields, m_fields, U1, U2, phi, nsteps, t, numsteps, seconds):
+    """One oracle process: step until `seconds` elapse (at least one step)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_binding as orc
+    import gfm_gb300 as g
+    desc = g.GridDesc(**desc_fields)
+    m = g.MethodDesc(**m_fields)
+    done = 0
+    t0 = time.perf_counter()
+    while done < nsteps:
+        r = orc.twofluid_run(desc, m, U1, U2, phi, 1, t, numsteps)
+        U1, U2, phi, t, numsteps = r["U1"], r["U2"], r["phi"], r["t"], r["numsteps"]
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    return done, time.perf_counter() - t0
+
+
+def _fields(s):
+    return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+def cpu_baseline(desc, m, ctx, seconds):
+    """The CPU oracle (single-threaded, like the reference) timed on this host on
+    a bounded sample: oracle steps of the same workload from the GPU's state."""
+    U1, U2, phi = ctx.download()
+    t, n, _ = ctx.time()
+    done, el = _oracle_steps(_fields(desc), _fields(m), U1, U2, phi, 10 ** 6, t, n, seconds)
+    cells = desc.Nx * desc.Ny
+    return {"value": cells * done / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d oracle steps of the 1000x400 shock-bubble from the GPU state at step %d (%.1f s)"
+                      % (done, n, el)}
+
+
+def run_reference(args):
+    """--impl reference: the CPU oracle (the reference itself cannot be built
+    here) on this host's cores: one independent run per core, aggregate."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import gfm_gb300 as g
+    W = WORKLOAD
+    desc, T = g.case_params("twofluid", W["test_case"], W["Nx"], W["Ny"])
+    U1, U2, phi = g.case_init("twofluid", W["test_case"], desc)
+    m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_binding as orc
+    r = orc.twofluid_run(desc, m, U1, U2, phi, args.warmup)
+    cores = os.cpu_count() or 1
+    budget = 60.0
+    ctxm = mp.get_context("spawn")
+    with ctxm.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.starmap(_oracle_steps, [(_fields(desc), _fields(m), r["U1"], r["U2"], r["phi"], args.steps,
+                                            r["t"], r["numsteps"], budget)] * cores)
+        wall = time.perf_counter() - t0
+    total_steps = sum(d for d, _ in res)
+    cells = desc.Nx * desc.Ny
+    value = cells * total_steps / wall
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, total_steps / cores),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": W["workload"], "Nx": desc.Nx, "Ny": desc.Ny, "GFM": W["GFM"], "FS": W["FS"],
+                       "ITM": W["ITM"], "CFL": W["CFL"], "parallelism": "%d independent CPU runs" % cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d independent oracle runs x up to %d steps from step %d, %.0f s budget"
+                                       % (cores, args.steps, args.warmup, budget)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gfm(args)
+
+
+if __name__ == "__main__":
+    main()

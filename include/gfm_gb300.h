@@ -119,6 +119,16 @@ gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid);
  * T do nothing, as the reference's loop would have stopped. */
 gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps);
 
+/* gfm_step with CUDA events recorded on the context's stream around each
+ * phase; adds the milliseconds of each phase to phase_ms[GFM_NPHASES]:
+ * 0 CFL/dt, 1 ghost fill, 2 flux update (both fluids, one launch),
+ * 3 level set, 4 boundary conditions + end of step. */
+#define GFM_NPHASES 5
+gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
+
+/* number of kernels this library has launched since it was loaded */
+int64_t gfm_launch_count(void);
+
 /* Status word OR-ed by kernels since the last clear (GFM_ST_* bits). */
 gfm_status_t gfm_get_device_status(gfm_ctx* ctx, uint32_t* status);
 gfm_status_t gfm_clear_device_status(gfm_ctx* ctx);

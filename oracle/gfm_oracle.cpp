@@ -431,29 +431,29 @@ struct Levelset {
            (phi[i + 1][j] <= 0.0) != s;
   }
 
-  // HOUC5 one-sided derivative in x for velocity sign a
+  // HOUC5 one-sided derivative for velocity sign a; inv60h = 1 / (60 h)
   static double houc5(double a, double fm3, double fm2, double fm1, double f0, double fp1, double fp2, double fp3,
-                      double h) {
+                      double inv60h) {
     if (a >= 0.0)
-      return (-2.0 * fm3 + 15.0 * fm2 - 60.0 * fm1 + 20.0 * f0 + 30.0 * fp1 - 3.0 * fp2) / (60.0 * h);
-    return (3.0 * fm2 - 30.0 * fm1 - 20.0 * f0 + 60.0 * fp1 - 15.0 * fp2 + 2.0 * fp3) / (60.0 * h);
+      return (-2.0 * fm3 + 15.0 * fm2 - 60.0 * fm1 + 20.0 * f0 + 30.0 * fp1 - 3.0 * fp2) * inv60h;
+    return (3.0 * fm2 - 30.0 * fm1 - 20.0 * f0 + 60.0 * fp1 - 15.0 * fp2 + 2.0 * fp3) * inv60h;
   }
 
-  // rate L(f) = -(u f_x + v f_y) on real cells
+  // rate L(f) = -(u f_x + v f_y) on real cells (derivatives multiply by 1/dx)
   void rate(const griddoubletype& f, const gridVector2dtype& vel, griddoubletype& out) const {
     const int g = params.numGC;
+    const double idx = 1.0 / params.dx, idy = 1.0 / params.dy;
+    const double i60x = 1.0 / (60.0 * params.dx), i60y = 1.0 / (60.0 * params.dy);
     for (int i = g; i < params.Ny + g; i++)
       for (int j = g; j < params.Nx + g; j++) {
         double u = vel[i][j][0], v = vel[i][j][1];
         double fx, fy;
         if (order == 1) {
-          fx = (u >= 0.0) ? (f[i][j] - f[i][j - 1]) / params.dx : (f[i][j + 1] - f[i][j]) / params.dx;
-          fy = (v >= 0.0) ? (f[i][j] - f[i - 1][j]) / params.dy : (f[i + 1][j] - f[i][j]) / params.dy;
+          fx = (u >= 0.0) ? (f[i][j] - f[i][j - 1]) * idx : (f[i][j + 1] - f[i][j]) * idx;
+          fy = (v >= 0.0) ? (f[i][j] - f[i - 1][j]) * idy : (f[i + 1][j] - f[i][j]) * idy;
         } else {
-          fx = houc5(u, f[i][j - 3], f[i][j - 2], f[i][j - 1], f[i][j], f[i][j + 1], f[i][j + 2], f[i][j + 3],
-                     params.dx);
-          fy = houc5(v, f[i - 3][j], f[i - 2][j], f[i - 1][j], f[i][j], f[i + 1][j], f[i + 2][j], f[i + 3][j],
-                     params.dy);
+          fx = houc5(u, f[i][j - 3], f[i][j - 2], f[i][j - 1], f[i][j], f[i][j + 1], f[i][j + 2], f[i][j + 3], i60x);
+          fy = houc5(v, f[i - 3][j], f[i - 2][j], f[i - 1][j], f[i][j], f[i + 1][j], f[i + 2][j], f[i + 3][j], i60y);
         }
         out[i][j] = -(u * fx + v * fy);
       }
@@ -489,16 +489,17 @@ struct Levelset {
     const int g = params.numGC;
     const double h = std::min(params.dx, params.dy);
     const double dtau = 0.5 * h;
+    const double idx = 1.0 / params.dx, idy = 1.0 / params.dy;
     griddoubletype phi0 = phi, next = phi;
     for (int it = 0; it < reinit_iters; it++) {
       for (int i = g; i < params.Ny + g; i++)
         for (int j = g; j < params.Nx + g; j++) {
           double p0 = phi0[i][j];
           double S = p0 / std::sqrt(p0 * p0 + h * h);
-          double a = (phi[i][j] - phi[i][j - 1]) / params.dx;
-          double b = (phi[i][j + 1] - phi[i][j]) / params.dx;
-          double c = (phi[i][j] - phi[i - 1][j]) / params.dy;
-          double d = (phi[i + 1][j] - phi[i][j]) / params.dy;
+          double a = (phi[i][j] - phi[i][j - 1]) * idx;
+          double b = (phi[i][j + 1] - phi[i][j]) * idx;
+          double c = (phi[i][j] - phi[i - 1][j]) * idy;
+          double d = (phi[i + 1][j] - phi[i][j]) * idy;
           double gx, gy;
           if (p0 > 0.0) {
             double ap = std::max(a, 0.0), bm = std::min(b, 0.0), cp = std::max(c, 0.0), dm = std::min(d, 0.0);

@@ -13,6 +13,8 @@ void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out);
 
 using namespace gfm;
 
+std::atomic<long long> gfm::g_launches{0};
+
 namespace {
 
 struct CtxExtra {
@@ -256,6 +258,7 @@ gfm_status_t gfm_fs_update(gfm_ctx* ctx, int fs, int fluid) {
   if (!ctx || (fs != GFM_FS_GODUNOV && fs != GFM_FS_MUSCL)) return GFM_ERR_ARG;
   if (fluid < 1 || fluid > (ctx->two_fluid ? 2 : 1)) return GFM_ERR_ARG;
   launch_fs_update(ctx, fs, 1 << (fluid - 1));
+  launch_commit(ctx, 1 << (fluid - 1), false);
   return last_error();
 }
 
@@ -273,32 +276,68 @@ gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid) {
   return last_error();
 }
 
-gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps) {
+static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms) {
   if (!ctx || nsteps < 0) return GFM_ERR_ARG;
   gfm_status_t r = check_method(ctx, m);
   if (r != GFM_OK) return r;
   ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
+  cudaEvent_t ev[GFM_NPHASES + 1];
+  if (phase_ms)
+    for (int q = 0; q <= GFM_NPHASES; q++) CK(cudaEventCreate(&ev[q]));
+  auto mark = [&](int q) {
+    if (phase_ms) cudaEventRecord(ev[q], ctx->stream);
+  };
   for (int s = 0; s < nsteps; s++) {
     bool ogfm = ctx->two_fluid && m->gfm == GFM_OGFM;
+    mark(0);
     launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
+    mark(1);
     if (ctx->two_fluid) {
       launch_ghost_fill(ctx, m);
+      mark(2);
       launch_fs_update(ctx, m->fs, 3);
+      mark(3);
       launch_ls_update(ctx, m);
       int upd = ctx->steps_done_host + 1;
       if (m->reinit_every > 0 && upd % m->reinit_every == 0 && m->reinit_iters > 0) launch_reinit(ctx, m);
-      launch_bcs(ctx, 3);
+      mark(4);
+      launch_commit(ctx, 3, true);   // U := new values + apply_BCs_euler
     } else {
+      mark(2);
       launch_fs_update(ctx, m->fs, 1);
-      launch_bcs(ctx, 1);
+      mark(3);
+      mark(4);
+      launch_commit(ctx, 1, true);
     }
     launch_end_step(ctx);
+    mark(5);
     ctx->steps_done_host++;
     r = last_error();
-    if (r != GFM_OK) return r;
+    if (r != GFM_OK) break;
+    if (phase_ms) {
+      CK(cudaEventSynchronize(ev[GFM_NPHASES]));
+      for (int q = 0; q < GFM_NPHASES; q++) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+        phase_ms[q] += ms;
+      }
+    }
   }
-  return GFM_OK;
+  if (phase_ms)
+    for (int q = 0; q <= GFM_NPHASES; q++) cudaEventDestroy(ev[q]);
+  return r;
 }
+
+gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps) {
+  return step_impl(ctx, m, nsteps, nullptr);
+}
+
+gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms) {
+  if (!phase_ms) return GFM_ERR_ARG;
+  return step_impl(ctx, m, nsteps, phase_ms);
+}
+
+int64_t gfm_launch_count(void) { return (int64_t)g_launches.load(); }
 
 gfm_status_t gfm_get_device_status(gfm_ctx* ctx, uint32_t* status) {
   if (!ctx || !status) return GFM_ERR_ARG;
@@ -377,7 +416,7 @@ gfm_status_t gfm_rs_pure_batch(int n, int paralleltox, double gamma, double pinf
   int blocks = (n + 127) / 128;
   if (blocks > 152 * 8) blocks = 152 * 8;
   k_rs_pure<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(n, paralleltox, make_gas(gamma, pinf), UL, UR,
-                                                                   flux, status);
+                                                                   flux, status); counted();
   return last_error();
 }
 
@@ -388,7 +427,7 @@ gfm_status_t gfm_rs_mixed_batch(int n, double gammaL, double pinfL, double gamma
   int blocks = (n + 127) / 128;
   if (blocks > 152 * 8) blocks = 152 * 8;
   k_rs_mixed<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(n, make_gas(gammaL, pinfL),
-                                                                    make_gas(gammaR, pinfR), UL, UR, out, status);
+                                                                    make_gas(gammaR, pinfR), UL, UR, out, status); counted();
   return last_error();
 }
 

@@ -86,8 +86,9 @@ __global__ void __launch_bounds__(NT) k_flux_update(FluxArgs a) {
   const int* rc = &a.dtime->rc[4 * fluid];
   const int imin = rc[0], imax = rc[1], jmin = rc[2], jmax = rc[3];
 
-  // tile outside the realcells box (or step inactive): copy
-  const bool tile_live = active && !(i0 + TY <= imin || i0 >= imax || j0 + TX <= jmin || j0 >= jmax);
+  if (!active) return;   // the step after t reaches T changes nothing
+  // tile outside the realcells box: its cells keep their values
+  const bool tile_live = !(i0 + TY <= imin || i0 >= imax || j0 + TX <= jmin || j0 >= jmax);
   if (!tile_live) {
     for (int k = tid; k < TX * TY; k += NT) {
       int i = i0 + k / TX, j = j0 + k % TX;
@@ -244,10 +245,8 @@ void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
     k_flux_update<true><<<grid, NT, sm, ctx->stream>>>(a);
   else
     k_flux_update<false><<<grid, NT, sm, ctx->stream>>>(a);
-  for (int f = 0; f < 2; f++) {
-    if (!(fluid_mask & (1 << f))) continue;
-    double* t = ctx->U[f]; ctx->U[f] = ctx->Unew[f]; ctx->Unew[f] = t;
-  }
+  counted();
+  // the new values are in Unew; launch_commit copies them (with the BCs) to U
 }
 
 }  // namespace gfm

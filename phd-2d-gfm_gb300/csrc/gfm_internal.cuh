@@ -5,10 +5,15 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include "gfm_math.cuh"
 #include "../../include/gfm_gb300.h"
 
 namespace gfm {
+
+// kernels launched by this library (reported by gfm_launch_count)
+extern std::atomic<long long> g_launches;
+inline void counted(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // Geometry + EOS of one instance, passed by value to kernels.
 struct GridP {
@@ -114,6 +119,7 @@ __device__ __forceinline__ void raise_status(DevTime* dt, uint32_t bits) {
 // kernel launch helpers (defined in the .cu files)
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask);
 void launch_bcs(gfm_ctx* ctx, int fluid_mask);
+void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);

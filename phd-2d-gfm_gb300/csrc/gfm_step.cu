@@ -147,7 +147,7 @@ void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int
   int64_t n = (int64_t)ctx->P.Nx * ctx->P.Ny;
   int blocks = (int)((n + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
-  k_cfl<<<blocks, 256, 0, ctx->stream>>>(a);
+  k_cfl<<<blocks, 256, 0, ctx->stream>>>(a); counted();
 }
 
 // ---------------------------------------------------------------------------
@@ -168,12 +168,46 @@ __global__ void k_bc_u(GridP P, double* U, const DevTime* D) {
   }
 }
 
+// End of the flux update: U := Unew on real cells and, with bcs, the ghost
+// layers of apply_BCs_euler computed from the new real cells (one pass).
+// Without bcs the ghost layers keep their values, as pure_fluid_update leaves them.
+__global__ void k_commit_u(GridP P, const double* Unew, double* U, int bcs, const DevTime* D) {
+  if (!D->active) return;
+  int64_t n = (int64_t)P.nr * P.nc;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    bool r = is_real(P, i, j);
+    if (!r && !bcs) continue;
+    BCSrc s;
+    if (r) { s.i = i; s.j = j; s.flipu = false; s.flipv = false; }
+    else s = bc_source(P, i, j);
+    V4 v = load4(Unew, P, cidx(P, s.i, s.j));
+    if (s.flipu) v.b = -v.b;
+    if (s.flipv) v.c = -v.c;
+    store4(U, P, cidx(P, i, j), v);
+  }
+}
+
+void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs) {
+  int64_t n = (int64_t)ctx->P.nr * ctx->P.nc;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  for (int f = 0; f < 2; f++)
+    if (fluid_mask & (1 << f)) {
+      k_commit_u<<<blocks, 256, 0, ctx->stream>>>(ctx->P, ctx->Unew[f], ctx->U[f], bcs ? 1 : 0, ctx->dtime);
+      counted();
+    }
+}
+
 void launch_bcs(gfm_ctx* ctx, int fluid_mask) {
   int64_t n = (int64_t)ctx->P.nr * ctx->P.nc;
   int blocks = (int)((n + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
   for (int f = 0; f < 2; f++)
-    if (fluid_mask & (1 << f)) k_bc_u<<<blocks, 256, 0, ctx->stream>>>(ctx->P, ctx->U[f], ctx->dtime);
+    if (fluid_mask & (1 << f)) {
+      k_bc_u<<<blocks, 256, 0, ctx->stream>>>(ctx->P, ctx->U[f], ctx->dtime);
+      counted();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -774,6 +808,12 @@ __global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, cons
   }
 }
 
+__global__ void k_copy_plane(GridP P, const double* src, double* dst, const DevTime* D) {
+  if (!D->active) return;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < P.plane; k += (int64_t)gridDim.x * blockDim.x)
+    dst[k] = src[k];
+}
+
 // S(phi0) = phi0 / sqrt(phi0^2 + h^2), cached for the reinitialisation
 __global__ void k_reinit_sign(GridP P, const double* phi, double* S, const DevTime* D) {
   if (!D->active) return;
@@ -873,7 +913,7 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.D1 = ctx->Wt[0]; e.D2 = ctx->Wt[1];
     e.phi = ctx->phi; e.nrm = ctx->nrm; e.mask = ctx->mask; e.D = ctx->dtime;
     e.mgfm = mgfm ? 1 : 0;
-    k_extrap<<<blocks, 256, 0, ctx->stream>>>(e);
+    k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
   }
 }
@@ -882,7 +922,7 @@ static void run_ext_vfield(gfm_ctx* ctx, int N) {
   const GridP& P = ctx->P;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
   for (int it = 0; it < N; it++) {
-    k_ext_vel<<<blocks, 256, 0, ctx->stream>>>(P, ctx->vel, ctx->vel_t, ctx->phi, ctx->nrm, ctx->mask, ctx->dtime);
+    k_ext_vel<<<blocks, 256, 0, ctx->stream>>>(P, ctx->vel, ctx->vel_t, ctx->phi, ctx->nrm, ctx->mask, ctx->dtime); counted();
     double* t = ctx->vel; ctx->vel = ctx->vel_t; ctx->vel_t = t;
   }
 }
@@ -908,9 +948,9 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
   pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
   pa.check_both = (variant == GFM_OGFM || variant == GFM_RIEMANN) ? 1 : 0;
-  k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa);
+  k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa); counted();
   k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
-                                              ctx->ifc_map, ctx->dtime);
+                                              ctx->ifc_map, ctx->dtime); counted();
   const bool ext = m->use_extension_vfield != 0;
   int fblocks = grid_blocks((int64_t)P.nr * P.nc, 256);
   if (variant == GFM_OGFM) {
@@ -925,8 +965,8 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
     f.vel = ctx->vel; f.D = ctx->dtime;
     f.ogfm = 1;
     f.vel_mode = ext ? 1 : 0;
-    k_finalize<<<fblocks, 256, 0, s>>>(f);
-    k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime);
+    k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
+    k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted();
     if (ext) run_ext_vfield(ctx, 20);
     return;
   }
@@ -934,7 +974,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (variant != GFM_REAL) run_extrap(ctx, 2, false);
   // 3. interface loop
   int cap = P.Nx * P.Ny;
-  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime);
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime); counted();
   IfcArgs ia;
   ia.P = P;
   ia.W1 = ctx->W[0]; ia.W2 = ctx->W[1];
@@ -948,6 +988,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (variant == GFM_RIEMANN) k_interface<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
   else if (variant == GFM_REAL) k_interface<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
   else k_interface<IFC_MODIFIED><<<iblocks, 128, 0, s>>>(ia);
+  counted();
   if (ext) cudaMemsetAsync(ctx->vel, 0, sizeof(double) * 2 * P.plane, s);
   ScatterArgs sa;
   sa.P = P;
@@ -957,7 +998,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   sa.vel = ext ? ctx->vel : nullptr;
   sa.D = ctx->dtime;
   sa.modified = modified ? 1 : 0;
-  k_ifc_scatter<<<grid_blocks(cap, 256), 256, 0, s>>>(sa);
+  k_ifc_scatter<<<grid_blocks(cap, 256), 256, 0, s>>>(sa); counted();
   // 4. extrapolate_vector(6) / extrapolate_vector_mgfm(6)
   run_extrap(ctx, 6, modified);
   // 5. conserved grids and velocity field
@@ -972,7 +1013,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   f.vel = ctx->vel; f.D = ctx->dtime;
   f.ogfm = 0;
   f.vel_mode = ext ? 2 : 0;
-  k_finalize<<<fblocks, 256, 0, s>>>(f);
+  k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
   if (ext) run_ext_vfield(ctx, 20);
 }
 
@@ -981,34 +1022,43 @@ void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
   cudaStream_t s = ctx->stream;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
   if (m->ls_order == 1) {
-    k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime);
+    k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
   } else {
-    k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime);
-    k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime);
-    k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime);
+    k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
+    k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime); counted();
+    k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
   }
-  { double* t = ctx->phi; ctx->phi = ctx->phi_a; ctx->phi_a = t; }
+  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime); counted();
 }
 
+// reinitialisation: iterations alternate phi -> phi_a -> phi ...; an odd
+// count ends with a copy back, so phi stays the one buffer holding the level set
 void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m) {
   const GridP& P = ctx->P;
   cudaStream_t s = ctx->stream;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
-  k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime);
+  k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime); counted();
   for (int it = 0; it < m->reinit_iters; it++) {
-    k_reinit_iter<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->phi_a, ctx->dtime);
-    double* t = ctx->phi; ctx->phi = ctx->phi_a; ctx->phi_a = t;
+    const double* src = (it & 1) ? ctx->phi_a : ctx->phi;
+    double* dst = (it & 1) ? ctx->phi : ctx->phi_a;
+    k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime); counted();
+  }
+  if (m->reinit_iters & 1) {
+    k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime); counted();
   }
 }
 
-void launch_end_step(gfm_ctx* ctx) { k_end_step<<<1, 1, 0, ctx->stream>>>(ctx->dtime); }
+void launch_end_step(gfm_ctx* ctx) {
+  k_end_step<<<1, 1, 0, ctx->stream>>>(ctx->dtime);
+  counted();
+}
 
 void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out) {
   const GridP& P = ctx->P;
   int nb = 256;
   k_mass_partial<<<nb, 256, 0, ctx->stream>>>(P, sign < 0.0 ? ctx->U[0] : ctx->U[ctx->two_fluid ? 1 : 0],
-                                               ctx->two_fluid ? ctx->phi : nullptr, sign, part);
-  k_mass_final<<<1, 32, 0, ctx->stream>>>(part, nb, out);
+                                               ctx->two_fluid ? ctx->phi : nullptr, sign, part); counted();
+  k_mass_final<<<1, 32, 0, ctx->stream>>>(part, nb, out); counted();
 }
 
 }  // namespace gfm
