@@ -537,8 +537,9 @@ inline vec2 unit_normal(const Levelset& ls, int i, int j) {
 // grid_bilinear_interpolate (PhD-Common; absent): bilinear in the four cell
 // centres surrounding x.
 vec4type grid_bilinear_interpolate(const sim_info& params, const grideuler2type& grid, const vec2& x) {
-  double s = (x[0] - params.x0) / params.dx + static_cast<double>(params.numGC) - 0.5;
-  double t = (x[1] - params.y0) / params.dy + static_cast<double>(params.numGC) - 0.5;
+  const double idx = 1.0 / params.dx, idy = 1.0 / params.dy;
+  double s = (x[0] - params.x0) * idx + static_cast<double>(params.numGC) - 0.5;
+  double t = (x[1] - params.y0) * idy + static_cast<double>(params.numGC) - 0.5;
   int j0 = static_cast<int>(std::floor(s));
   int i0 = static_cast<int>(std::floor(t));
   const int nrow = params.Ny + 2 * params.numGC, ncol = params.Nx + 2 * params.numGC;

@@ -126,7 +126,8 @@ inline double isentropic_extrapolation(double gamma, double pinf, double rho1, d
 // Operation order (shared with the kernels): gamma constants
 // G1 = (g-1)/(2g), G2 = (g+1)/(2g), G3 = 2g/(g-1), G4 = 2/(g-1), G5 = 2/(g+1),
 // G6 = (g-1)/(g+1), G7 = (g-1)/2, IG = 1/g; per side pb = p + pinf,
-// c = sqrt(g pb / rho), A = G5/rho, B = G6 pb, 1/pb, G4 c, 1/(rho c);
+// 1/rho, 1/pb, c = sqrt(g pb (1/rho)), A = G5 (1/rho), B = G6 pb, G4 c,
+// 1/(rho c) = c (1/pb) (1/g);
 // Newton stops when 2|p - p_old| <= 1e-12 (p + p_old + 2 min(pinf)).
 class exact_rs_stiffenedgas {
  public:
@@ -147,19 +148,20 @@ class exact_rs_stiffenedgas {
     double rho, u, p, pb, c, A, B, ipb, G4c, irc;
     Side(const double W[3], const Gas& k) : rho(W[0]), u(W[1]), p(W[2]) {
       pb = p + k.pinf;
-      c = std::sqrt(k.g * pb / rho);
-      A = k.G5 / rho;
-      B = k.G6 * pb;
+      const double irho = 1.0 / rho;
       ipb = 1.0 / pb;
+      c = std::sqrt(k.g * pb * irho);
+      A = k.G5 * irho;
+      B = k.G6 * pb;
       G4c = k.G4 * c;
-      irc = 1.0 / (rho * c);
+      irc = c * ipb * k.IG;   // 1/(rho c) = c/(g pb)
     }
   };
 
   Gas KL, KR;
   double P_STAR = 0.0, S_STAR = 0.0, rho_star_L = 0.0, rho_star_R = 0.0;
   int iterations = 0;
-  bool vacuum = false, converged = true;
+  bool vacuum = false, converged = true, trivial = false;
 
   exact_rs_stiffenedgas(double gammaL, double gammaR, double pinf_L, double pinf_R)
       : KL(gammaL, pinf_L), KR(gammaR, pinf_R) {}
@@ -192,11 +194,16 @@ class exact_rs_stiffenedgas {
     const Side SL(L, KL), SR(R, KR);
     vacuum = false;
     converged = true;
-    if (SL.u == SR.u && SL.p == SR.p) {
-      // No pressure or velocity jump: a contact at most.
+    trivial = SL.u == SR.u && SL.p == SR.p;
+    if (trivial) {
+      // No pressure or velocity jump: a contact at most; the star states are
+      // the data themselves.
       P_STAR = SL.p;
       S_STAR = SL.u;
       iterations = 0;
+      rho_star_L = SL.rho;
+      rho_star_R = SR.rho;
+      return;
     } else {
       const double udiff = SR.u - SL.u;
       if (SL.G4c + SR.G4c <= udiff) vacuum = true;
@@ -229,6 +236,11 @@ class exact_rs_stiffenedgas {
 
   // Toro's SAMPLE at wave speed S = x/t, after solve_RP.
   void sample_solution(const double L[3], const double R[3], double S, double out[3]) const {
+    if (trivial) {
+      const double* W = (S <= S_STAR) ? L : R;
+      out[0] = W[0]; out[1] = W[1]; out[2] = W[2];
+      return;
+    }
     const Side SL(L, KL), SR(R, KR);
     if (S <= S_STAR) {
       if (P_STAR <= SL.p) {

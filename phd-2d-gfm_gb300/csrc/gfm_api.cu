@@ -88,6 +88,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
   P.pitch = (P.nc + 31) / 32 * 32;
   P.plane = (int64_t)P.nr * P.pitch;
   P.x0 = d->x0; P.y0 = d->y0; P.dx = d->dx; P.dy = d->dy;
+  P.idx = 1.0 / P.dx; P.idy = 1.0 / P.dy;
   P.bcL = d->BC_L; P.bcR = d->BC_R; P.bcB = d->BC_B; P.bcT = d->BC_T;
   P.g1 = d->gamma1; P.p1 = d->pinf1;
   P.g2 = two_fluid ? d->gamma2 : d->gamma1;

@@ -154,29 +154,25 @@ __global__ void __launch_bounds__(NT) k_flux_update(FluxArgs a) {
     if (xdir) { fr = k / (TX + 1); fc = k % (TX + 1); }
     else { int q = k - NXF; fr = q / TX; fc = q % TX; }
     if (MUSCL) {
-      bool ok1 = true, ok2 = true;
-      if (xdir) {
-        // face between cell (i0+fr, j0+fc-1) [left, its R face] and (i0+fr, j0+fc) [right, its L face]
-        V4 Cl = sFS(s, 0, fr + 1, fc + 1);
-        V4 Lr = sFS(s, 1, fr + 1, fc);
-        if (!is_physical_primitives(gam, pinf, Cl) || !is_physical_primitives(gam, pinf, Lr)) {
-          Cl = sW(s, fr + 2, fc + 2);
-          Lr = sW(s, fr + 2, fc + 1);
-        }
-        UL = prims_to_cons(gam, pinf, Lr, &ok1);
-        UR = prims_to_cons(gam, pinf, Cl, &ok2);
-      } else {
-        // face between cell (i0+fr-1, j0+fc) [below, its T face] and (i0+fr, j0+fc) [above, its B face]
-        V4 Cb = sFS(s, 2, fr + 1, fc + 1);
-        V4 Bt = sFS(s, 3, fr, fc + 1);
-        if (!is_physical_primitives(gam, pinf, Cb) || !is_physical_primitives(gam, pinf, Bt)) {
-          Cb = sW(s, fr + 2, fc + 2);
-          Bt = sW(s, fr + 1, fc + 2);
-        }
-        UL = prims_to_cons(gam, pinf, Bt, &ok1);
-        UR = prims_to_cons(gam, pinf, Cb, &ok2);
+      // x face: right state = L face of cell (i0+fr, j0+fc), left state = R face
+      //         of cell (i0+fr, j0+fc-1);
+      // y face: upper state = B face of cell (i0+fr, j0+fc), lower state = T face
+      //         of cell (i0+fr-1, j0+fc).
+      // The second physicality fallback (FS_MUSCL.cpp:276-285) and
+      // primitives_to_conserved share e = specific_ie of each state.
+      V4 Sr = xdir ? sFS(s, 0, fr + 1, fc + 1) : sFS(s, 2, fr + 1, fc + 1);
+      V4 Sl = xdir ? sFS(s, 1, fr + 1, fc) : sFS(s, 3, fr, fc + 1);
+      double er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
+      double el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
+      if (!(er >= 0.0 && Sr.a >= 0.0) || !(el >= 0.0 && Sl.a >= 0.0)) {
+        Sr = sW(s, fr + 2, fc + 2);
+        Sl = xdir ? sW(s, fr + 2, fc + 1) : sW(s, fr + 1, fc + 2);
+        er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
+        el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
       }
-      if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
+      if (!(Sl.a >= 0.0 && el >= 0.0) || !(Sr.a >= 0.0 && er >= 0.0)) st |= ST_UNPHYSICAL;
+      UL = prims_to_cons_e(Sl, el);
+      UR = prims_to_cons_e(Sr, er);
     } else {
       if (xdir) { UL = sW(s, fr + 2, fc + 1); UR = sW(s, fr + 2, fc + 2); }
       else { UL = sW(s, fr + 1, fc + 2); UR = sW(s, fr + 2, fc + 2); }

@@ -22,6 +22,7 @@ struct GridP {
   int pitch;            // doubles per row in device planes (>= nc)
   int64_t plane;        // doubles per plane = nr * pitch
   double x0, y0, dx, dy;
+  double idx, idy;      // 1/dx, 1/dy
   int bcL, bcR, bcB, bcT;
   double g1, p1, g2, p2;  // gamma1, pinf1, gamma2, pinf2
   Gas gas1, gas2;         // gamma-derived constants of each material

@@ -241,6 +241,24 @@ GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
   double p = eos_pressure(g, pinf, e, rho);
   return V4{rho, u, v, p};
 }
+// conserved_to_primitives together with is_physical_state of the same state:
+// both compute u, v and e with the same operations, done here once.
+GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys) {
+  double rho = U.a;
+  double u = U.b / rho;
+  double v = U.c / rho;
+  double e = (U.d / rho) - 0.5 * (u * u + v * v);
+  *phys = rho >= 0.0 && e >= 0.0;
+  double p = eos_pressure(g, pinf, e, rho);
+  return V4{rho, u, v, p};
+}
+// primitives_to_conserved given e = specific_ie(p, rho) already computed
+// (by is_physical_primitives of the same state)
+GFM_HD V4 prims_to_cons_e(const V4& W, double e) {
+  double rho = W.a, u = W.b, v = W.c;
+  return V4{rho, rho * u, rho * v, rho * e + 0.5 * rho * (u * u + v * v)};
+}
+
 // euler_misc.hpp:70-86
 GFM_HD V4 flux_primitive_var(double g, double pinf, const V4& W) {
   double rho = W.a, u = W.b, v = W.c, p = W.d;
@@ -293,17 +311,25 @@ struct RSSide {
   double irc;         // 1 / (rho c)
 };
 
+// The state itself; the constants that only iteration and wave sampling use
+// are filled in by rs_side_consts (skipped when the data hold no waves).
 GFM_HD RSSide rs_side(double rho, double u, double p, const Gas& k) {
   RSSide s;
   s.rho = rho; s.u = u; s.p = p;
   s.pb = p + k.pinf;
-  s.c = sqrt(k.g * s.pb / rho);
-  s.AK = k.G5 / rho;
-  s.BK = k.G6 * s.pb;
-  s.ipb = 1.0 / s.pb;
-  s.G4c = k.G4 * s.c;
-  s.irc = 1.0 / (rho * s.c);
+  s.c = 0.0; s.AK = 0.0; s.BK = 0.0; s.ipb = 0.0; s.G4c = 0.0; s.irc = 0.0;
   return s;
+}
+// Two divisions and one square root per side (1/rho, 1/pb, c); A = G5/rho and
+// 1/(rho c) = c / (g pb) follow by multiplication.
+GFM_HD void rs_side_consts(RSSide& s, const Gas& k) {
+  double irho = 1.0 / s.rho;
+  s.ipb = 1.0 / s.pb;
+  s.c = sqrt(k.g * s.pb * irho);
+  s.AK = k.G5 * irho;
+  s.BK = k.G6 * s.pb;
+  s.G4c = k.G4 * s.c;
+  s.irc = s.c * s.ipb * k.IG;
 }
 
 // Toro's PREFUN: pressure function f_K and its derivative at pressure p.
@@ -326,6 +352,7 @@ struct RSStar {
   double p, u;        // P_STAR, S_STAR
   int iters;
   uint32_t status;
+  bool trivial;       // equal u and p: no waves, W_L | W_R across the contact
 };
 
 #define GFM_RS_TOL 1e-12
@@ -369,16 +396,21 @@ GFM_HD double rs_guess_pvrs(const RSSide& L, const RSSide& R) {
 
 // Whole solve.  When u and p agree on both sides the data hold at most a
 // contact and the exact answer p* = p, u* = u is returned without iterating.
-GFM_HD RSStar rs_solve(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR) {
+GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR) {
   if (L.u == R.u && L.p == R.p) {
     RSStar s;
     s.p = L.p;
     s.u = L.u;
     s.iters = 0;
     s.status = ST_OK;
+    s.trivial = true;
     return s;
   }
-  return rs_star(L, kL, R, kR, rs_guess_pvrs(L, R));
+  rs_side_consts(L, kL);
+  rs_side_consts(R, kR);
+  RSStar s = rs_star(L, kL, R, kR, rs_guess_pvrs(L, R));
+  s.trivial = false;
+  return s;
 }
 
 // Star density behind the K wave (shock or rarefaction).
@@ -393,6 +425,11 @@ struct RS1D { double rho, u, p; };
 GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, const RSStar& st,
                       double S) {
   RS1D w;
+  if (st.trivial) {
+    if (S <= st.u) { w.rho = L.rho; w.u = L.u; w.p = L.p; }
+    else { w.rho = R.rho; w.u = R.u; w.p = R.p; }
+    return w;
+  }
   if (S <= st.u) {  // left of contact
     if (st.p <= L.p) {  // left rarefaction
       double shl = L.u - L.c;
@@ -437,9 +474,10 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
 // pure_RS_exact::solve_RP (sourcecode/pure_RS_exact.cpp:9-73): flux of the
 // exact solution at x/t = 0 between conserved states UL and UR, one material.
 GFM_HD V4 pure_rs_flux(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
-  if (!is_physical_state(UL) || !is_physical_state(UR)) *status |= ST_UNPHYSICAL;
-  V4 Lp = cons_to_prims(k.g, k.pinf, UL);
-  V4 Rp = cons_to_prims(k.g, k.pinf, UR);
+  bool okL, okR;
+  V4 Lp = cons_to_prims_phys(k.g, k.pinf, UL, &okL);
+  V4 Rp = cons_to_prims_phys(k.g, k.pinf, UR, &okR);
+  if (!okL || !okR) *status |= ST_UNPHYSICAL;
   double uLn = paralleltox ? Lp.b : Lp.c;
   double uRn = paralleltox ? Rp.b : Rp.c;
   RSSide L = rs_side(Lp.a, uLn, Lp.d, k);
@@ -457,9 +495,10 @@ GFM_HD V4 pure_rs_flux(bool paralleltox, const Gas& k, const V4& UL, const V4& U
 // mixed_RS_exact::solve_mixed_RP (sourcecode/mixed_RS_exact.cpp:8-48).
 struct MixedStar { double p_star, u_star, rho_star_L, rho_star_R; };
 GFM_HD MixedStar mixed_rs(const Gas& kL, const Gas& kR, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
-  if (!is_physical_state(UL) || !is_physical_state(UR)) *status |= ST_UNPHYSICAL;
-  V4 Lp = cons_to_prims(kL.g, kL.pinf, UL);
-  V4 Rp = cons_to_prims(kR.g, kR.pinf, UR);
+  bool okL, okR;
+  V4 Lp = cons_to_prims_phys(kL.g, kL.pinf, UL, &okL);
+  V4 Rp = cons_to_prims_phys(kR.g, kR.pinf, UR, &okR);
+  if (!okL || !okR) *status |= ST_UNPHYSICAL;
   RSSide L = rs_side(Lp.a, Lp.b, Lp.d, kL);
   RSSide R = rs_side(Rp.a, Rp.b, Rp.d, kR);
   RSStar st = rs_solve(L, kL, R, kR);
@@ -468,8 +507,8 @@ GFM_HD MixedStar mixed_rs(const Gas& kL, const Gas& kR, const V4& UL, const V4& 
   MixedStar m;
   m.p_star = st.p;
   m.u_star = st.u;
-  m.rho_star_L = rs_rho_star(L, kL, st.p);
-  m.rho_star_R = rs_rho_star(R, kR, st.p);
+  m.rho_star_L = st.trivial ? L.rho : rs_rho_star(L, kL, st.p);
+  m.rho_star_R = st.trivial ? R.rho : rs_rho_star(R, kR, st.p);
   if (m.p_star != m.p_star) *status |= ST_NAN;
   return m;
 }

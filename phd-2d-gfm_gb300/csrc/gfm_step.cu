@@ -444,8 +444,8 @@ __device__ V4 ifc_read(const IfcArgs& a, int f, int i, int j, int64_t lin, bool&
 // grid_bilinear_interpolate at x (the project's definition, shared with the oracle)
 __device__ V4 ifc_bilinear(const IfcArgs& a, int f, double x, double y, int64_t lin, bool resolve, bool& ok) {
   const GridP& P = a.P;
-  double s = (x - P.x0) / P.dx + (double)P.g - 0.5;
-  double t = (y - P.y0) / P.dy + (double)P.g - 0.5;
+  double s = (x - P.x0) * P.idx + (double)P.g - 0.5;
+  double t = (y - P.y0) * P.idy + (double)P.g - 0.5;
   int j0 = (int)floor(s), i0 = (int)floor(t);
   j0 = min(max(j0, 0), P.nc - 2);
   i0 = min(max(i0, 0), P.nr - 2);
@@ -477,9 +477,17 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
   const int n = a.D->n_ifc;
   uint32_t st = 0;
   int iters = 0;
+  // One interfacial cell per warp, solved by lane 0: on GB300 an FP64
+  // instruction occupies its sub-partition's FP64 pipe for the same time
+  // whether 1 or 32 lanes are active, so lanes of one warp working on
+  // dependent cells would only serialise each other.
+  const int lane = threadIdx.x & 31;
   for (;;) {
-    int k = (int)atomicAdd(a.ticket, 1u);
+    int k = 0;
+    if (lane == 0) k = (int)atomicAdd(a.ticket, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
     if (k >= n) break;
+    if (lane != 0) continue;
     int64_t lin = a.list[k];
     int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
     int64_t c = cidx(P, i, j);
@@ -984,7 +992,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.ticket = (unsigned int*)(ctx->ifc_opp);
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
-  int iblocks = 152 * 4;
+  int iblocks = 152;   // 4 warps per CTA: one chain warp per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
   else if (variant == GFM_REAL) k_interface<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
   else k_interface<IFC_MODIFIED><<<iblocks, 128, 0, s>>>(ia);
