@@ -163,6 +163,23 @@ gfm_status_t gfm_case_params(const char* sim_type, const char* test_case, int Nx
 gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gfm_grid_desc* grid, double* U1,
                            double* U2, double* phi);
 
+/* One-fluid time steps for callers that cannot allocate device memory.
+ * No counterpart in the reference: it is an addition of this library.
+ * Some callers cannot call cudaMalloc (a host runtime whose memory pool owns
+ * the device; real-time code that may not block on an allocation after
+ * start-up).  This entry point advances the caller's DEVICE grid U (layout as
+ * above, unpitched) in place by up to nsteps steps of sim_onefluid's loop
+ * (sourcecode/sim_onefluid.cpp:40-54); t and numsteps are in/out, status
+ * receives the GFM_ST_* bits.  It calls no cudaMalloc/cudaFree: its scratch
+ * is a built-in 16 MiB device array, which limits the grid to
+ * GFM_NOALLOC_MAX_CELLS padded cells ((Nx+2 numGC)(Ny+2 numGC)); larger
+ * grids are rejected with GFM_ERR_ARG.  The first call on each device looks
+ * up the array's address and should come before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race. */
+#define GFM_NOALLOC_MAX_CELLS 524272
+gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* grid, const gfm_method_desc* m, double* U, int nsteps,
+                                       double* t, int* numsteps, uint32_t* status, void* cuda_stream);
+
 /* library version string */
 const char* gfm_version(void);
 
