@@ -124,7 +124,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->phi_a, plane_b);
     alloc((void**)&ctx->phi_b, plane_b);
     alloc((void**)&ctx->phi0, plane_b);
-    alloc((void**)&ctx->nrm, 2 * plane_b);
+    alloc((void**)&ctx->nrm, 5 * plane_b);   // gradient (2), unit normal (2), |gradient|
     alloc((void**)&ctx->vel, 2 * plane_b);
     alloc((void**)&ctx->vel_t, 2 * plane_b);
     alloc((void**)&ctx->mask, (size_t)P.plane);

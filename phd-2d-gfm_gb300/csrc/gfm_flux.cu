@@ -68,10 +68,57 @@ __device__ __forceinline__ V4 B_times(double s, const V4& W, double irho, double
   return V4{sv * d.a + (s * W.a) * d.c, sv * d.b, sv * d.c + (s * irho) * d.d, (s * rcc) * d.c + sv * d.d};
 }
 
+// Phase 2 for one cell: minmod slopes (FS_MUSCL.cpp:189-196), boundary
+// extrapolated values (:199-210), first physicality fallback (:213-247) and
+// the half-step evolution with both quasilinear matrices (:250-272).
+// out = evolved L, R, B, T face states of the cell.
+__device__ __forceinline__ void cell_face_states(const V4& W, const V4& Ww, const V4& We, const V4& Ws,
+                                                 const V4& Wn, double gam, double pinf, double sx, double sy,
+                                                 V4 out[4]) {
+  V4 dxL = v4sub(W, Ww), dxR = v4sub(We, W);
+  V4 dyL = v4sub(W, Ws), dyR = v4sub(Wn, W);
+  V4 sxv = V4{minmod(dxL.a, dxR.a), minmod(dxL.b, dxR.b), minmod(dxL.c, dxR.c), minmod(dxL.d, dxR.d)};
+  V4 syv = V4{minmod(dyL.a, dyR.a), minmod(dyL.b, dyR.b), minmod(dyL.c, dyR.c), minmod(dyL.d, dyR.d)};
+  V4 L = V4{W.a - 0.5 * sxv.a, W.b - 0.5 * sxv.b, W.c - 0.5 * sxv.c, W.d - 0.5 * sxv.d};
+  V4 R = V4{W.a + 0.5 * sxv.a, W.b + 0.5 * sxv.b, W.c + 0.5 * sxv.c, W.d + 0.5 * sxv.d};
+  V4 B = V4{W.a - 0.5 * syv.a, W.b - 0.5 * syv.b, W.c - 0.5 * syv.c, W.d - 0.5 * syv.d};
+  V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
+  if (!is_physical_primitives(gam, pinf, L) || !is_physical_primitives(gam, pinf, R)) { L = W; R = W; }
+  if (!is_physical_primitives(gam, pinf, B) || !is_physical_primitives(gam, pinf, T)) { B = W; T = W; }
+  double cs = eos_soundspeed(gam, pinf, W.d, W.a);
+  double irho = 1.0 / W.a, rcc = W.a * cs * cs;
+  V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
+  V4 Y = B_times(sy, W, irho, rcc, v4sub(B, T));
+  out[0] = V4{(L.a + X.a) + Y.a, (L.b + X.b) + Y.b, (L.c + X.c) + Y.c, (L.d + X.d) + Y.d};
+  out[1] = V4{(R.a + X.a) + Y.a, (R.b + X.b) + Y.b, (R.c + X.c) + Y.c, (R.d + X.d) + Y.d};
+  out[2] = V4{(B.a + X.a) + Y.a, (B.b + X.b) + Y.b, (B.c + X.c) + Y.c, (B.d + X.d) + Y.d};
+  out[3] = V4{(T.a + X.a) + Y.a, (T.b + X.b) + Y.b, (T.c + X.c) + Y.c, (T.d + X.d) + Y.d};
+}
+
+// Phase 3 for one face (MUSCL): second physicality fallback (FS_MUSCL.cpp:276-285)
+// to the cells' primitives Wr/Wl, primitives -> conserved sharing e with the
+// check, and the exact Riemann flux (:287-288).  Sr/Sl: evolved face states
+// of the cell on the high / low side of the face.
+__device__ __forceinline__ V4 muscl_face_flux(bool xdir, V4 Sr, V4 Sl, const V4& Wr, const V4& Wl, const Gas& gas,
+                                              uint32_t* st, int* iters) {
+  const double gam = gas.g, pinf = gas.pinf;
+  double er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
+  double el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
+  if (!(er >= 0.0 && Sr.a >= 0.0) || !(el >= 0.0 && Sl.a >= 0.0)) {
+    Sr = Wr;
+    Sl = Wl;
+    er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
+    el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
+  }
+  if (!(Sl.a >= 0.0 && el >= 0.0) || !(Sr.a >= 0.0 && er >= 0.0)) *st |= ST_UNPHYSICAL;
+  return pure_rs_flux(xdir, gas, prims_to_cons_e(Sl, el), prims_to_cons_e(Sr, er), st, iters);
+}
+
 template <bool MUSCL>
-__global__ void __launch_bounds__(NT) k_flux_update(FluxArgs a) {
+__global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FluxSmem& s = *reinterpret_cast<FluxSmem*>(smem_raw);
+  __shared__ V4 s_uniform_flux[2];
   const GridP& P = a.P;
   const int fluid = a.fluid_base + blockIdx.z;
   const double* __restrict__ U = a.U[blockIdx.z];
@@ -102,88 +149,89 @@ __global__ void __launch_bounds__(NT) k_flux_update(FluxArgs a) {
   const double dt = a.dtime->dt;
   const double dtodx = dt / P.dx;
   const double dtody = dt / P.dy;
+  const double sx = 0.5 * dtodx, sy = 0.5 * dtody;
   uint32_t st = 0;
   int iters = 0;
 
-  // phase 1
+  // phase 1: load (clamped to the padded grid), convert, and test whether the
+  // whole region holds one bit pattern
+  const int64_t c00 = cidx(P, min(max(i0 - 2, 0), P.nr - 1), min(max(j0 - 2, 0), P.nc - 1));
+  const V4 u00 = load4(U, P, c00);
+  bool same = true;
   for (int k = tid; k < WR * WC; k += NT) {
     int r = k / WC, c = k % WC;
     int i = min(max(i0 - 2 + r, 0), P.nr - 1);
     int j = min(max(j0 - 2 + c, 0), P.nc - 1);
     V4 u = load4(U, P, cidx(P, i, j));
+    same = same && as_bits(u.a) == as_bits(u00.a) && as_bits(u.b) == as_bits(u00.b) &&
+           as_bits(u.c) == as_bits(u00.c) && as_bits(u.d) == as_bits(u00.d);
     V4 w = MUSCL ? cons_to_prims(gam, pinf, u) : u;
     s.w[0][r][c] = w.a; s.w[1][r][c] = w.b; s.w[2][r][c] = w.c; s.w[3][r][c] = w.d;
   }
-  __syncthreads();
+  // Uniform region: every cell of the tile and its halo has the same state,
+  // so every cell computes the same face states and every face of a
+  // direction the same flux; one of each is evaluated (bit-identical).
+  const bool uniform = __syncthreads_and(same) != 0;
 
-  // phase 2: evolved face states of cells (i0-1 .. i0+TY) x (j0-1 .. j0+TX)
-  if (MUSCL) {
-    const double sx = 0.5 * dtodx, sy = 0.5 * dtody;
-    for (int k = tid; k < SR * SC; k += NT) {
-      int r = k / SC, c = k % SC;       // cell (i0-1+r, j0-1+c) = w[r+1][c+1]
-      V4 W = sW(s, r + 1, c + 1);
-      V4 Ww = sW(s, r + 1, c), We = sW(s, r + 1, c + 2);
-      V4 Ws = sW(s, r, c + 1), Wn = sW(s, r + 2, c + 1);
-      V4 dxL = v4sub(W, Ww), dxR = v4sub(We, W);
-      V4 dyL = v4sub(W, Ws), dyR = v4sub(Wn, W);
-      V4 sxv = V4{minmod(dxL.a, dxR.a), minmod(dxL.b, dxR.b), minmod(dxL.c, dxR.c), minmod(dxL.d, dxR.d)};
-      V4 syv = V4{minmod(dyL.a, dyR.a), minmod(dyL.b, dyR.b), minmod(dyL.c, dyR.c), minmod(dyL.d, dyR.d)};
-      V4 L = V4{W.a - 0.5 * sxv.a, W.b - 0.5 * sxv.b, W.c - 0.5 * sxv.c, W.d - 0.5 * sxv.d};
-      V4 R = V4{W.a + 0.5 * sxv.a, W.b + 0.5 * sxv.b, W.c + 0.5 * sxv.c, W.d + 0.5 * sxv.d};
-      V4 B = V4{W.a - 0.5 * syv.a, W.b - 0.5 * syv.b, W.c - 0.5 * syv.c, W.d - 0.5 * syv.d};
-      V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
-      if (!is_physical_primitives(gam, pinf, L) || !is_physical_primitives(gam, pinf, R)) { L = W; R = W; }
-      if (!is_physical_primitives(gam, pinf, B) || !is_physical_primitives(gam, pinf, T)) { B = W; T = W; }
-      double cs = eos_soundspeed(gam, pinf, W.d, W.a);
-      double irho = 1.0 / W.a, rcc = W.a * cs * cs;
-      V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
-      V4 Y = B_times(sy, W, irho, rcc, v4sub(B, T));
-      putFS(s, 0, r, c, V4{(L.a + X.a) + Y.a, (L.b + X.b) + Y.b, (L.c + X.c) + Y.c, (L.d + X.d) + Y.d});
-      putFS(s, 1, r, c, V4{(R.a + X.a) + Y.a, (R.b + X.b) + Y.b, (R.c + X.c) + Y.c, (R.d + X.d) + Y.d});
-      putFS(s, 2, r, c, V4{(B.a + X.a) + Y.a, (B.b + X.b) + Y.b, (B.c + X.c) + Y.c, (B.d + X.d) + Y.d});
-      putFS(s, 3, r, c, V4{(T.a + X.a) + Y.a, (T.b + X.b) + Y.b, (T.c + X.c) + Y.c, (T.d + X.d) + Y.d});
+  if (uniform) {
+    if (tid == 0) {
+      V4 W = sW(s, 2, 2);
+      V4 fx, fy;
+      int itx = 0, ity = 0;
+      if (MUSCL) {
+        V4 fs[4];
+        cell_face_states(W, W, W, W, W, gam, pinf, sx, sy, fs);
+        fx = muscl_face_flux(true, fs[0], fs[1], W, W, gas, &st, &itx);
+        fy = muscl_face_flux(false, fs[2], fs[3], W, W, gas, &st, &ity);
+      } else {
+        fx = pure_rs_flux(true, gas, W, W, &st, &itx);
+        fy = pure_rs_flux(false, gas, W, W, &st, &ity);
+      }
+      iters = itx * NXF + ity * NYF;
+      s_uniform_flux[0] = fx;
+      s_uniform_flux[1] = fy;
+    }
+    __syncthreads();
+  } else {
+    // phase 2: evolved face states of cells (i0-1 .. i0+TY) x (j0-1 .. j0+TX)
+    if (MUSCL) {
+      for (int k = tid; k < SR * SC; k += NT) {
+        int r = k / SC, c = k % SC;       // cell (i0-1+r, j0-1+c) = w[r+1][c+1]
+        V4 fs[4];
+        cell_face_states(sW(s, r + 1, c + 1), sW(s, r + 1, c), sW(s, r + 1, c + 2), sW(s, r, c + 1),
+                         sW(s, r + 2, c + 1), gam, pinf, sx, sy, fs);
+        for (int f = 0; f < 4; f++) putFS(s, f, r, c, fs[f]);
+      }
+      __syncthreads();
+    }
+    // phase 3: x faces (TY rows x TX+1) then y faces (TY+1 rows x TX)
+    //   x face (fr, fc): between cells (i0+fr, j0+fc-1) and (i0+fr, j0+fc)
+    //   y face (fr, fc): between cells (i0+fr-1, j0+fc) and (i0+fr, j0+fc)
+    for (int k = tid; k < NXF + NYF; k += NT) {
+      bool xdir = k < NXF;
+      int fr, fc;
+      if (xdir) { fr = k / (TX + 1); fc = k % (TX + 1); }
+      else { int q = k - NXF; fr = q / TX; fc = q % TX; }
+      V4 f;
+      if (MUSCL) {
+        if (xdir)
+          f = muscl_face_flux(true, sFS(s, 0, fr + 1, fc + 1), sFS(s, 1, fr + 1, fc), sW(s, fr + 2, fc + 2),
+                              sW(s, fr + 2, fc + 1), gas, &st, &iters);
+        else
+          f = muscl_face_flux(false, sFS(s, 2, fr + 1, fc + 1), sFS(s, 3, fr, fc + 1), sW(s, fr + 2, fc + 2),
+                              sW(s, fr + 1, fc + 2), gas, &st, &iters);
+      } else {
+        if (xdir) f = pure_rs_flux(true, gas, sW(s, fr + 2, fc + 1), sW(s, fr + 2, fc + 2), &st, &iters);
+        else f = pure_rs_flux(false, gas, sW(s, fr + 1, fc + 2), sW(s, fr + 2, fc + 2), &st, &iters);
+      }
+      if (xdir) { s.fx[0][fr][fc] = f.a; s.fx[1][fr][fc] = f.b; s.fx[2][fr][fc] = f.c; s.fx[3][fr][fc] = f.d; }
+      else { s.fy[0][fr][fc] = f.a; s.fy[1][fr][fc] = f.b; s.fy[2][fr][fc] = f.c; s.fy[3][fr][fc] = f.d; }
     }
     __syncthreads();
   }
 
-  // phase 3: x faces (TY rows x TX+1) then y faces (TY+1 rows x TX)
-  for (int k = tid; k < NXF + NYF; k += NT) {
-    V4 UL, UR;
-    bool xdir = k < NXF;
-    int fr, fc;
-    if (xdir) { fr = k / (TX + 1); fc = k % (TX + 1); }
-    else { int q = k - NXF; fr = q / TX; fc = q % TX; }
-    if (MUSCL) {
-      // x face: right state = L face of cell (i0+fr, j0+fc), left state = R face
-      //         of cell (i0+fr, j0+fc-1);
-      // y face: upper state = B face of cell (i0+fr, j0+fc), lower state = T face
-      //         of cell (i0+fr-1, j0+fc).
-      // The second physicality fallback (FS_MUSCL.cpp:276-285) and
-      // primitives_to_conserved share e = specific_ie of each state.
-      V4 Sr = xdir ? sFS(s, 0, fr + 1, fc + 1) : sFS(s, 2, fr + 1, fc + 1);
-      V4 Sl = xdir ? sFS(s, 1, fr + 1, fc) : sFS(s, 3, fr, fc + 1);
-      double er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
-      double el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
-      if (!(er >= 0.0 && Sr.a >= 0.0) || !(el >= 0.0 && Sl.a >= 0.0)) {
-        Sr = sW(s, fr + 2, fc + 2);
-        Sl = xdir ? sW(s, fr + 2, fc + 1) : sW(s, fr + 1, fc + 2);
-        er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
-        el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
-      }
-      if (!(Sl.a >= 0.0 && el >= 0.0) || !(Sr.a >= 0.0 && er >= 0.0)) st |= ST_UNPHYSICAL;
-      UL = prims_to_cons_e(Sl, el);
-      UR = prims_to_cons_e(Sr, er);
-    } else {
-      if (xdir) { UL = sW(s, fr + 2, fc + 1); UR = sW(s, fr + 2, fc + 2); }
-      else { UL = sW(s, fr + 1, fc + 2); UR = sW(s, fr + 2, fc + 2); }
-    }
-    V4 f = pure_rs_flux(xdir, gas, UL, UR, &st, &iters);
-    if (xdir) { s.fx[0][fr][fc] = f.a; s.fx[1][fr][fc] = f.b; s.fx[2][fr][fc] = f.c; s.fx[3][fr][fc] = f.d; }
-    else { s.fy[0][fr][fc] = f.a; s.fy[1][fr][fc] = f.b; s.fy[2][fr][fc] = f.c; s.fy[3][fr][fc] = f.d; }
-  }
-  __syncthreads();
-
-  // phase 4
+  // phase 4: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn
+  const V4 ufx = s_uniform_flux[0], ufy = s_uniform_flux[1];
   for (int k = tid; k < TX * TY; k += NT) {
     int r = k / TX, c = k % TX;
     int i = i0 + r, j = j0 + c;
@@ -193,10 +241,15 @@ __global__ void __launch_bounds__(NT) k_flux_update(FluxArgs a) {
     if (i >= imin && i < imax && j >= jmin && j < jmax) {
       if (!is_physical_state(u)) st |= ST_UNPHYSICAL;
       double o[4] = {u.a, u.b, u.c, u.d};
+      const double ux[4] = {ufx.a, ufx.b, ufx.c, ufx.d}, uy[4] = {ufy.a, ufy.b, ufy.c, ufy.d};
       for (int q = 0; q < 4; q++) {
-        double v = o[q] + (dtodx * s.fx[q][r][c] + dtody * s.fy[q][r][c]);
-        v = v - dtodx * s.fx[q][r][c + 1];
-        v = v - dtody * s.fy[q][r + 1][c];
+        double fw = uniform ? ux[q] : s.fx[q][r][c];
+        double fe = uniform ? ux[q] : s.fx[q][r][c + 1];
+        double fs_ = uniform ? uy[q] : s.fy[q][r][c];
+        double fn = uniform ? uy[q] : s.fy[q][r + 1][c];
+        double v = o[q] + (dtodx * fw + dtody * fs_);
+        v = v - dtodx * fe;
+        v = v - dtody * fn;
         o[q] = v;
       }
       u = V4{o[0], o[1], o[2], o[3]};

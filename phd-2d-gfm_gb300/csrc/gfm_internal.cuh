@@ -59,7 +59,7 @@ struct gfm_ctx {
   double* phi_a;     // level-set stage buffers
   double* phi_b;
   double* phi0;      // reinitialisation reference
-  double* nrm;       // 2 planes: raw central-difference gradient of phi
+  double* nrm;       // 5 planes: gradient of phi (2), unit normal (2), |gradient|
   double* vel;       // 2 planes: velocity field handed to the level set
   double* vel_t;     // 2 planes: extension-velocity pong
   uint8_t* mask;     // interfacial-cell mask (real cells only)

@@ -24,12 +24,12 @@ constexpr int CHUNK_T = 512;
 __device__ __forceinline__ double dmax_std(double a, double b) { return (a < b) ? b : a; }  // std::max
 __device__ __forceinline__ double dmin_std(double a, double b) { return (b < a) ? b : a; }  // std::min
 
-// unit normal with the reference's fallback (sourcecode/GFM_riemann.cpp:58-68)
+// Normal planes (k_prims): 0,1 raw central-difference gradient of phi,
+// 2,3 unit normal with the reference's fallback to (1,0) below 1e-12
+// (sourcecode/GFM_riemann.cpp:58-68), 4 the gradient's norm.
 __device__ __forceinline__ void unit_normal(const double* nrm, const GridP& P, int64_t c, double& nx, double& ny) {
-  double gx = nrm[c], gy = nrm[c + P.plane];
-  double nn = sqrt(gx * gx + gy * gy);
-  if (nn < 1e-12) { nx = 1.0; ny = 0.0; return; }
-  nx = gx / nn; ny = gy / nn;
+  nx = nrm[c + 2 * P.plane];
+  ny = nrm[c + 3 * P.plane];
 }
 
 __device__ __forceinline__ V4 v4d(const V4& x, const V4& y) { return V4{x.a - y.a, x.b - y.b, x.c - y.c, x.d - y.d}; }
@@ -261,8 +261,16 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
       gx = (a.phi[c + 1] - a.phi[c - 1]) / (2.0 * P.dx);
       gy = (a.phi[c + P.pitch] - a.phi[c - P.pitch]) / (2.0 * P.dy);
     }
+    // raw gradient, its norm, and the unit normal with the reference's
+    // fallback (sourcecode/GFM_riemann.cpp:58-68), once per step
+    double nn = sqrt(gx * gx + gy * gy);
+    double ux = 1.0, uy = 0.0;
+    if (!(nn < 1e-12)) { ux = gx / nn; uy = gy / nn; }
     a.nrm[c] = gx;
     a.nrm[c + P.plane] = gy;
+    a.nrm[c + 2 * P.plane] = ux;
+    a.nrm[c + 3 * P.plane] = uy;
+    a.nrm[c + 4 * P.plane] = nn;
     uint8_t m = 0;
     if (is_real(P, i, j)) {
       bool s = ph <= 0.0;
@@ -498,21 +506,36 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
     V4 ip1, ip2;   // interfaceprims1, interfaceprims2
     if (MODE == IFC_REAL) {
       // neighbour with opposite phi sign and the closest normal (GFM_real.cpp:77-117)
-      double mindiff = 1e100;
-      int iopp = -1000, jopp = -1000;
+      // acos is decreasing with slope <= -1 and gfm_acos is accurate to a few
+      // ulps, so a candidate whose clamped dot product is more than 1e-6 below
+      // the largest one has a strictly larger angle than the minimum and can
+      // never be the first minimiser: acos is evaluated only for the others,
+      // in the reference's loop order with its strict comparison.
+      double dpk[9];
+      double dbest = -2.0;
       for (int xinc = -1; xinc <= 1; xinc++)
         for (int yinc = -1; yinc <= 1; yinc++) {
+          int q = (xinc + 1) * 3 + (yinc + 1);
           int64_t c2 = cidx(P, i + yinc, j + xinc);
-          double other = a.phi[c2];
-          if (lsval * other <= 0.0) {
+          dpk[q] = -3.0;
+          if (lsval * a.phi[c2] <= 0.0) {
             double ox, oy;
             unit_normal(a.nrm, P, c2, ox, oy);
             double dp = nx * ox + ny * oy;
             dp = (dp < -1.0) ? -1.0 : dp;
             dp = (1.0 < dp) ? 1.0 : dp;
-            double ang = gfm_acos(dp);
-            if (ang < mindiff) { iopp = i + yinc; jopp = j + xinc; mindiff = ang; }
+            dpk[q] = dp;
+            if (dp > dbest) dbest = dp;
           }
+        }
+      double mindiff = 1e100;
+      int iopp = -1000, jopp = -1000;
+      for (int xinc = -1; xinc <= 1; xinc++)
+        for (int yinc = -1; yinc <= 1; yinc++) {
+          double dp = dpk[(xinc + 1) * 3 + (yinc + 1)];
+          if (dp < -2.0 || dp < dbest - 1e-6) continue;
+          double ang = gfm_acos(dp);
+          if (ang < mindiff) { iopp = i + yinc; jopp = j + xinc; mindiff = ang; }
         }
       if (iopp == -1000) { st |= ST_BAD_ARGUMENT; iopp = i; jopp = j; }
       if (lsval <= 0.0) {
@@ -528,10 +551,12 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
       double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
       double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
       double gx = a.nrm[c], gy = a.nrm[c + P.plane];
-      double nm = sqrt(gx * gx + gy * gy);
+      double nm = a.nrm[c + 4 * P.plane];
       double lv = lsval;
       if (fabs(lv) > ds) lv = copysign(ds, lv);
-      double hx = gx / nm, hy = gy / nm;
+      // normal / normmag: the unit normal unless the gradient vanishes
+      double hx = nx, hy = ny;
+      if (nm < 1e-12) { hx = gx / nm; hy = gy / nm; }
       double ilx = ccx - lv * hx, ily = ccy - lv * hy;
       bool resolve = (MODE == IFC_RIEMANN);
       ip2 = ifc_bilinear(a, 1, ilx + ds * hx, ily + ds * hy, lin, resolve, ok);
@@ -741,10 +766,9 @@ __global__ void __launch_bounds__(256) k_ext_vel(GridP P, const double* S, doubl
     BCSrc s = bc_source(Q, i, j);
     int64_t c = cidx(P, s.i, s.j);
     double vx = S[c], vy = S[c + P.plane];
-    double gx = nrm[c], gy = nrm[c + P.plane];
-    double nn = sqrt(gx * gx + gy * gy);
+    double nn = nrm[c + 4 * P.plane];
     if (!mask[c] && nn > 1e-12) {
-      double nx = gx / nn, ny = gy / nn;
+      double nx = nrm[c + 2 * P.plane], ny = nrm[c + 3 * P.plane];
       double cx = (dt / P.dx) * nx, cy = (dt / P.dy) * ny;
       double dxx, dxy, dyx, dyy;
       if (phi[c] <= 0.0) {
