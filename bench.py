@@ -151,8 +151,8 @@ def run_gfm(args):
     torch.cuda.synchronize()
     ctx.clear_status()
     cells = desc.Nx * desc.Ny
-    phases = np.zeros(5)
-    ph = np.zeros(5)
+    phases = np.zeros(8)
+    ph = np.zeros(8)
     L = g.lib()
     L.gfm_step_timed.argtypes = [ctypes.c_void_p, ctypes.POINTER(g.MethodDesc), ctypes.c_int,
                                  ctypes.POINTER(ctypes.c_double)]
@@ -177,7 +177,7 @@ def run_gfm(args):
         torch.cuda.synchronize()
     wall = time.time() - t_wall
     launches = L.gfm_launch_count() - launches0
-    step_ms = float(phases.sum())
+    step_ms = float(phases[:5].sum())   # phases 5-7 are sub-intervals of 1-2
     if world > 1:
         import torch.distributed as tdist
         tt = torch.tensor([step_ms], device="cuda", dtype=torch.float64)
@@ -197,7 +197,8 @@ def run_gfm(args):
             "frac": round(achieved / peak, 5), "traffic": ncu_traffic(), "kernel": "k_flux_update<MUSCL>",
             "peak_source": peak_kind,
             "phase_ms_per_step": {n: round(v / args.steps, 5) for n, v in
-                                  zip(["cfl", "ghost_fill", "flux_update", "level_set", "bcs"], phases)}}
+                                  zip(["cfl", "ghost_fill", "flux_update", "level_set", "bcs", "interface_loop",
+                                       "far_partition", "near_extrapolation"], phases)}}
 
     # end to end through the C ABI: pinned host state -> device -> step -> host
     e2e = None

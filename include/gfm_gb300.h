@@ -122,9 +122,20 @@ gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps);
 /* gfm_step with CUDA events recorded on the context's stream around each
  * phase; adds the milliseconds of each phase to phase_ms[GFM_NPHASES]:
  * 0 CFL/dt, 1 ghost fill, 2 flux update (both fluids, one launch),
- * 3 level set, 4 boundary conditions + end of step. */
-#define GFM_NPHASES 5
+ * 3 level set, 4 boundary conditions + end of step.
+ * With the overlapped schedule of the Riemann and real GFM (interface loop
+ * on its own SM partition while the far field is updated on the rest),
+ * phase 1 runs up to the near-interface flux update, phase 2 is that
+ * update, and 5 the interface loop, 6 the far-field partition's work,
+ * 7 the exact extrapolation and conversion of near cells after the loop. */
+#define GFM_NPHASES 8
 gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
+
+/* Overlapped schedule of the Riemann and real GFM on (enable = 1, the
+ * default where the device supports SM partitions) or off (0: every phase
+ * runs on the context's stream in turn).  Results are identical either way.
+ * GFM_ERR_UNSUPPORTED when enable = 1 and the context has no partitions. */
+gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int enable);
 
 /* number of kernels this library has launched since it was loaded */
 int64_t gfm_launch_count(void);

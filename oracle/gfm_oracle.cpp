@@ -40,6 +40,9 @@ namespace {
 
 uint32_t g_status = 0;     // OR of GFM_ST_* raised where the reference asserts
 int64_t g_newton_iters = 0;
+int64_t g_mixed_calls = 0, g_mixed_iters = 0;   // mixed solves only
+int64_t g_iter_hist[16] = {0};                    // Newton iterations per solve (15 = 15 or more)
+static void count_iters(int it) { g_iter_hist[it < 15 ? it : 15]++; }
 
 inline vec4type add(const vec4type& a, const vec4type& b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2], a[3] + b[3]}; }
 inline vec4type sub(const vec4type& a, const vec4type& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2], a[3] - b[3]}; }
@@ -173,6 +176,7 @@ void pure_RS_solve_RP(bool paralleltox, double gamma, double pinf, const vec4typ
   if (RS.vacuum) g_status |= GFM_ST_VACUUM;
   if (!RS.converged) g_status |= GFM_ST_NEWTON_NO_CONVERGE;
   g_newton_iters += RS.iterations;
+  count_iters(RS.iterations);
 }
 
 // mixed_RS_exact::solve_mixed_RP (sourcecode/mixed_RS_exact.cpp:8-48)
@@ -194,6 +198,9 @@ void mixed_RS_solve(double gammaL, double pinfL, double gammaR, double pinfR, co
   if (!RS.converged) g_status |= GFM_ST_NEWTON_NO_CONVERGE;
   if (p_star != p_star) g_status |= GFM_ST_NAN;
   g_newton_iters += RS.iterations;
+  g_mixed_calls += 1;
+  count_iters(RS.iterations);
+  g_mixed_iters += RS.iterations;
 }
 
 // ----------------------------------------------------------------------------
@@ -1038,7 +1045,12 @@ void phi_to(const sim_info& p, const griddoubletype& g, double* f) {
 extern "C" {
 
 uint32_t oracle_status(void) { return g_status; }
-void oracle_clear_status(void) { g_status = 0; g_newton_iters = 0; }
+void oracle_clear_status(void) {
+  g_status = 0; g_newton_iters = 0; g_mixed_calls = 0; g_mixed_iters = 0;
+  for (int k = 0; k < 16; k++) g_iter_hist[k] = 0;
+}
+void oracle_iter_histogram(int64_t* h) { for (int k = 0; k < 16; k++) h[k] = g_iter_hist[k]; }
+void oracle_mixed_stats(int64_t* calls, int64_t* iters) { *calls = g_mixed_calls; *iters = g_mixed_iters; }
 int64_t oracle_newton_iters(void) { return g_newton_iters; }
 
 double oracle_exp(double x) { return omath::exp(x); }

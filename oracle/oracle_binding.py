@@ -116,3 +116,18 @@ def clear_status():
 
 def newton_iters():
     return lib().oracle_newton_iters()
+
+
+def mixed_stats():
+    """(calls, Newton iterations) of the mixed Riemann solves since the last clear."""
+    a, b = ctypes.c_int64(), ctypes.c_int64()
+    lib().oracle_mixed_stats(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def iter_histogram():
+    """Riemann solves (pure and mixed) by Newton iteration count since the last
+    clear; entry 15 counts 15 or more."""
+    h = np.zeros(16, dtype=np.int64)
+    lib().oracle_iter_histogram(h.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    return h

@@ -15,6 +15,81 @@ using namespace gfm;
 
 std::atomic<long long> gfm::g_launches{0};
 
+// ---------------------------------------------------------------------------
+// SM partitions for the overlapped ghost fill: a 16-SM green context for the
+// interface chain and one for the remaining SMs, with one stream each,
+// created once per device.  The driver entry points are fetched through the
+// runtime, so the library does not link libcuda.  Without green-context
+// support two ordinary streams are used (same results, less isolation).
+// ---------------------------------------------------------------------------
+#include <cudaTypedefs.h>
+#include <mutex>
+
+namespace {
+std::mutex g_green_mutex;
+struct GreenPair { bool init; bool ok; cudaStream_t chain, far; };
+GreenPair g_green[64];
+
+template <typename F>
+bool entry(const char* name, F* fn, unsigned version = 12040) {
+  cudaDriverEntryPointQueryResult q;
+  void* p = nullptr;
+  if (cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p)
+    return false;
+  *fn = reinterpret_cast<F>(p);
+  return true;
+}
+
+bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far) {
+  PFN_cuDeviceGet_v2000 pDeviceGet;
+  PFN_cuDeviceGetDevResource_v12040 pGetRes;
+  PFN_cuDevSmResourceSplitByCount_v12040 pSplit;
+  PFN_cuDevResourceGenerateDesc_v12040 pDesc;
+  PFN_cuGreenCtxCreate_v12040 pCreate;
+  PFN_cuGreenCtxStreamCreate_v12050 pStream;
+  if (!entry("cuDeviceGet", &pDeviceGet) || !entry("cuDeviceGetDevResource", &pGetRes) ||
+      !entry("cuDevSmResourceSplitByCount", &pSplit) || !entry("cuDevResourceGenerateDesc", &pDesc) ||
+      !entry("cuGreenCtxCreate", &pCreate) || !entry("cuGreenCtxStreamCreate", &pStream, 12050))
+    return false;
+  CUdevice d;
+  if (pDeviceGet(&d, dev) != CUDA_SUCCESS) return false;
+  CUdevResource res, grp[1], rem;
+  if (pGetRes(d, &res, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return false;
+  unsigned nb = 1;
+  if (pSplit(grp, &nb, &res, &rem, 0, 16) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
+  CUdevResourceDesc d1, d2;
+  if (pDesc(&d1, grp, 1) != CUDA_SUCCESS || pDesc(&d2, &rem, 1) != CUDA_SUCCESS) return false;
+  CUgreenCtx g1, g2;
+  if (pCreate(&g1, d1, d, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS) return false;
+  if (pCreate(&g2, d2, d, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS) return false;
+  CUstream s1, s2;
+  if (pStream(&s1, g1, CU_STREAM_NON_BLOCKING, 0) != CUDA_SUCCESS) return false;
+  if (pStream(&s2, g2, CU_STREAM_NON_BLOCKING, 0) != CUDA_SUCCESS) return false;
+  *chain = reinterpret_cast<cudaStream_t>(s1);
+  *far = reinterpret_cast<cudaStream_t>(s2);
+  return true;
+}
+}  // namespace
+
+bool gfm::green_streams(int dev, cudaStream_t* chain, cudaStream_t* far) {
+  if (dev < 0 || dev >= 64) return false;
+  std::lock_guard<std::mutex> lk(g_green_mutex);
+  GreenPair& g = g_green[dev];
+  if (!g.init) {
+    g.init = true;
+    g.ok = make_green(dev, &g.chain, &g.far);
+    if (!g.ok) {
+      cudaGetLastError();
+      g.ok = cudaStreamCreateWithFlags(&g.chain, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&g.far, cudaStreamNonBlocking) == cudaSuccess;
+    }
+  }
+  *chain = g.chain;
+  *far = g.far;
+  return g.ok;
+}
+
 namespace {
 
 struct CtxExtra {
@@ -135,6 +210,19 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->ifc_out, sizeof(double) * 8 * cap);
     ctx->n_chunks = (int)(((int64_t)P.nr * P.nc + 2047) / 2048);
     alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)ctx->n_chunks);
+    for (int b = 0; b < 2; b++)
+      for (int f = 0; f < 2; f++) alloc((void**)&ctx->S[b][f], 4 * plane_b);
+    alloc((void**)&ctx->near_cell, (size_t)P.plane);
+    alloc((void**)&ctx->tile_near, sizeof(int) * (size_t)flux_tiles_x(P) * flux_tiles_y(P));
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_chain, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_far, cudaEventDisableTiming);
+    for (int q = 0; q < 5; q++)
+      if (e == cudaSuccess) e = cudaEventCreate(&ctx->tev[q]);
+    if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
+    ctx->overlap = ctx->overlap_ok;
   }
   if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_dtime, sizeof(DevTime));
   if (e != cudaSuccess) {
@@ -158,6 +246,14 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->nrm); cudaFree(ctx->vel); cudaFree(ctx->vel_t);
   cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
   cudaFree(ctx->ifc_out); cudaFree(ctx->chunk_count);
+  for (int b = 0; b < 2; b++)
+    for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
+  cudaFree(ctx->near_cell); cudaFree(ctx->tile_near);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_chain) cudaEventDestroy(ctx->ev_chain);
+  if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);
+  for (int q = 0; q < 5; q++)
+    if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
   cudaFree(ctx->dtime);
   cudaFree(extra(ctx).counters);
   cudaFree(extra(ctx).mass_part);
@@ -282,9 +378,11 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
   gfm_status_t r = check_method(ctx, m);
   if (r != GFM_OK) return r;
   ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
-  cudaEvent_t ev[GFM_NPHASES + 1];
+  cudaEvent_t ev[6];
   if (phase_ms)
-    for (int q = 0; q <= GFM_NPHASES; q++) CK(cudaEventCreate(&ev[q]));
+    for (int q = 0; q < 6; q++) CK(cudaEventCreate(&ev[q]));
+  ctx->timing = phase_ms ? 1 : 0;
+  bool overlapped = false;
   auto mark = [&](int q) {
     if (phase_ms) cudaEventRecord(ev[q], ctx->stream);
   };
@@ -294,10 +392,18 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
     launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
     mark(1);
     if (ctx->two_fluid) {
-      launch_ghost_fill(ctx, m);
-      mark(2);
-      launch_fs_update(ctx, m->fs, 3);
-      mark(3);
+      overlapped = ctx->overlap && (m->gfm == GFM_RIEMANN || m->gfm == GFM_REAL) && !m->use_extension_vfield;
+      if (overlapped) {
+        // ghost fill and flux update interleaved across SM partitions; the
+        // flux phase here is the update of the tiles near the interface
+        launch_ghost_fill_overlapped(ctx, m);
+        mark(3);
+      } else {
+        launch_ghost_fill(ctx, m);
+        mark(2);
+        launch_fs_update(ctx, m->fs, 3);
+        mark(3);
+      }
       launch_ls_update(ctx, m);
       int upd = ctx->steps_done_host + 1;
       if (m->reinit_every > 0 && upd % m->reinit_every == 0 && m->reinit_iters > 0) launch_reinit(ctx, m);
@@ -316,16 +422,24 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
     r = last_error();
     if (r != GFM_OK) break;
     if (phase_ms) {
-      CK(cudaEventSynchronize(ev[GFM_NPHASES]));
-      for (int q = 0; q < GFM_NPHASES; q++) {
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
-        phase_ms[q] += ms;
+      CK(cudaEventSynchronize(ev[5]));
+      float ms = 0.0f;
+      if (overlapped) {
+        // phases 1 and 2 split at the start of the near-interface flux update
+        cudaEventElapsedTime(&ms, ev[0], ev[1]); phase_ms[0] += ms;
+        cudaEventElapsedTime(&ms, ev[1], ctx->tev[4]); phase_ms[1] += ms;
+        cudaEventElapsedTime(&ms, ctx->tev[4], ev[3]); phase_ms[2] += ms;
+        for (int q = 3; q < 5; q++) { cudaEventElapsedTime(&ms, ev[q], ev[q + 1]); phase_ms[q] += ms; }
+        cudaEventElapsedTime(&ms, ctx->tev[0], ctx->tev[1]); phase_ms[5] += ms;
+        cudaEventElapsedTime(&ms, ctx->tev[0], ctx->tev[2]); phase_ms[6] += ms;
+        cudaEventElapsedTime(&ms, ctx->tev[1], ctx->tev[3]); phase_ms[7] += ms;
+      } else {
+        for (int q = 0; q < 5; q++) { cudaEventElapsedTime(&ms, ev[q], ev[q + 1]); phase_ms[q] += ms; }
       }
     }
   }
   if (phase_ms)
-    for (int q = 0; q <= GFM_NPHASES; q++) cudaEventDestroy(ev[q]);
+    for (int q = 0; q < 6; q++) cudaEventDestroy(ev[q]);
   return r;
 }
 
@@ -336,6 +450,13 @@ gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps) {
 gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms) {
   if (!phase_ms) return GFM_ERR_ARG;
   return step_impl(ctx, m, nsteps, phase_ms);
+}
+
+gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int enable) {
+  if (!ctx || (enable != 0 && enable != 1)) return GFM_ERR_ARG;
+  if (enable && !ctx->overlap_ok) return GFM_ERR_UNSUPPORTED;
+  ctx->overlap = enable;
+  return GFM_OK;
 }
 
 int64_t gfm_launch_count(void) { return (int64_t)g_launches.load(); }

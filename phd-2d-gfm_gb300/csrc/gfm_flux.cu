@@ -19,8 +19,8 @@
 
 namespace gfm {
 
-constexpr int TX = 32;
-constexpr int TY = 8;
+constexpr int TX = FLUX_TX;
+constexpr int TY = FLUX_TY;
 constexpr int NT = 256;
 constexpr int WR = TY + 4;   // primitive region rows   (i0-2 .. i0+TY+1)
 constexpr int WC = TX + 4;   // primitive region columns (j0-2 .. j0+TX+1)
@@ -43,6 +43,8 @@ struct FluxArgs {
   const DevTime* dtime;
   DevTime* dtime_w;
   int fluid_base;
+  const int* tile_near;   // per tile: region holds a cell near the interface
+  int tiles;              // TILES_ALL, TILES_FAR or TILES_NEAR
 };
 
 __device__ __forceinline__ V4 sW(const FluxSmem& s, int r, int c) {
@@ -134,6 +136,10 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   const int imin = rc[0], imax = rc[1], jmin = rc[2], jmax = rc[3];
 
   if (!active) return;   // the step after t reaches T changes nothing
+  if (a.tiles != TILES_ALL) {
+    const bool near = a.tile_near[blockIdx.y * gridDim.x + blockIdx.x] != 0;
+    if ((a.tiles == TILES_NEAR) != near) return;   // the other pass owns this tile
+  }
   // tile outside the realcells box: its cells keep their values
   const bool tile_live = !(i0 + TY <= imin || i0 >= imax || j0 + TX <= jmin || j0 >= jmax);
   if (!tile_live) {
@@ -269,11 +275,17 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
 static size_t flux_smem() { return sizeof(FluxSmem); }
 
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
+  launch_fs_update_sel(ctx, fs, fluid_mask, TILES_ALL, ctx->stream);
+}
+
+void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaStream_t stream) {
   const GridP& P = ctx->P;
   FluxArgs a;
   a.P = P;
   a.dtime = ctx->dtime;
   a.dtime_w = ctx->dtime;
+  a.tile_near = ctx->tile_near;
+  a.tiles = tiles;
   int nz = 0;
   a.fluid_base = (fluid_mask & 1) ? 0 : 1;
   for (int f = 0; f < 2; f++) {
@@ -291,9 +303,9 @@ void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
     attr_set = true;
   }
   if (fs == GFM_FS_MUSCL)
-    k_flux_update<true><<<grid, NT, sm, ctx->stream>>>(a);
+    k_flux_update<true><<<grid, NT, sm, stream>>>(a);
   else
-    k_flux_update<false><<<grid, NT, sm, ctx->stream>>>(a);
+    k_flux_update<false><<<grid, NT, sm, stream>>>(a);
   counted();
   // the new values are in Unew; launch_commit copies them (with the BCs) to U
 }

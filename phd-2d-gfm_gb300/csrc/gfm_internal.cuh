@@ -75,6 +75,18 @@ struct gfm_ctx {
   gfm::DevTime* dtime;
   gfm::DevTime* h_dtime;  // pinned host mirror
   int steps_done_host;
+  // overlapped ghost fill (Riemann and real GFM): the interface chain runs on
+  // a small SM partition while the far field is extrapolated and updated on
+  // the rest (see launch_ghost_fill_overlapped)
+  double* S[2][2];        // speculative extrapolation ping-pong [buffer][fluid]
+  uint8_t* near_cell;     // real cells within 6 (Chebyshev) of an interfacial cell
+  int* tile_near;         // per flux tile: its region holds a near cell
+  cudaStream_t s_chain, s_far;
+  cudaEvent_t ev_fork, ev_chain, ev_far;
+  cudaEvent_t tev[5];     // timing events of the overlapped schedule (gfm_step_timed)
+  int timing;
+  int overlap_ok;         // SM partitions (or two side streams) exist
+  int overlap;            // overlapped schedule in use (gfm_set_overlap)
 };
 
 namespace gfm {
@@ -117,8 +129,20 @@ __device__ __forceinline__ void raise_status(DevTime* dt, uint32_t bits) {
   if (bits) atomicOr(&dt->status, bits);
 }
 
+// flux-update tiles (k_flux_update): TX x TY real cells per CTA, 2-cell halo
+constexpr int FLUX_TX = 32;
+constexpr int FLUX_TY = 8;
+inline int flux_tiles_x(const GridP& P) { return (P.Nx + FLUX_TX - 1) / FLUX_TX; }
+inline int flux_tiles_y(const GridP& P) { return (P.Ny + FLUX_TY - 1) / FLUX_TY; }
+
+// tile selection of the flux update
+enum { TILES_ALL = 0, TILES_FAR = 1, TILES_NEAR = 2 };
+
 // kernel launch helpers (defined in the .cu files)
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask);
+void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaStream_t stream);
+bool green_streams(int device, cudaStream_t* chain, cudaStream_t* far);
+void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_bcs(gfm_ctx* ctx, int fluid_mask);
 void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);

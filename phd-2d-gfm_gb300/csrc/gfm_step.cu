@@ -336,6 +336,8 @@ __global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mas
 // launch per iteration.  mode 1 = extrapolate_vector_mgfm (interfacial cells
 // are left unchanged).
 // ---------------------------------------------------------------------------
+constexpr int IFC_OUT = 8;   // doubles of interface output per interfacial cell
+
 struct ExtrapArgs {
   GridP P;
   const double* S1; const double* S2;   // grid1/grid2 of this iteration
@@ -345,7 +347,20 @@ struct ExtrapArgs {
   const uint8_t* mask;
   const DevTime* D;
   int mgfm;
+  // overlay: the interface loop's writes (star state into the real fluid of
+  // each interfacial cell) applied on the fly to the source reads
+  const double* ov_out;
+  const int* ov_map;
+  int overlay;
 };
+
+__device__ __forceinline__ V4 ex_rd(const ExtrapArgs& a, int f, int64_t c) {
+  if (a.overlay && a.mask[c] && ((a.phi[c] <= 0.0) == (f == 0))) {
+    const double* o = a.ov_out + (int64_t)a.ov_map[c] * IFC_OUT;
+    return V4{o[0], o[1], o[2], o[3]};
+  }
+  return load4(f == 0 ? a.S1 : a.S2, a.P, c);
+}
 
 __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
   const GridP& P = a.P;
@@ -356,7 +371,7 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
     int i = (int)(k / P.nc), j = (int)(k % P.nc);
     BCSrc s = bc_source(P, i, j);
     int64_t c = cidx(P, s.i, s.j);
-    V4 v1 = load4(a.S1, P, c), v2 = load4(a.S2, P, c);
+    V4 v1 = ex_rd(a, 0, c), v2 = ex_rd(a, 1, c);
     bool skip = a.mgfm && a.mask[c];
     if (!skip) {
       double nx, ny;
@@ -364,13 +379,13 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
       double cx = (dt / P.dx) * nx, cy = (dt / P.dy) * ny;
       if (a.phi[c] <= 0.0) {
         // fluid 2 is ghost: information flows along -normal
-        V4 dxv = (nx > 0.0) ? v4d(load4(a.S2, P, c + 1), v2) : v4d(v2, load4(a.S2, P, c - 1));
-        V4 dyv = (ny > 0.0) ? v4d(load4(a.S2, P, c + P.pitch), v2) : v4d(v2, load4(a.S2, P, c - P.pitch));
+        V4 dxv = (nx > 0.0) ? v4d(ex_rd(a, 1, c + 1), v2) : v4d(v2, ex_rd(a, 1, c - 1));
+        V4 dyv = (ny > 0.0) ? v4d(ex_rd(a, 1, c + P.pitch), v2) : v4d(v2, ex_rd(a, 1, c - P.pitch));
         v2 = V4{(v2.a + cx * dxv.a) + cy * dyv.a, (v2.b + cx * dxv.b) + cy * dyv.b,
                 (v2.c + cx * dxv.c) + cy * dyv.c, (v2.d + cx * dxv.d) + cy * dyv.d};
       } else {
-        V4 dxv = (nx > 0.0) ? v4d(v1, load4(a.S1, P, c - 1)) : v4d(load4(a.S1, P, c + 1), v1);
-        V4 dyv = (ny > 0.0) ? v4d(v1, load4(a.S1, P, c - P.pitch)) : v4d(load4(a.S1, P, c + P.pitch), v1);
+        V4 dxv = (nx > 0.0) ? v4d(v1, ex_rd(a, 0, c - 1)) : v4d(ex_rd(a, 0, c + 1), v1);
+        V4 dyv = (ny > 0.0) ? v4d(v1, ex_rd(a, 0, c - P.pitch)) : v4d(ex_rd(a, 0, c + P.pitch), v1);
         v1 = V4{(v1.a - cx * dxv.a) - cy * dyv.a, (v1.b - cx * dxv.b) - cy * dyv.b,
                 (v1.c - cx * dxv.c) - cy * dyv.c, (v1.d - cx * dxv.d) - cy * dyv.d};
       }
@@ -404,7 +419,6 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
 // runs out sets ST_SCHEDULE_LIMIT and the thread abandons its cell.
 // ---------------------------------------------------------------------------
 enum { IFC_RIEMANN = 0, IFC_REAL = 1, IFC_MODIFIED = 2 };
-constexpr int IFC_OUT = 8;
 constexpr long long IFC_SPIN_LIMIT = 1ll << 24;
 
 struct IfcArgs {
@@ -611,6 +625,240 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-wide interface solve of the Riemann and real GFM.
+//
+// An FP64 warp instruction holds its sub-partition's FP64 pipe for the same
+// time whether 1 or 32 lanes are active, and the interface loop is a chain of
+// dependent cells, so the loop's speed is set by the number of FP64
+// instructions one cell issues.  Here all 32 lanes of a warp share one cell:
+//   lane = 16 s + 4 q + kc : probe side s (0: fluid 1, 1: fluid 2), bilinear
+//   corner q (bit 0: next column, bit 1: next row), state component kc.
+// Each lane reads one corner value, the four products of a bilinear sum are
+// formed at once and added in the scalar order, and the Riemann problem is
+// solved with side L on lanes 0-15 and side R on lanes 16-31
+// (mixed_rs_pair).  Every value comes from the same operations as in
+// k_interface, so the results are identical.
+// ---------------------------------------------------------------------------
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+__device__ __forceinline__ double xside(double x) { return __shfl_xor_sync(FULL_MASK, x, 16); }
+
+// component kc of ifc_read
+__device__ __forceinline__ double ifc_read1(const IfcArgs& a, int f, int i, int j, int kc, int64_t lin, bool& ok) {
+  const GridP& P = a.P;
+  int64_t c = cidx(P, i, j);
+  int64_t l2 = (int64_t)i * P.nc + j;
+  if (a.mask[c] && ((a.phi[c] <= 0.0) == (f == 0)) && l2 < lin) {
+    int p = a.ifc_map[c];
+    if (!ifc_wait(a, p)) { ok = false; return 0.0; }
+    return __ldcg(a.out + (int64_t)p * IFC_OUT + kc);
+  }
+  return (f == 0 ? a.W1 : a.W2)[c + kc * P.plane];
+}
+
+struct PairStar { double p, u, rho_own; bool trivial; };
+
+// mixed_rs (gfm_math.cuh) for the conserved state Uown of this lane's side
+// (isR: side R, gas k).  Each lane evaluates only its own side's conversion,
+// wave constants, pressure function and star density; quantities of both
+// sides are exchanged and combined with the scalar solver's operations, so
+// p* and u* are the scalar ones on every lane and rho_own is the star
+// density of the lane's side.  The Newton loop is warp-uniform: both halves
+// compute the same pressure iterates.
+__device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const Gas& kL, const Gas& kR, const V4& Uown,
+                                  uint32_t* status, int* iters) {
+  bool ok;
+  V4 Wp = cons_to_prims_phys(k.g, k.pinf, Uown, &ok);
+  if (!ok) *status |= ST_UNPHYSICAL;
+  RSSide S = rs_side(Wp.a, Wp.b, Wp.d, k);
+  const double ou = xside(S.u), op = xside(S.p);
+  const double uL = isR ? ou : S.u, uR = isR ? S.u : ou;
+  const double pL = isR ? op : S.p, pR = isR ? S.p : op;
+  PairStar r;
+  if (uL == uR && pL == pR) {   // rs_solve's no-wave shortcut
+    r.p = pL; r.u = uL; r.rho_own = S.rho; r.trivial = true;
+    return r;
+  }
+  r.trivial = false;
+  rs_side_consts(S, k);
+  const double orho = xside(S.rho), oc = xside(S.c), oG4c = xside(S.G4c), opb = xside(S.pb);
+  const double rhoL = isR ? orho : S.rho, rhoR = isR ? S.rho : orho;
+  const double cL = isR ? oc : S.c, cR = isR ? S.c : oc;
+  const double G4cL = isR ? oG4c : S.G4c, G4cR = isR ? S.G4c : oG4c;
+  const double pbL = isR ? opb : S.pb, pbR = isR ? S.pb : opb;
+  // rs_guess_pvrs
+  const double p0 = 0.5 * (pL + pR) - 0.125 * (uR - uL) * (rhoL + rhoR) * (cL + cR);
+  // rs_star
+  const double udiff = uR - uL;
+  if (G4cL + G4cR <= udiff) *status |= ST_VACUUM;
+  const double pinf_min = kL.pinf < kR.pinf ? kL.pinf : kR.pinf;
+  const double pbmin = pbL < pbR ? pbL : pbR;
+  const double pfl = 1e-6 * pbmin - pinf_min;
+  double pold = p0 > pfl ? p0 : pfl;
+  double fL = 0.0, fR = 0.0, p = pold;
+  int it = 0;
+  for (;;) {
+    double f, fd;
+    rs_prefun(S, k, pold, &f, &fd);
+    const double of = xside(f), ofd = xside(fd);
+    fL = isR ? of : f;
+    fR = isR ? f : of;
+    const double fLd = isR ? ofd : fd, fRd = isR ? fd : ofd;
+    p = pold - (fL + fR + udiff) / (fLd + fRd);
+    if (p < pfl) p = pfl;
+    it++;
+    bool conv = 2.0 * fabs(p - pold) <= GFM_RS_TOL * (p + pold + 2.0 * pinf_min);
+    pold = p;
+    if (conv) break;
+    if (it >= GFM_RS_MAXIT) { *status |= ST_NEWTON_NO_CONVERGE; break; }
+  }
+  r.p = p;
+  r.u = 0.5 * (uL + uR + fR - fL);
+  r.rho_own = rs_rho_star(S, k, p);
+  *iters += it;
+  return r;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int n = a.D->n_ifc;
+  const int lane = threadIdx.x & 31;
+  const int s = lane >> 4, q = (lane >> 2) & 3, kc = lane & 3;
+  const bool isR = s == 1;
+  const Gas k = isR ? P.gas2 : P.gas1;
+  uint32_t st = 0;
+  int iters = 0;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(a.ticket, 1u);
+    t = __shfl_sync(FULL_MASK, t, 0);
+    if (t >= n) break;
+    const int64_t lin = a.list[t];
+    const int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
+    const int64_t c = cidx(P, i, j);
+    const double lsval = a.phi[c];
+    const int sr = (lsval <= 0.0) ? 0 : 1;   // side of the cell's real fluid
+    double nx, ny;
+    unit_normal(a.nrm, P, c, nx, ny);
+    bool ok = true;
+    double v = 0.0;   // lanes with q == 0: component kc of side s's state
+    if (MODE == IFC_REAL) {
+      // neighbour with opposite phi sign and the closest normal
+      // (GFM_real.cpp:77-117); lane l < 9 is loop position l (xinc-major).
+      // Candidates more than 1e-6 below the largest clamped dot product are
+      // skipped as in k_interface; acos runs on the others at once and the
+      // first minimiser in loop order wins, as with the reference's strict <.
+      double dp = -3.0;
+      if (lane < 9) {
+        const int xinc = lane / 3 - 1, yinc = lane % 3 - 1;
+        const int64_t c2 = cidx(P, i + yinc, j + xinc);
+        if (lsval * a.phi[c2] <= 0.0) {
+          double ox, oy;
+          unit_normal(a.nrm, P, c2, ox, oy);
+          double d = nx * ox + ny * oy;
+          d = (d < -1.0) ? -1.0 : d;
+          d = (1.0 < d) ? 1.0 : d;
+          dp = d;
+        }
+      }
+      double dbest = dp;
+      for (int o = 8; o >= 1; o >>= 1) {
+        const double x = __shfl_xor_sync(FULL_MASK, dbest, o);
+        dbest = (x > dbest) ? x : dbest;
+      }
+      const bool elig = lane < 9 && !(dp < -2.0 || dp < dbest - 1e-6);
+      long long key = 0x7ff0000000000000LL;   // +inf: not a candidate
+      if (elig) {
+        const double ang = gfm_acos(dp);
+        if (ang == ang) key = as_bits(ang);   // angles are >= +0: bits order as values
+      }
+      int bl = (key == 0x7ff0000000000000LL) ? 32 : lane;
+      for (int o = 8; o >= 1; o >>= 1) {
+        const long long xk = __shfl_xor_sync(FULL_MASK, key, o);
+        const int xl = __shfl_xor_sync(FULL_MASK, bl, o);
+        if (xk < key || (xk == key && xl < bl)) { key = xk; bl = xl; }
+      }
+      bl = __shfl_sync(FULL_MASK, bl, 0);
+      int iopp = i, jopp = j;
+      if (bl == 32) st |= ST_BAD_ARGUMENT;
+      else { iopp = i + (bl % 3 - 1); jopp = j + (bl / 3 - 1); }
+      if (q == 0) {
+        if (s == sr) v = (s == 0 ? a.W1 : a.W2)[c + kc * P.plane];
+        else v = ifc_read1(a, s, iopp, jopp, kc, lin, ok);
+      }
+    } else {
+      // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33)
+      const double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
+      const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
+      const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
+      const double gx = a.nrm[c], gy = a.nrm[c + P.plane];
+      const double nm = a.nrm[c + 4 * P.plane];
+      double lv = lsval;
+      if (fabs(lv) > ds) lv = copysign(ds, lv);
+      double hx = nx, hy = ny;
+      if (nm < 1e-12) { hx = gx / nm; hy = gy / nm; }
+      const double ilx = ccx - lv * hx, ily = ccy - lv * hy;
+      // probe of side s: interface point + ds n (side 1) or - ds n (side 0)
+      const double dsx = ds * hx, dsy = ds * hy;
+      const double px = ilx + (isR ? dsx : -dsx);
+      const double py = ily + (isR ? dsy : -dsy);
+      const double sx = (px - P.x0) * P.idx + (double)P.g - 0.5;
+      const double sy = (py - P.y0) * P.idy + (double)P.g - 0.5;
+      int j0 = (int)floor(sx), i0 = (int)floor(sy);
+      j0 = min(max(j0, 0), P.nc - 2);
+      i0 = min(max(i0, 0), P.nr - 2);
+      const double wa = sx - (double)j0, wb = sy - (double)i0;
+      const double fa = (q & 1) ? wa : 1.0 - wa;
+      const double fb = (q & 2) ? wb : 1.0 - wb;
+      const double g = ifc_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
+      const double pr = (fa * fb) * g;
+      const double p1 = __shfl_down_sync(FULL_MASK, pr, 4);
+      const double p2 = __shfl_down_sync(FULL_MASK, pr, 8);
+      const double p3 = __shfl_down_sync(FULL_MASK, pr, 12);
+      v = ((pr + p1) + p2) + p3;
+    }
+    ok = __all_sync(FULL_MASK, ok);
+    if (!ok) {
+      st |= ST_SCHEDULE_LIMIT;
+      if (lane == 0) {
+        __threadfence();
+        ((volatile int*)a.done)[t] = 2;
+      }
+      continue;
+    }
+    const int base = lane & 16;
+    const double ia = __shfl_sync(FULL_MASK, v, base), ib = __shfl_sync(FULL_MASK, v, base + 1);
+    const double ic = __shfl_sync(FULL_MASK, v, base + 2), id = __shfl_sync(FULL_MASK, v, base + 3);
+    // mixed Riemann problem in the normal frame (e.g. GFM_riemann.cpp:76-122)
+    const double un = ib * nx + ic * ny;
+    const double tx = ib - un * nx, ty = ic - un * ny;
+    bool okp = true;
+    const V4 Us = prims_to_cons(k.g, k.pinf, V4{ia, un, 0.0, (1e-6 < id) ? id : 1e-6}, &okp);
+    if (!okp) st |= ST_UNPHYSICAL;
+    int it = 0;
+    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it);
+    if (lane == 0) iters += it;
+    if (m.p != m.p) st |= ST_NAN;
+    if (lane == 16 * sr) {
+      double* o = a.out + (int64_t)t * IFC_OUT;
+      const double snx = m.u * nx, sny = m.u * ny;
+      o[0] = m.rho_own; o[1] = snx + tx; o[2] = sny + ty; o[3] = m.p;
+      o[4] = snx; o[5] = sny;
+      __threadfence();
+      ((volatile int*)a.done)[t] = 1;
+    }
+  }
+  uint32_t wst = __reduce_or_sync(FULL_MASK, st);
+  unsigned wit = __reduce_add_sync(FULL_MASK, (unsigned)iters);
+  if (lane == 0) {
+    if (wst) atomicOr(&a.D->status, wst);
+    if (wit) atomicAdd(&a.D->newton_iters, (unsigned long long)wit);
+  }
+}
+
 // Reset of the per-step interface bookkeeping.
 __global__ void k_ifc_reset(int* done, int cap, unsigned int* ticket, const DevTime* D) {
   if (!D->active) return;
@@ -675,6 +923,8 @@ struct FinalArgs {
   DevTime* D;
   int ogfm;
   int vel_mode;   // 0: real-fluid velocity, 1: extension seeds (OGFM interfacial), 2: leave vel alone
+  const uint8_t* near_cell;
+  int sel;        // 0: every cell, 1: cells far from the interface, 2: near cells
 };
 
 __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
@@ -686,6 +936,11 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     int i = (int)(k / P.nc), j = (int)(k % P.nc);
     int64_t c = cidx(P, i, j);
+    if (a.sel) {   // a ghost cell is near when its boundary-condition source is
+      BCSrc s = bc_source(P, i, j);
+      const bool nr = a.near_cell[cidx(P, s.i, s.j)] != 0;
+      if ((a.sel == 2) != nr) continue;
+    }
     bool f1 = a.phi[c] <= 0.0;
     if (a.ogfm) {
       V4 w1 = load4(a.W1, P, c), w2 = load4(a.W2, P, c);
@@ -945,6 +1200,7 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.D1 = ctx->Wt[0]; e.D2 = ctx->Wt[1];
     e.phi = ctx->phi; e.nrm = ctx->nrm; e.mask = ctx->mask; e.D = ctx->dtime;
     e.mgfm = mgfm ? 1 : 0;
+    e.ov_out = nullptr; e.ov_map = nullptr; e.overlay = 0;
     k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
   }
@@ -997,6 +1253,8 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
     f.vel = ctx->vel; f.D = ctx->dtime;
     f.ogfm = 1;
     f.vel_mode = ext ? 1 : 0;
+    f.near_cell = nullptr;
+    f.sel = 0;
     k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
     k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted();
     if (ext) run_ext_vfield(ctx, 20);
@@ -1017,8 +1275,8 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
   int iblocks = 152;   // 4 warps per CTA: one chain warp per SM sub-partition
-  if (variant == GFM_RIEMANN) k_interface<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
-  else if (variant == GFM_REAL) k_interface<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
+  if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
+  else if (variant == GFM_REAL) k_interface_warp<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
   else k_interface<IFC_MODIFIED><<<iblocks, 128, 0, s>>>(ia);
   counted();
   if (ext) cudaMemsetAsync(ctx->vel, 0, sizeof(double) * 2 * P.plane, s);
@@ -1045,8 +1303,193 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   f.vel = ctx->vel; f.D = ctx->dtime;
   f.ogfm = 0;
   f.vel_mode = ext ? 2 : 0;
+  f.near_cell = nullptr;
+  f.sel = 0;
   k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
   if (ext) run_ext_vfield(ctx, 20);
+}
+
+// ---------------------------------------------------------------------------
+// Overlapped ghost fill for the Riemann and real GFM.
+//
+// The interface loop only writes the real fluid of interfacial cells, and
+// the six Jacobi sweeps of extrapolate_vector that follow move information
+// one cell per sweep (5-point stencil; ghost cells copy their BC source), so
+// the extrapolated primitives of every cell more than 6 cells (Chebyshev)
+// from all interfacial cells do not depend on the interface loop.  Those far
+// cells, and the flux update of tiles that read only far cells, are computed
+// from the pre-loop primitives on a large SM partition while the interface
+// loop (a latency-bound dependency chain) runs on a small one; the near cells
+// and near tiles are finished after it.  Results are identical to the
+// sequential schedule: every value is computed from the same inputs by the
+// same kernels.
+// ---------------------------------------------------------------------------
+constexpr int NEAR_RADIUS = 6;
+
+__global__ void k_near_mark(GridP P, const int* list, const DevTime* D, uint8_t* near_cell) {
+  if (!D->active) return;
+  const int n = D->n_ifc;
+  const int side = 2 * NEAR_RADIUS + 1;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)n * side * side;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int k = (int)(q / (side * side));
+    int r = (int)(q % (side * side));
+    int64_t lin = list[k];
+    int i = (int)(lin / P.nc) + r / side - NEAR_RADIUS;
+    int j = (int)(lin % P.nc) + r % side - NEAR_RADIUS;
+    if (P.periodic) {
+      i = ((i - P.g) % P.Ny + P.Ny) % P.Ny + P.g;
+      j = ((j - P.g) % P.Nx + P.Nx) % P.Nx + P.g;
+    } else if (!is_real(P, i, j)) {
+      continue;
+    }
+    near_cell[cidx(P, i, j)] = 1;
+  }
+}
+
+// one warp per flux tile: does the tile's read region (tile + 2-cell halo,
+// clamped as the flux kernel clamps it) hold a near cell?
+__global__ void k_tile_flags(GridP P, const uint8_t* near_cell, int* tile_near, int ntx, int nty, const DevTime* D) {
+  if (!D->active) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= ntx * nty) return;
+  const int tx = warp % ntx, ty = warp / ntx;
+  const int i0 = P.g + ty * FLUX_TY, j0 = P.g + tx * FLUX_TX;
+  const int WR = FLUX_TY + 4, WC = FLUX_TX + 4;
+  int any = 0;
+  for (int q = lane; q < WR * WC; q += 32) {
+    int i = min(max(i0 - 2 + q / WC, 0), P.nr - 1);
+    int j = min(max(j0 - 2 + q % WC, 0), P.nc - 1);
+    BCSrc s = bc_source(P, i, j);
+    any |= near_cell[cidx(P, s.i, s.j)];
+  }
+  any = __any_sync(0xffffffffu, any);
+  if (lane == 0) tile_near[warp] = any ? 1 : 0;
+}
+
+static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, double* D1, double* D2, bool overlay,
+                         cudaStream_t s) {
+  const GridP& P = ctx->P;
+  ExtrapArgs e;
+  e.P = P;
+  e.S1 = S1; e.S2 = S2; e.D1 = D1; e.D2 = D2;
+  e.phi = ctx->phi; e.nrm = ctx->nrm; e.mask = ctx->mask; e.D = ctx->dtime;
+  e.mgfm = 0;
+  e.ov_out = overlay ? ctx->ifc_out : nullptr;
+  e.ov_map = overlay ? ctx->ifc_map : nullptr;
+  e.overlay = overlay ? 1 : 0;
+  k_extrap<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(e);
+  counted();
+}
+
+static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStream_t s) {
+  const GridP& P = ctx->P;
+  FinalArgs f;
+  f.P = P;
+  f.W1 = const_cast<double*>(Wf[0]); f.W2 = const_cast<double*>(Wf[1]);
+  f.C1 = Wf[0]; f.C2 = Wf[1];
+  f.V1 = Wf[0]; f.V2 = Wf[1];
+  f.mask = ctx->mask; f.phi = ctx->phi;
+  f.U1 = ctx->U[0]; f.U2 = ctx->U[1];
+  f.vel = ctx->vel; f.D = ctx->dtime;
+  f.ogfm = 0;
+  f.vel_mode = 0;
+  f.near_cell = ctx->near_cell;
+  f.sel = sel;
+  k_finalize<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(f);
+  counted();
+}
+
+void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
+  const GridP& P = ctx->P;
+  cudaStream_t s = ctx->stream;
+  const int variant = m->gfm;
+  // conversion, normals, mask, ordered list of interfacial cells
+  PrimArgs pa;
+  pa.P = P;
+  pa.U1 = ctx->U[0]; pa.U2 = ctx->U[1];
+  pa.W1 = ctx->W[0]; pa.W2 = ctx->W[1];
+  pa.Wc1 = nullptr; pa.Wc2 = nullptr;
+  pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
+  pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
+  pa.check_both = (variant == GFM_RIEMANN) ? 1 : 0;
+  k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa);
+  counted();
+  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
+                                              ctx->ifc_map, ctx->dtime);
+  counted();
+  // near field: cells within NEAR_RADIUS of an interfacial cell, and tiles reading them
+  cudaMemsetAsync(ctx->near_cell, 0, (size_t)P.plane, s);
+  const int cap = P.Nx * P.Ny;
+  k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->near_cell);
+  counted();
+  const int ntx = flux_tiles_x(P), nty = flux_tiles_y(P);
+  k_tile_flags<<<(ntx * nty + 7) / 8, 256, 0, s>>>(P, ctx->near_cell, ctx->tile_near, ntx, nty, ctx->dtime);
+  counted();
+  // extrapolate_vector(2) before the Riemann GFM's interface loop
+  if (variant == GFM_RIEMANN) run_extrap(ctx, 2, false);
+  cudaEventRecord(ctx->ev_fork, s);
+  if (ctx->timing) cudaEventRecord(ctx->tev[0], s);
+
+  // chain partition: the interface loop
+  cudaStreamWaitEvent(ctx->s_chain, ctx->ev_fork, 0);
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, ctx->s_chain>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp),
+                                                               ctx->dtime);
+  counted();
+  IfcArgs ia;
+  ia.P = P;
+  ia.W1 = ctx->W[0]; ia.W2 = ctx->W[1];
+  ia.phi = ctx->phi; ia.nrm = ctx->nrm; ia.mask = ctx->mask;
+  ia.list = ctx->ifc_list; ia.ifc_map = ctx->ifc_map;
+  ia.done = ctx->ifc_done; ia.out = ctx->ifc_out;
+  ia.ticket = (unsigned int*)(ctx->ifc_opp);
+  ia.D = ctx->dtime;
+  ia.slip = m->use_slip_BCs;
+  const int chain_ctas = 16;   // 8 warps each: two chain warps per SM sub-partition
+  if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
+  else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
+  counted();
+  cudaEventRecord(ctx->ev_chain, ctx->s_chain);
+  if (ctx->timing) cudaEventRecord(ctx->tev[1], ctx->s_chain);
+
+  // far partition: extrapolation without the interface loop's writes,
+  // conserved grids of far cells, flux update of far tiles
+  cudaStreamWaitEvent(ctx->s_far, ctx->ev_fork, 0);
+  {
+    const double* src1 = ctx->W[0];
+    const double* src2 = ctx->W[1];
+    for (int it = 0; it < 6; it++) {
+      double** dst = ctx->S[it & 1];
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far);
+      src1 = dst[0]; src2 = dst[1];
+    }
+    const double* fin[2] = {src1, src2};
+    finalize_sel(ctx, fin, 1, ctx->s_far);
+  }
+  launch_fs_update_sel(ctx, m->fs, 3, TILES_FAR, ctx->s_far);
+  cudaEventRecord(ctx->ev_far, ctx->s_far);
+  if (ctx->timing) cudaEventRecord(ctx->tev[2], ctx->s_far);
+
+  // after the chain: the true extrapolation (the loop's writes overlaid on the
+  // first sweep's reads), conserved grids of near cells, flux update of near tiles
+  cudaStreamWaitEvent(s, ctx->ev_chain, 0);
+  {
+    double* bufA[2] = {ctx->Wt[0], ctx->Wt[1]};
+    double* bufB[2] = {ctx->Wc[0], ctx->Wc[1]};
+    const double* src1 = ctx->W[0];
+    const double* src2 = ctx->W[1];
+    for (int it = 0; it < 6; it++) {
+      double** dst = (it & 1) ? bufB : bufA;
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, s);
+      src1 = dst[0]; src2 = dst[1];
+    }
+    const double* fin[2] = {src1, src2};
+    finalize_sel(ctx, fin, 2, s);
+  }
+  if (ctx->timing) cudaEventRecord(ctx->tev[3], s);
+  cudaStreamWaitEvent(s, ctx->ev_far, 0);
+  if (ctx->timing) cudaEventRecord(ctx->tev[4], s);
+  launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, s);
 }
 
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {

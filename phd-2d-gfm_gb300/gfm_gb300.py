@@ -89,6 +89,8 @@ def lib():
         "gfm_ls_update": [P, ctypes.POINTER(MethodDesc)],
         "gfm_apply_bcs": [P, I],
         "gfm_step": [P, ctypes.POINTER(MethodDesc), I],
+        "gfm_step_timed": [P, ctypes.POINTER(MethodDesc), I, pd],
+        "gfm_set_overlap": [P, I],
         "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
         "gfm_clear_device_status": [P],
         "gfm_get_stats": [P, ctypes.POINTER(ctypes.c_int64)] * 1 + [ctypes.POINTER(ctypes.c_int64)] * 2,
@@ -104,6 +106,8 @@ def lib():
         f.restype = ctypes.c_int
     L.gfm_version.restype = ctypes.c_char_p
     L.gfm_version.argtypes = []
+    L.gfm_launch_count.restype = ctypes.c_int64
+    L.gfm_launch_count.argtypes = []
     _lib = L
     return L
 
@@ -242,6 +246,22 @@ class Context:
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         _check(lib().gfm_get_stats(self._p, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "gfm_get_stats")
         return {"n_interfacial": a.value, "rounds": b.value, "newton_iters": c.value}
+
+    def set_overlap(self, enable):
+        """Overlapped (SM-partitioned) schedule of the Riemann / real GFM on or
+        off; returns False when the context has no partitions to turn it on."""
+        rc = lib().gfm_set_overlap(self._p, 1 if enable else 0)
+        if rc == 4:
+            return False
+        _check(rc, "gfm_set_overlap")
+        return True
+
+    def step_timed(self, m, nsteps=1):
+        """gfm_step with per-phase device times; returns GFM_NPHASES (8)
+        milliseconds summed over the steps."""
+        ph = np.zeros(8)
+        _check(lib().gfm_step_timed(self._p, ctypes.byref(m), nsteps, _dptr(ph)), "gfm_step_timed")
+        return ph
 
     def fluid_mass(self, interiorsign):
         m = ctypes.c_double()

@@ -131,3 +131,32 @@ def test_determinism():
         ctx.close()
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("case,Nx,Ny,gfm", [("shock_bubble", 200, 80, "riemannGFM"),
+                                            ("underwater_explosion_sg", 96, 96, "realGFM")])
+def test_overlapped_schedule_matches_sequential(case, Nx, Ny, gfm):
+    """The SM-partitioned schedule (interface loop beside the far-field
+    update) and the one-stream schedule give bit-identical steps."""
+    desc, T = g.case_params("twofluid", case, Nx, Ny)
+    U1, U2, phi = g.case_init("twofluid", case, desc)
+    m = g.method(gfm=gfm, T=T, CFL=0.6, reinit_every=5)
+    outs = []
+    for ovl in (False, True):
+        ctx = g.Context(desc, two_fluid=True)
+        if not ctx.set_overlap(ovl):
+            ctx.close()
+            pytest.skip("no SM partitions on this device")
+        ctx.upload(U1, U2, phi)
+        ph = ctx.step_timed(m, 15)
+        assert np.all(ph >= 0.0)
+        if ovl:
+            # interface loop and far-field work lie inside phases 1-2
+            assert ph[5] <= ph[1] + ph[2] + 1e-3 and ph[6] <= ph[1] + ph[2] + 1e-3
+        else:
+            assert np.all(ph[5:] == 0.0)
+        outs.append(ctx.download())
+        assert ctx.status() == 0
+        ctx.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
