@@ -6,7 +6,9 @@
 // -ffp-contract=off build agrees bit for bit with --fmad=false kernels):
 //   * Tang's table-driven exp and log (ACM TOMS 15(2) 1989, 16(4) 1990), pow
 //     as exp(y log x), and acos by the asin Taylor series with half-angle
-//     reduction.  The table data come from the generated gfm_tables.h.
+//     reduction, polynomials in Horner form with fused multiply-adds (std::fma
+//     is correctly rounded, like the GPU's).  The table data come from the
+//     generated gfm_tables.h.
 //   * the stiffened-gas EOS that the reference takes from its absent
 //     PhD-Common dependency (call sites headers/euler_misc.hpp:46,59,77,96).
 //   * exact_rs_stiffenedgas, the absent exact solver called at
@@ -32,53 +34,73 @@ static const double ASINC[28] = GFM_ASIN_COEFFS;
 inline int64_t bits_of(double x) { int64_t b; std::memcpy(&b, &x, 8); return b; }
 inline double double_of(int64_t b) { double x; std::memcpy(&x, &b, 8); return x; }
 
+// Rounding constant: fma(x, c, 1.5 * 2^52) rounds x c to an integer n that
+// sits in the low mantissa bits.
+static const double ROUND_MAGIC = 6755399441055744.0;
+
 inline double exp(double x) {
-  if (std::isnan(x)) return x;
-  if (x > 709.78) return HUGE_VAL;
-  if (x < -745.2) return 0.0;
-  const double kd = std::rint(x * GFM_INV_LN2_64);
-  const int k = static_cast<int>(kd);
-  const double r = (x - kd * GFM_LN2_64_HI) - kd * GFM_LN2_64_LO;
-  const int j = k & 63;
-  const int m = (k - j) / 64;
-  // expm1(r) to degree 6: r + r^2 (1/2 + r (1/6 + r (1/24 + r (1/120 + r/720))))
+  const uint64_t ax = static_cast<uint64_t>(bits_of(x)) & 0x7fffffffffffffffULL;
+  const bool wide = ax >= 0x4086000000000000ULL;  // |x| >= 704 (or inf/NaN)
+  if (wide) {
+    if (std::isnan(x)) return x;
+    if (x > 709.78) return HUGE_VAL;
+    if (x < -745.2) return 0.0;
+  }
+  const double t = std::fma(x, GFM_INV_LN2_64, ROUND_MAGIC);
+  const int n = static_cast<int32_t>(static_cast<uint32_t>(bits_of(t) & 0xffffffff));
+  const double nd = t - ROUND_MAGIC;
+  const double r = std::fma(nd, -GFM_LN2_64_LO, std::fma(nd, -GFM_LN2_64_HI, x));
+  // expm1(r) to degree 6, Horner with fma:
+  // r + r^2 (1/2 + r (1/6 + r (1/24 + r (1/120 + r/720))))
   const double c6 = 0x1.6c16c16c16c17p-10, c5 = 0x1.1111111111111p-7, c4 = 0x1.5555555555555p-5,
                c3 = 0x1.5555555555555p-3;
-  const double q = r + (r * r) * (0.5 + r * (c3 + r * (c4 + r * (c5 + r * c6))));
-  double y = EXP2T[j] + EXP2T[j] * q;
-  if (m < -1020) {
-    y = y * double_of(static_cast<int64_t>(m + 1023 + 200) << 52);
-    return y * double_of(static_cast<int64_t>(1023 - 200) << 52);
+  const double h = std::fma(std::fma(std::fma(std::fma(r, c6, c5), r, c4), r, c3), r, 0.5);
+  const double q = std::fma(r * r, h, r);
+  const double tab = EXP2T[n & 63];
+  const double y = std::fma(tab, q, tab);
+  const int m = n >> 6;
+  if (wide && m < -1020) {
+    const double z = y * double_of(static_cast<int64_t>(m + 1023 + 200) << 52);
+    return z * double_of(static_cast<int64_t>(1023 - 200) << 52);
   }
-  return y * double_of(static_cast<int64_t>(m + 1023) << 52);
+  return double_of(bits_of(y) + (static_cast<int64_t>(m) << 52));
 }
 
 inline double log(double x) {
-  if (!(x > 0.0)) return (x == 0.0) ? -HUGE_VAL : std::nan("");
-  if (std::isinf(x)) return x;
   int64_t b = bits_of(x);
-  int expo = static_cast<int>((b >> 52) & 0x7ff);
-  if (expo == 0) {
-    x = x * 0x1p54;
-    b = bits_of(x);
-    expo = static_cast<int>((b >> 52) & 0x7ff) - 54;
+  int expo = 0;
+  const bool normal_pos = b >= 0x0010000000000000LL && b < 0x7ff0000000000000LL;
+  if (!normal_pos) {
+    if (!(x > 0.0)) return (x == 0.0) ? -HUGE_VAL : std::nan("");
+    if (std::isinf(x)) return x;
+    b = bits_of(x * 0x1p54);
+    expo = -54;
   }
-  expo -= 1023;
-  double mant = double_of((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-  if (mant >= 1.5) {  // mantissa in [0.75, 1.5): no cancellation near x = 1
-    mant = mant * 0.5;
+  expo += static_cast<int>(b >> 52) - 1023;
+  const int64_t frac = b & 0x000fffffffffffffLL;
+  // mantissa m in [0.75, 1.5) (no cancellation near x = 1); j = round(128 (m - 1)),
+  // halves away from zero, and F = 1 + j/128, all from the bits
+  int j;
+  double m, F;
+  if (frac >= (int64_t(1) << 51)) {
     expo += 1;
+    m = double_of(frac | 0x3fe0000000000000LL);
+    j = static_cast<int>((frac + (int64_t(1) << 45)) >> 46) - 64;
+    F = 0.5 + (64 + j) * 0x1p-7;
+  } else {
+    m = double_of(frac | 0x3ff0000000000000LL);
+    j = static_cast<int>((frac + (int64_t(1) << 44)) >> 45);
+    F = 1.0 + j * 0x1p-7;
   }
-  const double jd = std::rint((mant - 1.0) * 128.0);
-  const double F = 1.0 + jd * 0x1p-7;
-  const double r = (mant - F) * INVFT[static_cast<int>(jd) + 32];
-  // log1p(r) - r to degree 7
+  const double r = (m - F) * INVFT[j + 32];
+  // log1p(r) - r to degree 7, Horner with fma
   const double c3 = 0x1.5555555555555p-2, c5 = 0x1.999999999999ap-3, c6 = -0x1.5555555555555p-3,
                c7 = 0x1.2492492492492p-3;
-  const double poly = (r * r) * (-0.5 + r * (c3 + r * (-0.25 + r * (c5 + r * (c6 + r * c7)))));
+  const double h = std::fma(std::fma(std::fma(std::fma(std::fma(r, c7, c6), r, c5), r, -0.25), r, c3), r, -0.5);
+  const double poly = (r * r) * h;
   const double e = static_cast<double>(expo);
-  const double hi = e * GFM_LN2_HI + LOGFT[static_cast<int>(jd) + 32];
-  const double lo = e * GFM_LN2_LO + poly;
+  const double hi = std::fma(e, GFM_LN2_HI, LOGFT[j + 32]);
+  const double lo = std::fma(e, GFM_LN2_LO, poly);
   return hi + (r + lo);
 }
 
@@ -90,8 +112,8 @@ inline double pow(double x, double y) {
 inline double asin_series(double x) {
   const double s = x * x;
   double acc = ASINC[27];
-  for (int n = 26; n >= 1; n--) acc = ASINC[n] + s * acc;
-  return x + x * (s * acc);
+  for (int n = 26; n >= 1; n--) acc = std::fma(s, acc, ASINC[n]);
+  return std::fma(x, s * acc, x);
 }
 
 inline double acos(double x) {

@@ -111,61 +111,89 @@ GFM_HD double gfm_inf() { return from_bits(0x7ff0000000000000LL); }
 GFM_HD double gfm_nan() { return from_bits(0x7ff8000000000000LL); }
 
 // ---------------------------------------------------------------------------
-// exp: Tang (ACM TOMS 15(2), 1989) with a 64-entry table.
-//   x = (64 m + j) ln2/64 + r,  |r| <= ln2/128
-//   exp(x) = 2^m * 2^(j/64) * (1 + q(r)),  q = r + r^2 (1/2 + r (1/6 + ...))
-// exp(0) == 1 exactly.
+// The elementary functions are arranged for GB300's FP64 pipe, which is the
+// bottleneck of every kernel here: explicit fused multiply-adds (fma is
+// correctly rounded on the GPU and in C, so host and device agree), and the
+// range reduction's rounding, exponent and table index done with integer
+// operations on the bit pattern instead of FP64 instructions.
 // ---------------------------------------------------------------------------
+#define GFM_ROUND_MAGIC 0x1.8p52   // 1.5 * 2^52: x + MAGIC rounds x to an integer
+
+// exp: Tang (ACM TOMS 15(2), 1989) with a 64-entry table.
+//   n = round(x 64/ln2) (fma into 1.5*2^52), x = n ln2/64 + r, |r| <= ln2/128
+//   exp(x) = 2^(n>>6) * 2^((n&63)/64) * (1 + q(r)),
+//   q = r + r^2 (1/2 + r (1/6 + r (1/24 + r (1/120 + r/720))))   (Horner, fma)
+// exp(0) == 1 exactly.  11 FP64 instructions for |x| < 704.
 GFM_HD double gfm_exp(double x) {
-  if (x != x) return x;
-  if (x > 709.78) return gfm_inf();
-  if (x < -745.2) return 0.0;
-  double kd = rint(x * GFM_INV_LN2_64);
-  int k = (int)kd;
-  double r = (x - kd * GFM_LN2_64_HI) - kd * GFM_LN2_64_LO;
-  int j = k & 63;
-  int m = (k - j) / 64;
-  double q = r + (r * r) * (0.5 + r * (0x1.5555555555555p-3 + r * (0x1.5555555555555p-5 +
-                 r * (0x1.1111111111111p-7 + r * 0x1.6c16c16c16c17p-10))));
-  double t = tab_exp2(j);
-  double y = t + t * q;
-  if (m < -1020) {  // result near or below the normal range: scale in two steps
-    y = y * from_bits((int64_t)(m + 1023 + 200) << 52);
-    return y * from_bits((int64_t)(1023 - 200) << 52);
+  const int64_t bx = as_bits(x);
+  const bool big = ((bx >> 32) & 0x7fffffff) >= 0x40860000;   // |x| >= 704, inf or NaN
+  if (big) {
+    if (x != x) return x;
+    if (x > 709.78) return gfm_inf();
+    if (x < -745.2) return 0.0;
   }
-  return y * from_bits((int64_t)(m + 1023) << 52);
+  const double t = fma(x, GFM_INV_LN2_64, GFM_ROUND_MAGIC);
+  const int k = (int)(uint32_t)as_bits(t);   // n, from the low mantissa bits
+  const double kd = t - GFM_ROUND_MAGIC;
+  double r = fma(kd, -GFM_LN2_64_HI, x);     // exact: kd * HI is exact
+  r = fma(kd, -GFM_LN2_64_LO, r);
+  double p = fma(r, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7);
+  p = fma(p, r, 0x1.5555555555555p-5);
+  p = fma(p, r, 0x1.5555555555555p-3);
+  p = fma(p, r, 0.5);
+  const double q = fma(r * r, p, r);
+  const double tj = tab_exp2(k & 63);
+  const double y = fma(tj, q, tj);
+  const int m = k >> 6;   // floor(n / 64)
+  if (big && m < -1020) {  // result near or below the normal range: scale in two steps
+    const double z = y * from_bits((int64_t)(m + 1023 + 200) << 52);
+    return z * from_bits((int64_t)(1023 - 200) << 52);
+  }
+  return from_bits(as_bits(y) + ((int64_t)m << 52));   // y * 2^m (normal result)
 }
 
-// ---------------------------------------------------------------------------
 // log: Tang (ACM TOMS 16(4), 1990) with a 97-entry table.
 //   x = 2^e * m, m in [0.75, 1.5) (so x near 1 has e = 0 and no cancellation)
-//   F = 1 + j/128 nearest to m (j = -32..64);  f = m - F (exact)
+//   F = 1 + j/128 nearest to m (j = -32..64, ties away from zero, from the
+//   mantissa bits);  f = m - F (exact)
 //   log(x) = e ln2 + log(F) + log1p(r),  r = f * (1/F),  |r| <= 2^-8 / 0.75
-// log(1) == 0 exactly.
-// ---------------------------------------------------------------------------
+//   log1p(r) - r = r^2 (-1/2 + r (1/3 + r (-1/4 + r (1/5 + r (-1/6 + r/7)))))
+// log(1) == 0 exactly.  14 FP64 instructions for normal positive x.
 GFM_HD double gfm_log(double x) {
-  if (!(x > 0.0)) return (x == 0.0) ? -gfm_inf() : gfm_nan();
-  if (x == gfm_inf()) return x;
   int64_t b = as_bits(x);
-  int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0) {  // subnormal
-    x = x * 0x1p54;
-    b = as_bits(x);
-    e = (int)((b >> 52) & 0x7ff) - 54;
+  int e = 0;
+  if ((uint64_t)(b - 0x0010000000000000LL) >= (uint64_t)(0x7ff0000000000000LL - 0x0010000000000000LL)) {
+    // zero, subnormal, negative, inf or NaN
+    if (!(x > 0.0)) return (x == 0.0) ? -gfm_inf() : gfm_nan();
+    if (x == gfm_inf()) return x;
+    b = as_bits(x * 0x1p54);   // subnormal
+    e = -54;
   }
-  e -= 1023;
-  double m = from_bits((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-  if (m >= 1.5) { m = m * 0.5; e += 1; }
-  double jd = rint((m - 1.0) * 128.0);
-  int j = (int)jd + 32;
-  double F = 1.0 + jd * 0x1p-7;
-  double f = m - F;
-  double r = f * tab_invf(j);
-  double p = (r * r) * (-0.5 + r * (0x1.5555555555555p-2 + r * (-0.25 + r * (0x1.999999999999ap-3 +
-                 r * (-0x1.5555555555555p-3 + r * 0x1.2492492492492p-3)))));
-  double ed = (double)e;
-  double hi = ed * GFM_LN2_HI + tab_logf(j);
-  double lo = ed * GFM_LN2_LO + p;
+  e += (int)(b >> 52) - 1023;
+  const int64_t mant = b & 0x000fffffffffffffLL;
+  int j;
+  int64_t mbits, fbits;
+  if (mant >= (1LL << 51)) {   // 1.mant >= 1.5: m = 1.mant / 2 in [0.75, 1)
+    e += 1;
+    mbits = mant | 0x3fe0000000000000LL;
+    j = (int)((mant + (1LL << 45)) >> 46) - 64;      // round(128 (m - 1))
+    fbits = 0x3fe0000000000000LL + ((int64_t)(64 + j) << 46);
+  } else {                     // m = 1.mant in [1, 1.5)
+    mbits = mant | 0x3ff0000000000000LL;
+    j = (int)((mant + (1LL << 44)) >> 45);
+    fbits = 0x3ff0000000000000LL + ((int64_t)j << 45);
+  }
+  const double f = from_bits(mbits) - from_bits(fbits);
+  const double r = f * tab_invf(j + 32);
+  double a = fma(r, 0x1.2492492492492p-3, -0x1.5555555555555p-3);
+  a = fma(a, r, 0x1.999999999999ap-3);
+  a = fma(a, r, -0.25);
+  a = fma(a, r, 0x1.5555555555555p-2);
+  a = fma(a, r, -0.5);
+  const double p = (r * r) * a;
+  const double ed = (double)e;
+  const double hi = fma(ed, GFM_LN2_HI, tab_logf(j + 32));   // exact product
+  const double lo = fma(ed, GFM_LN2_LO, p);
   return hi + (r + lo);
 }
 
@@ -179,8 +207,8 @@ GFM_HD double gfm_pow(double x, double y) {
 GFM_HD double gfm_asin_small(double x) {
   double s = x * x;
   double acc = tab_asin(27);
-  for (int n = 26; n >= 1; n--) acc = tab_asin(n) + s * acc;
-  return x + x * (s * acc);
+  for (int n = 26; n >= 1; n--) acc = fma(s, acc, tab_asin(n));
+  return fma(x, s * acc, x);
 }
 
 // acos on [-1, 1]: series for |x| <= 0.5, half-angle reduction otherwise.

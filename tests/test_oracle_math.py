@@ -76,3 +76,31 @@ def test_log_domain(x):
     L = orc.lib()
     assert math.isnan(L.oracle_log(x))
     assert L.oracle_log(0.0) == -math.inf
+
+
+def test_exp_range_ends():
+    """Arguments around the fast path's |x| < 704 limit, down to subnormal
+    and zero results and up to the overflow threshold."""
+    L = orc.lib()
+    xs = np.concatenate([np.linspace(-745.1, -690.0, 3001), np.linspace(690.0, 709.78, 2001),
+                         [703.999999, 704.0, -703.999999, -704.0, -708.4, -708.39641853226408]])
+    for x in xs:
+        ref = math.exp(float(x))
+        got = L.oracle_exp(float(x))
+        if ref < 2.2250738585072014e-308:   # subnormal result: absolute error in units of the smallest subnormal
+            assert abs(got - ref) <= 5e-324 * 2, (x, got, ref)
+        else:
+            assert ulp_err(got, ref) < 2.0, (x, got, ref)
+    assert L.oracle_exp(709.79) == math.inf and L.oracle_exp(-745.3) == 0.0
+
+
+def test_log_table_ties_and_boundaries():
+    """Mantissas exactly halfway between two table points (rounded away from
+    zero), and the 0.75 / 1.5 split of the reduced mantissa."""
+    L = orc.lib()
+    xs = [1.0 + (2 * k + 1) / 256.0 for k in range(64)] + [0.5 + (2 * k + 1) / 512.0 for k in range(32)]
+    xs += [1.5, np.nextafter(1.5, 0.0), 0.75, np.nextafter(0.75, 0.0), 3.0, np.nextafter(3.0, 0.0)]
+    for x in xs:
+        ref = math.log(float(x))
+        got = L.oracle_log(float(x))
+        assert abs(got - ref) <= 3.0 * abs(ref) * EPS + 1e-300, (x, got, ref)
