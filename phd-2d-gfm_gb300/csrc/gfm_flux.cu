@@ -12,7 +12,10 @@
 //            reference recomputes these per face (as cell C, L or B); each
 //            cell's values do not depend on which face asks for them.
 //   phase 3  per face: the second fallback, primitives -> conserved, and the
-//            exact Riemann flux (pure_RS_exact::solve_RP).
+//            exact Riemann flux (pure_RS_exact::solve_RP).  Faces whose data
+//            hold no waves are finished at once; the others are queued and
+//            solved by consecutive threads afterwards, so that the Newton
+//            iterations run with few idle lanes.
 //   phase 4  per cell: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn, the
 //            accumulation order of the reference's face loop (:290-292).
 #include "gfm_internal.cuh"
@@ -34,6 +37,8 @@ struct FluxSmem {
   double fs[4][4][SR][SC];      // [face L,R,B,T][component][r][c]
   double fx[4][TY][TX + 1];
   double fy[4][TY + 1][TX];
+  double qd[4][NXF + NYF];      // queued faces: uR, pR, utL, utR (rhoL, uL, pL, rhoR sit in the flux slot)
+  unsigned short qid[NXF + NYF];
 };
 
 struct FluxArgs {
@@ -85,8 +90,8 @@ __device__ __forceinline__ void cell_face_states(const V4& W, const V4& Ww, cons
   V4 R = V4{W.a + 0.5 * sxv.a, W.b + 0.5 * sxv.b, W.c + 0.5 * sxv.c, W.d + 0.5 * sxv.d};
   V4 B = V4{W.a - 0.5 * syv.a, W.b - 0.5 * syv.b, W.c - 0.5 * syv.c, W.d - 0.5 * syv.d};
   V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
-  if (!is_physical_primitives(gam, pinf, L) || !is_physical_primitives(gam, pinf, R)) { L = W; R = W; }
-  if (!is_physical_primitives(gam, pinf, B) || !is_physical_primitives(gam, pinf, T)) { B = W; T = W; }
+  if (!is_physical_primitives_fast(gam, pinf, L) || !is_physical_primitives_fast(gam, pinf, R)) { L = W; R = W; }
+  if (!is_physical_primitives_fast(gam, pinf, B) || !is_physical_primitives_fast(gam, pinf, T)) { B = W; T = W; }
   double cs = eos_soundspeed(gam, pinf, W.d, W.a);
   double irho = 1.0 / W.a, rcc = W.a * cs * cs;
   V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
@@ -98,22 +103,30 @@ __device__ __forceinline__ void cell_face_states(const V4& W, const V4& Ww, cons
 }
 
 // Phase 3 for one face (MUSCL): second physicality fallback (FS_MUSCL.cpp:276-285)
-// to the cells' primitives Wr/Wl, primitives -> conserved sharing e with the
-// check, and the exact Riemann flux (:287-288).  Sr/Sl: evolved face states
-// of the cell on the high / low side of the face.
-__device__ __forceinline__ V4 muscl_face_flux(bool xdir, V4 Sr, V4 Sl, const V4& Wr, const V4& Wl, const Gas& gas,
-                                              uint32_t* st, int* iters) {
+// to the cells' primitives Wr/Wl and primitives -> conserved sharing e with
+// the check; the exact Riemann flux (:287-288) follows.  Sr/Sl: evolved face
+// states of the cell on the high / low side of the face.
+__device__ __forceinline__ void muscl_face_cons(V4 Sr, V4 Sl, const V4& Wr, const V4& Wl, const Gas& gas,
+                                                uint32_t* st, V4& UL, V4& UR) {
   const double gam = gas.g, pinf = gas.pinf;
   double er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
   double el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
-  if (!(er >= 0.0 && Sr.a >= 0.0) || !(el >= 0.0 && Sl.a >= 0.0)) {
+  if (!(c_ge0(er) && c_ge0(Sr.a)) || !(c_ge0(el) && c_ge0(Sl.a))) {
     Sr = Wr;
     Sl = Wl;
     er = eos_specific_ie(gam, pinf, Sr.d, Sr.a);
     el = eos_specific_ie(gam, pinf, Sl.d, Sl.a);
   }
-  if (!(Sl.a >= 0.0 && el >= 0.0) || !(Sr.a >= 0.0 && er >= 0.0)) *st |= ST_UNPHYSICAL;
-  return pure_rs_flux(xdir, gas, prims_to_cons_e(Sl, el), prims_to_cons_e(Sr, er), st, iters);
+  if (!(c_ge0(Sl.a) && c_ge0(el)) || !(c_ge0(Sr.a) && c_ge0(er))) *st |= ST_UNPHYSICAL;
+  UL = prims_to_cons_e(Sl, el);
+  UR = prims_to_cons_e(Sr, er);
+}
+
+__device__ __forceinline__ V4 muscl_face_flux(bool xdir, V4 Sr, V4 Sl, const V4& Wr, const V4& Wl, const Gas& gas,
+                                              uint32_t* st, int* iters) {
+  V4 UL, UR;
+  muscl_face_cons(Sr, Sl, Wr, Wl, gas, st, UL, UR);
+  return pure_rs_flux(xdir, gas, UL, UR, st, iters);
 }
 
 template <bool MUSCL>
@@ -121,6 +134,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FluxSmem& s = *reinterpret_cast<FluxSmem*>(smem_raw);
   __shared__ V4 s_uniform_flux[2];
+  __shared__ int s_nq;   // queued faces (phase 3)
   const GridP& P = a.P;
   const int fluid = a.fluid_base + blockIdx.z;
   const double* __restrict__ U = a.U[blockIdx.z];
@@ -163,6 +177,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   // whole region holds one bit pattern
   const int64_t c00 = cidx(P, min(max(i0 - 2, 0), P.nr - 1), min(max(j0 - 2, 0), P.nc - 1));
   const V4 u00 = load4(U, P, c00);
+  if (tid == 0) s_nq = 0;
   bool same = true;
   for (int k = tid; k < WR * WC; k += NT) {
     int r = k / WC, c = k % WC;
@@ -210,28 +225,55 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
       }
       __syncthreads();
     }
-    // phase 3: x faces (TY rows x TX+1) then y faces (TY+1 rows x TX)
+    // phase 3a: x faces (TY rows x TX+1) then y faces (TY+1 rows x TX) up to
+    // the no-wave test; those without waves are finished, the others queued
     //   x face (fr, fc): between cells (i0+fr, j0+fc-1) and (i0+fr, j0+fc)
     //   y face (fr, fc): between cells (i0+fr-1, j0+fc) and (i0+fr, j0+fc)
+    // Flux slot of face k, component m: fx[m] (flat) + k, or fy[m] + k - NXF.
     for (int k = tid; k < NXF + NYF; k += NT) {
       bool xdir = k < NXF;
       int fr, fc;
       if (xdir) { fr = k / (TX + 1); fc = k % (TX + 1); }
       else { int q = k - NXF; fr = q / TX; fc = q % TX; }
-      V4 f;
+      V4 UL, UR;
       if (MUSCL) {
         if (xdir)
-          f = muscl_face_flux(true, sFS(s, 0, fr + 1, fc + 1), sFS(s, 1, fr + 1, fc), sW(s, fr + 2, fc + 2),
-                              sW(s, fr + 2, fc + 1), gas, &st, &iters);
+          muscl_face_cons(sFS(s, 0, fr + 1, fc + 1), sFS(s, 1, fr + 1, fc), sW(s, fr + 2, fc + 2),
+                          sW(s, fr + 2, fc + 1), gas, &st, UL, UR);
         else
-          f = muscl_face_flux(false, sFS(s, 2, fr + 1, fc + 1), sFS(s, 3, fr, fc + 1), sW(s, fr + 2, fc + 2),
-                              sW(s, fr + 1, fc + 2), gas, &st, &iters);
+          muscl_face_cons(sFS(s, 2, fr + 1, fc + 1), sFS(s, 3, fr, fc + 1), sW(s, fr + 2, fc + 2),
+                          sW(s, fr + 1, fc + 2), gas, &st, UL, UR);
       } else {
-        if (xdir) f = pure_rs_flux(true, gas, sW(s, fr + 2, fc + 1), sW(s, fr + 2, fc + 2), &st, &iters);
-        else f = pure_rs_flux(false, gas, sW(s, fr + 1, fc + 2), sW(s, fr + 2, fc + 2), &st, &iters);
+        if (xdir) { UL = sW(s, fr + 2, fc + 1); UR = sW(s, fr + 2, fc + 2); }
+        else { UL = sW(s, fr + 1, fc + 2); UR = sW(s, fr + 2, fc + 2); }
       }
-      if (xdir) { s.fx[0][fr][fc] = f.a; s.fx[1][fr][fc] = f.b; s.fx[2][fr][fc] = f.c; s.fx[3][fr][fc] = f.d; }
-      else { s.fy[0][fr][fc] = f.a; s.fy[1][fr][fc] = f.b; s.fy[2][fr][fc] = f.c; s.fy[3][fr][fc] = f.d; }
+      FaceData d;
+      const bool nowave = rs_face_front(xdir, gas, UL, UR, &st, d);
+      double* slot = xdir ? &s.fx[0][0][0] + k : &s.fy[0][0][0] + (k - NXF);
+      const int cs = xdir ? NXF : NYF;
+      if (nowave) {
+        V4 f = rs_face_finish(xdir, gas, d, &st, &iters);
+        slot[0] = f.a; slot[cs] = f.b; slot[2 * cs] = f.c; slot[3 * cs] = f.d;
+      } else {
+        const int e = atomicAdd(&s_nq, 1);
+        s.qid[e] = (unsigned short)k;
+        slot[0] = d.rhoL; slot[cs] = d.uL; slot[2 * cs] = d.pL; slot[3 * cs] = d.rhoR;
+        s.qd[0][k] = d.uR; s.qd[1][k] = d.pR; s.qd[2][k] = d.utL; s.qd[3][k] = d.utR;
+      }
+    }
+    __syncthreads();
+    // phase 3b: the queued faces
+    const int nq = s_nq;
+    for (int e = tid; e < nq; e += NT) {
+      const int k = s.qid[e];
+      const bool xdir = k < NXF;
+      double* slot = xdir ? &s.fx[0][0][0] + k : &s.fy[0][0][0] + (k - NXF);
+      const int cs = xdir ? NXF : NYF;
+      FaceData d;
+      d.rhoL = slot[0]; d.uL = slot[cs]; d.pL = slot[2 * cs]; d.rhoR = slot[3 * cs];
+      d.uR = s.qd[0][k]; d.pR = s.qd[1][k]; d.utL = s.qd[2][k]; d.utR = s.qd[3][k];
+      V4 f = rs_face_finish(xdir, gas, d, &st, &iters);
+      slot[0] = f.a; slot[cs] = f.b; slot[2 * cs] = f.c; slot[3 * cs] = f.d;
     }
     __syncthreads();
   }
@@ -245,7 +287,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
     int64_t ci = cidx(P, i, j);
     V4 u = load4(U, P, ci);
     if (i >= imin && i < imax && j >= jmin && j < jmax) {
-      if (!is_physical_state(u)) st |= ST_UNPHYSICAL;
+      if (!is_physical_state_fast(u)) st |= ST_UNPHYSICAL;
       double o[4] = {u.a, u.b, u.c, u.d};
       const double ux[4] = {ufx.a, ufx.b, ufx.c, ufx.d}, uy[4] = {ufy.a, ufy.b, ufy.c, ufy.d};
       for (int q = 0; q < 4; q++) {

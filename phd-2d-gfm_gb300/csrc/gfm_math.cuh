@@ -111,6 +111,85 @@ GFM_HD double gfm_inf() { return from_bits(0x7ff0000000000000LL); }
 GFM_HD double gfm_nan() { return from_bits(0x7ff8000000000000LL); }
 
 // ---------------------------------------------------------------------------
+// IEEE comparisons on the integer pipe.  On GB300 an FP64 compare holds the
+// FP64 pipe about as long as a multiply-add, and that pipe bounds every kernel
+// here, while integer instructions issue beside it.  Each function returns
+// exactly what the C comparison returns for all doubles, NaN and signed zeros
+// included; host builds use the C comparison itself.
+//   key: |x| bits for x >= +0, -(|x| bits) for x <= -0, so -0 and +0 share 0
+// ---------------------------------------------------------------------------
+#define GFM_MAG_BITS 0x7fffffffffffffffLL
+#define GFM_INF_BITS 0x7ff0000000000000LL
+
+GFM_HD bool nan_bits(int64_t b) { return (b & GFM_MAG_BITS) > GFM_INF_BITS; }
+GFM_HD int64_t order_key(int64_t b) { return b < 0 ? -(b & GFM_MAG_BITS) : b; }
+GFM_HD bool i_lt(double a, double b) {
+  const int64_t x = as_bits(a), y = as_bits(b);
+  return !nan_bits(x) && !nan_bits(y) && order_key(x) < order_key(y);
+}
+GFM_HD bool i_le(double a, double b) {
+  const int64_t x = as_bits(a), y = as_bits(b);
+  return !nan_bits(x) && !nan_bits(y) && order_key(x) <= order_key(y);
+}
+GFM_HD bool i_eq(double a, double b) {
+  const int64_t x = as_bits(a), y = as_bits(b);
+  return !nan_bits(x) && order_key(x) == order_key(y);
+}
+GFM_HD bool i_gt0(double a) { const int64_t x = as_bits(a); return x > 0 && x <= GFM_INF_BITS; }
+GFM_HD bool i_ge0(double a) {
+  const int64_t x = as_bits(a);
+  return (x >= 0 && x <= GFM_INF_BITS) || x == (int64_t)0x8000000000000000ULL;
+}
+GFM_HD bool i_lt0(double a) {
+  const int64_t x = as_bits(a), m = x & GFM_MAG_BITS;
+  return x < 0 && m != 0 && m <= GFM_INF_BITS;
+}
+GFM_HD bool i_le0(double a) {
+  const int64_t x = as_bits(a), m = x & GFM_MAG_BITS;
+  return m == 0 || (x < 0 && m <= GFM_INF_BITS);
+}
+// (n / d) >= 0.0 without the division where the operands decide it: the
+// quotient's sign is the XOR of the signs, NaN comes from a NaN operand, 0/0
+// or inf/inf, and a negative quotient reads as -0 (>= 0) only when it
+// underflows, which needs exponents about 1000 apart; then the division
+// itself decides.
+GFM_HD bool i_quotient_ge0(double n, double d) {
+  const int64_t x = as_bits(n), y = as_bits(d);
+  const int64_t mx = x & GFM_MAG_BITS, my = y & GFM_MAG_BITS;
+  if (mx > GFM_INF_BITS || my > GFM_INF_BITS) return false;
+  if (mx == 0) return my != 0;
+  if (mx == GFM_INF_BITS && my == GFM_INF_BITS) return false;
+  if ((x ^ y) >= 0) return true;
+  if (my == GFM_INF_BITS) return true;
+  if ((int)(mx >> 52) - (int)(my >> 52) > -900) return false;
+  return n / d >= 0.0;
+}
+#if defined(__CUDA_ARCH__)
+GFM_HD bool c_lt(double a, double b) { return i_lt(a, b); }
+GFM_HD bool c_le(double a, double b) { return i_le(a, b); }
+GFM_HD bool c_eq(double a, double b) { return i_eq(a, b); }
+GFM_HD bool c_gt0(double a) { return i_gt0(a); }
+GFM_HD bool c_ge0(double a) { return i_ge0(a); }
+GFM_HD bool c_lt0(double a) { return i_lt0(a); }
+GFM_HD bool c_le0(double a) { return i_le0(a); }
+GFM_HD bool c_isnan(double a) { return nan_bits(as_bits(a)); }
+GFM_HD bool quotient_ge0(double n, double d) { return i_quotient_ge0(n, d); }
+#else
+GFM_HD bool c_lt(double a, double b) { return a < b; }
+GFM_HD bool c_le(double a, double b) { return a <= b; }
+GFM_HD bool c_eq(double a, double b) { return a == b; }
+GFM_HD bool c_gt0(double a) { return a > 0.0; }
+GFM_HD bool c_ge0(double a) { return a >= 0.0; }
+GFM_HD bool c_lt0(double a) { return a < 0.0; }
+GFM_HD bool c_le0(double a) { return a <= 0.0; }
+GFM_HD bool c_isnan(double a) { return a != a; }
+GFM_HD bool quotient_ge0(double n, double d) { return n / d >= 0.0; }
+#endif
+GFM_HD bool c_gt(double a, double b) { return c_lt(b, a); }
+GFM_HD bool c_ge(double a, double b) { return c_le(b, a); }
+
+
+// ---------------------------------------------------------------------------
 // The elementary functions are arranged for GB300's FP64 pipe, which is the
 // bottleneck of every kernel here: explicit fused multiply-adds (fma is
 // correctly rounded on the GPU and in C, so host and device agree), and the
@@ -199,7 +278,7 @@ GFM_HD double gfm_log(double x) {
 
 // pow for x >= 0 (all uses have a positive base): exp(y log x); pow(1,y) == 1.
 GFM_HD double gfm_pow(double x, double y) {
-  if (x == 0.0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : gfm_inf());
+  if ((as_bits(x) & GFM_MAG_BITS) == 0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : gfm_inf());
   return gfm_exp(y * gfm_log(x));
 }
 
@@ -253,12 +332,29 @@ GFM_HD bool is_physical_state(const V4& U) {
   double u = U.b / rho;
   double v = U.c / rho;
   double e = (U.d / rho) - 0.5 * (u * u + v * v);
-  return rho >= 0.0 && e >= 0.0;
+  return c_ge0(rho) && c_ge0(e);
+}
+// is_physical_state without its three divisions when the state is plainly
+// physical: rho > 0, E > 0 and 2 E rho >= (1 + 2^-40) ((rho u)^2 + (rho v)^2)
+// with 2 E rho a normal number well inside the range put e = E/rho -
+// (u^2 + v^2)/2 above zero by far more than the rounding of either form.
+GFM_HD bool is_physical_state_fast(const V4& U) {
+  if (c_gt0(U.a) && c_gt0(U.d)) {
+    const double lhs = 2.0 * (U.d * U.a);
+    const double rhs = (U.b * U.b + U.c * U.c) * (1.0 + 0x1p-40);
+    const int el = (int)(as_bits(lhs) >> 52);
+    if (el > 200 && el < 2047 && c_le(rhs, lhs)) return true;
+  }
+  return is_physical_state(U);
 }
 // euler_misc.hpp:44-49
 GFM_HD bool is_physical_primitives(double g, double pinf, const V4& W) {
   double e = eos_specific_ie(g, pinf, W.d, W.a);
-  return e >= 0.0 && W.a >= 0.0;
+  return c_ge0(e) && c_ge0(W.a);
+}
+// the same test with e's sign taken from its numerator and denominator
+GFM_HD bool is_physical_primitives_fast(double g, double pinf, const V4& W) {
+  return quotient_ge0(W.d + g * pinf, (g - 1.0) * W.a) && c_ge0(W.a);
 }
 // euler_misc.hpp:52-67
 GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
@@ -276,7 +372,7 @@ GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys) {
   double u = U.b / rho;
   double v = U.c / rho;
   double e = (U.d / rho) - 0.5 * (u * u + v * v);
-  *phys = rho >= 0.0 && e >= 0.0;
+  *phys = c_ge0(rho) && c_ge0(e);
   double p = eos_pressure(g, pinf, e, rho);
   return V4{rho, u, v, p};
 }
@@ -298,7 +394,7 @@ GFM_HD V4 flux_primitive_var(double g, double pinf, const V4& W) {
 GFM_HD V4 prims_to_cons(double g, double pinf, const V4& W, bool* ok) {
   double rho = W.a, u = W.b, v = W.c, p = W.d;
   double e = eos_specific_ie(g, pinf, p, rho);
-  if (ok) *ok = (rho >= 0.0) && (e >= 0.0);
+  if (ok) *ok = c_ge0(rho) && c_ge0(e);
   return V4{rho, rho * u, rho * v, rho * e + 0.5 * rho * (u * u + v * v)};
 }
 
@@ -363,7 +459,7 @@ GFM_HD void rs_side_consts(RSSide& s, const Gas& k) {
 // Toro's PREFUN: pressure function f_K and its derivative at pressure p.
 GFM_HD void rs_prefun(const RSSide& K, const Gas& k, double p, double* f, double* fd) {
   double pb = p + k.pinf;
-  if (p > K.p) {  // shock
+  if (c_gt(p, K.p)) {  // shock
     double r = 1.0 / (pb + K.BK);
     double qrt = sqrt(K.AK * r);
     *f = (p - K.p) * qrt;
@@ -392,21 +488,32 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   RSStar s;
   s.status = ST_OK;
   double udiff = R.u - L.u;
-  if (L.G4c + R.G4c <= udiff) s.status |= ST_VACUUM;
-  double pinf_min = kL.pinf < kR.pinf ? kL.pinf : kR.pinf;
-  double pbmin = L.pb < R.pb ? L.pb : R.pb;
+  if (c_le(L.G4c + R.G4c, udiff)) s.status |= ST_VACUUM;
+  double pinf_min = c_lt(kL.pinf, kR.pinf) ? kL.pinf : kR.pinf;
+  double pbmin = c_lt(L.pb, R.pb) ? L.pb : R.pb;
   double pfl = 1e-6 * pbmin - pinf_min;
-  double pold = p0 > pfl ? p0 : pfl;
+  double pold = c_gt(p0, pfl) ? p0 : pfl;
   double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0;
   double p = pold;
   int it = 0;
+  // The lower-pressure side is evaluated first: with p between the two side
+  // pressures it takes the shock branch and the other side the rarefaction
+  // branch, so neighbouring solves (the lanes of a warp) tend to take the
+  // same branch in each call.  Each call depends only on its own side, so
+  // the values are those of evaluating L then R.
+  const bool rfirst = c_lt(R.p, L.p);
+  const RSSide A = rfirst ? R : L, B = rfirst ? L : R;
+  const Gas kA = rfirst ? kR : kL, kB = rfirst ? kL : kR;
   for (;;) {
-    rs_prefun(L, kL, pold, &fL, &fLd);
-    rs_prefun(R, kR, pold, &fR, &fRd);
+    double fA, fAd, fB, fBd;
+    rs_prefun(A, kA, pold, &fA, &fAd);
+    rs_prefun(B, kB, pold, &fB, &fBd);
+    fL = rfirst ? fB : fA; fLd = rfirst ? fBd : fAd;
+    fR = rfirst ? fA : fB; fRd = rfirst ? fAd : fBd;
     p = pold - (fL + fR + udiff) / (fLd + fRd);
-    if (p < pfl) p = pfl;
+    if (c_lt(p, pfl)) p = pfl;
     it++;
-    bool conv = 2.0 * fabs(p - pold) <= GFM_RS_TOL * (p + pold + 2.0 * pinf_min);
+    bool conv = c_le(2.0 * fabs(p - pold), GFM_RS_TOL * (p + pold + 2.0 * pinf_min));
     pold = p;
     if (conv) break;
     if (it >= GFM_RS_MAXIT) { s.status |= ST_NEWTON_NO_CONVERGE; break; }
@@ -425,7 +532,7 @@ GFM_HD double rs_guess_pvrs(const RSSide& L, const RSSide& R) {
 // Whole solve.  When u and p agree on both sides the data hold at most a
 // contact and the exact answer p* = p, u* = u is returned without iterating.
 GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR) {
-  if (L.u == R.u && L.p == R.p) {
+  if (c_eq(L.u, R.u) && c_eq(L.p, R.p)) {
     RSStar s;
     s.p = L.p;
     s.u = L.u;
@@ -444,7 +551,7 @@ GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR) {
 // Star density behind the K wave (shock or rarefaction).
 GFM_HD double rs_rho_star(const RSSide& K, const Gas& k, double pstar) {
   double pr = (pstar + k.pinf) * K.ipb;
-  if (pstar > K.p) return K.rho * ((pr + k.G6) / (pr * k.G6 + 1.0));
+  if (c_gt(pstar, K.p)) return K.rho * ((pr + k.G6) / (pr * k.G6 + 1.0));
   return K.rho * gfm_pow(pr, k.IG);
 }
 
@@ -454,17 +561,17 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
                       double S) {
   RS1D w;
   if (st.trivial) {
-    if (S <= st.u) { w.rho = L.rho; w.u = L.u; w.p = L.p; }
+    if (c_le(S, st.u)) { w.rho = L.rho; w.u = L.u; w.p = L.p; }
     else { w.rho = R.rho; w.u = R.u; w.p = R.p; }
     return w;
   }
-  if (S <= st.u) {  // left of contact
-    if (st.p <= L.p) {  // left rarefaction
+  if (c_le(S, st.u)) {  // left of contact
+    if (c_le(st.p, L.p)) {  // left rarefaction
       double shl = L.u - L.c;
-      if (S <= shl) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
+      if (c_le(S, shl)) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
       double cml = L.c * gfm_pow((st.p + kL.pinf) * L.ipb, kL.G1);
       double stl = st.u - cml;
-      if (S > stl) { w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w; }
+      if (c_gt(S, stl)) { w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w; }
       double c = kL.G5 * (L.c + kL.G7 * (L.u - S));
       double cr = c / L.c;
       w.rho = L.rho * gfm_pow(cr, kL.G4);
@@ -474,21 +581,21 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
     } else {  // left shock
       double pml = (st.p + kL.pinf) * L.ipb;
       double sl = L.u - L.c * sqrt(kL.G2 * pml + kL.G1);
-      if (S <= sl) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
+      if (c_le(S, sl)) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
       w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w;
     }
   } else {  // right of contact
-    if (st.p > R.p) {  // right shock
+    if (c_gt(st.p, R.p)) {  // right shock
       double pmr = (st.p + kR.pinf) * R.ipb;
       double sr = R.u + R.c * sqrt(kR.G2 * pmr + kR.G1);
-      if (S >= sr) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
+      if (c_ge(S, sr)) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
       w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w;
     } else {  // right rarefaction
       double shr = R.u + R.c;
-      if (S >= shr) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
+      if (c_ge(S, shr)) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
       double cmr = R.c * gfm_pow((st.p + kR.pinf) * R.ipb, kR.G1);
       double str = st.u + cmr;
-      if (S <= str) { w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w; }
+      if (c_le(S, str)) { w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w; }
       double c = kR.G5 * (R.c - kR.G7 * (R.u - S));
       double cr = c / R.c;
       w.rho = R.rho * gfm_pow(cr, kR.G4);
@@ -500,24 +607,45 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
 }
 
 // pure_RS_exact::solve_RP (sourcecode/pure_RS_exact.cpp:9-73): flux of the
-// exact solution at x/t = 0 between conserved states UL and UR, one material.
-GFM_HD V4 pure_rs_flux(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
+// exact solution at x/t = 0 between conserved states UL and UR, one material,
+// in two parts so that a kernel can set aside the faces whose data hold waves
+// and solve those together:
+//   rs_face_front  the conversions, the 1D states (rho, u_n, p) of both sides
+//                  and their tangential velocities; returns rs_solve's
+//                  no-wave test (equal u_n and p)
+//   rs_face_finish the solve, the sample at x/t = 0 and the flux.
+struct FaceData { double rhoL, uL, pL, rhoR, uR, pR, utL, utR; };
+
+GFM_HD bool rs_face_front(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status,
+                          FaceData& d) {
   bool okL, okR;
   V4 Lp = cons_to_prims_phys(k.g, k.pinf, UL, &okL);
   V4 Rp = cons_to_prims_phys(k.g, k.pinf, UR, &okR);
   if (!okL || !okR) *status |= ST_UNPHYSICAL;
-  double uLn = paralleltox ? Lp.b : Lp.c;
-  double uRn = paralleltox ? Rp.b : Rp.c;
-  RSSide L = rs_side(Lp.a, uLn, Lp.d, k);
-  RSSide R = rs_side(Rp.a, uRn, Rp.d, k);
+  d.rhoL = Lp.a; d.uL = paralleltox ? Lp.b : Lp.c; d.pL = Lp.d;
+  d.rhoR = Rp.a; d.uR = paralleltox ? Rp.b : Rp.c; d.pR = Rp.d;
+  d.utL = paralleltox ? Lp.c : Lp.b;
+  d.utR = paralleltox ? Rp.c : Rp.b;
+  return c_eq(d.uL, d.uR) && c_eq(d.pL, d.pR);
+}
+
+GFM_HD V4 rs_face_finish(bool paralleltox, const Gas& k, const FaceData& d, uint32_t* status, int* iters) {
+  RSSide L = rs_side(d.rhoL, d.uL, d.pL, k);
+  RSSide R = rs_side(d.rhoR, d.uR, d.pR, k);
   RSStar st = rs_solve(L, k, R, k);
   *status |= st.status;
   *iters += st.iters;
   RS1D w = rs_sample(L, k, R, k, st, 0.0);
-  double ut = paralleltox ? (st.u <= 0.0 ? Rp.c : Lp.c) : (st.u <= 0.0 ? Rp.b : Lp.b);
+  double ut = c_le0(st.u) ? d.utR : d.utL;
   V4 f = flux_primitive_var(k.g, k.pinf, V4{w.rho, w.u, ut, w.p});
   if (!paralleltox) { double t = f.b; f.b = f.c; f.c = t; }
   return f;
+}
+
+GFM_HD V4 pure_rs_flux(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
+  FaceData d;
+  rs_face_front(paralleltox, k, UL, UR, status, d);
+  return rs_face_finish(paralleltox, k, d, status, iters);
 }
 
 // mixed_RS_exact::solve_mixed_RP (sourcecode/mixed_RS_exact.cpp:8-48).
@@ -537,18 +665,18 @@ GFM_HD MixedStar mixed_rs(const Gas& kL, const Gas& kR, const V4& UL, const V4& 
   m.u_star = st.u;
   m.rho_star_L = st.trivial ? L.rho : rs_rho_star(L, kL, st.p);
   m.rho_star_R = st.trivial ? R.rho : rs_rho_star(R, kR, st.p);
-  if (m.p_star != m.p_star) *status |= ST_NAN;
+  if (c_isnan(m.p_star)) *status |= ST_NAN;
   return m;
 }
 
 // minmod slope, one component (sourcecode/FS_MUSCL.cpp:310-327)
 GFM_HD double minmod(double dL, double dR) {
-  if (dR > 0.0) {
-    double m = (dR < dL) ? dR : dL;     // std::min(dL, dR)
-    return (0.0 < m) ? m : 0.0;         // std::max(0.0, m)
+  if (c_gt0(dR)) {
+    double m = c_lt(dR, dL) ? dR : dL;  // std::min(dL, dR)
+    return c_gt0(m) ? m : 0.0;          // std::max(0.0, m)
   }
-  double m = (dL < dR) ? dR : dL;       // std::max(dL, dR)
-  return (m < 0.0) ? m : 0.0;           // std::min(0.0, m)
+  double m = c_lt(dL, dR) ? dR : dL;    // std::max(dL, dR)
+  return c_lt0(m) ? m : 0.0;            // std::min(0.0, m)
 }
 
 }  // namespace gfm

@@ -836,7 +836,7 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
     const double un = ib * nx + ic * ny;
     const double tx = ib - un * nx, ty = ic - un * ny;
     bool okp = true;
-    const V4 Us = prims_to_cons(k.g, k.pinf, V4{ia, un, 0.0, (1e-6 < id) ? id : 1e-6}, &okp);
+    const V4 Us = prims_to_cons(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
     if (!okp) st |= ST_UNPHYSICAL;
     int it = 0;
     const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it);
