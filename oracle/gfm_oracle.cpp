@@ -189,6 +189,7 @@ void mixed_RS_solve(double gammaL, double pinfL, double gammaR, double pinfR, co
   double Lb[3] = {Lprims[0], Lprims[1], Lprims[3]};
   double Rb[3] = {Rprims[0], Rprims[1], Rprims[3]};
   exact_rs_stiffenedgas RS(gammaL, gammaR, pinfL, pinfR);
+  RS.two_shock_guess = true;
   RS.solve_RP(Lb, Rb);
   p_star = RS.P_STAR;
   u_star = RS.S_STAR;

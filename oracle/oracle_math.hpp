@@ -150,7 +150,12 @@ inline double isentropic_extrapolation(double gamma, double pinf, double rho1, d
 // G6 = (g-1)/(g+1), G7 = (g-1)/2, IG = 1/g; per side pb = p + pinf,
 // 1/rho, 1/pb, c = sqrt(g pb (1/rho)), A = G5 (1/rho), B = G6 pb, G4 c,
 // 1/(rho c) = c (1/pb) (1/g);
-// Newton stops when 2|p - p_old| <= 1e-12 (p + p_old + 2 min(pinf)).
+// Newton stops when 2|p - p_old| <= 1e-7 (p + p_old + 2 min(pinf)): the
+// pressure function f is increasing and concave with |f''/f'| <= 3.5/(p+pinf),
+// so a step that small leaves the new iterate within about 2e-14 (relative) of
+// the root.  Initial guess: PVRS (Toro eq. 4.47); the mixed (two-material)
+// solve refines it by the two-shock approximation (TSRS, Toro eq. 9.42) with
+// the shock constants taken at max(PVRS, floor).
 class exact_rs_stiffenedgas {
  public:
   struct Gas {
@@ -184,6 +189,7 @@ class exact_rs_stiffenedgas {
   double P_STAR = 0.0, S_STAR = 0.0, rho_star_L = 0.0, rho_star_R = 0.0;
   int iterations = 0;
   bool vacuum = false, converged = true, trivial = false;
+  bool two_shock_guess = false;   // set for mixed_RS_exact's solves
 
   exact_rs_stiffenedgas(double gammaL, double gammaR, double pinf_L, double pinf_R)
       : KL(gammaL, pinf_L), KR(gammaR, pinf_R) {}
@@ -234,8 +240,15 @@ class exact_rs_stiffenedgas {
       const double pfloor = 1e-6 * pbmin - pinfmin;
       // PVRS initial guess (Toro eq. 4.47)
       const double ppv = 0.5 * (SL.p + SR.p) - 0.125 * (SR.u - SL.u) * (SL.rho + SR.rho) * (SL.c + SR.c);
-      double pold = ppv > pfloor ? ppv : pfloor;
-      double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0, p = pold;
+      double p0 = ppv;
+      if (two_shock_guess) {
+        const double pg = ppv > pfloor ? ppv : pfloor;
+        const double gL = std::sqrt(SL.A / (pg + KL.pinf + SL.B));
+        const double gR = std::sqrt(SR.A / (pg + KR.pinf + SR.B));
+        p0 = (gL * SL.p + gR * SR.p - (SR.u - SL.u)) / (gL + gR);
+      }
+      double pold = p0 > pfloor ? p0 : pfloor;
+      double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0, p = pold, dp = 0.0;
       int it = 0;
       while (true) {
         prefun(pold, SL, KL, fL, fLd);
@@ -243,13 +256,16 @@ class exact_rs_stiffenedgas {
         p = pold - (fL + fR + udiff) / (fLd + fRd);
         if (p < pfloor) p = pfloor;
         it++;
-        const bool conv = 2.0 * std::fabs(p - pold) <= 1e-12 * (p + pold + 2.0 * pinfmin);
+        const bool conv = 2.0 * std::fabs(p - pold) <= 1e-7 * (p + pold + 2.0 * pinfmin);
+        dp = p - pold;
         pold = p;
         if (conv) break;
         if (it >= MAXIT) { converged = false; break; }
       }
       P_STAR = p;
-      S_STAR = 0.5 * (SL.u + SR.u + fR - fL);
+      // pressure functions carried from the last evaluation point to p* along
+      // their tangents, so u* keeps the accuracy of p*
+      S_STAR = 0.5 * (SL.u + SR.u + (fR + fRd * dp) - (fL + fLd * dp));
       iterations = it;
     }
     rho_star_L = star_density(P_STAR, SL, KL);

@@ -15,7 +15,8 @@
 //   * misc:: state algebra, headers/euler_misc.hpp:23-180.
 //   * exact stiffened-gas Riemann solver: Toro, "Riemann Solvers and Numerical
 //     Methods for Fluid Dynamics", ch. 4 (pressure functions, Newton-Raphson
-//     from the PVRS guess, sampling), with p -> p + p_inf.  It replaces the
+//     from the PVRS guess, refined by the two-shock guess for two materials,
+//     sampling), with p -> p + p_inf.  It replaces the
 //     absent exact_rs_stiffenedgas used at sourcecode/pure_RS_exact.cpp:29-45
 //     and sourcecode/mixed_RS_exact.cpp:33-47.
 #pragma once
@@ -404,7 +405,10 @@ GFM_HD V4 prims_to_cons(double g, double pinf, const V4& W, bool* ok) {
 // Arithmetic is arranged for GB300, where an FP64 division or square root
 // costs about ten multiplies: every gamma-derived constant is computed once
 // per material (Gas), every per-side reciprocal once per solve (RSSide), and
-// Newton's stopping test is 2|p - p_old| <= TOL (p + p_old + 2 pinf_min).
+// Newton's stopping test is 2|p - p_old| <= TOL (p + p_old + 2 pinf_min) with
+// TOL = 1e-7: the pressure function f is increasing and concave with
+// |f''/f'| <= 3.5/(p + pinf), so a step that small leaves the new iterate
+// within about 2e-14 (relative) of the root.
 // ---------------------------------------------------------------------------
 struct Gas {
   double g, pinf;
@@ -479,11 +483,11 @@ struct RSStar {
   bool trivial;       // equal u and p: no waves, W_L | W_R across the contact
 };
 
-#define GFM_RS_TOL 1e-12
+#define GFM_RS_TOL 1e-7
 #define GFM_RS_MAXIT 60
 
 // Newton-Raphson on p* (Toro's STARPU) from the initial guess p0, then u*
-// from the last pressure-function evaluation.
+// from the last pressure-function evaluation taken to p* along its tangent.
 GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, double p0) {
   RSStar s;
   s.status = ST_OK;
@@ -494,7 +498,7 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   double pfl = 1e-6 * pbmin - pinf_min;
   double pold = c_gt(p0, pfl) ? p0 : pfl;
   double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0;
-  double p = pold;
+  double p = pold, dp = 0.0;
   int it = 0;
   // The lower-pressure side is evaluated first: with p between the two side
   // pressures it takes the shock branch and the other side the rarefaction
@@ -514,12 +518,15 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
     if (c_lt(p, pfl)) p = pfl;
     it++;
     bool conv = c_le(2.0 * fabs(p - pold), GFM_RS_TOL * (p + pold + 2.0 * pinf_min));
+    dp = p - pold;
     pold = p;
     if (conv) break;
     if (it >= GFM_RS_MAXIT) { s.status |= ST_NEWTON_NO_CONVERGE; break; }
   }
   s.p = p;
-  s.u = 0.5 * (L.u + R.u + fR - fL);
+  // the pressure functions carried from the last evaluation point to p along
+  // their tangents, so u* keeps the accuracy of p*
+  s.u = 0.5 * (L.u + R.u + (fR + fRd * dp) - (fL + fLd * dp));
   s.iters = it;
   return s;
 }
@@ -529,9 +536,17 @@ GFM_HD double rs_guess_pvrs(const RSSide& L, const RSSide& R) {
   return 0.5 * (L.p + R.p) - 0.125 * (R.u - L.u) * (L.rho + R.rho) * (L.c + R.c);
 }
 
+// Two-shock guess (TSRS, Toro eq. 9.42) with the shock constants taken at pg;
+// used by the mixed (two-material) solve, whose data hold strong waves.
+GFM_HD double rs_guess_tsrs(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, double pg) {
+  const double gL = sqrt(L.AK / (pg + kL.pinf + L.BK));
+  const double gR = sqrt(R.AK / (pg + kR.pinf + R.BK));
+  return (gL * L.p + gR * R.p - (R.u - L.u)) / (gL + gR);
+}
+
 // Whole solve.  When u and p agree on both sides the data hold at most a
 // contact and the exact answer p* = p, u* = u is returned without iterating.
-GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR) {
+GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR, bool two_shock = false) {
   if (c_eq(L.u, R.u) && c_eq(L.p, R.p)) {
     RSStar s;
     s.p = L.p;
@@ -543,7 +558,14 @@ GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR) {
   }
   rs_side_consts(L, kL);
   rs_side_consts(R, kR);
-  RSStar s = rs_star(L, kL, R, kR, rs_guess_pvrs(L, R));
+  double p0 = rs_guess_pvrs(L, R);
+  if (two_shock) {   // at max(PVRS, the Newton floor of rs_star)
+    const double pinf_min = c_lt(kL.pinf, kR.pinf) ? kL.pinf : kR.pinf;
+    const double pbmin = c_lt(L.pb, R.pb) ? L.pb : R.pb;
+    const double pfl = 1e-6 * pbmin - pinf_min;
+    p0 = rs_guess_tsrs(L, kL, R, kR, c_gt(p0, pfl) ? p0 : pfl);
+  }
+  RSStar s = rs_star(L, kL, R, kR, p0);
   s.trivial = false;
   return s;
 }
@@ -657,7 +679,7 @@ GFM_HD MixedStar mixed_rs(const Gas& kL, const Gas& kR, const V4& UL, const V4& 
   if (!okL || !okR) *status |= ST_UNPHYSICAL;
   RSSide L = rs_side(Lp.a, Lp.b, Lp.d, kL);
   RSSide R = rs_side(Rp.a, Rp.b, Rp.d, kR);
-  RSStar st = rs_solve(L, kL, R, kR);
+  RSStar st = rs_solve(L, kL, R, kR, true);
   *status |= st.status;
   *iters += st.iters;
   MixedStar m;

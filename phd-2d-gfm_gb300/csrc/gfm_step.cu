@@ -676,7 +676,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   const double uL = isR ? ou : S.u, uR = isR ? S.u : ou;
   const double pL = isR ? op : S.p, pR = isR ? S.p : op;
   PairStar r;
-  if (uL == uR && pL == pR) {   // rs_solve's no-wave shortcut
+  if (c_eq(uL, uR) && c_eq(pL, pR)) {   // rs_solve's no-wave shortcut
     r.p = pL; r.u = uL; r.rho_own = S.rho; r.trivial = true;
     return r;
   }
@@ -687,16 +687,22 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   const double cL = isR ? oc : S.c, cR = isR ? S.c : oc;
   const double G4cL = isR ? oG4c : S.G4c, G4cR = isR ? S.G4c : oG4c;
   const double pbL = isR ? opb : S.pb, pbR = isR ? S.pb : opb;
-  // rs_guess_pvrs
-  const double p0 = 0.5 * (pL + pR) - 0.125 * (uR - uL) * (rhoL + rhoR) * (cL + cR);
+  // rs_guess_pvrs, then rs_guess_tsrs at max(PVRS, floor): each lane forms
+  // its own side's shock constant
+  const double ppv = 0.5 * (pL + pR) - 0.125 * (uR - uL) * (rhoL + rhoR) * (cL + cR);
+  const double pinf_min = c_lt(kL.pinf, kR.pinf) ? kL.pinf : kR.pinf;
+  const double pbmin = c_lt(pbL, pbR) ? pbL : pbR;
+  const double pfl = 1e-6 * pbmin - pinf_min;
+  const double pg = c_gt(ppv, pfl) ? ppv : pfl;
+  const double gown = sqrt(S.AK / (pg + k.pinf + S.BK));
+  const double goth = xside(gown);
+  const double gL = isR ? goth : gown, gR = isR ? gown : goth;
+  const double p0 = (gL * pL + gR * pR - (uR - uL)) / (gL + gR);
   // rs_star
   const double udiff = uR - uL;
-  if (G4cL + G4cR <= udiff) *status |= ST_VACUUM;
-  const double pinf_min = kL.pinf < kR.pinf ? kL.pinf : kR.pinf;
-  const double pbmin = pbL < pbR ? pbL : pbR;
-  const double pfl = 1e-6 * pbmin - pinf_min;
-  double pold = p0 > pfl ? p0 : pfl;
-  double fL = 0.0, fR = 0.0, p = pold;
+  if (c_le(G4cL + G4cR, udiff)) *status |= ST_VACUUM;
+  double pold = c_gt(p0, pfl) ? p0 : pfl;
+  double fL = 0.0, fR = 0.0, fLd = 0.0, fRd = 0.0, p = pold, dp = 0.0;
   int it = 0;
   for (;;) {
     double f, fd;
@@ -704,17 +710,19 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
     const double of = xside(f), ofd = xside(fd);
     fL = isR ? of : f;
     fR = isR ? f : of;
-    const double fLd = isR ? ofd : fd, fRd = isR ? fd : ofd;
+    fLd = isR ? ofd : fd;
+    fRd = isR ? fd : ofd;
     p = pold - (fL + fR + udiff) / (fLd + fRd);
-    if (p < pfl) p = pfl;
+    if (c_lt(p, pfl)) p = pfl;
     it++;
-    bool conv = 2.0 * fabs(p - pold) <= GFM_RS_TOL * (p + pold + 2.0 * pinf_min);
+    bool conv = c_le(2.0 * fabs(p - pold), GFM_RS_TOL * (p + pold + 2.0 * pinf_min));
+    dp = p - pold;
     pold = p;
     if (conv) break;
     if (it >= GFM_RS_MAXIT) { *status |= ST_NEWTON_NO_CONVERGE; break; }
   }
   r.p = p;
-  r.u = 0.5 * (uL + uR + fR - fL);
+  r.u = 0.5 * (uL + uR + (fR + fRd * dp) - (fL + fLd * dp));
   r.rho_own = rs_rho_star(S, k, p);
   *iters += it;
   return r;
@@ -841,7 +849,7 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
     int it = 0;
     const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it);
     if (lane == 0) iters += it;
-    if (m.p != m.p) st |= ST_NAN;
+    if (c_isnan(m.p)) st |= ST_NAN;
     if (lane == 16 * sr) {
       double* o = a.out + (int64_t)t * IFC_OUT;
       const double snx = m.u * nx, sny = m.u * ny;

@@ -81,8 +81,8 @@ def test_toro_table(case):
         tol = max(1.01 * 10.0 ** (-decimals), 4e-6 * abs(float(text)))
         assert abs(got - float(text)) <= tol, (got, text)
     pi, ui = star_independent(g, 0.0, g, 0.0, L, R)
-    assert abs(p - pi) <= 1e-11 * abs(pi)
-    assert abs(u - ui) <= 1e-9 * max(abs(ui), 1.0)
+    assert abs(p - pi) <= 1e-13 * abs(pi)
+    assert abs(u - ui) <= 1e-12 * max(abs(ui), 1.0)
 
 
 RNG = np.random.default_rng(7)
