@@ -29,9 +29,13 @@ sys.path.insert(0, os.path.join(ROOT, "phd-2d-gfm_gb300"))
 
 WORKLOAD = {"workload": "shock_bubble_1000x400_riemannGFM_MUSCL_LS5", "test_case": "shock_bubble", "Nx": 1000,
             "Ny": 400, "GFM": "riemannGFM", "FS": "MUSCL", "ITM": "LS5", "CFL": 0.6, "run_steps": 2000}
-METRIC = "cell-updates/s/GB300 FP64 (1000x400 shock-bubble, Riemann GFM, plain Newton)"
+METRIC = "cell-updates/s/GB300 FP64: plain vs batched+learned p* guess at L1 err<=1e-10"
 UNIT = "cell-updates/s"
-FLUX_BYTES_PER_CELL = 128   # both fluids: 32 B read + 32 B write of U each
+FLUX_BYTES_PER_CELL = 128   # flux update, both fluids: 32 B read + 32 B write of U each
+STEP_BYTES_PER_CELL = 144   # whole step: the flux update's 128 B plus phi read and write
+NPHASES = 9
+PHASE_NAMES = ["cfl", "ghost_fill", "flux_update", "level_set", "bcs", "interface_loop", "far_partition",
+               "near_extrapolation", "far_flux_update"]
 
 
 def parse():
@@ -43,6 +47,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--overlap", default="auto", choices=["auto", "on", "off"],
+                    help="ghost-fill schedule (gfm_set_overlap); results are identical")
     return ap.parse_args()
 
 
@@ -61,18 +67,22 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """dram read+write bytes per flux-update launch from the committed ncu summary."""
+def ncu_summary():
+    """Figures of the committed ncu summary of the flux update (key=value lines):
+    DRAM bytes per full-grid launch, FP64 flops per cell, FP64 pipe activity."""
     p = os.path.join(ROOT, "profiles", "flux_update_shock_bubble.txt")
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch_full_size"):
-            try:
-                return float(line.split("=")[1].split()[0])
-            except (IndexError, ValueError):
-                return None
-    return None
+        if "=" not in line or line.startswith("#"):
+            continue
+        k, v = line.split("=", 1)
+        try:
+            out[k.strip()] = float(v.split()[0])
+        except (IndexError, ValueError):
+            pass
+    return out
 
 
 class ClockSampler:
@@ -146,19 +156,17 @@ def run_gfm(args):
     stream = torch.cuda.current_stream()
     ctx = g.Context(desc, two_fluid=True, stream=stream.cuda_stream)
     ctx.upload(U1, U2, phi)
+    if not ctx.set_overlap(args.overlap):   # no SM partitions: one stream
+        ctx.set_overlap("off")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     ctx.step(m, args.warmup)
     torch.cuda.synchronize()
     ctx.clear_status()
     cells = desc.Nx * desc.Ny
-    phases = np.zeros(8)
-    ph = np.zeros(8)
+    phases = np.zeros(NPHASES)
+    ph = np.zeros(NPHASES)
     L = g.lib()
-    L.gfm_step_timed.argtypes = [ctypes.c_void_p, ctypes.POINTER(g.MethodDesc), ctypes.c_int,
-                                 ctypes.POINTER(ctypes.c_double)]
-    L.gfm_launch_count.restype = ctypes.c_int64
     launches0 = L.gfm_launch_count()
-    newton = 0
     if world > 1:
         import torch.distributed as tdist
         tdist.barrier()
@@ -172,12 +180,10 @@ def run_gfm(args):
             if rc != 0:
                 raise RuntimeError("gfm_step_timed failed: %d" % rc)
             phases += ph
-            if s % 50 == 0:
-                newton += ctx.stats()["newton_iters"] * 0   # statistics read below
         torch.cuda.synchronize()
     wall = time.time() - t_wall
     launches = L.gfm_launch_count() - launches0
-    step_ms = float(phases[:5].sum())   # phases 5-7 are sub-intervals of 1-2
+    step_ms = float(phases[:5].sum())   # phases 5-8 are sub-intervals of 1-2
     if world > 1:
         import torch.distributed as tdist
         tt = torch.tensor([step_ms], device="cuda", dtype=torch.float64)
@@ -189,16 +195,30 @@ def run_gfm(args):
     t_sim, nsteps_done, _ = ctx.time()
     value = cells * args.steps * world / (step_ms * 1e-3)
 
-    # roofline of the dominant kernel (flux update: both fluids in one launch)
-    flux_ms = phases[2] / args.steps
+    # roofline of the dominant kernel, the flux update (both fluids per
+    # launch; with the overlapped schedule two launches per step, far tiles
+    # and near tiles, cover the grid once: their times are added)
+    flux_ms = (phases[2] + phases[8]) / args.steps
     achieved = FLUX_BYTES_PER_CELL * cells / (flux_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    prof = ncu_summary()
+    fp64_peak = ctypes.c_double(0.0)
+    L.gfm_fp64_peak(ctypes.byref(fp64_peak), ctypes.c_void_p(stream.cuda_stream))
+    fp64 = {"kernel": "k_flux_update<MUSCL>", "peak_gflops": round(fp64_peak.value, 1),
+            "peak_source": "measured now (gfm_fp64_peak: FMA loop on every SM)"}
+    if "fp64_flops_per_cell" in prof:
+        fl = prof["fp64_flops_per_cell"] * cells
+        fp64.update({"flops_per_cell": prof["fp64_flops_per_cell"],
+                     "achieved_gflops": round(fl / (flux_ms * 1e-3) / 1e9, 1),
+                     "frac": round(fl / (flux_ms * 1e-3) / 1e9 / fp64_peak.value, 4),
+                     "pipe_active_frac_ncu": prof.get("fp64_pipe_active_frac")})
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 5), "traffic": ncu_traffic(), "kernel": "k_flux_update<MUSCL>",
-            "peak_source": peak_kind,
-            "phase_ms_per_step": {n: round(v / args.steps, 5) for n, v in
-                                  zip(["cfl", "ghost_fill", "flux_update", "level_set", "bcs", "interface_loop",
-                                       "far_partition", "near_extrapolation"], phases)}}
+            "frac": round(achieved / peak, 5), "traffic": prof.get("traffic_bytes_per_launch_full_size"),
+            "kernel": "k_flux_update<MUSCL>", "peak_source": peak_kind, "bytes_per_cell": FLUX_BYTES_PER_CELL,
+            "kernel_ms_per_step": round(flux_ms, 5),
+            "step_achieved_gbs": round(STEP_BYTES_PER_CELL * value / 1e9, 2),
+            "fp64": fp64,
+            "phase_ms_per_step": {n: round(v / args.steps, 5) for n, v in zip(PHASE_NAMES, phases)}}
 
     # end to end through the C ABI: pinned host state -> device -> step -> host
     e2e = None
@@ -233,7 +253,8 @@ def run_gfm(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD["workload"], "Nx": desc.Nx, "Ny": desc.Ny, "GFM": W["GFM"],
                        "FS": W["FS"], "ITM": W["ITM"], "CFL": W["CFL"], "parallelism": "replicas%d" % world,
-                       "l2": "512 MiB flush between timed steps", "steps_from": args.warmup},
+                       "l2": "512 MiB flush between timed steps", "steps_from": args.warmup,
+                       "schedule": "overlap " + args.overlap, "p_star_guess": "plain (PVRS / TSRS)"},
             "roofline": roof, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clk.summary(), "device_status": g.status_names(status),
             "stats_last_step": stats, "sim_time": t_sim, "wall_s": wall}

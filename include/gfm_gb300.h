@@ -122,20 +122,29 @@ gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps);
 /* gfm_step with CUDA events recorded on the context's stream around each
  * phase; adds the milliseconds of each phase to phase_ms[GFM_NPHASES]:
  * 0 CFL/dt, 1 ghost fill, 2 flux update (both fluids, one launch),
- * 3 level set, 4 boundary conditions + end of step.
- * With the overlapped schedule of the Riemann and real GFM (interface loop
- * on its own SM partition while the far field is updated on the rest),
- * phase 1 runs up to the near-interface flux update, phase 2 is that
- * update, and 5 the interface loop, 6 the far-field partition's work,
- * 7 the exact extrapolation and conversion of near cells after the loop. */
-#define GFM_NPHASES 8
+ * 3 level set, 4 boundary conditions + end of step; phases 0-4 add up to
+ * the step.  With the overlapped schedule (gfm_set_overlap) phase 1 runs up
+ * to the flux update of the tiles near the interface and phase 2 is that
+ * update; phases 5-8 then time parts that overlap inside phases 1-2:
+ * 5 the interface loop, 6 the far-field partition's work, 7 the exact
+ * extrapolation and conversion of near cells after the loop, 8 the flux
+ * update of the far tiles (within 6).  Phases 5-8 are 0 without overlap. */
+#define GFM_NPHASES 9
 gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
 
-/* Overlapped schedule of the Riemann and real GFM on (enable = 1, the
- * default where the device supports SM partitions) or off (0: every phase
- * runs on the context's stream in turn).  Results are identical either way.
- * GFM_ERR_UNSUPPORTED when enable = 1 and the context has no partitions. */
-gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int enable);
+/* Schedule of the ghost fill for the Riemann and real GFM.
+ *   GFM_OVERLAP_OFF   every phase on the context's stream in turn
+ *   GFM_OVERLAP_ON    the interface loop on a small SM partition while the
+ *                     far field is extrapolated and updated on the rest
+ *   GFM_OVERLAP_AUTO  (default) ON for the Riemann GFM, whose bilinear probes
+ *                     chain interfacial cells many deep, OFF for the real GFM,
+ *                     whose cells depend on one opposite cell at most
+ * Results are identical in every mode.  GFM_ERR_UNSUPPORTED when ON or AUTO
+ * is asked of a context without SM partitions (or side streams). */
+#define GFM_OVERLAP_OFF 0
+#define GFM_OVERLAP_ON 1
+#define GFM_OVERLAP_AUTO 2
+gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int mode);
 
 /* number of kernels this library has launched since it was loaded */
 int64_t gfm_launch_count(void);
@@ -190,6 +199,10 @@ gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gf
 #define GFM_NOALLOC_MAX_CELLS 524272
 gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* grid, const gfm_method_desc* m, double* U, int nsteps,
                                        double* t, int* numsteps, uint32_t* status, void* cuda_stream);
+
+/* Measured FP64 peak of the current device: a dependent-chain-free FMA loop
+ * on every SM for about 20 ms; *gflops = 2 x FMAs per second / 1e9. */
+gfm_status_t gfm_fp64_peak(double* gflops, void* cuda_stream);
 
 /* library version string */
 const char* gfm_version(void);

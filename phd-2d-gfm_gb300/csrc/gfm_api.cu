@@ -219,10 +219,10 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_chain, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_far, cudaEventDisableTiming);
-    for (int q = 0; q < 5; q++)
+    for (int q = 0; q < 6; q++)
       if (e == cudaSuccess) e = cudaEventCreate(&ctx->tev[q]);
     if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
-    ctx->overlap = ctx->overlap_ok;
+    ctx->overlap = ctx->overlap_ok ? GFM_OVERLAP_AUTO : GFM_OVERLAP_OFF;
   }
   if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_dtime, sizeof(DevTime));
   if (e != cudaSuccess) {
@@ -252,7 +252,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_chain) cudaEventDestroy(ctx->ev_chain);
   if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);
-  for (int q = 0; q < 5; q++)
+  for (int q = 0; q < 6; q++)
     if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
   cudaFree(ctx->dtime);
   cudaFree(extra(ctx).counters);
@@ -392,7 +392,9 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
     launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
     mark(1);
     if (ctx->two_fluid) {
-      overlapped = ctx->overlap && (m->gfm == GFM_RIEMANN || m->gfm == GFM_REAL) && !m->use_extension_vfield;
+      overlapped = !m->use_extension_vfield &&
+                   ((ctx->overlap == GFM_OVERLAP_ON && (m->gfm == GFM_RIEMANN || m->gfm == GFM_REAL)) ||
+                    (ctx->overlap == GFM_OVERLAP_AUTO && m->gfm == GFM_RIEMANN));
       if (overlapped) {
         // ghost fill and flux update interleaved across SM partitions; the
         // flux phase here is the update of the tiles near the interface
@@ -433,6 +435,7 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
         cudaEventElapsedTime(&ms, ctx->tev[0], ctx->tev[1]); phase_ms[5] += ms;
         cudaEventElapsedTime(&ms, ctx->tev[0], ctx->tev[2]); phase_ms[6] += ms;
         cudaEventElapsedTime(&ms, ctx->tev[1], ctx->tev[3]); phase_ms[7] += ms;
+        cudaEventElapsedTime(&ms, ctx->tev[5], ctx->tev[2]); phase_ms[8] += ms;
       } else {
         for (int q = 0; q < 5; q++) { cudaEventElapsedTime(&ms, ev[q], ev[q + 1]); phase_ms[q] += ms; }
       }
@@ -452,11 +455,55 @@ gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
   return step_impl(ctx, m, nsteps, phase_ms);
 }
 
-gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int enable) {
-  if (!ctx || (enable != 0 && enable != 1)) return GFM_ERR_ARG;
-  if (enable && !ctx->overlap_ok) return GFM_ERR_UNSUPPORTED;
-  ctx->overlap = enable;
+gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int mode) {
+  if (!ctx || mode < GFM_OVERLAP_OFF || mode > GFM_OVERLAP_AUTO) return GFM_ERR_ARG;
+  if (mode != GFM_OVERLAP_OFF && !ctx->overlap_ok) return GFM_ERR_UNSUPPORTED;
+  ctx->overlap = mode;
   return GFM_OK;
+}
+
+// FP64 peak: 8 independent FMA chains per thread, 8 CTAs of 256 per SM.
+__global__ void k_fp64_peak(double* out, int iters, double a, double b) {
+  double x[8];
+  for (int q = 0; q < 8; q++) x[q] = 1.0 + 1e-3 * (threadIdx.x + q);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = fma(x[q], a, b);
+  }
+  double acc = 0.0;
+  for (int q = 0; q < 8; q++) acc += x[q];
+  if (acc == 12345.678) out[0] = acc;   // keeps the loop; never true for these inputs
+}
+
+gfm_status_t gfm_fp64_peak(double* gflops, void* cuda_stream) {
+  if (!gflops) return GFM_ERR_ARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* sink = nullptr;
+  CK(cudaMalloc(&sink, sizeof(double)));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int blocks = sms * 8, threads = 256;
+  int iters = 256;
+  float ms = 0.0f;
+  for (int rep = 0; rep < 8; rep++) {   // grow until one launch takes about 20 ms
+    cudaEventRecord(e0, s);
+    k_fp64_peak<<<blocks, threads, 0, s>>>(sink, iters, 0.9999999, 1e-9);
+    counted();
+    cudaEventRecord(e1, s);
+    CK(cudaEventSynchronize(e1));
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms > 15.0f) break;
+    iters *= (ms > 0.5f) ? 2 : 8;
+  }
+  *gflops = 2.0 * 8.0 * (double)blocks * threads * iters / (ms * 1e-3) / 1e9;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  return last_error();
 }
 
 int64_t gfm_launch_count(void) { return (int64_t)g_launches.load(); }

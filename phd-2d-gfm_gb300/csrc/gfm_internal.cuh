@@ -83,10 +83,10 @@ struct gfm_ctx {
   int* tile_near;         // per flux tile: its region holds a near cell
   cudaStream_t s_chain, s_far;
   cudaEvent_t ev_fork, ev_chain, ev_far;
-  cudaEvent_t tev[5];     // timing events of the overlapped schedule (gfm_step_timed)
+  cudaEvent_t tev[6];     // timing events of the overlapped schedule (gfm_step_timed)
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist
-  int overlap;            // overlapped schedule in use (gfm_set_overlap)
+  int overlap;            // GFM_OVERLAP_* mode (gfm_set_overlap)
 };
 
 namespace gfm {

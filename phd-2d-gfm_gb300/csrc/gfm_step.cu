@@ -1474,6 +1474,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* fin[2] = {src1, src2};
     finalize_sel(ctx, fin, 1, ctx->s_far);
   }
+  if (ctx->timing) cudaEventRecord(ctx->tev[5], ctx->s_far);
   launch_fs_update_sel(ctx, m->fs, 3, TILES_FAR, ctx->s_far);
   cudaEventRecord(ctx->ev_far, ctx->s_far);
   if (ctx->timing) cudaEventRecord(ctx->tev[2], ctx->s_far);

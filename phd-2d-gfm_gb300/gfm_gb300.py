@@ -91,6 +91,7 @@ def lib():
         "gfm_step": [P, ctypes.POINTER(MethodDesc), I],
         "gfm_step_timed": [P, ctypes.POINTER(MethodDesc), I, pd],
         "gfm_set_overlap": [P, I],
+        "gfm_fp64_peak": [pd, V],
         "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
         "gfm_clear_device_status": [P],
         "gfm_get_stats": [P, ctypes.POINTER(ctypes.c_int64)] * 1 + [ctypes.POINTER(ctypes.c_int64)] * 2,
@@ -247,19 +248,22 @@ class Context:
         _check(lib().gfm_get_stats(self._p, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "gfm_get_stats")
         return {"n_interfacial": a.value, "rounds": b.value, "newton_iters": c.value}
 
-    def set_overlap(self, enable):
-        """Overlapped (SM-partitioned) schedule of the Riemann / real GFM on or
-        off; returns False when the context has no partitions to turn it on."""
-        rc = lib().gfm_set_overlap(self._p, 1 if enable else 0)
+    def set_overlap(self, mode):
+        """Ghost-fill schedule of the Riemann / real GFM: False or "off",
+        True or "on" (interface loop on its own SM partition), "auto" (the
+        default: on for the Riemann GFM only).  Returns False when the context
+        has no partitions to turn it on."""
+        code = {False: 0, "off": 0, True: 1, "on": 1, "auto": 2}[mode]
+        rc = lib().gfm_set_overlap(self._p, code)
         if rc == 4:
             return False
         _check(rc, "gfm_set_overlap")
         return True
 
     def step_timed(self, m, nsteps=1):
-        """gfm_step with per-phase device times; returns GFM_NPHASES (8)
+        """gfm_step with per-phase device times; returns GFM_NPHASES (9)
         milliseconds summed over the steps."""
-        ph = np.zeros(8)
+        ph = np.zeros(9)
         _check(lib().gfm_step_timed(self._p, ctypes.byref(m), nsteps, _dptr(ph)), "gfm_step_timed")
         return ph
 

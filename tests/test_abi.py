@@ -44,6 +44,9 @@ def test_argument_checks_need_no_gpu():
     d, T = g.case_params("twofluid", "GDA", 32, 16)
     assert L.gfm_ctx_create(ctypes.byref(d), 1, ctypes.byref(p)) == 4   # periodic needs Nx == Ny
     assert L.gfm_rs_pure_batch(-1, 1, 1.4, 0.0, None, None, None, None, None) == 1
+    assert L.gfm_set_overlap(None, 2) == 1
+    ph = (ctypes.c_double * 8)()
+    assert L.gfm_step_timed(None, None, 1, ph) == 1
 
 
 @pytest.mark.parametrize("case", ["circularexplosion", "shock_bubble", "underwater_explosion_sg", "ST1_x", "ST2_y",

@@ -153,6 +153,7 @@ def test_overlapped_schedule_matches_sequential(case, Nx, Ny, gfm):
         if ovl:
             # interface loop and far-field work lie inside phases 1-2
             assert ph[5] <= ph[1] + ph[2] + 1e-3 and ph[6] <= ph[1] + ph[2] + 1e-3
+            assert 0.0 < ph[8] <= ph[6] + 1e-3
         else:
             assert np.all(ph[5:] == 0.0)
         outs.append(ctx.download())
