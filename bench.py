@@ -27,8 +27,20 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "phd-2d-gfm_gb300"))
 
-WORKLOAD = {"workload": "shock_bubble_1000x400_riemannGFM_MUSCL_LS5", "test_case": "shock_bubble", "Nx": 1000,
-            "Ny": 400, "GFM": "riemannGFM", "FS": "MUSCL", "ITM": "LS5", "CFL": 0.6, "run_steps": 2000}
+# The configurations this metric is quoted on (the default is the headline one).
+WORKLOADS = {
+    "shock_bubble": {"workload": "shock_bubble_1000x400_riemannGFM_MUSCL_LS5", "sim": "twofluid",
+                     "test_case": "shock_bubble", "Nx": 1000, "Ny": 400, "GFM": "riemannGFM", "FS": "MUSCL",
+                     "ITM": "LS5", "CFL": 0.6, "reinit_every": 1, "run_steps": 2000},
+    "underwater_explosion": {"workload": "underwater_explosion_800x800_realGFM_MUSCL_LS5", "sim": "twofluid",
+                             "test_case": "underwater_explosion_sg", "Nx": 800, "Ny": 800, "GFM": "realGFM",
+                             "FS": "MUSCL", "ITM": "LS5", "CFL": 0.5, "reinit_every": 5, "run_steps": 1500},
+    # CFL 0.4 as in the reference's settings files: at 0.8 the unsplit
+    # MUSCL-Hancock update diverges at step 23 (oracle and GPU alike)
+    "circular_explosion": {"workload": "circular_explosion_200x200_onefluid_MUSCL_CFL0.4", "sim": "onefluid",
+                           "test_case": "circularexplosion", "Nx": 200, "Ny": 200, "GFM": None, "FS": "MUSCL",
+                           "ITM": None, "CFL": 0.4, "reinit_every": 0, "run_steps": 132},
+}
 METRIC = "cell-updates/s/GB300 FP64: plain vs batched+learned p* guess at L1 err<=1e-10"
 UNIT = "cell-updates/s"
 FLUX_BYTES_PER_CELL = 128   # flux update, both fluids: 32 B read + 32 B write of U each
@@ -41,10 +53,12 @@ PHASE_NAMES = ["cfl", "ghost_fill", "flux_update", "level_set", "bcs", "interfac
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--workload", default="shock_bubble", choices=sorted(WORKLOADS))
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gfm", choices=["gfm", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=-1,
+                    help="steps of the end-to-end leg (default: the same steps as the timed region)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--overlap", default="auto", choices=["auto", "on", "off"],
@@ -138,6 +152,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def setup(W):
+    import gfm_gb300 as g
+    desc, T = g.case_params(W["sim"], W["test_case"], W["Nx"], W["Ny"])
+    U1, U2, phi = g.case_init(W["sim"], W["test_case"], desc)
+    if W["sim"] == "twofluid":
+        m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T, reinit_every=W["reinit_every"])
+    else:
+        m = g.method(fs=W["FS"], CFL=W["CFL"], T=T)
+    return desc, T, U1, U2, phi, m
+
+
 def run_gfm(args):
     import ctypes
     import numpy as np
@@ -149,19 +174,22 @@ def run_gfm(args):
     if world > 1:
         import torch.distributed as tdist
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    W = WORKLOAD
-    desc, T = g.case_params("twofluid", W["test_case"], W["Nx"], W["Ny"])
-    U1, U2, phi = g.case_init("twofluid", W["test_case"], desc)
-    m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T)
+    W = WORKLOADS[args.workload]
+    two = W["sim"] == "twofluid"
+    desc, T, U1, U2, phi, m = setup(W)
+    # a run shorter than warm-up + steps (the circular explosion ends at T after
+    # 132 steps) is timed over the steps it has
+    args.steps = max(1, min(args.steps, W["run_steps"] - args.warmup))
     stream = torch.cuda.current_stream()
-    ctx = g.Context(desc, two_fluid=True, stream=stream.cuda_stream)
+    ctx = g.Context(desc, two_fluid=two, stream=stream.cuda_stream)
     ctx.upload(U1, U2, phi)
-    if not ctx.set_overlap(args.overlap):   # no SM partitions: one stream
+    if two and not ctx.set_overlap(args.overlap):   # no SM partitions: one stream
         ctx.set_overlap("off")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     ctx.step(m, args.warmup)
     torch.cuda.synchronize()
     ctx.clear_status()
+    e2e_start = ctx.download() + ctx.time()[:2]
     cells = desc.Nx * desc.Ny
     phases = np.zeros(NPHASES)
     ph = np.zeros(NPHASES)
@@ -222,36 +250,43 @@ def run_gfm(args):
 
     # end to end through the C ABI: pinned host state -> device -> step -> host
     e2e = None
-    if args.e2e_steps > 0:
+    if args.e2e_steps != 0:
+        # the same steps again from the pre-timing state (a one-fluid run that
+        # reached T would do nothing more)
         shp = desc.shape
         hU1 = torch.empty((4,) + shp, dtype=torch.float64, pin_memory=True).numpy()
         hU2 = torch.empty((4,) + shp, dtype=torch.float64, pin_memory=True).numpy()
         hphi = torch.empty(shp, dtype=torch.float64, pin_memory=True).numpy()
-        G1, G2, Gp = ctx.download()
-        hU1[...] = G1
-        hU2[...] = G2
-        hphi[...] = Gp
+        hU1[...] = e2e_start[0]
+        if two:
+            hU2[...] = e2e_start[1]
+            hphi[...] = e2e_start[2]
+        L.gfm_set_time(ctx._p, e2e_start[3], e2e_start[4])
         pd = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        n_e2e = args.steps if args.e2e_steps < 0 else min(args.e2e_steps, args.steps)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for s in range(args.e2e_steps):
+        for s in range(n_e2e):
             L.gfm_upload(ctx._p, 1, pd(hU1))
-            L.gfm_upload(ctx._p, 2, pd(hU2))
-            L.gfm_upload_phi(ctx._p, pd(hphi))
+            if two:
+                L.gfm_upload(ctx._p, 2, pd(hU2))
+                L.gfm_upload_phi(ctx._p, pd(hphi))
             L.gfm_step(ctx._p, ctypes.byref(m), 1)
             L.gfm_download(ctx._p, 1, pd(hU1))
-            L.gfm_download(ctx._p, 2, pd(hU2))
-            L.gfm_download_phi(ctx._p, pd(hphi))
+            if two:
+                L.gfm_download(ctx._p, 2, pd(hU2))
+                L.gfm_download_phi(ctx._p, pd(hphi))
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
-        nbytes = (hU1.nbytes + hU2.nbytes + hphi.nbytes)
+        args.e2e_steps = n_e2e
+        nbytes = hU1.nbytes + ((hU2.nbytes + hphi.nbytes) if two else 0)
         e2e = {"value": cells * args.e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD["workload"], "Nx": desc.Nx, "Ny": desc.Ny, "GFM": W["GFM"],
+            "config": {"workload": W["workload"], "Nx": desc.Nx, "Ny": desc.Ny, "GFM": W["GFM"],
                        "FS": W["FS"], "ITM": W["ITM"], "CFL": W["CFL"], "parallelism": "replicas%d" % world,
                        "l2": "512 MiB flush between timed steps", "steps_from": args.warmup,
                        "schedule": "overlap " + args.overlap, "p_star_guess": "plain (PVRS / TSRS)"},
@@ -259,7 +294,7 @@ def run_gfm(args):
             "clocks": clk.summary(), "device_status": g.status_names(status),
             "stats_last_step": stats, "sim_time": t_sim, "wall_s": wall}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(desc, m, ctx, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(W, desc, m, e2e_start, args.cpu_seconds)
     ctx.close()
     if rank == 0:
         print(json.dumps(line))
@@ -278,8 +313,13 @@ def _oracle_steps(desc_fields, m_fields, U1, U2, phi, nsteps, t, numsteps, secon
     done = 0
     t0 = time.perf_counter()
     while done < nsteps:
-        r = orc.twofluid_run(desc, m, U1, U2, phi, 1, t, numsteps)
-        U1, U2, phi, t, numsteps = r["U1"], r["U2"], r["phi"], r["t"], r["numsteps"]
+        if U2 is None:   # one fluid
+            U1, t, numsteps, taken = orc.onefluid_run(desc, m, U1, 1, t, numsteps)
+            if taken == 0:   # reached T
+                break
+        else:
+            r = orc.twofluid_run(desc, m, U1, U2, phi, 1, t, numsteps)
+            U1, U2, phi, t, numsteps = r["U1"], r["U2"], r["phi"], r["t"], r["numsteps"]
         done += 1
         if time.perf_counter() - t0 > seconds:
             break
@@ -290,16 +330,16 @@ def _fields(s):
     return {k: getattr(s, k) for k, _ in s._fields_}
 
 
-def cpu_baseline(desc, m, ctx, seconds):
+def cpu_baseline(W, desc, m, start, seconds):
     """The CPU oracle (single-threaded, like the reference) timed on this host on
-    a bounded sample: oracle steps of the same workload from the GPU's state."""
-    U1, U2, phi = ctx.download()
-    t, n, _ = ctx.time()
+    a bounded sample: oracle steps of the same workload from the GPU's state
+    after the warm-up (the first timed step)."""
+    U1, U2, phi, t, n = start
     done, el = _oracle_steps(_fields(desc), _fields(m), U1, U2, phi, 10 ** 6, t, n, seconds)
     cells = desc.Nx * desc.Ny
     return {"value": cells * done / el, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "%d oracle steps of the 1000x400 shock-bubble from the GPU state at step %d (%.1f s)"
-                      % (done, n, el)}
+            "sample": "%d oracle steps of %s from the state after %d steps (%.1f s)"
+                      % (done, W["workload"], n, el)}
 
 
 def run_reference(args):
@@ -310,20 +350,23 @@ def run_reference(args):
         return
     import multiprocessing as mp
     import gfm_gb300 as g
-    W = WORKLOAD
-    desc, T = g.case_params("twofluid", W["test_case"], W["Nx"], W["Ny"])
-    U1, U2, phi = g.case_init("twofluid", W["test_case"], desc)
-    m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T)
+    W = WORKLOADS[args.workload]
+    desc, T, U1, U2, phi, m = setup(W)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_binding as orc
-    r = orc.twofluid_run(desc, m, U1, U2, phi, args.warmup)
+    if W["sim"] == "twofluid":
+        r = orc.twofluid_run(desc, m, U1, U2, phi, args.warmup)
+        start = (r["U1"], r["U2"], r["phi"], r["t"], r["numsteps"])
+    else:
+        U, t, n, _ = orc.onefluid_run(desc, m, U1, args.warmup)
+        start = (U, None, None, t, n)
     cores = os.cpu_count() or 1
     budget = 60.0
     ctxm = mp.get_context("spawn")
     with ctxm.Pool(cores) as pool:
         t0 = time.perf_counter()
-        res = pool.starmap(_oracle_steps, [(_fields(desc), _fields(m), r["U1"], r["U2"], r["phi"], args.steps,
-                                            r["t"], r["numsteps"], budget)] * cores)
+        res = pool.starmap(_oracle_steps, [(_fields(desc), _fields(m), start[0], start[1], start[2], args.steps,
+                                            start[3], start[4], budget)] * cores)
         wall = time.perf_counter() - t0
     total_steps = sum(d for d, _ in res)
     cells = desc.Nx * desc.Ny
