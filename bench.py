@@ -53,7 +53,7 @@ PHASE_NAMES = ["cfl", "ghost_fill", "flux_update", "level_set", "bcs", "interfac
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--workload", default="shock_bubble", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="shock_bubble", choices=sorted(WORKLOADS) + ["batch64"])
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gfm", choices=["gfm", "reference"])
@@ -350,6 +350,8 @@ def run_reference(args):
         return
     import multiprocessing as mp
     import gfm_gb300 as g
+    if args.workload == "batch64":
+        return run_reference_batch(args)
     W = WORKLOADS[args.workload]
     desc, T, U1, U2, phi, m = setup(W)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -384,10 +386,160 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _oracle_member(spec, nsteps, seconds):
+    """One oracle process on one batch member from its initial state."""
+    import gfm_gb300 as g
+    d, T, U1, U2, phi = g.shock_bubble_case(*spec)
+    m = g.method(gfm="riemannGFM", CFL=0.6, T=1.0)
+    done, el = _oracle_steps(_fields(d), _fields(m), U1, U2, phi, nsteps, 0.0, 0, seconds)
+    return d.Nx * d.Ny * done, el
+
+
+def run_reference_batch(args):
+    """--impl reference for the batched workload: the oracle on every host
+    core, each core stepping batch members (members spread over the cores)."""
+    import multiprocessing as mp
+    spec = batch_members()
+    cores = os.cpu_count() or 1
+    budget = 60.0
+    per = max(1.0, budget * cores / len(spec))
+    ctxm = mp.get_context("spawn")
+    with ctxm.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.starmap(_oracle_member, [(sp, args.steps, per) for sp in spec])
+        wall = time.perf_counter() - t0
+    value = sum(c for c, _ in res) / wall
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "batch64_shock_bubble_riemannGFM", "instances": len(spec), "seed": BATCH_SEED,
+                       "parallelism": "%d CPU processes over the members" % cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "each of %d members stepped by the oracle for up to %.1f s from its initial "
+                                       "state (at most %d steps), %d processes" % (len(spec), per, args.steps, cores)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+BATCH_SEED = 0x6F4D
+
+
+def batch_members(n=64, seed=BATCH_SEED):
+    """The batched workload: n shock-bubble instances, sides 128..1024 in steps
+    of 64, aspect ratio U[1,3] (Ny = max(128, Nx/aspect rounded to 64)), Mach
+    U[1.1,3], bubble gamma U[1.09,1.67], density ratio log-U[0.1,10], radius
+    U[0.1,0.3] of the height."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx = int(rng.integers(2, 17)) * 64
+        aspect = rng.uniform(1.0, 3.0)
+        ny = max(128, int(round(nx / aspect / 64.0)) * 64)
+        out.append((nx, ny, rng.uniform(1.1, 3.0), rng.uniform(1.09, 1.67), float(np.exp(rng.uniform(np.log(0.1),
+                    np.log(10.0)))), rng.uniform(0.1, 0.3)))
+    return out
+
+
+def run_batch(args):
+    """64 independent shock-bubble instances: K steps of all of them through
+    the recorded step graph (instances side by side), and the same K steps one
+    instance after another (the unbatched path), from the same state."""
+    import ctypes
+    import numpy as np
+    import torch
+    import gfm_gb300 as g
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    spec = batch_members()
+    cases = [g.shock_bubble_case(*p) for p in spec]
+    m = g.method(gfm="riemannGFM", CFL=0.6, T=1.0)
+    b = g.Batch([c[0] for c in cases], two_fluid=True)
+    for ctx, (d, T, U1, U2, phi) in zip(b.instances, cases):
+        ctx.upload(U1, U2, phi)
+    b.step(m, args.warmup, graph=True)
+    b.synchronize()
+    start = [ctx.download() + ctx.time()[:2] for ctx in b.instances]
+    cells = sum(c[0].Nx * c[0].Ny for c in cases)
+    L = g.lib()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    L.gfm_batch_set_stream(b._p, ctypes.c_void_p(stream.cuda_stream))
+
+    def timed(graph):
+        for ctx, st in zip(b.instances, start):
+            ctx.upload(st[0], st[1], st[2], t=st[3], numsteps=st[4])
+        torch.cuda.synchronize()
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = L.gfm_launch_count()
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            b.step(m, args.steps, graph=graph)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1), L.gfm_launch_count() - l0, clk.summary()
+
+    ms_seq, launches_seq, clk_seq = timed(False)
+    ms_graph, launches, clk = timed(True)
+    stats = [ctx.status() for ctx in b.instances]
+    value = cells * args.steps / (ms_graph * 1e-3)
+    plain = cells * args.steps / (ms_seq * 1e-3)
+    # end to end: every step uploads all instances' state from pinned host
+    # memory, steps the batch and downloads it again
+    e2e = None
+    if args.e2e_steps != 0:
+        n_e2e = min(args.steps, 20) if args.e2e_steps < 0 else min(args.e2e_steps, args.steps)
+        pinned = []
+        for st in start:
+            arrs = []
+            for a in st[:3]:
+                h = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+                h[...] = a
+                arrs.append(h)
+            pinned.append(arrs)
+        for ctx, st in zip(b.instances, start):
+            L.gfm_set_time(ctx._p, st[3], st[4])
+        pd = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            for ctx, (h1, h2, hp) in zip(b.instances, pinned):
+                L.gfm_upload(ctx._p, 1, pd(h1))
+                L.gfm_upload(ctx._p, 2, pd(h2))
+                L.gfm_upload_phi(ctx._p, pd(hp))
+            b.step(m, 1, graph=True)
+            for ctx, (h1, h2, hp) in zip(b.instances, pinned):
+                L.gfm_download(ctx._p, 1, pd(h1))
+                L.gfm_download(ctx._p, 2, pd(h2))
+                L.gfm_download_phi(ctx._p, pd(hp))
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        nbytes = sum(sum(a.nbytes for a in arrs) for arrs in pinned)
+        e2e = {"value": cells * n_e2e / el, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "steps": n_e2e}
+    b.close()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_graph / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batch64_shock_bubble_riemannGFM", "instances": len(spec), "cells": cells,
+                       "seed": BATCH_SEED, "sides": "128..1024 step 64, aspect U[1,3]", "CFL": 0.6,
+                       "p_star_guess": "plain (PVRS / TSRS)", "schedule": "recorded CUDA graph, 8 steps per replay",
+                       "l2": "inputs larger than L2 (%.1f GB of state)" % (cells * 9 * 8 / 1e9)},
+            "plain_sequential": {"value": plain, "ms_per_step": ms_seq / args.steps, "gpu_launches": launches_seq,
+                                 "clocks": clk_seq},
+            "batched_over_plain": value / plain,
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+            "device_status_nonzero": int(sum(1 for x in stats if x))}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch64":
+        run_batch(args)
     else:
         run_gfm(args)
 

@@ -183,6 +183,46 @@ gfm_status_t gfm_case_params(const char* sim_type, const char* test_case, int Nx
 gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gfm_grid_desc* grid, double* U1,
                            double* U2, double* phi);
 
+/* Batches: many independent instances (grids of any size, their own EOS
+ * parameters, time and dt; one fluid count for all) stepped together.
+ * The reference runs one simulation per process; a batch advances many in
+ * one call, which fills the GPU with small grids and overlaps the instances'
+ * latency-bound interface loops.  Each instance is an ordinary context
+ * (gfm_batch_instance): upload, download, time and status calls work on it
+ * as on a context of its own, ordered on the instance's stream.
+ *   gfm_step_batched_graph       nsteps steps of every instance: 8 steps of
+ *                                all instances are recorded once into a CUDA
+ *                                graph (per method descriptor) and replayed;
+ *                                a remainder is issued directly; instances run
+ *                                side by side on their own streams
+ *   gfm_step_batched_sequential  the same steps, one instance after another
+ *                                on the batch stream (the unbatched way)
+ * Both give each instance the results of stepping it alone.  The batch
+ * stream (gfm_batch_set_stream, default: the batch's own) orders the call
+ * after earlier work on the instance streams and before later work on them.
+ * Instances use the one-stream ghost-fill schedule (GFM_OVERLAP_OFF). */
+typedef struct gfm_batch gfm_batch;
+gfm_status_t gfm_batch_create(const gfm_grid_desc* grids, int n, int two_fluid, gfm_batch** out);
+gfm_status_t gfm_batch_destroy(gfm_batch* b);
+gfm_status_t gfm_batch_instance(gfm_batch* b, int i, gfm_ctx** ctx);
+gfm_status_t gfm_batch_set_stream(gfm_batch* b, void* cuda_stream);
+gfm_status_t gfm_step_batched_graph(gfm_batch* b, const gfm_method_desc* m, int nsteps);
+gfm_status_t gfm_step_batched_sequential(gfm_batch* b, const gfm_method_desc* m, int nsteps);
+gfm_status_t gfm_batch_synchronize(gfm_batch* b);
+
+/* Shock-bubble family of the batched workload: the 1000x400 shock-bubble's
+ * geometry on any grid (width 0.25, square cells, height 0.25 Ny/Nx,
+ * reflective top and bottom, transmissive ends), air (gamma 1.4, rho 1,
+ * p 1e5) with a left-moving shock of Mach number `mach` at x = 0.9 width, a
+ * bubble of fluid 1 (gamma_bubble, rho = rho_ratio, p 1e5) of radius
+ * radius_frac x height at (0.7 width, height/2).  T is 1 (run by steps). */
+typedef struct {
+  double mach, gamma_bubble, rho_ratio, radius_frac;
+} gfm_bubble_params;
+gfm_status_t gfm_case_shock_bubble(const gfm_bubble_params* p, int Nx, int Ny, gfm_grid_desc* grid, double* T);
+gfm_status_t gfm_case_init_shock_bubble(const gfm_bubble_params* p, const gfm_grid_desc* grid, double* U1,
+                                        double* U2, double* phi);
+
 /* One-fluid time steps for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library.
  * Some callers cannot call cudaMalloc (a host runtime whose memory pool owns

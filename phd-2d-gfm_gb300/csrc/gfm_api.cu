@@ -7,7 +7,7 @@
 
 namespace gfm {
 void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter);
-void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m);
+void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every);
 void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out);
 }  // namespace gfm
 
@@ -133,6 +133,9 @@ gfm_status_t last_error() {
 }
 
 }  // namespace
+
+gfm_status_t gfm::validate_method(gfm_ctx* ctx, const gfm_method_desc* m) { return check_method(ctx, m); }
+gfm_status_t gfm::launch_status() { return last_error(); }
 
 extern "C" {
 
@@ -373,7 +376,9 @@ gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid) {
   return last_error();
 }
 
-static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms) {
+}  // extern "C"
+
+gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms) {
   if (!ctx || nsteps < 0) return GFM_ERR_ARG;
   gfm_status_t r = check_method(ctx, m);
   if (r != GFM_OK) return r;
@@ -407,8 +412,12 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
         mark(3);
       }
       launch_ls_update(ctx, m);
-      int upd = ctx->steps_done_host + 1;
-      if (m->reinit_every > 0 && upd % m->reinit_every == 0 && m->reinit_iters > 0) launch_reinit(ctx, m);
+      if (m->reinit_every > 0 && m->reinit_iters > 0) {
+        if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
+          launch_reinit(ctx, m, m->reinit_every);
+        else if ((ctx->steps_done_host + 1) % m->reinit_every == 0)
+          launch_reinit(ctx, m, 0);
+      }
       mark(4);
       launch_commit(ctx, 3, true);   // U := new values + apply_BCs_euler
     } else {
@@ -446,13 +455,15 @@ static gfm_status_t step_impl(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps
   return r;
 }
 
+extern "C" {
+
 gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps) {
-  return step_impl(ctx, m, nsteps, nullptr);
+  return run_steps(ctx, m, nsteps, nullptr);
 }
 
 gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms) {
   if (!phase_ms) return GFM_ERR_ARG;
-  return step_impl(ctx, m, nsteps, phase_ms);
+  return run_steps(ctx, m, nsteps, phase_ms);
 }
 
 gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int mode) {

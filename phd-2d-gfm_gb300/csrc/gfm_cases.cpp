@@ -275,4 +275,46 @@ gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gf
   return GFM_OK;
 }
 
+// Shock-bubble family of the batched workload: the 1000x400 case's geometry
+// scaled to any grid (width 0.25, square cells, height 0.25 Ny/Nx), bubble
+// of fluid 1 centred at (0.7 W, H/2), left-moving shock in air at x = 0.9 W.
+gfm_status_t gfm_case_shock_bubble(const gfm_bubble_params* p, int Nx, int Ny, gfm_grid_desc* d, double* T) {
+  if (!p || !d || !T || Nx < 8 || Ny < 8) return GFM_ERR_ARG;
+  if (!(p->mach > 1.0) || !(p->gamma_bubble > 1.0) || !(p->rho_ratio > 0.0) || !(p->radius_frac > 0.0) ||
+      !(p->radius_frac <= 0.45))
+    return GFM_ERR_ARG;
+  memset(d, 0, sizeof(*d));
+  d->Nx = Nx; d->Ny = Ny; d->numGC = 8;
+  d->x0 = 0.0; d->y0 = 0.0;
+  d->dx = 0.25 / Nx; d->dy = d->dx;
+  d->BC_L = d->BC_R = GFM_BC_TRANSMISSIVE;
+  d->BC_B = d->BC_T = GFM_BC_REFLECTIVE;
+  d->gamma1 = p->gamma_bubble; d->pinf1 = 0.0;
+  d->gamma2 = 1.4; d->pinf2 = 0.0;
+  *T = 1.0;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_case_init_shock_bubble(const gfm_bubble_params* p, const gfm_grid_desc* d, double* U1, double* U2,
+                                        double* phi) {
+  if (!p || !d || !U1 || !U2 || !phi) return GFM_ERR_ARG;
+  Geo G = geo_of(d);
+  const double W = d->dx * d->Nx, H = d->dy * d->Ny;
+  const double xc = 0.7 * W, yc = 0.5 * H, r = p->radius_frac * H, xs = 0.9 * W;
+  double rho2, u2, p2;
+  post_shock(d->gamma2, p->mach, 1.0, 1e5, rho2, u2, p2);
+  const V4 bub = p2c(d->gamma1, d->pinf1, p->rho_ratio, 0, 0, 1e5);
+  const V4 pre = p2c(d->gamma2, d->pinf2, 1.0, 0, 0, 1e5), post = p2c(d->gamma2, d->pinf2, rho2, u2, 0, p2);
+  for (int i = 0; i < G.nr; i++)
+    for (int j = 0; j < G.nc; j++) {
+      const double x = G.ccx(j), y = G.ccy(i);
+      put(G, U1, i, j, bub);
+      put(G, U2, i, j, (x < xs) ? pre : post);
+      phi[(size_t)i * G.nc + j] = std::sqrt((x - xc) * (x - xc) + (y - yc) * (y - yc)) - r;
+    }
+  host_bcs(d, U1);
+  host_bcs(d, U2);
+  return GFM_OK;
+}
+
 }  // extern "C"

@@ -19,6 +19,7 @@
 //   phase 4  per cell: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn, the
 //            accumulation order of the reference's face loop (:290-292).
 #include "gfm_internal.cuh"
+#include <mutex>
 
 namespace gfm {
 
@@ -316,6 +317,16 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
 
 static size_t flux_smem() { return sizeof(FluxSmem); }
 
+// Kernel attributes, set once per process before any launch (and so before
+// any stream capture).
+void prepare_kernels() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_flux_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem());
+    cudaFuncSetAttribute(k_flux_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem());
+  });
+}
+
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
   launch_fs_update_sel(ctx, fs, fluid_mask, TILES_ALL, ctx->stream);
 }
@@ -338,12 +349,7 @@ void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaS
   }
   dim3 grid((P.Nx + TX - 1) / TX, (P.Ny + TY - 1) / TY, nz);
   size_t sm = flux_smem();
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_flux_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaFuncSetAttribute(k_flux_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    attr_set = true;
-  }
+  prepare_kernels();
   if (fs == GFM_FS_MUSCL)
     k_flux_update<true><<<grid, NT, sm, stream>>>(a);
   else

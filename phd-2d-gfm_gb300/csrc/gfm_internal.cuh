@@ -87,6 +87,7 @@ struct gfm_ctx {
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist
   int overlap;            // GFM_OVERLAP_* mode (gfm_set_overlap)
+  int graph_mode;         // launches are being recorded into a CUDA graph
 };
 
 namespace gfm {
@@ -149,5 +150,10 @@ void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_end_step(gfm_ctx* ctx);
+void prepare_kernels();
+// nsteps iterations of the time loop on ctx's stream (gfm_step, gfm_step_timed)
+gfm_status_t run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
+gfm_status_t validate_method(gfm_ctx* ctx, const gfm_method_desc* m);
+gfm_status_t launch_status();   // GFM_ERR_CUDA (and a message) if a launch failed
 
 }  // namespace gfm

@@ -1103,15 +1103,22 @@ __global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, cons
   }
 }
 
-__global__ void k_copy_plane(GridP P, const double* src, double* dst, const DevTime* D) {
-  if (!D->active) return;
+// every > 1: part of a reinitialisation that runs only on steps whose number
+// (counting from 1) is a multiple of `every`, decided on the device so that a
+// captured step graph replays correctly on every step
+__device__ __forceinline__ bool reinit_skipped(const DevTime* D, int every) {
+  return every > 1 && (D->numsteps + 1) % every != 0;
+}
+
+__global__ void k_copy_plane(GridP P, const double* src, double* dst, const DevTime* D, int every) {
+  if (!D->active || reinit_skipped(D, every)) return;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < P.plane; k += (int64_t)gridDim.x * blockDim.x)
     dst[k] = src[k];
 }
 
 // S(phi0) = phi0 / sqrt(phi0^2 + h^2), cached for the reinitialisation
-__global__ void k_reinit_sign(GridP P, const double* phi, double* S, const DevTime* D) {
-  if (!D->active) return;
+__global__ void k_reinit_sign(GridP P, const double* phi, double* S, const DevTime* D, int every) {
+  if (!D->active || reinit_skipped(D, every)) return;
   const int64_t n = (int64_t)P.nr * P.nc;
   const double h = dmin_std(P.dx, P.dy);
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
@@ -1124,8 +1131,8 @@ __global__ void k_reinit_sign(GridP P, const double* phi, double* S, const DevTi
 
 // one Sussman-Smereka-Osher iteration with Godunov upwinding
 __global__ void __launch_bounds__(256) k_reinit_iter(GridP P, const double* cur, const double* S, double* out,
-                                                     const DevTime* D) {
-  if (!D->active) return;
+                                                     const DevTime* D, int every) {
+  if (!D->active || reinit_skipped(D, every)) return;
   const int64_t n = (int64_t)P.nr * P.nc;
   GridP Q = P;
   if (!P.periodic) { Q.bcL = Q.bcR = Q.bcB = Q.bcT = GFM_BC_TRANSMISSIVE; }
@@ -1512,23 +1519,23 @@ void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
     k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime); counted();
     k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
   }
-  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime); counted();
+  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0); counted();
 }
 
 // reinitialisation: iterations alternate phi -> phi_a -> phi ...; an odd
 // count ends with a copy back, so phi stays the one buffer holding the level set
-void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m) {
+void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every) {
   const GridP& P = ctx->P;
   cudaStream_t s = ctx->stream;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
-  k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime); counted();
+  k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime, every); counted();
   for (int it = 0; it < m->reinit_iters; it++) {
     const double* src = (it & 1) ? ctx->phi_a : ctx->phi;
     double* dst = (it & 1) ? ctx->phi : ctx->phi_a;
-    k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime); counted();
+    k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime, every); counted();
   }
   if (m->reinit_iters & 1) {
-    k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime); counted();
+    k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, every); counted();
   }
 }
 

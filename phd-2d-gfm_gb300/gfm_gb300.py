@@ -92,6 +92,13 @@ def lib():
         "gfm_step_timed": [P, ctypes.POINTER(MethodDesc), I, pd],
         "gfm_set_overlap": [P, I],
         "gfm_fp64_peak": [pd, V],
+        "gfm_batch_create": [ctypes.POINTER(GridDesc), I, I, ctypes.POINTER(P)],
+        "gfm_batch_destroy": [P], "gfm_batch_instance": [P, I, ctypes.POINTER(P)],
+        "gfm_batch_set_stream": [P, V], "gfm_batch_synchronize": [P],
+        "gfm_step_batched_graph": [P, ctypes.POINTER(MethodDesc), I],
+        "gfm_step_batched_sequential": [P, ctypes.POINTER(MethodDesc), I],
+        "gfm_case_shock_bubble": [V, I, I, ctypes.POINTER(GridDesc), pd],
+        "gfm_case_init_shock_bubble": [V, ctypes.POINTER(GridDesc), pd, pd, pd],
         "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
         "gfm_clear_device_status": [P],
         "gfm_get_stats": [P, ctypes.POINTER(ctypes.c_int64)] * 1 + [ctypes.POINTER(ctypes.c_int64)] * 2,
@@ -173,9 +180,13 @@ def method(fs="MUSCL", gfm="riemannGFM", itm="LS5", CFL=0.6, T=1.0, reinit_every
 class Context:
     """Device-resident grids of one instance (gfm_ctx)."""
 
-    def __init__(self, desc, two_fluid=True, stream=None):
+    def __init__(self, desc, two_fluid=True, stream=None, _borrowed=None):
         self.desc = desc
         self.two_fluid = bool(two_fluid)
+        self._owned = _borrowed is None
+        if _borrowed is not None:   # an instance of a Batch: the batch owns it
+            self._p = _borrowed
+            return
         self._p = ctypes.c_void_p()
         _check(lib().gfm_ctx_create(ctypes.byref(desc), int(self.two_fluid), ctypes.byref(self._p)),
                "gfm_ctx_create")
@@ -183,9 +194,9 @@ class Context:
             _check(lib().gfm_set_stream(self._p, ctypes.c_void_p(stream)), "gfm_set_stream")
 
     def close(self):
-        if self._p:
+        if self._p and self._owned:
             lib().gfm_ctx_destroy(self._p)
-            self._p = ctypes.c_void_p()
+        self._p = ctypes.c_void_p()
 
     def __del__(self):
         try:
@@ -271,6 +282,70 @@ class Context:
         m = ctypes.c_double()
         _check(lib().gfm_fluid_mass(self._p, interiorsign, ctypes.byref(m)), "gfm_fluid_mass")
         return m.value
+
+
+# ---------------------------------------------------------------------------
+# batches of instances
+# ---------------------------------------------------------------------------
+class Batch:
+    """Many independent instances stepped together (gfm_batch): `instances`
+    are Contexts (upload, download, time, status) owned by the batch."""
+
+    def __init__(self, descs, two_fluid=True, stream=None):
+        descs = list(descs)
+        arr = (GridDesc * len(descs))(*descs)
+        self._p = ctypes.c_void_p()
+        _check(lib().gfm_batch_create(arr, len(descs), int(bool(two_fluid)), ctypes.byref(self._p)),
+               "gfm_batch_create")
+        self.instances = []
+        for i, d in enumerate(descs):
+            c = ctypes.c_void_p()
+            _check(lib().gfm_batch_instance(self._p, i, ctypes.byref(c)), "gfm_batch_instance")
+            self.instances.append(Context(d, two_fluid, _borrowed=c))
+        if stream is not None:
+            _check(lib().gfm_batch_set_stream(self._p, ctypes.c_void_p(stream)), "gfm_batch_set_stream")
+
+    def step(self, m, nsteps=1, graph=True):
+        """nsteps steps of every instance: recorded CUDA graph with the
+        instances side by side (graph=True), or one instance after another."""
+        f = lib().gfm_step_batched_graph if graph else lib().gfm_step_batched_sequential
+        _check(f(self._p, ctypes.byref(m), nsteps), "gfm_step_batched_%s" % ("graph" if graph else "sequential"))
+
+    def synchronize(self):
+        _check(lib().gfm_batch_synchronize(self._p), "gfm_batch_synchronize")
+
+    def close(self):
+        for c in getattr(self, "instances", []):
+            c._p = ctypes.c_void_p()
+        if self._p:
+            lib().gfm_batch_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BubbleParams(ctypes.Structure):
+    _fields_ = [("mach", ctypes.c_double), ("gamma_bubble", ctypes.c_double), ("rho_ratio", ctypes.c_double),
+                ("radius_frac", ctypes.c_double)]
+
+
+def shock_bubble_case(Nx, Ny, mach, gamma_bubble, rho_ratio, radius_frac):
+    """Grid, T and initial state of one member of the shock-bubble family
+    (gfm_case_shock_bubble / gfm_case_init_shock_bubble)."""
+    p = BubbleParams(mach, gamma_bubble, rho_ratio, radius_frac)
+    d = GridDesc()
+    T = ctypes.c_double(0.0)
+    _check(lib().gfm_case_shock_bubble(ctypes.byref(p), Nx, Ny, ctypes.byref(d), ctypes.byref(T)),
+           "gfm_case_shock_bubble")
+    nr, nc = d.shape
+    U1, U2, phi = np.empty((4, nr, nc)), np.empty((4, nr, nc)), np.empty((nr, nc))
+    _check(lib().gfm_case_init_shock_bubble(ctypes.byref(p), ctypes.byref(d), _dptr(U1), _dptr(U2), _dptr(phi)),
+           "gfm_case_init_shock_bubble")
+    return d, T.value, U1, U2, phi
 
 
 # ---------------------------------------------------------------------------

@@ -89,3 +89,18 @@ def test_onefluid_circularexplosion_area_fractions():
     assert abs(frac.sum() * d.dx * d.dy - np.pi * 0.16) < 2e-3
     # 8-fold symmetry of the initial condition
     assert np.allclose(rho, rho.T) and np.allclose(rho, rho[::-1, :])
+
+
+def test_shock_bubble_family():
+    d, T, U1, U2, phi = g.shock_bubble_case(192, 64, 2.0, 1.2, 3.0, 0.3)
+    assert d.dx == d.dy == 0.25 / 192 and d.gamma1 == 1.2 and d.gamma2 == 1.4 and d.BC_B == 1
+    gc = d.numGC
+    H = d.dy * d.Ny
+    # bubble: phi < 0 within radius 0.3 H of (0.7 W, H/2), density ratio 3
+    i, j = gc + d.Ny // 2, gc + int(0.7 * d.Nx)
+    assert phi[i, j] < 0 and abs(U1[0, i, j] - 3.0) < 1e-12
+    assert abs(phi[i, j] + 0.3 * H) < 2 * d.dx
+    # post-shock air right of 0.9 W moves left; Rankine-Hugoniot for Mach 2
+    assert U2[1, i, -gc - 1] < 0 and abs(U2[0, i, -gc - 1] - 8.0 / 3.0) < 1e-12
+    with pytest.raises(g.GFMError):
+        g.shock_bubble_case(64, 64, 0.9, 1.4, 1.0, 0.2)
