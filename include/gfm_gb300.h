@@ -210,6 +210,44 @@ gfm_status_t gfm_step_batched_graph(gfm_batch* b, const gfm_method_desc* m, int 
 gfm_status_t gfm_step_batched_sequential(gfm_batch* b, const gfm_method_desc* m, int nsteps);
 gfm_status_t gfm_batch_synchronize(gfm_batch* b);
 
+/* Learned star-pressure proposal (no counterpart in the reference): a
+ * multilayer perceptron 10 -> 64 -> 64 -> 64 -> 1 (SiLU) maps a two-material
+ * Riemann problem's normalised states (rho, u, p + pinf, gamma, pinf of both
+ * sides) to the log of p* relative to the solver's two-shock guess; it is
+ * applied where that guess moved far (|log| > 1e-2) from the PVRS guess, and
+ * Newton's method runs from the proposal to the usual tolerance.
+ *   gfm_mlp_create            He-initialised parameters (9089 floats,
+ *                             layout W1[10][64] b1 W2[64][64] b2 W3 b3 w4[64] b4)
+ *   gfm_mlp_get/set_params    host copies (save / load)
+ *   gfm_mlp_generate          n training problems on the device (DEVICE X[n][10],
+ *                             Y[n]): gammas U[1.09,4.4], pinf in {0,6e8},
+ *                             p_L 10^U[3,8], p_R/p_L log-U[1e-3,1e5], rho_L
+ *                             10^U[-1,3], rho_R/rho_L log-U[1e-3,1e3], jump in u
+ *                             U[-3,3] x mean sound speed; targets from the exact solver
+ *   gfm_mlp_gradient          mean-square-error gradient over DEVICE X, Y (host grad)
+ *   gfm_mlp_train             Adam over shuffled minibatches, cosine learning
+ *                             rate; loss_per_epoch (host, epochs floats) or NULL
+ *   gfm_mlp_infer             DEVICE X[n][10] -> out[n]: FP32 on CUDA cores
+ *                             (tensor_cores = 0) or BF16 tensor cores (1)
+ *   gfm_rs_mixed_batch_learned  gfm_rs_mixed_batch with the proposal (use_net =
+ *                             1) or the two-shock guess (0); iters[n] receives
+ *                             each solve's Newton iteration count */
+typedef struct gfm_mlp gfm_mlp;
+gfm_status_t gfm_mlp_create(uint64_t seed, gfm_mlp** out);
+gfm_status_t gfm_mlp_destroy(gfm_mlp* m);
+gfm_status_t gfm_mlp_set_params(gfm_mlp* m, const float* params);
+gfm_status_t gfm_mlp_get_params(gfm_mlp* m, float* params);
+int gfm_mlp_param_count(void);
+gfm_status_t gfm_mlp_generate(uint64_t seed, int n, float* X, float* Y, int* n_out, void* cuda_stream);
+gfm_status_t gfm_mlp_gradient(gfm_mlp* m, const float* X, const float* Y, int n, float* grad, float* loss,
+                              void* cuda_stream);
+gfm_status_t gfm_mlp_train(gfm_mlp* m, const float* X, const float* Y, int n, int epochs, int batch, float lr,
+                           uint64_t seed, float* loss_per_epoch, void* cuda_stream);
+gfm_status_t gfm_mlp_infer(gfm_mlp* m, const float* X, int n, float* out, int tensor_cores, void* cuda_stream);
+gfm_status_t gfm_rs_mixed_batch_learned(gfm_mlp* m, int n, double gammaL, double pinfL, double gammaR, double pinfR,
+                                        const double* UL, const double* UR, double* out, int* iters,
+                                        uint32_t* status, int use_net, void* cuda_stream);
+
 /* Shock-bubble family of the batched workload: the 1000x400 shock-bubble's
  * geometry on any grid (width 0.25, square cells, height 0.25 Ny/Nx,
  * reflective top and bottom, transmissive ends), air (gamma 1.4, rho 1,

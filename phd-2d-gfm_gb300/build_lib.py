@@ -23,9 +23,9 @@ LIBDIR = os.path.join(HERE, "lib", MACHINE)
 ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_LIBDIR = os.path.join(ORACLE, "lib", MACHINE)
 
-CU_SOURCES = ["gfm_flux.cu", "gfm_step.cu", "gfm_api.cu", "gfm_noalloc.cu", "gfm_batch.cu"]
+CU_SOURCES = ["gfm_flux.cu", "gfm_step.cu", "gfm_api.cu", "gfm_noalloc.cu", "gfm_batch.cu", "gfm_mlp.cu"]
 CPP_SOURCES = ["gfm_cases.cpp"]
-HEADERS = ["gfm_math.cuh", "gfm_internal.cuh", "gfm_tables.h"]
+HEADERS = ["gfm_math.cuh", "gfm_internal.cuh", "gfm_tables.h", "gfm_mlp.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off"]

@@ -98,6 +98,13 @@ def lib():
         "gfm_step_batched_graph": [P, ctypes.POINTER(MethodDesc), I],
         "gfm_step_batched_sequential": [P, ctypes.POINTER(MethodDesc), I],
         "gfm_case_shock_bubble": [V, I, I, ctypes.POINTER(GridDesc), pd],
+        "gfm_mlp_create": [ctypes.c_uint64, ctypes.POINTER(P)], "gfm_mlp_destroy": [P],
+        "gfm_mlp_set_params": [P, V], "gfm_mlp_get_params": [P, V],
+        "gfm_mlp_generate": [ctypes.c_uint64, I, V, V, ctypes.POINTER(I), V],
+        "gfm_mlp_gradient": [P, V, V, I, V, ctypes.POINTER(ctypes.c_float), V],
+        "gfm_mlp_train": [P, V, V, I, I, I, ctypes.c_float, ctypes.c_uint64, V, V],
+        "gfm_mlp_infer": [P, V, I, V, I, V],
+        "gfm_rs_mixed_batch_learned": [P, I, D, D, D, D, V, V, V, V, V, I, V],
         "gfm_case_init_shock_bubble": [V, ctypes.POINTER(GridDesc), pd, pd, pd],
         "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
         "gfm_clear_device_status": [P],
@@ -116,6 +123,8 @@ def lib():
     L.gfm_version.argtypes = []
     L.gfm_launch_count.restype = ctypes.c_int64
     L.gfm_launch_count.argtypes = []
+    L.gfm_mlp_param_count.restype = ctypes.c_int
+    L.gfm_mlp_param_count.argtypes = []
     _lib = L
     return L
 
@@ -346,6 +355,73 @@ def shock_bubble_case(Nx, Ny, mach, gamma_bubble, rho_ratio, radius_frac):
     _check(lib().gfm_case_init_shock_bubble(ctypes.byref(p), ctypes.byref(d), _dptr(U1), _dptr(U2), _dptr(phi)),
            "gfm_case_init_shock_bubble")
     return d, T.value, U1, U2, phi
+
+
+# ---------------------------------------------------------------------------
+# learned star-pressure proposal
+# ---------------------------------------------------------------------------
+class MLP:
+    """The learned proposal (gfm_mlp).  Device arrays are passed as raw
+    pointers (e.g. torch tensors' data_ptr())."""
+
+    NPARAM = 9089
+
+    def __init__(self, seed=1):
+        self._p = ctypes.c_void_p()
+        _check(lib().gfm_mlp_create(seed, ctypes.byref(self._p)), "gfm_mlp_create")
+
+    def params(self):
+        out = np.empty(self.NPARAM, dtype=np.float32)
+        _check(lib().gfm_mlp_get_params(self._p, out.ctypes.data_as(ctypes.c_void_p)), "gfm_mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().gfm_mlp_set_params(self._p, p.ctypes.data_as(ctypes.c_void_p)), "gfm_mlp_set_params")
+
+    def gradient(self, X_ptr, Y_ptr, n, stream=0):
+        g = np.empty(self.NPARAM, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(lib().gfm_mlp_gradient(self._p, ctypes.c_void_p(X_ptr), ctypes.c_void_p(Y_ptr), n,
+                                      g.ctypes.data_as(ctypes.c_void_p), ctypes.byref(loss), ctypes.c_void_p(stream)),
+               "gfm_mlp_gradient")
+        return g, loss.value
+
+    def train(self, X_ptr, Y_ptr, n, epochs, batch=8192, lr=2e-3, seed=7, stream=0):
+        losses = np.zeros(epochs, dtype=np.float32)
+        _check(lib().gfm_mlp_train(self._p, ctypes.c_void_p(X_ptr), ctypes.c_void_p(Y_ptr), n, epochs, batch, lr, seed,
+                                   losses.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(stream)), "gfm_mlp_train")
+        return losses
+
+    def infer(self, X_ptr, n, out_ptr, tensor_cores=True, stream=0):
+        _check(lib().gfm_mlp_infer(self._p, ctypes.c_void_p(X_ptr), n, ctypes.c_void_p(out_ptr), int(tensor_cores),
+                                   ctypes.c_void_p(stream)), "gfm_mlp_infer")
+
+    def rs_mixed(self, gL, pinfL, gR, pinfR, UL_ptr, UR_ptr, n, out_ptr, iters_ptr, status_ptr, use_net=True,
+                 stream=0):
+        _check(lib().gfm_rs_mixed_batch_learned(self._p, n, gL, pinfL, gR, pinfR, ctypes.c_void_p(UL_ptr),
+                                                ctypes.c_void_p(UR_ptr), ctypes.c_void_p(out_ptr),
+                                                ctypes.c_void_p(iters_ptr), ctypes.c_void_p(status_ptr), int(use_net),
+                                                ctypes.c_void_p(stream)), "gfm_rs_mixed_batch_learned")
+
+    def close(self):
+        if self._p:
+            lib().gfm_mlp_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mlp_generate(seed, n, X_ptr, Y_ptr, stream=0):
+    """n training problems into device arrays X (n x 10 float) and Y (n)."""
+    got = ctypes.c_int(0)
+    _check(lib().gfm_mlp_generate(seed, n, ctypes.c_void_p(X_ptr), ctypes.c_void_p(Y_ptr), ctypes.byref(got),
+                                  ctypes.c_void_p(stream)), "gfm_mlp_generate")
+    return got.value
 
 
 # ---------------------------------------------------------------------------

@@ -1,0 +1,164 @@
+"""The learned star-pressure proposal (gfm_mlp): the training kernels'
+gradients against a float64 numpy forward/backward pass, the generated
+training problems, the BF16 tensor-core inference against the FP32 CUDA-core
+inference, and the Riemann solve from the trained proposal (same p*, fewer
+Newton iterations than the two-shock guess on strong-wave problems)."""
+import numpy as np
+import pytest
+
+import gfm_gb300 as g
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+H = 64
+
+
+def unpack(p):
+    p = p.astype(np.float64)
+    o = 0
+    W1 = p[o:o + 10 * H].reshape(10, H); o += 10 * H
+    b1 = p[o:o + H]; o += H
+    W2 = p[o:o + H * H].reshape(H, H); o += H * H
+    b2 = p[o:o + H]; o += H
+    W3 = p[o:o + H * H].reshape(H, H); o += H * H
+    b3 = p[o:o + H]; o += H
+    w4 = p[o:o + H]; o += H
+    b4 = p[o]
+    return W1, b1, W2, b2, W3, b3, w4, b4
+
+
+def silu(z):
+    return z / (1.0 + np.exp(-z))
+
+
+def dsilu(z):
+    s = 1.0 / (1.0 + np.exp(-z))
+    return s * (1.0 + z * (1.0 - s))
+
+
+def forward(p, X):
+    W1, b1, W2, b2, W3, b3, w4, b4 = unpack(p)
+    z1 = X @ W1 + b1
+    z2 = silu(z1) @ W2 + b2
+    z3 = silu(z2) @ W3 + b3
+    return silu(z3) @ w4 + b4, (z1, z2, z3)
+
+
+def grad_ref(p, X, Y):
+    W1, b1, W2, b2, W3, b3, w4, b4 = unpack(p)
+    y, (z1, z2, z3) = forward(p, X)
+    n = len(Y)
+    dy = 2.0 * (y - Y) / n
+    gw4 = silu(z3).T @ dy
+    gb4 = dy.sum()
+    d3 = np.outer(dy, w4) * dsilu(z3)
+    gW3 = silu(z2).T @ d3
+    gb3 = d3.sum(0)
+    d2 = (d3 @ W3.T) * dsilu(z2)
+    gW2 = silu(z1).T @ d2
+    gb2 = d2.sum(0)
+    d1 = (d2 @ W2.T) * dsilu(z1)
+    gW1 = X.T @ d1
+    gb1 = d1.sum(0)
+    grad = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3, gw4, [gb4]])
+    return grad, ((y - Y) ** 2).mean()
+
+
+def test_gradient_matches_float64_reference():
+    m = g.MLP(seed=3)
+    rng = np.random.default_rng(5)
+    n = 300
+    X = rng.standard_normal((n, 10)).astype(np.float32)
+    Y = rng.standard_normal(n).astype(np.float32)
+    Xd, Yd = torch.from_numpy(X).cuda(), torch.from_numpy(Y).cuda()
+    gg, loss = m.gradient(Xd.data_ptr(), Yd.data_ptr(), n)
+    gr, lr = grad_ref(m.params(), X.astype(np.float64), Y.astype(np.float64))
+    m.close()
+    assert len(gg) == g.MLP.NPARAM == len(gr)
+    assert abs(loss - lr) <= 1e-4 * lr
+    assert np.max(np.abs(gg - gr)) <= 1e-4 * np.max(np.abs(gr))
+
+
+def test_generated_problems():
+    n = 8192
+    X = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+    Y = torch.empty(n, dtype=torch.float32, device="cuda")
+    got = g.mlp_generate(11, n, X.data_ptr(), Y.data_ptr())
+    assert got == n
+    X, Y = X.cpu().numpy(), Y.cpu().numpy()
+    assert np.isfinite(X).all() and np.isfinite(Y).all() and np.abs(Y).max() < 30
+    assert (X[:, 0] <= 0).all() and (X[:, 1] <= 0).all() and (X[:, 4] <= 0).all() and (X[:, 5] <= 0).all()
+    assert np.allclose(np.maximum(X[:, 4], X[:, 5]), 0.0)          # one side sets the pressure scale
+    assert (X[:, 6] >= (1.09 - 2.7) / 1.7 - 1e-6).all() and (X[:, 6] <= (4.4 - 2.7) / 1.7 + 1e-6).all()
+    assert ((X[:, 8] >= 0) & (X[:, 8] <= 1)).all()
+    assert np.allclose(X[:, 2], -X[:, 3], atol=1e-6)                # velocities about their mean
+    # the gate selects strong waves: the two-shock guess is off by more than rounding
+    assert np.median(np.abs(Y)) > 1e-4
+
+
+def test_tensor_core_inference_matches_fp32():
+    m = g.MLP(seed=9)
+    n = 1000   # not a multiple of the 128-row tile
+    X = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+    Y = torch.empty(n, dtype=torch.float32, device="cuda")
+    g.mlp_generate(12, n, X.data_ptr(), Y.data_ptr())
+    o32 = torch.zeros(n, dtype=torch.float32, device="cuda")
+    otc = torch.zeros(n, dtype=torch.float32, device="cuda")
+    m.infer(X.data_ptr(), n, o32.data_ptr(), tensor_cores=False)
+    m.infer(X.data_ptr(), n, otc.data_ptr(), tensor_cores=True)
+    torch.cuda.synchronize()
+    a, b = o32.cpu().numpy(), otc.cpu().numpy()
+    ref, _ = forward(m.params(), X.cpu().numpy().astype(np.float64))
+    m.close()
+    assert np.max(np.abs(a - ref)) <= 1e-4 * (1 + np.max(np.abs(ref)))        # FP32 path
+    scale = np.max(np.abs(ref)) + 1.0
+    assert np.max(np.abs(b - ref)) <= 0.03 * scale, np.max(np.abs(b - ref))   # BF16 operands, FP32 accumulation
+    assert np.corrcoef(b, ref)[0, 1] > 0.999
+
+
+def stiffened_cons(g_, pinf, rho, u, p):
+    E = (p + g_ * pinf) / (g_ - 1.0) + 0.5 * rho * u * u
+    return np.stack([rho, rho * u, np.zeros_like(rho), E], 1)
+
+
+def test_trained_proposal_keeps_pstar_and_saves_iterations():
+    n = 1 << 18
+    X = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+    Y = torch.empty(n, dtype=torch.float32, device="cuda")
+    got = g.mlp_generate(21, n, X.data_ptr(), Y.data_ptr())
+    m = g.MLP(seed=4)
+    losses = m.train(X.data_ptr(), Y.data_ptr(), got, epochs=12, batch=4096, lr=2e-3)
+    assert np.isfinite(losses).all() and losses[-1] < 0.5 * losses[0]
+    # air | water problems with strong waves, solved from the two-shock guess and from the proposal
+    rng = np.random.default_rng(8)
+    k = 4096
+    gL, qL, gR, qR = 1.4, 0.0, 4.4, 6e8
+    pL = 10 ** rng.uniform(3, 8, k)
+    pR = pL * np.exp(rng.uniform(np.log(1e-3), np.log(1e5), k))
+    rL = 10 ** rng.uniform(-1, 3, k)
+    rR = rL * np.exp(rng.uniform(np.log(1e-3), np.log(1e3), k))
+    cL, cR = np.sqrt(gL * (pL + qL) / rL), np.sqrt(gR * (pR + qR) / rR)
+    du = rng.uniform(-2.0, 1.0, k) * 0.5 * (cL + cR)
+    UL = torch.from_numpy(np.ascontiguousarray(stiffened_cons(gL, qL, rL, -0.5 * du, pL))).cuda()
+    UR = torch.from_numpy(np.ascontiguousarray(stiffened_cons(gR, qR, rR, 0.5 * du, pR))).cuda()
+    res = {}
+    for net in (False, True):
+        out = torch.zeros((k, 4), dtype=torch.float64, device="cuda")
+        its = torch.zeros(k, dtype=torch.int32, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        m.rs_mixed(gL, qL, gR, qR, UL.data_ptr(), UR.data_ptr(), k, out.data_ptr(), its.data_ptr(), st.data_ptr(),
+                   use_net=net)
+        torch.cuda.synchronize()
+        res[net] = (out.cpu().numpy(), its.cpu().numpy(), int(st.item()))
+    m.close()
+    (o0, i0, s0), (o1, i1, s1) = res[False], res[True]
+    vac = (2.0 / (gL - 1.0)) * cL + (2.0 / (gR - 1.0)) * cR <= du
+    good = ~vac & np.isfinite(o0[:, 0]) & np.isfinite(o1[:, 0])
+    assert good.mean() > 0.5
+    scale = np.abs(o0[:, 0]) + 1e-6 * np.maximum(pL, pR)
+    rel = np.abs(o1[:, 0] - o0[:, 0]) / scale
+    assert np.all(rel[good] <= 1e-10), rel[good].max()
+    print("Newton iterations: two-shock guess %.3f, learned proposal %.3f (%d problems)"
+          % (i0[good].mean(), i1[good].mean(), good.sum()))
+    assert i1[good].mean() < i0[good].mean(), (i1[good].mean(), i0[good].mean())
