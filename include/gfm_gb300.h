@@ -248,6 +248,26 @@ gfm_status_t gfm_rs_mixed_batch_learned(gfm_mlp* m, int n, double gammaL, double
                                         const double* UL, const double* UR, double* out, int* iters,
                                         uint32_t* status, int use_net, void* cuda_stream);
 
+/* The context's interface solves (Riemann and real GFM) start Newton's
+ * method from the learned proposal where it applies (NULL: the two-shock
+ * guess everywhere, the default).  Each warp of the interface loop evaluates
+ * the network in FP32 on its cell's actual states (one problem at a time, on
+ * the loop's latency-bound critical path).  The network is read at each step
+ * (training it between steps takes effect).  Results differ from the default
+ * only within the Newton tolerance (p* within about 2e-14); they are not
+ * bit-identical to the oracle. */
+gfm_status_t gfm_set_mlp(gfm_ctx* ctx, gfm_mlp* mlp);
+/* Training data from the solver itself: while set, every step of the Riemann
+ * or real GFM appends its gated interface problems (features of the states
+ * the interface loop solves, and the target from the solved p*) to the
+ * DEVICE arrays X[cap][10], Y[cap]; *count (DEVICE int, zeroed by the caller)
+ * counts them (and may exceed cap: the rest are dropped).  NULL arrays stop
+ * the capture. */
+gfm_status_t gfm_capture_interface_problems(gfm_ctx* ctx, float* X, float* Y, int cap, int* count);
+/* Interface solves of the last step: count, Newton iterations, and how many
+ * started from the learned proposal. */
+gfm_status_t gfm_get_interface_stats(gfm_ctx* ctx, int64_t* n_solves, int64_t* newton_iters, int64_t* n_proposed);
+
 /* Shock-bubble family of the batched workload: the 1000x400 shock-bubble's
  * geometry on any grid (width 0.25, square cells, height 0.25 Ny/Nx,
  * reflective top and bottom, transmissive ends), air (gamma 1.4, rho 1,

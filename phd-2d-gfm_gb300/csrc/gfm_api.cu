@@ -466,6 +466,36 @@ gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
   return run_steps(ctx, m, nsteps, phase_ms);
 }
 
+gfm_status_t gfm_set_mlp(gfm_ctx* ctx, gfm_mlp* mlp) {
+  if (!ctx || !ctx->two_fluid) return GFM_ERR_ARG;
+  if (!mlp) {
+    ctx->mlp = nullptr;
+    return GFM_OK;
+  }
+  ctx->mlp = mlp;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_capture_interface_problems(gfm_ctx* ctx, float* X, float* Y, int cap, int* count) {
+  if (!ctx || !ctx->two_fluid || cap < 0) return GFM_ERR_ARG;
+  if (!X || !Y || !count || cap == 0) {
+    ctx->cap_X = nullptr; ctx->cap_Y = nullptr; ctx->cap_count = nullptr; ctx->cap = 0;
+    return GFM_OK;
+  }
+  ctx->cap_X = X; ctx->cap_Y = Y; ctx->cap_count = count; ctx->cap = cap;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_get_interface_stats(gfm_ctx* ctx, int64_t* n_solves, int64_t* newton_iters, int64_t* n_proposed) {
+  if (!ctx) return GFM_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (n_solves) *n_solves = ctx->h_dtime->n_ifc;
+  if (newton_iters) *newton_iters = (int64_t)ctx->h_dtime->ifc_iters;
+  if (n_proposed) *n_proposed = ctx->h_dtime->ifc_gated;
+  return GFM_OK;
+}
+
 gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int mode) {
   if (!ctx || mode < GFM_OVERLAP_OFF || mode > GFM_OVERLAP_AUTO) return GFM_ERR_ARG;
   if (mode != GFM_OVERLAP_OFF && !ctx->overlap_ok) return GFM_ERR_UNSUPPORTED;

@@ -39,6 +39,8 @@ struct DevTime {
   int n_ifc;               // interfacial cells of the last ghost fill
   int n_rounds;            // schedule rounds of the last interface solve
   unsigned long long newton_iters;
+  unsigned long long ifc_iters;   // Newton iterations of the interface solves (Riemann, real GFM)
+  int ifc_gated;                  // interface solves started from the learned proposal
   int rc[8];               // realcells1 (imin,imax,jmin,jmax), realcells2
 };
 
@@ -87,6 +89,11 @@ struct gfm_ctx {
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist
   int overlap;            // GFM_OVERLAP_* mode (gfm_set_overlap)
+  struct gfm_mlp* mlp;    // learned proposal for the interface solves (gfm_set_mlp), or null
+  float* cap_X;           // capture of gated interface problems (gfm_capture_interface_problems), or null
+  float* cap_Y;
+  int* cap_count;
+  int cap;
   int graph_mode;         // launches are being recorded into a CUDA graph
 };
 
@@ -151,6 +158,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_end_step(gfm_ctx* ctx);
 void prepare_kernels();
+const float* mlp_params(const struct gfm_mlp* m);   // the network's FP32 parameters (device)
 // nsteps iterations of the time loop on ctx's stream (gfm_step, gfm_step_timed)
 gfm_status_t run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
 gfm_status_t validate_method(gfm_ctx* ctx, const gfm_method_desc* m);

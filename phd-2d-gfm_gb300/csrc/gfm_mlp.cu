@@ -578,6 +578,8 @@ size_t tc_smem() { return sizeof(TcSmem); }
 
 }  // namespace
 
+const float* gfm::mlp_params(const gfm_mlp* m) { return m->P; }
+
 extern "C" {
 
 gfm_status_t gfm_mlp_create(uint64_t seed, gfm_mlp** out) {

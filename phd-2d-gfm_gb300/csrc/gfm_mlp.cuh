@@ -58,22 +58,26 @@ GFM_HD GuessInfo rs_guess_info(const RSSide& L, const Gas& kL, const RSSide& R, 
   return g;
 }
 
-// the ten input features, in float
+// the ten input features, computed in float (velocity jump in double)
+GFM_HD void mlp_features_f(double rhoL, double uL, double pbL, double gL, double qL, double rhoR, double uR,
+                           double pbR, double gR, double qR, float x[MLP_IN]) {
+  const float rl = (float)rhoL, rr = (float)rhoR, pl = (float)pbL, pr = (float)pbR;
+  const float rref = fmaxf(rl, rr), pref = fmaxf(pl, pr);
+  const float cref = sqrtf(pref / rref);
+  const float half_jump = (float)(0.5 * (uR - uL)) / cref;
+  x[0] = logf(rl / rref);
+  x[1] = logf(rr / rref);
+  x[2] = -half_jump;
+  x[3] = half_jump;
+  x[4] = logf(pl / pref);
+  x[5] = logf(pr / pref);
+  x[6] = ((float)gL - 2.7f) / 1.7f;
+  x[7] = ((float)gR - 2.7f) / 1.7f;
+  x[8] = (float)qL / pref;
+  x[9] = (float)qR / pref;
+}
 GFM_HD void mlp_features(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, float x[MLP_IN]) {
-  const double pref = c_lt(L.pb, R.pb) ? R.pb : L.pb;
-  const double rref = c_lt(L.rho, R.rho) ? R.rho : L.rho;
-  const double cref = sqrt(pref / rref);
-  const double ub = 0.5 * (L.u + R.u);
-  x[0] = (float)gfm_log(L.rho / rref);
-  x[1] = (float)gfm_log(R.rho / rref);
-  x[2] = (float)((L.u - ub) / cref);
-  x[3] = (float)((R.u - ub) / cref);
-  x[4] = (float)gfm_log(L.pb / pref);
-  x[5] = (float)gfm_log(R.pb / pref);
-  x[6] = (float)((kL.g - 2.7) / 1.7);
-  x[7] = (float)((kR.g - 2.7) / 1.7);
-  x[8] = (float)(kL.pinf / pref);
-  x[9] = (float)(kR.pinf / pref);
+  mlp_features_f(L.rho, L.u, L.pb, kL.g, kL.pinf, R.rho, R.u, R.pb, kR.g, kR.pinf, x);
 }
 
 // start of Newton given the network's output y for a gated problem
@@ -83,6 +87,38 @@ GFM_HD double mlp_apply(const GuessInfo& g, float y) {
 }
 
 __host__ __device__ inline float mlp_silu(float z) { return z / (1.0f + expf(-z)); }
+
+#if defined(__CUDACC__)
+// The network in FP32 by one warp (all 32 lanes, warp-uniform): lane l
+// computes neurons l and l + 32 of each layer from the parameters P in
+// global memory; hbuf holds a layer's 64 outputs (per-warp shared memory).
+__device__ inline float mlp_forward_warp(const float* __restrict__ P, const float x[MLP_IN], float* hbuf) {
+  const int l = threadIdx.x & 31;
+  float z0 = __ldg(P + MLP_B1 + l), z1 = __ldg(P + MLP_B1 + l + 32);
+  for (int k = 0; k < MLP_IN; k++) {
+    z0 += x[k] * __ldg(P + MLP_W1 + k * MLP_H + l);
+    z1 += x[k] * __ldg(P + MLP_W1 + k * MLP_H + l + 32);
+  }
+  for (int layer = 0; layer < 2; layer++) {
+    __syncwarp();
+    hbuf[l] = mlp_silu(z0);
+    hbuf[l + 32] = mlp_silu(z1);
+    __syncwarp();
+    const float* W = P + (layer == 0 ? MLP_W2 : MLP_W3);
+    const float* b = P + (layer == 0 ? MLP_B2 : MLP_B3);
+    z0 = __ldg(b + l);
+    z1 = __ldg(b + l + 32);
+    for (int k = 0; k < MLP_H; k++) {
+      const float h = hbuf[k];
+      z0 += h * __ldg(W + k * MLP_H + l);
+      z1 += h * __ldg(W + k * MLP_H + l + 32);
+    }
+  }
+  float y = mlp_silu(z0) * __ldg(P + MLP_W4 + l) + mlp_silu(z1) * __ldg(P + MLP_W4 + l + 32);
+  for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+  return y + __ldg(P + MLP_B4);
+}
+#endif
 
 // counter-based generator (splitmix64 finaliser): uniform in [0, 1)
 __host__ __device__ inline uint64_t mlp_mix(uint64_t z) {

@@ -11,6 +11,7 @@
 // ghost-layer cells itself: a ghost cell is a mirrored real cell, so its
 // thread evaluates that real cell's update and applies the reflective signs.
 #include "gfm_internal.cuh"
+#include "gfm_mlp.cuh"
 #include <climits>
 
 namespace gfm {
@@ -122,6 +123,8 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs a) {
       }
     }
     D->newton_iters = 0ull;
+    D->ifc_iters = 0ull;
+    D->ifc_gated = 0;
     *a.counter = 0u;
   }
 }
@@ -431,6 +434,11 @@ struct IfcArgs {
   unsigned int* ticket;
   DevTime* D;
   int slip;             // GFM_base::use_slip_BCs
+  const float* mlp;     // learned-proposal network (gfm_mlp.cuh), or null
+  float* cap_X;         // gated problems appended here (features, target), or null
+  float* cap_Y;
+  int* cap_count;
+  int cap;
 };
 
 __device__ __forceinline__ bool ifc_wait(const IfcArgs& a, int p) {
@@ -666,8 +674,14 @@ struct PairStar { double p, u, rho_own; bool trivial; };
 // p* and u* are the scalar ones on every lane and rho_own is the star
 // density of the lane's side.  The Newton loop is warp-uniform: both halves
 // compute the same pressure iterates.
+//
+// With a network (a.mlp), problems whose two-shock guess moved far from PVRS
+// (the gate of gfm_mlp.cuh) start from the network's proposal, evaluated by
+// the warp in FP32 on the actual states; with a capture buffer, such problems
+// are recorded (features and the solved p* relative to the two-shock guess).
 __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const Gas& kL, const Gas& kR, const V4& Uown,
-                                  uint32_t* status, int* iters) {
+                                                  uint32_t* status, int* iters, const IfcArgs& a, float* hbuf,
+                                                  int* proposed) {
   bool ok;
   V4 Wp = cons_to_prims_phys(k.g, k.pinf, Uown, &ok);
   if (!ok) *status |= ST_UNPHYSICAL;
@@ -697,7 +711,20 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   const double gown = sqrt(S.AK / (pg + k.pinf + S.BK));
   const double goth = xside(gown);
   const double gL = isR ? goth : gown, gR = isR ? gown : goth;
-  const double p0 = (gL * pL + gR * pR - (uR - uL)) / (gL + gR);
+  const double pts = (gL * pL + gR * pR - (uR - uL)) / (gL + gR);
+  double p0 = pts;
+  bool gated = false;
+  float x[MLP_IN];
+  if (a.mlp || a.cap_X) {   // warp-uniform: both halves hold the same values
+    const double ratio = (pts + pinf_min) / (pg + pinf_min);
+    gated = c_gt(ratio, 0.0) && c_gt(fabs(gfm_log(ratio)), MLP_GATE);
+    if (gated) mlp_features_f(rhoL, uL, pbL, kL.g, kL.pinf, rhoR, uR, pbR, kR.g, kR.pinf, x);
+    if (gated && a.mlp) {
+      const float y = fminf(fmaxf(mlp_forward_warp(a.mlp, x, hbuf), -20.0f), 20.0f);
+      p0 = (pts + pinf_min) * gfm_exp((double)y) - pinf_min;
+      *proposed += 1;
+    }
+  }
   // rs_star
   const double udiff = uR - uL;
   if (c_le(G4cL + G4cR, udiff)) *status |= ST_VACUUM;
@@ -725,7 +752,136 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   r.u = 0.5 * (uL + uR + (fR + fRd * dp) - (fL + fLd * dp));
   r.rho_own = rs_rho_star(S, k, p);
   *iters += it;
+  if (gated && a.cap_X && (threadIdx.x & 31) == 0 && it < GFM_RS_MAXIT && !c_le(G4cL + G4cR, udiff)) {
+    const double y = gfm_log((p + pinf_min) / (pts + pinf_min));
+    if (fabs(y) < 30.0) {
+      const int slot = atomicAdd(a.cap_count, 1);
+      if (slot < a.cap) {
+        for (int q = 0; q < MLP_IN; q++) a.cap_X[(int64_t)slot * MLP_IN + q] = x[q];
+        a.cap_Y[slot] = (float)y;
+      }
+    }
+  }
   return r;
+}
+
+// One interfacial cell's Riemann data in the lane layout above: on return
+// every lane holds its side's conserved normal-frame state Us (and the
+// tangential velocity tx, ty).  Returns false, on every lane, when a wait
+// ran out.
+struct IfcCell {
+  int64_t c;
+  int sr;             // side of the cell's real fluid
+  double nx, ny, tx, ty;
+  V4 Us;
+};
+
+template <int MODE>
+__device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k, uint32_t& st, IfcCell& cell) {
+  const GridP& P = a.P;
+  const int lane = threadIdx.x & 31;
+  const int s = lane >> 4, q = (lane >> 2) & 3, kc = lane & 3;
+  const bool isR = s == 1;
+  const int64_t lin = a.list[t];
+  const int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
+  const int64_t c = cidx(P, i, j);
+  const double lsval = a.phi[c];
+  const int sr = (lsval <= 0.0) ? 0 : 1;
+  double nx, ny;
+  unit_normal(a.nrm, P, c, nx, ny);
+  bool ok = true;
+  double v = 0.0;   // lanes with q == 0: component kc of side s's state
+  if (MODE == IFC_REAL) {
+    // neighbour with opposite phi sign and the closest normal
+    // (GFM_real.cpp:77-117); lane l < 9 is loop position l (xinc-major).
+    // Candidates more than 1e-6 below the largest clamped dot product are
+    // skipped as in k_interface; acos runs on the others at once and the
+    // first minimiser in loop order wins, as with the reference's strict <.
+    double dp = -3.0;
+    if (lane < 9) {
+      const int xinc = lane / 3 - 1, yinc = lane % 3 - 1;
+      const int64_t c2 = cidx(P, i + yinc, j + xinc);
+      if (lsval * a.phi[c2] <= 0.0) {
+        double ox, oy;
+        unit_normal(a.nrm, P, c2, ox, oy);
+        double d = nx * ox + ny * oy;
+        d = (d < -1.0) ? -1.0 : d;
+        d = (1.0 < d) ? 1.0 : d;
+        dp = d;
+      }
+    }
+    double dbest = dp;
+    for (int o = 8; o >= 1; o >>= 1) {
+      const double x = __shfl_xor_sync(FULL_MASK, dbest, o);
+      dbest = (x > dbest) ? x : dbest;
+    }
+    const bool elig = lane < 9 && !(dp < -2.0 || dp < dbest - 1e-6);
+    long long key = 0x7ff0000000000000LL;   // +inf: not a candidate
+    if (elig) {
+      const double ang = gfm_acos(dp);
+      if (ang == ang) key = as_bits(ang);   // angles are >= +0: bits order as values
+    }
+    int bl = (key == 0x7ff0000000000000LL) ? 32 : lane;
+    for (int o = 8; o >= 1; o >>= 1) {
+      const long long xk = __shfl_xor_sync(FULL_MASK, key, o);
+      const int xl = __shfl_xor_sync(FULL_MASK, bl, o);
+      if (xk < key || (xk == key && xl < bl)) { key = xk; bl = xl; }
+    }
+    bl = __shfl_sync(FULL_MASK, bl, 0);
+    int iopp = i, jopp = j;
+    if (bl == 32) st |= ST_BAD_ARGUMENT;
+    else { iopp = i + (bl % 3 - 1); jopp = j + (bl / 3 - 1); }
+    if (q == 0) {
+      if (s == sr) v = (s == 0 ? a.W1 : a.W2)[c + kc * P.plane];
+      else v = ifc_read1(a, s, iopp, jopp, kc, lin, ok);
+    }
+  } else {
+    // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33)
+    const double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
+    const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
+    const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
+    const double gx = a.nrm[c], gy = a.nrm[c + P.plane];
+    const double nm = a.nrm[c + 4 * P.plane];
+    double lv = lsval;
+    if (fabs(lv) > ds) lv = copysign(ds, lv);
+    double hx = nx, hy = ny;
+    if (nm < 1e-12) { hx = gx / nm; hy = gy / nm; }
+    const double ilx = ccx - lv * hx, ily = ccy - lv * hy;
+    // probe of side s: interface point + ds n (side 1) or - ds n (side 0)
+    const double dsx = ds * hx, dsy = ds * hy;
+    const double px = ilx + (isR ? dsx : -dsx);
+    const double py = ily + (isR ? dsy : -dsy);
+    const double sx = (px - P.x0) * P.idx + (double)P.g - 0.5;
+    const double sy = (py - P.y0) * P.idy + (double)P.g - 0.5;
+    int j0 = (int)floor(sx), i0 = (int)floor(sy);
+    j0 = min(max(j0, 0), P.nc - 2);
+    i0 = min(max(i0, 0), P.nr - 2);
+    const double wa = sx - (double)j0, wb = sy - (double)i0;
+    const double fa = (q & 1) ? wa : 1.0 - wa;
+    const double fb = (q & 2) ? wb : 1.0 - wb;
+    const double g = ifc_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
+    const double pr = (fa * fb) * g;
+    const double p1 = __shfl_down_sync(FULL_MASK, pr, 4);
+    const double p2 = __shfl_down_sync(FULL_MASK, pr, 8);
+    const double p3 = __shfl_down_sync(FULL_MASK, pr, 12);
+    v = ((pr + p1) + p2) + p3;
+  }
+  if (!__all_sync(FULL_MASK, ok)) return false;
+  const int base = lane & 16;
+  const double ia = __shfl_sync(FULL_MASK, v, base), ib = __shfl_sync(FULL_MASK, v, base + 1);
+  const double ic = __shfl_sync(FULL_MASK, v, base + 2), id = __shfl_sync(FULL_MASK, v, base + 3);
+  // mixed Riemann problem in the normal frame (e.g. GFM_riemann.cpp:76-122)
+  const double un = ib * nx + ic * ny;
+  cell.c = c;
+  cell.sr = sr;
+  cell.nx = nx;
+  cell.ny = ny;
+  cell.tx = ib - un * nx;
+  cell.ty = ic - un * ny;
+  bool okp = true;
+  cell.Us = prims_to_cons(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
+  if (!okp) st |= ST_UNPHYSICAL;
+  return true;
 }
 
 template <int MODE>
@@ -734,102 +890,19 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
   if (!a.D->active) return;
   const int n = a.D->n_ifc;
   const int lane = threadIdx.x & 31;
-  const int s = lane >> 4, q = (lane >> 2) & 3, kc = lane & 3;
-  const bool isR = s == 1;
+  const bool isR = (lane >> 4) == 1;
   const Gas k = isR ? P.gas2 : P.gas1;
+  __shared__ float s_h[8][MLP_H];   // per-warp layer outputs of the learned proposal
+  float* hbuf = s_h[(threadIdx.x >> 5) & 7];
   uint32_t st = 0;
-  int iters = 0;
+  int iters = 0, gated = 0;
   for (;;) {
     int t = 0;
     if (lane == 0) t = (int)atomicAdd(a.ticket, 1u);
     t = __shfl_sync(FULL_MASK, t, 0);
     if (t >= n) break;
-    const int64_t lin = a.list[t];
-    const int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
-    const int64_t c = cidx(P, i, j);
-    const double lsval = a.phi[c];
-    const int sr = (lsval <= 0.0) ? 0 : 1;   // side of the cell's real fluid
-    double nx, ny;
-    unit_normal(a.nrm, P, c, nx, ny);
-    bool ok = true;
-    double v = 0.0;   // lanes with q == 0: component kc of side s's state
-    if (MODE == IFC_REAL) {
-      // neighbour with opposite phi sign and the closest normal
-      // (GFM_real.cpp:77-117); lane l < 9 is loop position l (xinc-major).
-      // Candidates more than 1e-6 below the largest clamped dot product are
-      // skipped as in k_interface; acos runs on the others at once and the
-      // first minimiser in loop order wins, as with the reference's strict <.
-      double dp = -3.0;
-      if (lane < 9) {
-        const int xinc = lane / 3 - 1, yinc = lane % 3 - 1;
-        const int64_t c2 = cidx(P, i + yinc, j + xinc);
-        if (lsval * a.phi[c2] <= 0.0) {
-          double ox, oy;
-          unit_normal(a.nrm, P, c2, ox, oy);
-          double d = nx * ox + ny * oy;
-          d = (d < -1.0) ? -1.0 : d;
-          d = (1.0 < d) ? 1.0 : d;
-          dp = d;
-        }
-      }
-      double dbest = dp;
-      for (int o = 8; o >= 1; o >>= 1) {
-        const double x = __shfl_xor_sync(FULL_MASK, dbest, o);
-        dbest = (x > dbest) ? x : dbest;
-      }
-      const bool elig = lane < 9 && !(dp < -2.0 || dp < dbest - 1e-6);
-      long long key = 0x7ff0000000000000LL;   // +inf: not a candidate
-      if (elig) {
-        const double ang = gfm_acos(dp);
-        if (ang == ang) key = as_bits(ang);   // angles are >= +0: bits order as values
-      }
-      int bl = (key == 0x7ff0000000000000LL) ? 32 : lane;
-      for (int o = 8; o >= 1; o >>= 1) {
-        const long long xk = __shfl_xor_sync(FULL_MASK, key, o);
-        const int xl = __shfl_xor_sync(FULL_MASK, bl, o);
-        if (xk < key || (xk == key && xl < bl)) { key = xk; bl = xl; }
-      }
-      bl = __shfl_sync(FULL_MASK, bl, 0);
-      int iopp = i, jopp = j;
-      if (bl == 32) st |= ST_BAD_ARGUMENT;
-      else { iopp = i + (bl % 3 - 1); jopp = j + (bl / 3 - 1); }
-      if (q == 0) {
-        if (s == sr) v = (s == 0 ? a.W1 : a.W2)[c + kc * P.plane];
-        else v = ifc_read1(a, s, iopp, jopp, kc, lin, ok);
-      }
-    } else {
-      // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33)
-      const double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
-      const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
-      const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
-      const double gx = a.nrm[c], gy = a.nrm[c + P.plane];
-      const double nm = a.nrm[c + 4 * P.plane];
-      double lv = lsval;
-      if (fabs(lv) > ds) lv = copysign(ds, lv);
-      double hx = nx, hy = ny;
-      if (nm < 1e-12) { hx = gx / nm; hy = gy / nm; }
-      const double ilx = ccx - lv * hx, ily = ccy - lv * hy;
-      // probe of side s: interface point + ds n (side 1) or - ds n (side 0)
-      const double dsx = ds * hx, dsy = ds * hy;
-      const double px = ilx + (isR ? dsx : -dsx);
-      const double py = ily + (isR ? dsy : -dsy);
-      const double sx = (px - P.x0) * P.idx + (double)P.g - 0.5;
-      const double sy = (py - P.y0) * P.idy + (double)P.g - 0.5;
-      int j0 = (int)floor(sx), i0 = (int)floor(sy);
-      j0 = min(max(j0, 0), P.nc - 2);
-      i0 = min(max(i0, 0), P.nr - 2);
-      const double wa = sx - (double)j0, wb = sy - (double)i0;
-      const double fa = (q & 1) ? wa : 1.0 - wa;
-      const double fb = (q & 2) ? wb : 1.0 - wb;
-      const double g = ifc_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
-      const double pr = (fa * fb) * g;
-      const double p1 = __shfl_down_sync(FULL_MASK, pr, 4);
-      const double p2 = __shfl_down_sync(FULL_MASK, pr, 8);
-      const double p3 = __shfl_down_sync(FULL_MASK, pr, 12);
-      v = ((pr + p1) + p2) + p3;
-    }
-    ok = __all_sync(FULL_MASK, ok);
-    if (!ok) {
+    IfcCell cell;
+    if (!ifc_front<MODE>(a, t, k, st, cell)) {
       st |= ST_SCHEDULE_LIMIT;
       if (lane == 0) {
         __threadfence();
@@ -837,23 +910,14 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
       }
       continue;
     }
-    const int base = lane & 16;
-    const double ia = __shfl_sync(FULL_MASK, v, base), ib = __shfl_sync(FULL_MASK, v, base + 1);
-    const double ic = __shfl_sync(FULL_MASK, v, base + 2), id = __shfl_sync(FULL_MASK, v, base + 3);
-    // mixed Riemann problem in the normal frame (e.g. GFM_riemann.cpp:76-122)
-    const double un = ib * nx + ic * ny;
-    const double tx = ib - un * nx, ty = ic - un * ny;
-    bool okp = true;
-    const V4 Us = prims_to_cons(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
-    if (!okp) st |= ST_UNPHYSICAL;
-    int it = 0;
-    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it);
-    if (lane == 0) iters += it;
+    int it = 0, gt = 0;
+    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, cell.Us, &st, &it, a, hbuf, &gt);
+    if (lane == 0) { iters += it; gated += gt; }
     if (c_isnan(m.p)) st |= ST_NAN;
-    if (lane == 16 * sr) {
+    if (lane == 16 * cell.sr) {
       double* o = a.out + (int64_t)t * IFC_OUT;
-      const double snx = m.u * nx, sny = m.u * ny;
-      o[0] = m.rho_own; o[1] = snx + tx; o[2] = sny + ty; o[3] = m.p;
+      const double snx = m.u * cell.nx, sny = m.u * cell.ny;
+      o[0] = m.rho_own; o[1] = snx + cell.tx; o[2] = sny + cell.ty; o[3] = m.p;
       o[4] = snx; o[5] = sny;
       __threadfence();
       ((volatile int*)a.done)[t] = 1;
@@ -861,9 +925,14 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
   }
   uint32_t wst = __reduce_or_sync(FULL_MASK, st);
   unsigned wit = __reduce_add_sync(FULL_MASK, (unsigned)iters);
+  unsigned wgt = __reduce_add_sync(FULL_MASK, (unsigned)gated);
   if (lane == 0) {
     if (wst) atomicOr(&a.D->status, wst);
-    if (wit) atomicAdd(&a.D->newton_iters, (unsigned long long)wit);
+    if (wit) {
+      atomicAdd(&a.D->newton_iters, (unsigned long long)wit);
+      atomicAdd(&a.D->ifc_iters, (unsigned long long)wit);
+    }
+    if (wgt) atomicAdd(&a.D->ifc_gated, (int)wgt);
   }
 }
 
@@ -1236,6 +1305,12 @@ void launch_cfl_ogfm(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int
   launch_cfl_impl(ctx, CFL, T, ogfm, counter);
 }
 
+// the learned proposal and the capture of training problems (both off by default)
+static void set_learning(gfm_ctx* ctx, IfcArgs& ia) {
+  ia.mlp = ctx->mlp ? mlp_params(ctx->mlp) : nullptr;
+  ia.cap_X = ctx->cap_X; ia.cap_Y = ctx->cap_Y; ia.cap_count = ctx->cap_count; ia.cap = ctx->cap;
+}
+
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   const GridP& P = ctx->P;
   cudaStream_t s = ctx->stream;
@@ -1289,6 +1364,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.ticket = (unsigned int*)(ctx->ifc_opp);
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
+  set_learning(ctx, ia);
   int iblocks = 152;   // 4 warps per CTA: one chain warp per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
   else if (variant == GFM_REAL) k_interface_warp<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
@@ -1460,6 +1536,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.ticket = (unsigned int*)(ctx->ifc_opp);
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
+  set_learning(ctx, ia);
   const int chain_ctas = 16;   // 8 warps each: two chain warps per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);

@@ -105,6 +105,10 @@ def lib():
         "gfm_mlp_train": [P, V, V, I, I, I, ctypes.c_float, ctypes.c_uint64, V, V],
         "gfm_mlp_infer": [P, V, I, V, I, V],
         "gfm_rs_mixed_batch_learned": [P, I, D, D, D, D, V, V, V, V, V, I, V],
+        "gfm_set_mlp": [P, P],
+        "gfm_capture_interface_problems": [P, V, V, I, V],
+        "gfm_get_interface_stats": [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                    ctypes.POINTER(ctypes.c_int64)],
         "gfm_case_init_shock_bubble": [V, ctypes.POINTER(GridDesc), pd, pd, pd],
         "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
         "gfm_clear_device_status": [P],
@@ -286,6 +290,23 @@ class Context:
         ph = np.zeros(9)
         _check(lib().gfm_step_timed(self._p, ctypes.byref(m), nsteps, _dptr(ph)), "gfm_step_timed")
         return ph
+
+    def set_mlp(self, mlp):
+        """Start the interface solves from a learned proposal (an MLP), or
+        from the two-shock guess again (None)."""
+        _check(lib().gfm_set_mlp(self._p, mlp._p if mlp is not None else None), "gfm_set_mlp")
+
+    def capture_interface_problems(self, X_ptr, Y_ptr, cap, count_ptr):
+        """Append each step's gated interface problems (features, exact target)
+        to device arrays; X_ptr None stops."""
+        _check(lib().gfm_capture_interface_problems(self._p, ctypes.c_void_p(X_ptr), ctypes.c_void_p(Y_ptr), cap,
+                                                    ctypes.c_void_p(count_ptr)), "gfm_capture_interface_problems")
+
+    def interface_stats(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().gfm_get_interface_stats(self._p, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "gfm_get_interface_stats")
+        return {"solves": a.value, "newton_iters": b.value, "proposed": c.value}
 
     def fluid_mass(self, interiorsign):
         m = ctypes.c_double()
