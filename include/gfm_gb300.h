@@ -122,8 +122,8 @@ gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps);
 /* gfm_step with CUDA events recorded on the context's stream around each
  * phase; adds the milliseconds of each phase to phase_ms[GFM_NPHASES]:
  * 0 CFL/dt, 1 ghost fill, 2 flux update (both fluids, one launch),
- * 3 level set, 4 boundary conditions + end of step; phases 0-4 add up to
- * the step.  With the overlapped schedule (gfm_set_overlap) phase 1 runs up
+ * 3 level set (the part not hidden: it runs beside the flux update),
+ * 4 boundary conditions + end of step; phases 0-4 add up to the step.  With the overlapped schedule (gfm_set_overlap) phase 1 runs up
  * to the flux update of the tiles near the interface and phase 2 is that
  * update; phases 5-8 then time parts that overlap inside phases 1-2:
  * 5 the interface loop, 6 the far-field partition's work, 7 the exact

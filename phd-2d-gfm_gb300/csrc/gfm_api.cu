@@ -7,7 +7,7 @@
 
 namespace gfm {
 void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter);
-void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every);
+void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream_t s);
 void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out);
 }  // namespace gfm
 
@@ -224,6 +224,9 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_far, cudaEventDisableTiming);
     for (int q = 0; q < 6; q++)
       if (e == cudaSuccess) e = cudaEventCreate(&ctx->tev[q]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s_ls, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_done, cudaEventDisableTiming);
     if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
     ctx->overlap = ctx->overlap_ok ? GFM_OVERLAP_AUTO : GFM_OVERLAP_OFF;
   }
@@ -257,6 +260,12 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);
   for (int q = 0; q < 6; q++)
     if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
+  if (ctx->s_ls) {
+    cudaStreamSynchronize(ctx->s_ls);
+    cudaStreamDestroy(ctx->s_ls);
+  }
+  if (ctx->ev_ls_fork) cudaEventDestroy(ctx->ev_ls_fork);
+  if (ctx->ev_ls_done) cudaEventDestroy(ctx->ev_ls_done);
   cudaFree(ctx->dtime);
   cudaFree(extra(ctx).counters);
   cudaFree(extra(ctx).mass_part);
@@ -366,7 +375,7 @@ gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (!ctx || !ctx->two_fluid) return GFM_ERR_ARG;
   gfm_status_t r = check_method(ctx, m);
   if (r != GFM_OK) return r;
-  launch_ls_update(ctx, m);
+  launch_ls_update(ctx, m, ctx->stream);
   return last_error();
 }
 
@@ -400,24 +409,36 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
       overlapped = !m->use_extension_vfield &&
                    ((ctx->overlap == GFM_OVERLAP_ON && (m->gfm == GFM_RIEMANN || m->gfm == GFM_REAL)) ||
                     (ctx->overlap == GFM_OVERLAP_AUTO && m->gfm == GFM_RIEMANN));
+      // The level-set update reads phi and the velocity field of the ghost
+      // fill and writes only level-set buffers: it runs on its own stream
+      // beside the flux update (which reads and writes the fluid grids).
+      auto fork_level_set = [&]() {
+        cudaEventRecord(ctx->ev_ls_fork, ctx->stream);
+        cudaStreamWaitEvent(ctx->s_ls, ctx->ev_ls_fork, 0);
+        launch_ls_update(ctx, m, ctx->s_ls);
+        if (m->reinit_every > 0 && m->reinit_iters > 0) {
+          if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
+            launch_reinit(ctx, m, m->reinit_every, ctx->s_ls);
+          else if ((ctx->steps_done_host + 1) % m->reinit_every == 0)
+            launch_reinit(ctx, m, 0, ctx->s_ls);
+        }
+        cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
+      };
       if (overlapped) {
         // ghost fill and flux update interleaved across SM partitions; the
         // flux phase here is the update of the tiles near the interface
         launch_ghost_fill_overlapped(ctx, m);
+        fork_level_set();
+        launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->stream);
         mark(3);
       } else {
         launch_ghost_fill(ctx, m);
         mark(2);
+        fork_level_set();
         launch_fs_update(ctx, m->fs, 3);
         mark(3);
       }
-      launch_ls_update(ctx, m);
-      if (m->reinit_every > 0 && m->reinit_iters > 0) {
-        if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
-          launch_reinit(ctx, m, m->reinit_every);
-        else if ((ctx->steps_done_host + 1) % m->reinit_every == 0)
-          launch_reinit(ctx, m, 0);
-      }
+      cudaStreamWaitEvent(ctx->stream, ctx->ev_ls_done, 0);
       mark(4);
       launch_commit(ctx, 3, true);   // U := new values + apply_BCs_euler
     } else {

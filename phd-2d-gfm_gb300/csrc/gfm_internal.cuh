@@ -89,6 +89,8 @@ struct gfm_ctx {
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist
   int overlap;            // GFM_OVERLAP_* mode (gfm_set_overlap)
+  cudaStream_t s_ls;      // level-set update beside the flux update
+  cudaEvent_t ev_ls_fork, ev_ls_done;
   struct gfm_mlp* mlp;    // learned proposal for the interface solves (gfm_set_mlp), or null
   float* cap_X;           // capture of gated interface problems (gfm_capture_interface_problems), or null
   float* cap_Y;
@@ -155,7 +157,7 @@ void launch_bcs(gfm_ctx* ctx, int fluid_mask);
 void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
-void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
+void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
 void launch_end_step(gfm_ctx* ctx);
 void prepare_kernels();
 const float* mlp_params(const struct gfm_mlp* m);   // the network's FP32 parameters (device)

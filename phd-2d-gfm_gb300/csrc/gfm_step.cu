@@ -1582,12 +1582,11 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (ctx->timing) cudaEventRecord(ctx->tev[3], s);
   cudaStreamWaitEvent(s, ctx->ev_far, 0);
   if (ctx->timing) cudaEventRecord(ctx->tev[4], s);
-  launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, s);
+  // the caller launches the flux update of the near tiles
 }
 
-void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
+void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
   const GridP& P = ctx->P;
-  cudaStream_t s = ctx->stream;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
   if (m->ls_order == 1) {
     k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
@@ -1601,9 +1600,8 @@ void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
 
 // reinitialisation: iterations alternate phi -> phi_a -> phi ...; an odd
 // count ends with a copy back, so phi stays the one buffer holding the level set
-void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every) {
+void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream_t s) {
   const GridP& P = ctx->P;
-  cudaStream_t s = ctx->stream;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
   k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime, every); counted();
   for (int it = 0; it < m->reinit_iters; it++) {
