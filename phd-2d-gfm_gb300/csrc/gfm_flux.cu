@@ -93,8 +93,9 @@ __device__ __forceinline__ void cell_face_states(const V4& W, const V4& Ww, cons
   V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
   if (!is_physical_primitives_fast(gam, pinf, L) || !is_physical_primitives_fast(gam, pinf, R)) { L = W; R = W; }
   if (!is_physical_primitives_fast(gam, pinf, B) || !is_physical_primitives_fast(gam, pinf, T)) { B = W; T = W; }
-  double cs = eos_soundspeed(gam, pinf, W.d, W.a);
-  double irho = 1.0 / W.a, rcc = W.a * cs * cs;
+  const Recip Rr = recip(W.a);
+  double cs = eos_soundspeed_r(gam, pinf, W.d, Rr);
+  double irho = Rr.y, rcc = W.a * cs * cs;   // irho = 1.0 / W.a
   V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
   V4 Y = B_times(sy, W, irho, rcc, v4sub(B, T));
   out[0] = V4{(L.a + X.a) + Y.a, (L.b + X.b) + Y.b, (L.c + X.c) + Y.c, (L.d + X.d) + Y.d};

@@ -191,6 +191,44 @@ GFM_HD bool c_ge(double a, double b) { return c_le(b, a); }
 
 
 // ---------------------------------------------------------------------------
+// Several quotients with one divisor b: a / b correctly rounded from one
+// reciprocal (Markstein, IBM J. Res. Dev. 34(1), 1990): with y = RN(1/b),
+// q = RN(a y) lies within an ulp of a/b, the remainder r = a - b q is exact
+// (one fma), and RN(q + r y) = RN(a/b) while every value stays in the normal
+// range -- here |a| and |b| within 2^-500 .. 2^500 (a = +-0 gives q);
+// outside it the division itself is used.  Three multiply-adds per quotient
+// instead of a division; the same bits as the division
+// (tests/compare_bits_check.cpp).
+// ---------------------------------------------------------------------------
+struct Recip { double b, y; bool fast; };
+
+GFM_HD bool mid_range(double x) {   // 2^-500 <= |x| < 2^500 (exponent field 523 .. 1522)
+  const int e = (int)((as_bits(x) >> 52) & 0x7ff);
+  return e >= 523 && e < 1523;
+}
+GFM_HD Recip recip(double b) {
+  Recip r;
+  r.b = b;
+  r.y = 1.0 / b;
+  r.fast = mid_range(b);
+  return r;
+}
+GFM_HD double i_rdiv(double a, const Recip& R) {
+  if (R.fast && mid_range(a)) {
+    const double q = a * R.y;
+    const double rem = fma(-R.b, q, a);
+    return fma(rem, R.y, q);
+  }
+  if (R.fast && (as_bits(a) & GFM_MAG_BITS) == 0) return a * R.y;   // signed zero
+  return a / R.b;
+}
+#if defined(__CUDA_ARCH__)
+GFM_HD double rdiv(double a, const Recip& R) { return i_rdiv(a, R); }
+#else
+GFM_HD double rdiv(double a, const Recip& R) { return a / R.b; }
+#endif
+
+// ---------------------------------------------------------------------------
 // The elementary functions are arranged for GB300's FP64 pipe, which is the
 // bottleneck of every kernel here: explicit fused multiply-adds (fma is
 // correctly rounded on the GPU and in C, so host and device agree), and the
@@ -310,6 +348,10 @@ GFM_HD double eos_specific_ie(double g, double pinf, double p, double rho) {
 GFM_HD double eos_soundspeed(double g, double pinf, double p, double rho) {
   return sqrt(g * (p + pinf) / rho);
 }
+// the same with a reciprocal of rho at hand
+GFM_HD double eos_soundspeed_r(double g, double pinf, double p, const Recip& R) {
+  return sqrt(rdiv(g * (p + pinf), R));
+}
 GFM_HD double eos_isentropic_extrapolation(double g, double pinf, double rho1, double p1, double p2) {
   return rho1 * gfm_pow((p2 + pinf) / (p1 + pinf), 1.0 / g);
 }
@@ -323,16 +365,18 @@ struct V4 { double a, b, c, d; };
 // euler_misc.hpp:23-29
 GFM_HD double misc_specific_ie(const V4& U) {
   double rho = U.a;
-  double u = U.b / rho;
-  double v = U.c / rho;
-  return (U.d / rho) - 0.5 * (u * u + v * v);
+  const Recip R = recip(rho);
+  double u = rdiv(U.b, R);
+  double v = rdiv(U.c, R);
+  return rdiv(U.d, R) - 0.5 * (u * u + v * v);
 }
 // euler_misc.hpp:32-41
 GFM_HD bool is_physical_state(const V4& U) {
   double rho = U.a;
-  double u = U.b / rho;
-  double v = U.c / rho;
-  double e = (U.d / rho) - 0.5 * (u * u + v * v);
+  const Recip R = recip(rho);
+  double u = rdiv(U.b, R);
+  double v = rdiv(U.c, R);
+  double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
   return c_ge0(rho) && c_ge0(e);
 }
 // is_physical_state without its three divisions when the state is plainly
@@ -360,9 +404,10 @@ GFM_HD bool is_physical_primitives_fast(double g, double pinf, const V4& W) {
 // euler_misc.hpp:52-67
 GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
   double rho = U.a;
-  double u = U.b / rho;
-  double v = U.c / rho;
-  double e = (U.d / rho) - 0.5 * (u * u + v * v);
+  const Recip R = recip(rho);
+  double u = rdiv(U.b, R);
+  double v = rdiv(U.c, R);
+  double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
   double p = eos_pressure(g, pinf, e, rho);
   return V4{rho, u, v, p};
 }
@@ -370,9 +415,10 @@ GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
 // both compute u, v and e with the same operations, done here once.
 GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys) {
   double rho = U.a;
-  double u = U.b / rho;
-  double v = U.c / rho;
-  double e = (U.d / rho) - 0.5 * (u * u + v * v);
+  const Recip R = recip(rho);
+  double u = rdiv(U.b, R);
+  double v = rdiv(U.c, R);
+  double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
   *phys = c_ge0(rho) && c_ge0(e);
   double p = eos_pressure(g, pinf, e, rho);
   return V4{rho, u, v, p};

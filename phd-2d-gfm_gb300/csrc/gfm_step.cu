@@ -74,11 +74,12 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs a) {
     double gm = f1 ? P.g1 : P.g2, pinf = f1 ? P.p1 : P.p2;
     V4 u = load4(U, P, c);
     double rho = u.a;
-    double e = misc_specific_ie(u);
+    const Recip R = recip(rho);   // the seven divisions by rho share one reciprocal
+    double e = rdiv(u.d, R) - 0.5 * (rdiv(u.b, R) * rdiv(u.b, R) + rdiv(u.c, R) * rdiv(u.c, R));
     double p = eos_pressure(gm, pinf, e, rho);
-    double cs = eos_soundspeed(gm, pinf, p, rho);
-    double xu = fabs(u.b) / rho + cs;
-    double xv = fabs(u.c) / rho + cs;
+    double cs = eos_soundspeed_r(gm, pinf, p, R);
+    double xu = rdiv(fabs(u.b), R) + cs;
+    double xv = rdiv(fabs(u.c), R) + cs;
     mu = dmax_std(mu, xu);   // NaN never replaces the running max (std::max semantics)
     mv = dmax_std(mv, xv);
   }

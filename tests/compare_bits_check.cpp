@@ -72,6 +72,40 @@ int main() {
     if (i_quotient_ge0(num, den) != quotient_ge0(num, den)) { std::printf("mismatch iq %a %a\n", num, den); return 1; }
     n += 3;
   }
-  std::printf("ok %ld\n", n);
+  // shared-reciprocal quotients against the division: random operands over
+  // the whole exponent range and mantissas with long runs of ones or zeros
+  auto mant = [&](int kind) -> uint64_t {
+    s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+    switch (kind) {
+      case 0: return s & 0xfffffffffffffULL;
+      case 1: return 0xfffffffffffffULL ^ (s & 0xffULL);            // near all ones
+      case 2: return s & 0xffULL;                                    // near a power of two
+      default: return (s & 1) ? 0xfffffffffffffULL : (1ULL << (s % 52));
+    }
+  };
+  long nd = 0;
+  for (int k = 0; k < 20000000; k++) {
+    s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+    const uint64_t ea = 1 + (s % 2046), eb = 1 + ((s >> 12) % 2046);
+    const uint64_t sa = (s >> 30) & 1, sb = (s >> 31) & 1;
+    const double a = dbl((sa << 63) | (ea << 52) | mant(k & 3));
+    const double b = dbl((sb << 63) | (eb << 52) | mant((k >> 2) & 3));
+    const Recip R = recip(b);
+    const double q = i_rdiv(a, R), ref = a / b;
+    uint64_t qb, rb; std::memcpy(&qb, &q, 8); std::memcpy(&rb, &ref, 8);
+    if (qb != rb && !(std::isnan(q) && std::isnan(ref))) {
+      std::printf("mismatch rdiv %a / %a: %a vs %a\n", a, b, q, ref); return 1;
+    }
+    nd++;
+  }
+  for (double a : v)
+    for (size_t q = 0; q < v.size(); q += 13) {
+      const Recip R = recip(v[q]);
+      const double x = i_rdiv(a, R), ref = a / v[q];
+      uint64_t xb, rb; std::memcpy(&xb, &x, 8); std::memcpy(&rb, &ref, 8);
+      if (xb != rb && !(std::isnan(x) && std::isnan(ref))) { std::printf("mismatch rdiv %a / %a\n", a, v[q]); return 1; }
+      nd++;
+    }
+  std::printf("ok %ld rdiv %ld\n", n, nd);
   return 0;
 }
