@@ -82,6 +82,7 @@ struct gfm_ctx {
   // the rest (see launch_ghost_fill_overlapped)
   double* S[2][2];        // speculative extrapolation ping-pong [buffer][fluid]
   uint8_t* near_cell;     // real cells within 6 (Chebyshev) of an interfacial cell
+  uint8_t* band_cell;     // real cells within 12: those the exact extrapolation writes
   int* tile_near;         // per flux tile: its region holds a near cell
   cudaStream_t s_chain, s_far;
   cudaEvent_t ev_fork, ev_chain, ev_far;

@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
   __syncthreads();
   const int64_t n = (int64_t)P.nr * P.nc;
   const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  const Recip r2dx = recip(2.0 * P.dx), r2dy = recip(2.0 * P.dy);   // central-difference divisors
   uint32_t st = 0;
   int cnt = 0;
   for (int q = threadIdx.x; q < CHUNK; q += CHUNK_T) {
@@ -250,26 +251,32 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
     int64_t c = cidx(P, i, j);
     V4 u1 = load4(a.U1, P, c), u2 = load4(a.U2, P, c);
     double ph = a.phi[c];
+    // conversion and is_physical_state of the same state share their operations
+    bool ok1, ok2;
+    V4 w1 = cons_to_prims_phys(P.g1, P.p1, u1, &ok1);
+    V4 w2 = cons_to_prims_phys(P.g2, P.p2, u2, &ok2);
     if (a.check_both) {
-      if (!is_physical_state(u1) || !is_physical_state(u2)) st |= ST_UNPHYSICAL;
+      if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
     } else {
-      if (!is_physical_state(ph <= 0.0 ? u1 : u2)) st |= ST_UNPHYSICAL;
+      if (!(ph <= 0.0 ? ok1 : ok2)) st |= ST_UNPHYSICAL;
     }
-    V4 w1 = cons_to_prims(P.g1, P.p1, u1);
-    V4 w2 = cons_to_prims(P.g2, P.p2, u2);
     store4(a.W1, P, c, w1);
     store4(a.W2, P, c, w2);
     if (a.Wc1) { store4(a.Wc1, P, c, w1); store4(a.Wc2, P, c, w2); }
     double gx = 0.0, gy = 0.0;
     if (i >= 1 && i < P.nr - 1 && j >= 1 && j < P.nc - 1) {
-      gx = (a.phi[c + 1] - a.phi[c - 1]) / (2.0 * P.dx);
-      gy = (a.phi[c + P.pitch] - a.phi[c - P.pitch]) / (2.0 * P.dy);
+      gx = rdiv(a.phi[c + 1] - a.phi[c - 1], r2dx);
+      gy = rdiv(a.phi[c + P.pitch] - a.phi[c - P.pitch], r2dy);
     }
     // raw gradient, its norm, and the unit normal with the reference's
     // fallback (sourcecode/GFM_riemann.cpp:58-68), once per step
     double nn = sqrt(gx * gx + gy * gy);
     double ux = 1.0, uy = 0.0;
-    if (!(nn < 1e-12)) { ux = gx / nn; uy = gy / nn; }
+    if (!(nn < 1e-12)) {
+      const Recip rn = recip(nn);
+      ux = rdiv(gx, rn);
+      uy = rdiv(gy, rn);
+    }
     a.nrm[c] = gx;
     a.nrm[c + P.plane] = gy;
     a.nrm[c + 2 * P.plane] = ux;
@@ -356,6 +363,9 @@ struct ExtrapArgs {
   const double* ov_out;
   const int* ov_map;
   int overlay;
+  // band: only cells whose boundary-condition source is marked are written
+  // (the others keep the buffer's earlier values), or null for every cell
+  const uint8_t* band;
 };
 
 __device__ __forceinline__ V4 ex_rd(const ExtrapArgs& a, int f, int64_t c) {
@@ -375,6 +385,7 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
     int i = (int)(k / P.nc), j = (int)(k % P.nc);
     BCSrc s = bc_source(P, i, j);
     int64_t c = cidx(P, s.i, s.j);
+    if (a.band && !a.band[c]) continue;
     V4 v1 = ex_rd(a, 0, c), v2 = ex_rd(a, 1, c);
     bool skip = a.mgfm && a.mask[c];
     if (!skip) {
@@ -1286,6 +1297,7 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.phi = ctx->phi; e.nrm = ctx->nrm; e.mask = ctx->mask; e.D = ctx->dtime;
     e.mgfm = mgfm ? 1 : 0;
     e.ov_out = nullptr; e.ov_map = nullptr; e.overlay = 0;
+    e.band = nullptr;
     k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
   }
@@ -1417,18 +1429,24 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
 // same kernels.
 // ---------------------------------------------------------------------------
 constexpr int NEAR_RADIUS = 6;
+// The exact extrapolation after the loop writes only cells within BAND_RADIUS
+// of an interfacial cell.  Cells outside read stale values at the band's
+// edge, and a sweep carries a value one cell, so after the six sweeps the
+// values within 12 - 5 = 7 cells are exact, which covers the near cells.
+constexpr int BAND_RADIUS = 12;
 
-__global__ void k_near_mark(GridP P, const int* list, const DevTime* D, uint8_t* near_cell) {
+// marks the real cells within `radius` (Chebyshev) of an interfacial cell
+__global__ void k_near_mark(GridP P, const int* list, const DevTime* D, uint8_t* near_cell, int radius) {
   if (!D->active) return;
   const int n = D->n_ifc;
-  const int side = 2 * NEAR_RADIUS + 1;
+  const int side = 2 * radius + 1;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)n * side * side;
        q += (int64_t)gridDim.x * blockDim.x) {
     int k = (int)(q / (side * side));
     int r = (int)(q % (side * side));
     int64_t lin = list[k];
-    int i = (int)(lin / P.nc) + r / side - NEAR_RADIUS;
-    int j = (int)(lin % P.nc) + r % side - NEAR_RADIUS;
+    int i = (int)(lin / P.nc) + r / side - radius;
+    int j = (int)(lin % P.nc) + r % side - radius;
     if (P.periodic) {
       i = ((i - P.g) % P.Ny + P.Ny) % P.Ny + P.g;
       j = ((j - P.g) % P.Nx + P.Nx) % P.Nx + P.g;
@@ -1460,7 +1478,7 @@ __global__ void k_tile_flags(GridP P, const uint8_t* near_cell, int* tile_near, 
 }
 
 static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, double* D1, double* D2, bool overlay,
-                         cudaStream_t s) {
+                         cudaStream_t s, const uint8_t* band) {
   const GridP& P = ctx->P;
   ExtrapArgs e;
   e.P = P;
@@ -1470,6 +1488,7 @@ static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, doubl
   e.ov_out = overlay ? ctx->ifc_out : nullptr;
   e.ov_map = overlay ? ctx->ifc_map : nullptr;
   e.overlay = overlay ? 1 : 0;
+  e.band = band;
   k_extrap<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(e);
   counted();
 }
@@ -1512,9 +1531,13 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   counted();
   // near field: cells within NEAR_RADIUS of an interfacial cell, and tiles reading them
   cudaMemsetAsync(ctx->near_cell, 0, (size_t)P.plane, s);
+  cudaMemsetAsync(ctx->band_cell, 0, (size_t)P.plane, s);
   const int cap = P.Nx * P.Ny;
-  k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->near_cell);
-  counted();
+  k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->near_cell,
+                                                              NEAR_RADIUS);
+  k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->band_cell,
+                                                              BAND_RADIUS);
+  counted(2);
   const int ntx = flux_tiles_x(P), nty = flux_tiles_y(P);
   k_tile_flags<<<(ntx * nty + 7) / 8, 256, 0, s>>>(P, ctx->near_cell, ctx->tile_near, ntx, nty, ctx->dtime);
   counted();
@@ -1553,7 +1576,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = ctx->S[it & 1];
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far);
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
@@ -1574,7 +1597,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = (it & 1) ? bufB : bufA;
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, s);
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, s, ctx->band_cell);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
