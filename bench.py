@@ -73,6 +73,21 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, device):
+    """The largest of the ranks' values (the slowest replica sets the job's time)."""
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells, steps, world, step_ms_max):
+    """Whole-job cell-updates/s of `world` independent replicas of the same
+    workload, timed by the slowest one (weak scaling)."""
+    return cells * steps * world / (step_ms_max * 1e-3)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -214,14 +229,12 @@ def run_gfm(args):
     step_ms = float(phases[:5].sum())   # phases 5-8 are sub-intervals of 1-2
     if world > 1:
         import torch.distributed as tdist
-        tt = torch.tensor([step_ms], device="cuda", dtype=torch.float64)
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        step_ms = float(tt.item())
+        step_ms = max_over_ranks(step_ms, "cuda")
         tdist.barrier()
     status = ctx.status()
     stats = ctx.stats()
     t_sim, nsteps_done, _ = ctx.time()
-    value = cells * args.steps * world / (step_ms * 1e-3)
+    value = replica_throughput(cells, args.steps, world, step_ms)
 
     # roofline of the dominant kernel, the flux update (both fluids per
     # launch; with the overlapped schedule two launches per step, far tiles
