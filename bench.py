@@ -96,10 +96,11 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_summary():
-    """Figures of the committed ncu summary of the flux update (key=value lines):
-    DRAM bytes per full-grid launch, FP64 flops per cell, FP64 pipe activity."""
-    p = os.path.join(ROOT, "profiles", "flux_update_shock_bubble.txt")
+def ncu_summary(workload):
+    """Figures of the committed ncu summary of the flux update on `workload`
+    (key=value lines): DRAM bytes per full-grid launch, FP64 flops per cell,
+    FP64 pipe activity, the step the captured launch belongs to."""
+    p = os.path.join(ROOT, "profiles", "flux_update_%s.txt" % workload)
     out = {}
     if not os.path.exists(p):
         return out
@@ -209,6 +210,9 @@ def run_gfm(args):
     phases = np.zeros(NPHASES)
     ph = np.zeros(NPHASES)
     L = g.lib()
+    prof = ncu_summary(args.workload)
+    prof_step = int(prof.get("profiled_step", -1))
+    flux_ms_prof = None
     launches0 = L.gfm_launch_count()
     if world > 1:
         import torch.distributed as tdist
@@ -223,6 +227,8 @@ def run_gfm(args):
             if rc != 0:
                 raise RuntimeError("gfm_step_timed failed: %d" % rc)
             phases += ph
+            if args.warmup + s == prof_step:   # the step of the profiled launch
+                flux_ms_prof = ph[2] + ph[8]
         torch.cuda.synchronize()
     wall = time.time() - t_wall
     launches = L.gfm_launch_count() - launches0
@@ -242,16 +248,18 @@ def run_gfm(args):
     flux_ms = (phases[2] + phases[8]) / args.steps
     achieved = FLUX_BYTES_PER_CELL * cells / (flux_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    prof = ncu_summary()
     fp64_peak = ctypes.c_double(0.0)
     L.gfm_fp64_peak(ctypes.byref(fp64_peak), ctypes.c_void_p(stream.cuda_stream))
     fp64 = {"kernel": "k_flux_update<MUSCL>", "peak_gflops": round(fp64_peak.value, 1),
             "peak_source": "measured now (gfm_fp64_peak: FMA loop on every SM)"}
-    if "fp64_flops_per_cell" in prof:
+    if "fp64_flops_per_cell" in prof and flux_ms_prof:
+        # the flop count of the profiled launch over that same step's flux
+        # time, measured here with CUDA events (the count varies along the run)
         fl = prof["fp64_flops_per_cell"] * cells
-        fp64.update({"flops_per_cell": prof["fp64_flops_per_cell"],
-                     "achieved_gflops": round(fl / (flux_ms * 1e-3) / 1e9, 1),
-                     "frac": round(fl / (flux_ms * 1e-3) / 1e9 / fp64_peak.value, 4),
+        fp64.update({"flops_per_cell": prof["fp64_flops_per_cell"], "step": prof_step,
+                     "kernel_ms_at_step": round(flux_ms_prof, 5),
+                     "achieved_gflops": round(fl / (flux_ms_prof * 1e-3) / 1e9, 1),
+                     "frac": round(fl / (flux_ms_prof * 1e-3) / 1e9 / fp64_peak.value, 4),
                      "pipe_active_frac_ncu": prof.get("fp64_pipe_active_frac")})
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 5), "traffic": prof.get("traffic_bytes_per_launch_full_size"),

@@ -217,6 +217,9 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
       for (int f = 0; f < 2; f++) alloc((void**)&ctx->S[b][f], 4 * plane_b);
     alloc((void**)&ctx->near_cell, (size_t)P.plane);
     alloc((void**)&ctx->band_cell, (size_t)P.plane);
+    alloc((void**)&ctx->band_list, (size_t)P.nr * P.nc * sizeof(int));
+    alloc((void**)&ctx->near_list, (size_t)P.nr * P.nc * sizeof(int));
+    alloc((void**)&ctx->list_n, 2 * sizeof(int));
     alloc((void**)&ctx->tile_near, sizeof(int) * (size_t)flux_tiles_x(P) * flux_tiles_y(P));
     int dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
@@ -256,6 +259,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   for (int b = 0; b < 2; b++)
     for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cell); cudaFree(ctx->tile_near);
+  cudaFree(ctx->band_list); cudaFree(ctx->near_list); cudaFree(ctx->list_n);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_chain) cudaEventDestroy(ctx->ev_chain);
   if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);

@@ -83,6 +83,9 @@ struct gfm_ctx {
   double* S[2][2];        // speculative extrapolation ping-pong [buffer][fluid]
   uint8_t* near_cell;     // real cells within 6 (Chebyshev) of an interfacial cell
   uint8_t* band_cell;     // real cells within 12: those the exact extrapolation writes
+  int* band_list;         // cells (ghost cells included) whose source is a band cell
+  int* near_list;         // cells whose source is a near cell
+  int* list_n;            // 2 counts: band_list, near_list
   int* tile_near;         // per flux tile: its region holds a near cell
   cudaStream_t s_chain, s_far;
   cudaEvent_t ev_fork, ev_chain, ev_far;

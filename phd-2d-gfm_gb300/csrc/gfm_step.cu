@@ -366,6 +366,12 @@ struct ExtrapArgs {
   // band: only cells whose boundary-condition source is marked are written
   // (the others keep the buffer's earlier values), or null for every cell
   const uint8_t* band;
+  // list: the cells to write (linear indices over the padded rows, count in
+  // *list_n), or null for every cell; a list replaces the band test
+  const int* list;
+  const int* list_n;
+  // (0.5 min(dx, dy)) / dx and / dy, formed once on the host
+  double cdx, cdy;
 };
 
 __device__ __forceinline__ V4 ex_rd(const ExtrapArgs& a, int f, int64_t c) {
@@ -376,40 +382,82 @@ __device__ __forceinline__ V4 ex_rd(const ExtrapArgs& a, int f, int64_t c) {
   return load4(f == 0 ? a.S1 : a.S2, a.P, c);
 }
 
+__device__ __forceinline__ void extrap_cell(const ExtrapArgs& a, int64_t k) {
+  const GridP& P = a.P;
+  int i = (int)(k / P.nc), j = (int)(k % P.nc);
+  BCSrc s = bc_source(P, i, j);
+  int64_t c = cidx(P, s.i, s.j);
+  if (a.band && !a.band[c]) return;
+  V4 v1 = ex_rd(a, 0, c), v2 = ex_rd(a, 1, c);
+  bool skip = a.mgfm && a.mask[c];
+  if (!skip) {
+    double nx, ny;
+    unit_normal(a.nrm, P, c, nx, ny);
+    double cx = a.cdx * nx, cy = a.cdy * ny;
+    if (c_le0(a.phi[c])) {
+      // fluid 2 is ghost: information flows along -normal
+      V4 dxv = c_gt0(nx) ? v4d(ex_rd(a, 1, c + 1), v2) : v4d(v2, ex_rd(a, 1, c - 1));
+      V4 dyv = c_gt0(ny) ? v4d(ex_rd(a, 1, c + P.pitch), v2) : v4d(v2, ex_rd(a, 1, c - P.pitch));
+      v2 = V4{(v2.a + cx * dxv.a) + cy * dyv.a, (v2.b + cx * dxv.b) + cy * dyv.b,
+              (v2.c + cx * dxv.c) + cy * dyv.c, (v2.d + cx * dxv.d) + cy * dyv.d};
+    } else {
+      V4 dxv = c_gt0(nx) ? v4d(v1, ex_rd(a, 0, c - 1)) : v4d(ex_rd(a, 0, c + 1), v1);
+      V4 dyv = c_gt0(ny) ? v4d(v1, ex_rd(a, 0, c - P.pitch)) : v4d(ex_rd(a, 0, c + P.pitch), v1);
+      v1 = V4{(v1.a - cx * dxv.a) - cy * dyv.a, (v1.b - cx * dxv.b) - cy * dyv.b,
+              (v1.c - cx * dxv.c) - cy * dyv.c, (v1.d - cx * dxv.d) - cy * dyv.d};
+    }
+  }
+  if (s.flipu) { v1.b = -v1.b; v2.b = -v2.b; }
+  if (s.flipv) { v1.c = -v1.c; v2.c = -v2.c; }
+  int64_t o = cidx(P, i, j);
+  store4(a.D1, P, o, v1);
+  store4(a.D2, P, o, v2);
+}
+
 __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
+  if (a.list) {
+    const int n = *a.list_n;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) extrap_cell(a, a.list[q]);
+    return;
+  }
   const int64_t n = (int64_t)P.nr * P.nc;
-  const double dt = 0.5 * dmin_std(P.dx, P.dy);
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    int i = (int)(k / P.nc), j = (int)(k % P.nc);
-    BCSrc s = bc_source(P, i, j);
-    int64_t c = cidx(P, s.i, s.j);
-    if (a.band && !a.band[c]) continue;
-    V4 v1 = ex_rd(a, 0, c), v2 = ex_rd(a, 1, c);
-    bool skip = a.mgfm && a.mask[c];
-    if (!skip) {
-      double nx, ny;
-      unit_normal(a.nrm, P, c, nx, ny);
-      double cx = (dt / P.dx) * nx, cy = (dt / P.dy) * ny;
-      if (a.phi[c] <= 0.0) {
-        // fluid 2 is ghost: information flows along -normal
-        V4 dxv = (nx > 0.0) ? v4d(ex_rd(a, 1, c + 1), v2) : v4d(v2, ex_rd(a, 1, c - 1));
-        V4 dyv = (ny > 0.0) ? v4d(ex_rd(a, 1, c + P.pitch), v2) : v4d(v2, ex_rd(a, 1, c - P.pitch));
-        v2 = V4{(v2.a + cx * dxv.a) + cy * dyv.a, (v2.b + cx * dxv.b) + cy * dyv.b,
-                (v2.c + cx * dxv.c) + cy * dyv.c, (v2.d + cx * dxv.d) + cy * dyv.d};
-      } else {
-        V4 dxv = (nx > 0.0) ? v4d(v1, ex_rd(a, 0, c - 1)) : v4d(ex_rd(a, 0, c + 1), v1);
-        V4 dyv = (ny > 0.0) ? v4d(v1, ex_rd(a, 0, c - P.pitch)) : v4d(ex_rd(a, 0, c + P.pitch), v1);
-        v1 = V4{(v1.a - cx * dxv.a) - cy * dyv.a, (v1.b - cx * dxv.b) - cy * dyv.b,
-                (v1.c - cx * dxv.c) - cy * dyv.c, (v1.d - cx * dxv.d) - cy * dyv.d};
-      }
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    extrap_cell(a, k);
+}
+
+// The cells (over the padded rows, ghost cells included) whose
+// boundary-condition source is marked in `band`, and in `near`, appended to
+// band_list and near_list; counts in n2[0] and n2[1] (zeroed by the caller).
+// Order within a list is free: a sweep writes each listed cell from reads of
+// the previous buffer only.
+__global__ void k_band_lists(GridP P, const uint8_t* band, const uint8_t* near_cell, int* band_list, int* near_list,
+                             int* n2, const DevTime* D) {
+  if (!D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = base + lane;
+    bool inb = false, inn = false;
+    if (k < n) {
+      BCSrc s = bc_source(P, (int)(k / P.nc), (int)(k % P.nc));
+      const int64_t c = cidx(P, s.i, s.j);
+      inb = band[c] != 0;
+      inn = near_cell[c] != 0;
     }
-    if (s.flipu) { v1.b = -v1.b; v2.b = -v2.b; }
-    if (s.flipv) { v1.c = -v1.c; v2.c = -v2.c; }
-    int64_t o = cidx(P, i, j);
-    store4(a.D1, P, o, v1);
-    store4(a.D2, P, o, v2);
+    const unsigned mb = __ballot_sync(0xffffffffu, inb), mn = __ballot_sync(0xffffffffu, inn);
+    int ob = 0, on = 0;
+    if (lane == 0) {
+      if (mb) ob = atomicAdd(&n2[0], __popc(mb));
+      if (mn) on = atomicAdd(&n2[1], __popc(mn));
+    }
+    ob = __shfl_sync(0xffffffffu, ob, 0);
+    on = __shfl_sync(0xffffffffu, on, 0);
+    const unsigned below = (1u << lane) - 1u;
+    if (inb) band_list[ob + __popc(mb & below)] = (int)k;
+    if (inn) near_list[on + __popc(mn & below)] = (int)k;
   }
 }
 
@@ -1014,18 +1062,22 @@ struct FinalArgs {
   int vel_mode;   // 0: real-fluid velocity, 1: extension seeds (OGFM interfacial), 2: leave vel alone
   const uint8_t* near_cell;
   int sel;        // 0: every cell, 1: cells far from the interface, 2: near cells
+  // the near cells as a list (count in *list_n) for sel 2, or null
+  const int* list;
+  const int* list_n;
 };
 
 __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
-  const int64_t n = (int64_t)P.nr * P.nc;
+  const int64_t n = a.list ? (int64_t)*a.list_n : (int64_t)P.nr * P.nc;
   uint32_t st = 0;
   int bb[8] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = a.list ? (int64_t)a.list[q] : q;
     int i = (int)(k / P.nc), j = (int)(k % P.nc);
     int64_t c = cidx(P, i, j);
-    if (a.sel) {   // a ghost cell is near when its boundary-condition source is
+    if (a.sel && !a.list) {   // a ghost cell is near when its boundary-condition source is
       BCSrc s = bc_source(P, i, j);
       const bool nr = a.near_cell[cidx(P, s.i, s.j)] != 0;
       if ((a.sel == 2) != nr) continue;
@@ -1286,6 +1338,14 @@ static int grid_blocks(int64_t n, int per) {
   return (int)b;
 }
 
+// the sweep's coefficients dt/dx, dt/dy with dt = 0.5 min(dx, dy), correctly
+// rounded here exactly as a device division would round them
+static void extrap_coeffs(const GridP& P, ExtrapArgs& e) {
+  const double dt = 0.5 * ((P.dy < P.dx) ? P.dy : P.dx);
+  e.cdx = dt / P.dx;
+  e.cdy = dt / P.dy;
+}
+
 static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
   const GridP& P = ctx->P;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
@@ -1298,6 +1358,8 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.mgfm = mgfm ? 1 : 0;
     e.ov_out = nullptr; e.ov_map = nullptr; e.overlay = 0;
     e.band = nullptr;
+    e.list = nullptr; e.list_n = nullptr;
+    extrap_coeffs(P, e);
     k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
   }
@@ -1357,6 +1419,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
     f.ogfm = 1;
     f.vel_mode = ext ? 1 : 0;
     f.near_cell = nullptr;
+    f.list = nullptr; f.list_n = nullptr;
     f.sel = 0;
     k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
     k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted();
@@ -1408,6 +1471,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   f.ogfm = 0;
   f.vel_mode = ext ? 2 : 0;
   f.near_cell = nullptr;
+  f.list = nullptr; f.list_n = nullptr;
   f.sel = 0;
   k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
   if (ext) run_ext_vfield(ctx, 20);
@@ -1478,7 +1542,7 @@ __global__ void k_tile_flags(GridP P, const uint8_t* near_cell, int* tile_near, 
 }
 
 static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, double* D1, double* D2, bool overlay,
-                         cudaStream_t s, const uint8_t* band) {
+                         cudaStream_t s, const int* list, const int* list_n) {
   const GridP& P = ctx->P;
   ExtrapArgs e;
   e.P = P;
@@ -1488,8 +1552,12 @@ static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, doubl
   e.ov_out = overlay ? ctx->ifc_out : nullptr;
   e.ov_map = overlay ? ctx->ifc_map : nullptr;
   e.overlay = overlay ? 1 : 0;
-  e.band = band;
-  k_extrap<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(e);
+  e.band = nullptr;
+  e.list = list; e.list_n = list_n;
+  extrap_coeffs(P, e);
+  // a listed sweep covers the band around the interface: a few percent of the grid
+  const int blocks = list ? 2 * 152 : grid_blocks((int64_t)P.nr * P.nc, 256);
+  k_extrap<<<blocks, 256, 0, s>>>(e);
   counted();
 }
 
@@ -1507,7 +1575,9 @@ static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStr
   f.vel_mode = 0;
   f.near_cell = ctx->near_cell;
   f.sel = sel;
-  k_finalize<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(f);
+  f.list = (sel == 2) ? ctx->near_list : nullptr;
+  f.list_n = (sel == 2) ? ctx->list_n + 1 : nullptr;
+  k_finalize<<<(sel == 2) ? 2 * 152 : grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(f);
   counted();
 }
 
@@ -1538,6 +1608,11 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->band_cell,
                                                               BAND_RADIUS);
   counted(2);
+  cudaMemsetAsync(ctx->list_n, 0, 2 * sizeof(int), s);
+  k_band_lists<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(P, ctx->band_cell, ctx->near_cell,
+                                                                      ctx->band_list, ctx->near_list, ctx->list_n,
+                                                                      ctx->dtime);
+  counted();
   const int ntx = flux_tiles_x(P), nty = flux_tiles_y(P);
   k_tile_flags<<<(ntx * nty + 7) / 8, 256, 0, s>>>(P, ctx->near_cell, ctx->tile_near, ntx, nty, ctx->dtime);
   counted();
@@ -1576,7 +1651,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = ctx->S[it & 1];
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr);
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr, nullptr);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
@@ -1597,7 +1672,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = (it & 1) ? bufB : bufA;
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, s, ctx->band_cell);
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, s, ctx->band_list, ctx->list_n);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
