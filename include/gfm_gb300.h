@@ -56,6 +56,12 @@ typedef int gfm_status_t;
 #define GFM_RIEMANN 1
 #define GFM_REAL 2
 #define GFM_MODIFIED 3
+#define GFM_VOF 4          /* GFM_VOF: needs the VOF interface tracker */
+#define GFM_OGFM_VOF 5     /* OGFM_VOF: needs the VOF interface tracker */
+
+/* interface trackers (settings key ITM) */
+#define GFM_ITM_LEVELSET 0 /* LS1 / LS5: phi is a signed distance, negative in fluid 1 */
+#define GFM_ITM_VOF 1      /* PYVOF: phi holds z, the volume fraction of fluid 1 */
 
 /* device status bits (gfm_get_device_status) */
 #define GFM_ST_UNPHYSICAL (1u << 0)
@@ -84,6 +90,7 @@ typedef struct {
   int use_slip_BCs;          /* GFM_base::use_slip_BCs */
   double CFL;                /* settings key CFL */
   double T;                  /* end time */
+  int itm;                   /* GFM_ITM_*: level set (0, the default) or VOF */
 } gfm_method_desc;
 
 typedef struct gfm_ctx gfm_ctx;
@@ -99,6 +106,10 @@ gfm_status_t gfm_download(gfm_ctx* ctx, int fluid, double* U);
 gfm_status_t gfm_upload_phi(gfm_ctx* ctx, const double* phi);
 gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi);
 
+/* the velocity field of the last ghost fill (GFM_base::vfield, handed to the
+ * interface tracker): 2 planes (u, v), layout of phi */
+gfm_status_t gfm_download_velocity(gfm_ctx* ctx, double* vel);
+
 /* interfacial-cell mask of the last ghost fill (Levelset::is_interfacial_cell
  * over real cells; 1 byte per padded cell, same layout as phi) */
 gfm_status_t gfm_download_mask(gfm_ctx* ctx, uint8_t* mask);
@@ -113,6 +124,10 @@ gfm_status_t gfm_set_ghost_states(gfm_ctx* ctx, const gfm_method_desc* m);
 gfm_status_t gfm_fs_update(gfm_ctx* ctx, int fs, int fluid);
 gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
 gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid);
+/* The interface field's kind for gfm_compute_dt before any call that takes a
+ * method (gfm_set_ghost_states, gfm_ls_update and gfm_step record it): with
+ * GFM_ITM_VOF, phi holds z and fluid 1 is where 0.5 - z < 0. */
+gfm_status_t gfm_set_interface_tracker(gfm_ctx* ctx, int itm);
 
 /* nsteps iterations of the reference's time loop body (CFL ramp, dt, ghost
  * fill, two flux updates, level set, BCs, t += dt).  Steps after t reaches
@@ -274,6 +289,10 @@ gfm_status_t gfm_get_interface_stats(gfm_ctx* ctx, int64_t* n_solves, int64_t* n
  * p 1e5) with a left-moving shock of Mach number `mach` at x = 0.9 width, a
  * bubble of fluid 1 (gamma_bubble, rho = rho_ratio, p 1e5) of radius
  * radius_frac x height at (0.7 width, height/2).  T is 1 (run by steps). */
+/* volume fraction z of fluid 1 (one padded plane, layout of phi) of a named
+ * two-fluid case, the initial field of the VOF interface tracker */
+gfm_status_t gfm_case_init_z(const char* test_case, const gfm_grid_desc* grid, double* z);
+
 typedef struct {
   double mach, gamma_bubble, rho_ratio, radius_frac;
 } gfm_bubble_params;

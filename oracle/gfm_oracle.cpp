@@ -534,6 +534,175 @@ struct Levelset {
   }
 };
 
+// ----------------------------------------------------------------------------
+// VOF interface tracker.  The reference's VOF class (settings ITM "PYVOF",
+// sourcecode/sim_twofluid.cpp:575-579) lives in the absent
+// PhD-Interface-tracking-methods library; GFM_VOF and OGFM_VOF use its
+// get_z, get_mixedcell_normal and get_interfacelocation
+// (sourcecode/GFM_VOF.cpp:20,59,80-98; sourcecode/OGFM_VOF.cpp:23,60,118-152)
+// and compute_dt its get_sdf (sourcecode/sim_twofluid.cpp:129).  This is the
+// project's own definition from published methods:
+//   z        volume fraction of fluid 1; a cell is mixed when 0 < z < 1
+//   normal   Youngs (1982) with the Parker & Youngs (1992) 3x3 weights: minus
+//            the weighted central-difference gradient of z, unit length,
+//            pointing from fluid 1 into fluid 2; (1, 0) where it vanishes
+//   PLIC     the line with that normal cutting the cell at area fraction z
+//            (Scardovelli & Zaleski, J. Comput. Phys. 164 (2000), analytic
+//            area / line-constant relations); the interface location is the
+//            midpoint of the line's segment inside the cell
+//   advection  directional splitting (x then y on even steps, y then x on
+//            odd ones), each face's flux the PLIC fluid-1 area of the donor
+//            strip of width |u_f| dt / h, u_f the mean of the two cells'
+//            velocities, with the divergence term of Weymouth & Yue
+//            (J. Comput. Phys. 229 (2010)), c = 1 where z > 0.5 at the start
+//            of the step, else 0; values within 1e-8 of 0 or 1 become 0 or 1,
+//            and the mirror / wrap BCs of phi follow each sweep
+//   get_sdf  0.5 - z (negative in fluid 1, as the level set's phi)
+// ----------------------------------------------------------------------------
+namespace vof {
+constexpr double ZEPS = 1e-8;
+
+inline double lo(double a, double b) { return (b < a) ? b : a; }
+inline double hi(double a, double b) { return (b < a) ? a : b; }
+
+// area fraction of {c1 t + c2 s <= b} in the unit square (c1, c2 >= 0)
+inline double area(double b, double c1, double c2) {
+  const double m1 = lo(c1, c2), m2 = hi(c1, c2);
+  if (b <= 0.0) return 0.0;
+  const double s = m1 + m2;
+  if (b >= s) return 1.0;
+  if (m1 == 0.0) return b / m2;
+  const double d = (2.0 * m1) * m2;
+  if (b < m1) return (b * b) / d;
+  if (b <= m2) return (b - 0.5 * m1) / m2;
+  const double r = s - b;
+  return 1.0 - (r * r) / d;
+}
+
+// the line constant b with area(b, m1, m2) = z, 0 < z < 1, m1 <= m2, m2 > 0
+inline double line_constant(double z, double m1, double m2) {
+  if (m1 == 0.0) return z * m2;
+  const double v1 = m1 / (2.0 * m2);
+  const double d = (2.0 * m1) * m2;
+  if (z < v1) return std::sqrt(d * z);
+  if (z <= 1.0 - v1) return z * m2 + 0.5 * m1;
+  return (m1 + m2) - std::sqrt(d * (1.0 - z));
+}
+
+// PLIC reconstruction of a mixed cell.  In the unit cell with the axes
+// reflected where the normal component is negative, fluid 1 fills
+// {a xi + b eta <= beta}, a = |nx| dx, b = |ny| dy.
+struct Plic {
+  double nx, ny, a, b, beta;
+};
+
+inline Plic reconstruct(const sim_info& p, const griddoubletype& z, int i, int j) {
+  const double gx = ((z[i - 1][j + 1] + 2.0 * z[i][j + 1]) + z[i + 1][j + 1]) -
+                    ((z[i - 1][j - 1] + 2.0 * z[i][j - 1]) + z[i + 1][j - 1]);
+  const double gy = ((z[i + 1][j - 1] + 2.0 * z[i + 1][j]) + z[i + 1][j + 1]) -
+                    ((z[i - 1][j - 1] + 2.0 * z[i - 1][j]) + z[i - 1][j + 1]);
+  const double mx = -gx / p.dx, my = -gy / p.dy;
+  const double nn = std::sqrt(mx * mx + my * my);
+  Plic r;
+  if (nn > 0.0) { r.nx = mx / nn; r.ny = my / nn; }
+  else { r.nx = 1.0; r.ny = 0.0; }
+  r.a = std::fabs(r.nx) * p.dx;
+  r.b = std::fabs(r.ny) * p.dy;
+  r.beta = line_constant(z[i][j], lo(r.a, r.b), hi(r.a, r.b));
+  return r;
+}
+
+// midpoint of the PLIC segment in physical coordinates
+inline vec2 segment_midpoint(const sim_info& p, const Plic& r, int i, int j) {
+  const double m1 = lo(r.a, r.b), m2 = hi(r.a, r.b);
+  const bool swapped = r.b < r.a;   // the m1 axis is eta
+  const double be = r.beta;
+  double u1, w1, u2, w2;
+  if (be < m1) { u1 = be / m1; w1 = 0.0; u2 = 0.0; w2 = be / m2; }
+  else if (be <= m2) { u1 = 0.0; w1 = be / m2; u2 = 1.0; w2 = (be - m1) / m2; }
+  else { u1 = 1.0; w1 = (be - m1) / m2; u2 = (be - m2) / m1; w2 = 1.0; }
+  const double um = 0.5 * (u1 + u2), wm = 0.5 * (w1 + w2);
+  const double xr = swapped ? wm : um, er = swapped ? um : wm;
+  const double xi = (r.nx < 0.0) ? 1.0 - xr : xr;
+  const double eta = (r.ny < 0.0) ? 1.0 - er : er;
+  const vec2 cc = p.cellcentre_coord(i, j);
+  return {cc[0] + (xi - 0.5) * p.dx, cc[1] + (eta - 0.5) * p.dy};
+}
+
+// fluid-1 volume of cell (i,j), as a fraction of the cell, inside the strip of
+// width w (0 < w <= 1) along axis dir (0: x, 1: y) touching the cell's high
+// face (high = true) or its low face
+inline double strip_fraction(const sim_info& p, const griddoubletype& z, int i, int j, int dir, bool high,
+                             double w) {
+  const double zc = z[i][j];
+  if (zc == 1.0) return w;
+  if (zc == 0.0) return 0.0;
+  const Plic r = reconstruct(p, z, i, j);
+  const double n = dir == 0 ? r.nx : r.ny;
+  const double cd = dir == 0 ? r.a : r.b, co = dir == 0 ? r.b : r.a;
+  const bool refl = n < 0.0;
+  const double start = (high != refl) ? 1.0 - w : 0.0;   // strip start in reflected coordinates
+  return w * area(r.beta - cd * start, cd * w, co);
+}
+}  // namespace vof
+
+struct VOFTracker {
+  sim_info params;
+  griddoubletype z;
+  int steps = 0;   // interface updates so far (sets the sweep order)
+
+  double get_z(int i, int j) const { return z[i][j]; }
+  double get_sdf(int i, int j) const { return 0.5 - z[i][j]; }
+  vec2 get_mixedcell_normal(int i, int j) const {
+    vof::Plic r = vof::reconstruct(params, z, i, j);
+    return {r.nx, r.ny};
+  }
+  vec2 get_interfacelocation(int i, int j) const {
+    return vof::segment_midpoint(params, vof::reconstruct(params, z, i, j), i, j);
+  }
+
+  // face flux (signed, + towards the high cell) between cell lo and the next
+  // cell along dir, for Courant number s
+  double face_flux(const griddoubletype& zz, int i, int j, int dir, double s) const {
+    const int i2 = dir == 0 ? i : i + 1, j2 = dir == 0 ? j + 1 : j;
+    if (s > 0.0) return vof::strip_fraction(params, zz, i, j, dir, true, s);
+    if (s < 0.0) return -vof::strip_fraction(params, zz, i2, j2, dir, false, -s);
+    return 0.0;
+  }
+
+  void sweep(int dir, const gridVector2dtype& vel, double dt, const griddoubletype& z0) {
+    const int g = params.numGC;
+    const double dtdh = dt / (dir == 0 ? params.dx : params.dy);
+    griddoubletype out = z;
+    for (int i = g; i < params.Ny + g; i++)
+      for (int j = g; j < params.Nx + g; j++) {
+        const int il = dir == 0 ? i : i - 1, jl = dir == 0 ? j - 1 : j;
+        const int ih = dir == 0 ? i : i + 1, jh = dir == 0 ? j + 1 : j;
+        const double uL = 0.5 * (vel[il][jl][dir] + vel[i][j][dir]);
+        const double uH = 0.5 * (vel[i][j][dir] + vel[ih][jh][dir]);
+        const double sL = uL * dtdh, sH = uH * dtdh;
+        const double FL = face_flux(z, il, jl, dir, sL);
+        const double FH = face_flux(z, i, j, dir, sH);
+        const double c = (z0[i][j] > 0.5) ? 1.0 : 0.0;
+        double zn = z[i][j] - ((FH - c * sH) - (FL - c * sL));
+        if (zn < vof::ZEPS) zn = 0.0;
+        else if (zn > 1.0 - vof::ZEPS) zn = 1.0;
+        out[i][j] = zn;
+      }
+    apply_BCs_scalar(params, out);
+    z = out;
+  }
+
+  // update_interface_coupled(vfield, t, dt)
+  void update_interface_coupled(const gridVector2dtype& vel, double dt) {
+    const griddoubletype z0 = z;
+    const int first = (steps % 2 == 0) ? 0 : 1;
+    sweep(first, vel, dt, z0);
+    sweep(1 - first, vel, dt, z0);
+    steps++;
+  }
+};
+
 // unit normal with the reference's fallback (e.g. sourcecode/GFM_riemann.cpp:58-68)
 inline vec2 unit_normal(const Levelset& ls, int i, int j) {
   vec2 n = ls.get_normal(i, j);
@@ -965,11 +1134,218 @@ void GFM_original_set_ghost_states(const sim_info& params, const Levelset& ls, c
     real_fluid_velocities(params, ls, prims1, prims2, st.newvelocities);
 }
 
+// GFM_base::get_interpolated_mixedRPstates_VOF (sourcecode/GFM_base.cpp:36-55)
+void get_interpolated_mixedRPstates_VOF(const sim_info& params, const grideuler2type& prims1,
+                                        const grideuler2type& prims2, const vec2& normal, const vec2& loc,
+                                        double ds, vec4type& Lprims, vec4type& Rprims) {
+  vec2 sampleposL = {loc[0] + ds * normal[0], loc[1] + ds * normal[1]};
+  vec2 sampleposR = {loc[0] - ds * normal[0], loc[1] - ds * normal[1]};
+  Lprims = grid_bilinear_interpolate(params, prims2, sampleposL);
+  Rprims = grid_bilinear_interpolate(params, prims1, sampleposR);
+}
+
+// The flags of the VOF GFMs' mixed-cell loop: every cell within ghostrad of a
+// mixed cell gets 1 (z == 0), 2 (z == 1) or 0 (mixed).
+void vof_set_flags(const VOFTracker& vof, int i, int j, int ghostrad, std::vector<std::vector<int>>& flag) {
+  for (int xinc = -ghostrad; xinc <= ghostrad; xinc++)
+    for (int yinc = -ghostrad; yinc <= ghostrad; yinc++) {
+      double zz = vof.get_z(i + yinc, j + xinc);
+      flag[i + yinc][j + xinc] = (zz == 0.0) ? 1 : (zz == 1.0) ? 2 : 0;
+    }
+}
+
+// Inverse-distance average of the mixed cells' states (flag 0) within
+// ghostrad of real cell (i,j) (e.g. sourcecode/GFM_VOF.cpp:240-262).
+vec4type vof_invdist_average(const sim_info& params, const std::vector<std::vector<int>>& flag,
+                             const grideuler2type& MRPsoln, int i, int j, int ghostrad) {
+  vec2 CC = params.cellcentre_coord(i, j);
+  double suminvdist = 0.0;
+  vec4type sumprims = {0.0, 0.0, 0.0, 0.0};
+  for (int xinc = -ghostrad; xinc <= ghostrad; xinc++)
+    for (int yinc = -ghostrad; yinc <= ghostrad; yinc++) {
+      if (flag[i + yinc][j + xinc] != 0) continue;
+      vec2 thisCC = params.cellcentre_coord(i + yinc, j + xinc);
+      double ddx = thisCC[0] - CC[0], ddy = thisCC[1] - CC[1];
+      double thisinvdist = 1.0 / std::sqrt(ddx * ddx + ddy * ddy);
+      suminvdist += thisinvdist;
+      sumprims = add(sumprims, scale(thisinvdist, MRPsoln[i + yinc][j + xinc]));
+    }
+  return {sumprims[0] / suminvdist, sumprims[1] / suminvdist, sumprims[2] / suminvdist, sumprims[3] / suminvdist};
+}
+
+// GFM_VOF::set_ghost_states (sourcecode/GFM_VOF.cpp:8-325)
+void GFM_VOF_set_ghost_states(const sim_info& params, const VOFTracker& vof, const binarySGparams& eos,
+                              const gfm_method_desc& m, grideuler2type& grid1, grideuler2type& grid2,
+                              GFMState& st) {
+  const int g = params.numGC;
+  const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+  grideuler2type prims1(nr, std::vector<vec4type>(nc)), prims2(nr, std::vector<vec4type>(nc));
+  grideuler2type MRPsoln1(nr, std::vector<vec4type>(nc, vec4type{0.0, 0.0, 0.0, 0.0}));
+  grideuler2type MRPsoln2 = MRPsoln1;
+  std::vector<std::vector<int>> flag(nr, std::vector<int>(nc, -1));
+  st.newvelocities.assign(nr, std::vector<vec2>(nc, vec2{0.0, 0.0}));
+  const double ds = 1.0 * std::min(params.dx, params.dy);
+  const int ghostrad = 3;
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      double z = vof.get_z(i, j);
+      prims1[i][j] = misc::conserved_to_primitives(eos.gamma1, eos.pinf1, grid1[i][j]);
+      prims2[i][j] = misc::conserved_to_primitives(eos.gamma2, eos.pinf2, grid2[i][j]);
+      bool ok = (z >= 0.5) ? misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j])
+                           : misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]);
+      if (!ok) g_status |= GFM_ST_UNPHYSICAL;
+    }
+  st.n_interfacial = 0;
+  for (int i = g - ghostrad; i < params.Ny + g + ghostrad; i++)
+    for (int j = g - ghostrad; j < params.Nx + g + ghostrad; j++) {
+      double z = vof.get_z(i, j);
+      if (!(0.0 < z && z < 1.0)) continue;
+      st.n_interfacial++;
+      vof_set_flags(vof, i, j, ghostrad, flag);
+      vec2 normal = vof.get_mixedcell_normal(i, j);
+      vec2 loc = vof.get_interfacelocation(i, j);
+      vec4type interfaceprims1, interfaceprims2;
+      get_interpolated_mixedRPstates_VOF(params, prims1, prims2, normal, loc, ds, interfaceprims2, interfaceprims1);
+      MRPResult r = solve_interface_RP(eos, interfaceprims1, interfaceprims2, normal);
+      vec2 u1_star, u2_star;
+      if (m.use_slip_BCs) {
+        u1_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+        u2_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+      } else if (z > 0.5) {
+        u1_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+        u2_star = {r.u_star * normal[0] + r.u1_tang[0], r.u_star * normal[1] + r.u1_tang[1]};
+      } else {
+        u1_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+        u2_star = {r.u_star * normal[0] + r.u2_tang[0], r.u_star * normal[1] + r.u2_tang[1]};
+      }
+      MRPsoln1[i][j] = {r.rho_star_L, u1_star[0], u1_star[1], r.p_star};
+      MRPsoln2[i][j] = {r.rho_star_R, u2_star[0], u2_star[1], r.p_star};
+      if (z > 0.5) {
+        prims1[i][j][0] = eos::isentropic_extrapolation(eos.gamma1, eos.pinf1, r.rho_star_L, r.p_star, prims1[i][j][3]);
+        prims2[i][j] = {r.rho_star_R, u2_star[0], u2_star[1], r.p_star};
+      } else {
+        prims2[i][j][0] = eos::isentropic_extrapolation(eos.gamma2, eos.pinf2, r.rho_star_R, r.p_star, prims2[i][j][3]);
+        prims1[i][j] = {r.rho_star_L, u1_star[0], u1_star[1], r.p_star};
+      }
+    }
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      if (flag[i][j] == 1) prims1[i][j] = vof_invdist_average(params, flag, MRPsoln1, i, j, ghostrad);
+      else if (flag[i][j] == 2) prims2[i][j] = vof_invdist_average(params, flag, MRPsoln2, i, j, ghostrad);
+    }
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      grid1[i][j] = misc::primitives_to_conserved(eos.gamma1, eos.pinf1, prims1[i][j]);
+      grid2[i][j] = misc::primitives_to_conserved(eos.gamma2, eos.pinf2, prims2[i][j]);
+      if (!misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j]) ||
+          !misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]))
+        g_status |= GFM_ST_UNPHYSICAL;
+    }
+  apply_BCs_euler(params, grid1);
+  apply_BCs_euler(params, grid2);
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      if (vof.get_z(i, j) >= 0.5) st.newvelocities[i][j] = {prims1[i][j][1], prims1[i][j][2]};
+      else st.newvelocities[i][j] = {prims2[i][j][1], prims2[i][j][2]};
+    }
+}
+
+// OGFM_VOF::set_ghost_states (sourcecode/OGFM_VOF.cpp:8-274)
+void OGFM_VOF_set_ghost_states(const sim_info& params, const VOFTracker& vof, const binarySGparams& eos,
+                               grideuler2type& grid1, grideuler2type& grid2, BBrange& realcells1,
+                               BBrange& realcells2, GFMState& st) {
+  const int g = params.numGC;
+  const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+  grideuler2type prims1(nr, std::vector<vec4type>(nc)), prims2(nr, std::vector<vec4type>(nc));
+  grideuler2type MRPsoln1(nr, std::vector<vec4type>(nc, vec4type{0.0, 0.0, 0.0, 0.0}));
+  grideuler2type MRPsoln2 = MRPsoln1;
+  std::vector<std::vector<int>> flag(nr, std::vector<int>(nc, -1));
+  st.newvelocities.assign(nr, std::vector<vec2>(nc, vec2{0.0, 0.0}));
+  const double ds = 1.0 * std::min(params.dx, params.dy);
+  const int ghostrad = 3;
+  realcells1 = {g + params.Ny, g, g + params.Nx, g};
+  realcells2 = {g + params.Ny, g, g + params.Nx, g};
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      double z = vof.get_z(i, j);
+      prims1[i][j] = misc::conserved_to_primitives(eos.gamma1, eos.pinf1, grid1[i][j]);
+      prims2[i][j] = misc::conserved_to_primitives(eos.gamma2, eos.pinf2, grid2[i][j]);
+      if (z >= 0.5) {
+        if (!misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j])) g_status |= GFM_ST_UNPHYSICAL;
+        realcells1.imin = std::min(realcells1.imin, i - 2);
+        realcells1.imax = std::max(realcells1.imax, i + 2);
+        realcells1.jmin = std::min(realcells1.jmin, j - 2);
+        realcells1.jmax = std::max(realcells1.jmax, j + 2);
+      } else {
+        if (!misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j])) g_status |= GFM_ST_UNPHYSICAL;
+        realcells2.imin = std::min(realcells2.imin, i - 2);
+        realcells2.imax = std::max(realcells2.imax, i + 2);
+        realcells2.jmin = std::min(realcells2.jmin, j - 2);
+        realcells2.jmax = std::max(realcells2.jmax, j + 2);
+      }
+    }
+  realcells1.imin = std::max(realcells1.imin, g);
+  realcells1.imax = std::min(realcells1.imax, g + params.Ny);
+  realcells1.jmin = std::max(realcells1.jmin, g);
+  realcells1.jmax = std::min(realcells1.jmax, g + params.Nx);
+  realcells2.imin = std::max(realcells2.imin, g);
+  realcells2.imax = std::min(realcells2.imax, g + params.Ny);
+  realcells2.jmin = std::max(realcells2.jmin, g);
+  realcells2.jmax = std::min(realcells2.jmax, g + params.Nx);
+  st.n_interfacial = 0;
+  for (int i = g - ghostrad; i < params.Ny + g + ghostrad; i++)
+    for (int j = g - ghostrad; j < params.Nx + g + ghostrad; j++) {
+      double z = vof.get_z(i, j);
+      if (0.0 < z && z < 1.0) {
+        st.n_interfacial++;
+        vof_set_flags(vof, i, j, ghostrad, flag);
+        vec2 normal = vof.get_mixedcell_normal(i, j);
+        vec2 loc = vof.get_interfacelocation(i, j);
+        vec4type interfaceprims1, interfaceprims2;
+        get_interpolated_mixedRPstates_VOF(params, prims1, prims2, normal, loc, ds, interfaceprims2,
+                                           interfaceprims1);
+        MRPsoln1[i][j] = interfaceprims1;
+        MRPsoln2[i][j] = interfaceprims2;
+        if (z > 0.5) {
+          double rho = eos::isentropic_extrapolation(eos.gamma2, eos.pinf2, MRPsoln2[i][j][0], MRPsoln2[i][j][3],
+                                                     prims1[i][j][3]);
+          prims2[i][j] = {rho, prims1[i][j][1], prims1[i][j][2], prims1[i][j][3]};
+        } else {
+          double rho = eos::isentropic_extrapolation(eos.gamma1, eos.pinf1, MRPsoln1[i][j][0], MRPsoln1[i][j][3],
+                                                     prims2[i][j][3]);
+          prims1[i][j] = {rho, prims2[i][j][1], prims2[i][j][2], prims2[i][j][3]};
+        }
+      }
+      if (z >= 0.5) st.newvelocities[i][j] = {prims1[i][j][1], prims1[i][j][2]};
+      else st.newvelocities[i][j] = {prims2[i][j][1], prims2[i][j][2]};
+    }
+  for (int i = g; i < params.Ny + g; i++)
+    for (int j = g; j < params.Nx + g; j++) {
+      if (flag[i][j] == 1) {
+        vec4type s = vof_invdist_average(params, flag, MRPsoln1, i, j, ghostrad);
+        double rho = eos::isentropic_extrapolation(eos.gamma1, eos.pinf1, s[0], s[3], prims2[i][j][3]);
+        prims1[i][j] = {rho, prims2[i][j][1], prims2[i][j][2], prims2[i][j][3]};
+      } else if (flag[i][j] == 2) {
+        vec4type s = vof_invdist_average(params, flag, MRPsoln2, i, j, ghostrad);
+        double rho = eos::isentropic_extrapolation(eos.gamma2, eos.pinf2, s[0], s[3], prims1[i][j][3]);
+        prims2[i][j] = {rho, prims1[i][j][1], prims1[i][j][2], prims1[i][j][3]};
+      }
+      grid1[i][j] = misc::primitives_to_conserved(eos.gamma1, eos.pinf1, prims1[i][j]);
+      grid2[i][j] = misc::primitives_to_conserved(eos.gamma2, eos.pinf2, prims2[i][j]);
+      if (!misc::is_physical_state(eos.gamma1, eos.pinf1, grid1[i][j]) ||
+          !misc::is_physical_state(eos.gamma2, eos.pinf2, grid2[i][j]))
+        g_status |= GFM_ST_UNPHYSICAL;
+    }
+  apply_BCs_euler(params, grid1);
+  apply_BCs_euler(params, grid2);
+}
+
 // ----------------------------------------------------------------------------
 // compute_dt (sourcecode/sim_twofluid.cpp:108-157, sim_onefluid.cpp:68-91)
 // ----------------------------------------------------------------------------
+template <class ITM>
 double compute_dt_twofluid(double CFL, const sim_info& params, const grideuler2type& grid1,
-                           const grideuler2type& grid2, const Levelset& ls, const binarySGparams& eos, double T,
+                           const grideuler2type& grid2, const ITM& ls, const binarySGparams& eos, double T,
                            double t) {
   double maxu = 0.0, maxv = 0.0;
   for (int i = params.numGC; i < params.Ny + params.numGC; i++)
@@ -1112,6 +1488,46 @@ int oracle_twofluid_run(const gfm_grid_desc* d, const gfm_method_desc* m, double
   binarySGparams eos = {d->gamma1, d->pinf1, d->gamma2, d->pinf2};
   grideuler2type grid1 = from_soa(params, U1), grid2 = from_soa(params, U2);
   grideuler2type future_grid1 = grid1, future_grid2 = grid2;
+  if (m->itm == GFM_ITM_VOF) {
+    // phi holds the volume fraction z; GFM_VOF or OGFM_VOF
+    VOFTracker vof;
+    vof.params = params;
+    vof.z = phi_from(params, phi);
+    vof.steps = *numsteps;
+    const int g = params.numGC;
+    GFMState st;
+    int taken = 0;
+    while (*t < m->T && taken < nsteps) {
+      BBrange realcells1 = {g, params.Ny + g, g, params.Nx + g};
+      BBrange realcells2 = realcells1;
+      double CFL = (*numsteps < 5) ? std::min(m->CFL, 0.2) : m->CFL;
+      double dt = compute_dt_twofluid(CFL, params, grid1, grid2, vof, eos, m->T, *t);
+      if (m->gfm == GFM_OGFM_VOF) OGFM_VOF_set_ghost_states(params, vof, eos, grid1, grid2, realcells1, realcells2, st);
+      else GFM_VOF_set_ghost_states(params, vof, eos, *m, grid1, grid2, st);
+      FS_update(m->fs, params, eos.gamma1, eos.pinf1, dt, realcells1, grid1, future_grid1);
+      FS_update(m->fs, params, eos.gamma2, eos.pinf2, dt, realcells2, grid2, future_grid2);
+      vof.update_interface_coupled(st.newvelocities, dt);
+      apply_BCs_euler(params, grid1);
+      apply_BCs_euler(params, grid2);
+      (*numsteps)++;
+      *t += dt;
+      taken++;
+    }
+    to_soa(params, grid1, U1);
+    to_soa(params, grid2, U2);
+    phi_to(params, vof.z, phi);
+    if (vel && !st.newvelocities.empty()) {
+      const int nr = params.Ny + 2 * g, nc = params.Nx + 2 * g;
+      const size_t plane = static_cast<size_t>(nr) * nc;
+      for (int i = 0; i < nr; i++)
+        for (int j = 0; j < nc; j++) {
+          vel[static_cast<size_t>(i) * nc + j] = st.newvelocities[i][j][0];
+          vel[plane + static_cast<size_t>(i) * nc + j] = st.newvelocities[i][j][1];
+        }
+    }
+    if (n_interfacial) *n_interfacial = st.n_interfacial;
+    return taken;
+  }
   Levelset ls;
   ls.params = params;
   ls.phi = phi_from(params, phi);

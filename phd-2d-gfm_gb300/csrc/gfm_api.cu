@@ -115,9 +115,20 @@ gfm_status_t check_method(const gfm_ctx* ctx, const gfm_method_desc* m) {
   if (!m) return GFM_ERR_ARG;
   if (m->fs != GFM_FS_GODUNOV && m->fs != GFM_FS_MUSCL) return GFM_ERR_ARG;
   if (ctx->two_fluid) {
-    if (m->gfm < GFM_OGFM || m->gfm > GFM_MODIFIED) return GFM_ERR_ARG;
-    if (m->ls_order != 1 && m->ls_order != 5) return GFM_ERR_ARG;
-    if (m->reinit_every < 0 || m->reinit_iters < 0) return GFM_ERR_ARG;
+    if (m->itm == GFM_ITM_VOF) {
+      // the VOF GFMs need the VOF tracker (the reference's dynamic_cast,
+      // sourcecode/GFM_VOF.cpp:20) and the other GFMs a level set; the
+      // mixed-cell loop reads z up to 6 cells outside the real cells
+      if (m->gfm != GFM_VOF && m->gfm != GFM_OGFM_VOF) return GFM_ERR_ARG;
+      if (ctx->P.g < 6) return GFM_ERR_ARG;
+      if (m->gfm == GFM_OGFM_VOF && m->use_slip_BCs) return GFM_ERR_ARG;   // OGFM_VOF.cpp:21
+    } else if (m->itm == GFM_ITM_LEVELSET) {
+      if (m->gfm < GFM_OGFM || m->gfm > GFM_MODIFIED) return GFM_ERR_ARG;
+      if (m->ls_order != 1 && m->ls_order != 5) return GFM_ERR_ARG;
+      if (m->reinit_every < 0 || m->reinit_iters < 0) return GFM_ERR_ARG;
+    } else {
+      return GFM_ERR_ARG;
+    }
   }
   if (!(m->CFL > 0.0)) return GFM_ERR_ARG;
   return GFM_OK;
@@ -207,10 +218,13 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->vel_t, 2 * plane_b);
     alloc((void**)&ctx->mask, (size_t)P.plane);
     alloc((void**)&ctx->ifc_map, sizeof(int) * (size_t)P.plane);
-    size_t cap = (size_t)P.Nx * P.Ny;
+    // interface lists: at most one entry per padded cell (the VOF loop also
+    // visits a ring of ghost cells)
+    size_t cap = (size_t)P.nr * P.nc;
     alloc((void**)&ctx->ifc_list, sizeof(int) * cap);
     alloc((void**)&ctx->ifc_done, sizeof(int) * cap);
     alloc((void**)&ctx->ifc_out, sizeof(double) * 8 * cap);
+    alloc((void**)&ctx->ifc_mrp, sizeof(double) * 8 * cap);
     ctx->n_chunks = (int)(((int64_t)P.nr * P.nc + 2047) / 2048);
     alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)ctx->n_chunks);
     for (int b = 0; b < 2; b++)
@@ -255,7 +269,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->phi); cudaFree(ctx->phi_a); cudaFree(ctx->phi_b); cudaFree(ctx->phi0);
   cudaFree(ctx->nrm); cudaFree(ctx->vel); cudaFree(ctx->vel_t);
   cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
-  cudaFree(ctx->ifc_out); cudaFree(ctx->chunk_count);
+  cudaFree(ctx->ifc_out); cudaFree(ctx->ifc_mrp); cudaFree(ctx->chunk_count);
   for (int b = 0; b < 2; b++)
     for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cell); cudaFree(ctx->tile_near);
@@ -317,6 +331,11 @@ gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi) {
   return copy_grid(ctx, ctx->phi, nullptr, phi, 1);
 }
 
+gfm_status_t gfm_download_velocity(gfm_ctx* ctx, double* vel) {
+  if (!ctx || !vel || !ctx->two_fluid) return GFM_ERR_ARG;
+  return copy_grid(ctx, ctx->vel, nullptr, vel, 2);
+}
+
 gfm_status_t gfm_download_mask(gfm_ctx* ctx, uint8_t* mask) {
   if (!ctx || !mask || !ctx->two_fluid) return GFM_ERR_ARG;
   const GridP& P = ctx->P;
@@ -364,8 +383,17 @@ gfm_status_t gfm_set_ghost_states(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (r != GFM_OK) return r;
   // the ticket of the interface solve
   ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
-  launch_ghost_fill(ctx, m);
+  ctx->itm = m->itm;
+  if (m->itm == GFM_ITM_VOF) launch_ghost_fill_vof(ctx, m);
+  else launch_ghost_fill(ctx, m);
   return last_error();
+}
+
+gfm_status_t gfm_set_interface_tracker(gfm_ctx* ctx, int itm) {
+  if (!ctx || !ctx->two_fluid || (itm != GFM_ITM_LEVELSET && itm != GFM_ITM_VOF)) return GFM_ERR_ARG;
+  if (itm == GFM_ITM_VOF && ctx->P.g < 6) return GFM_ERR_ARG;
+  ctx->itm = itm;
+  return GFM_OK;
 }
 
 gfm_status_t gfm_fs_update(gfm_ctx* ctx, int fs, int fluid) {
@@ -380,7 +408,9 @@ gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (!ctx || !ctx->two_fluid) return GFM_ERR_ARG;
   gfm_status_t r = check_method(ctx, m);
   if (r != GFM_OK) return r;
-  launch_ls_update(ctx, m, ctx->stream);
+  ctx->itm = m->itm;
+  if (m->itm == GFM_ITM_VOF) launch_vof_update(ctx, ctx->stream);
+  else launch_ls_update(ctx, m, ctx->stream);
   return last_error();
 }
 
@@ -401,17 +431,19 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
   if (phase_ms)
     for (int q = 0; q < 6; q++) CK(cudaEventCreate(&ev[q]));
   ctx->timing = phase_ms ? 1 : 0;
+  if (ctx->two_fluid) ctx->itm = m->itm;
+  const bool vof = ctx->two_fluid && m->itm == GFM_ITM_VOF;
   bool overlapped = false;
   auto mark = [&](int q) {
     if (phase_ms) cudaEventRecord(ev[q], ctx->stream);
   };
   for (int s = 0; s < nsteps; s++) {
-    bool ogfm = ctx->two_fluid && m->gfm == GFM_OGFM;
+    bool ogfm = ctx->two_fluid && (m->gfm == GFM_OGFM || m->gfm == GFM_OGFM_VOF);
     mark(0);
     launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
     mark(1);
     if (ctx->two_fluid) {
-      overlapped = !m->use_extension_vfield &&
+      overlapped = !vof && !m->use_extension_vfield &&
                    ((ctx->overlap == GFM_OVERLAP_ON && (m->gfm == GFM_RIEMANN || m->gfm == GFM_REAL)) ||
                     (ctx->overlap == GFM_OVERLAP_AUTO && m->gfm == GFM_RIEMANN));
       // The level-set update reads phi and the velocity field of the ghost
@@ -420,6 +452,11 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
       auto fork_level_set = [&]() {
         cudaEventRecord(ctx->ev_ls_fork, ctx->stream);
         cudaStreamWaitEvent(ctx->s_ls, ctx->ev_ls_fork, 0);
+        if (vof) {   // the VOF advection reads z and the velocity field only
+          launch_vof_update(ctx, ctx->s_ls);
+          cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
+          return;
+        }
         launch_ls_update(ctx, m, ctx->s_ls);
         if (m->reinit_every > 0 && m->reinit_iters > 0) {
           if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
@@ -437,7 +474,8 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
         launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->stream);
         mark(3);
       } else {
-        launch_ghost_fill(ctx, m);
+        if (vof) launch_ghost_fill_vof(ctx, m);
+        else launch_ghost_fill(ctx, m);
         mark(2);
         fork_level_set();
         launch_fs_update(ctx, m->fs, 3);

@@ -8,6 +8,7 @@
 //   shock_bubble            1000x400 shock-bubble on [0,0.25]x[0,0.089]
 //   underwater_explosion_sg 800x800 stiffened-gas underwater explosion on [-1,1]^2
 //   circularexplosion       one-fluid 200x200 circular explosion on [0,2]^2
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -272,6 +273,33 @@ gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gf
   }
   host_bcs(d, U1);
   host_bcs(d, U2);
+  return GFM_OK;
+}
+
+// Volume fraction of fluid 1 for the VOF interface tracker: the zval of
+// set_sim_ICs (10x10 sub-sampled area fractions for circles,
+// sourcecode/sim_twofluid.cpp:646-668,825-856; the clipped linear profiles of
+// the planar tubes, :697,731; z = 1 for GDA, :769).
+gfm_status_t gfm_case_init_z(const char* test_case, const gfm_grid_desc* d, double* z) {
+  if (!test_case || !d || !z) return GFM_ERR_ARG;
+  std::string tc(test_case);
+  Geo G = geo_of(d);
+  auto clip01 = [](double v) { return std::min(1.0, std::max(0.0, v)); };
+  for (int i = 0; i < G.nr; i++)
+    for (int j = 0; j < G.nc; j++) {
+      const double x = G.ccx(j), y = G.ccy(i);
+      double v;
+      if (tc == "circularexplosion") v = area_fraction(G, i, j, 1.0, 1.0, 0.4);
+      else if (tc == "ST1_x") v = clip01((0.5 - x + 0.5 * G.dx) / G.dx);
+      else if (tc == "ST2_y") v = clip01((0.7 - y + 0.5 * G.dy) / G.dy);
+      else if (tc == "GDA") v = 1.0;
+      else if (tc == "shocked_helium_bubble") v = area_fraction(G, i, j, 175.0, 44.5, 25.0);
+      else if (tc == "shocked_R22_bubble") v = area_fraction(G, i, j, 0.225, 0.0445, 0.025);
+      else if (tc == "shock_bubble") v = area_fraction(G, i, j, 0.175, 0.0445, 0.025);
+      else if (tc == "underwater_explosion_sg") v = area_fraction(G, i, j, 0.0, 0.0, 0.2);
+      else return GFM_ERR_ARG;
+      z[(size_t)i * G.nc + j] = v;
+    }
   return GFM_OK;
 }
 

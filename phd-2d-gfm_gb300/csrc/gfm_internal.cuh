@@ -73,6 +73,8 @@ struct gfm_ctx {
   int* ifc_done;
   int* ifc_pred;     // 8 per interface
   double* ifc_out;   // 8 per interface: star state (4), extension velocity (2), rho* other side, spare
+  double* ifc_mrp;   // 8 per mixed cell of the VOF loop: MRPsoln1, MRPsoln2
+  int itm;           // interface tracker of the last method used (GFM_ITM_*)
   int* ifc_opp;      // real GFM: opposite cell
   gfm::DevTime* dtime;
   gfm::DevTime* h_dtime;  // pinned host mirror
@@ -162,6 +164,8 @@ void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
+void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m);
+void launch_vof_update(gfm_ctx* ctx, cudaStream_t s);
 void launch_end_step(gfm_ctx* ctx);
 void prepare_kernels();
 const float* mlp_params(const struct gfm_mlp* m);   // the network's FP32 parameters (device)

@@ -52,6 +52,7 @@ struct CflArgs {
   unsigned int* counter;
   double CFL, T;
   int ogfm;            // realcells boxes start empty (GFM_original.cpp:47-55)
+  int vof;             // phi holds the volume fraction z: get_sdf = 0.5 - z
 };
 
 __global__ void __launch_bounds__(256) k_cfl(CflArgs a) {
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs a) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     int i = (int)(k / P.Nx) + P.g, j = (int)(k % P.Nx) + P.g;
     int64_t c = cidx(P, i, j);
-    bool f1 = (a.phi == nullptr) || (a.phi[c] < 0.0);
+    bool f1 = (a.phi == nullptr) || (a.vof ? (0.5 - a.phi[c] < 0.0) : (a.phi[c] < 0.0));
     const double* U = f1 ? a.U1 : a.U2;
     double gm = f1 ? P.g1 : P.g2, pinf = f1 ? P.p1 : P.p2;
     V4 u = load4(U, P, c);
@@ -148,6 +149,7 @@ void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int
   a.CFL = CFL;
   a.T = T;
   a.ogfm = ogfm ? 1 : 0;
+  a.vof = (ctx->two_fluid && ctx->itm == GFM_ITM_VOF) ? 1 : 0;
   int64_t n = (int64_t)ctx->P.Nx * ctx->P.Ny;
   int blocks = (int)((n + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
@@ -996,6 +998,457 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// VOF interface tracker and the VOF ghost-fluid methods.
+//
+// The interface field (the context's phi plane) holds z, the volume fraction
+// of fluid 1.  The tracker is the project's own definition from published
+// methods, restated in the oracle:
+//   mixed cell   0 < z < 1
+//   normal       Youngs (1982) / Parker & Youngs (1992): minus the 3x3
+//                weighted central-difference gradient of z, unit length,
+//                pointing from fluid 1 into fluid 2; (1, 0) where it vanishes
+//   PLIC line    cutting the cell at area fraction z (Scardovelli & Zaleski
+//                2000); the interface location is its segment's midpoint
+//   advection    directional splitting (x then y on even steps, y then x on
+//                odd), geometric donor-strip fluxes of the PLIC fluid-1
+//                region, face velocity = mean of the two cells', divergence
+//                term of Weymouth & Yue (2010) with c = [z > 0.5] at the start
+//                of the step; values within 1e-8 of 0 or 1 become 0 or 1
+//   sign         get_sdf = 0.5 - z (negative in fluid 1)
+// GFM_VOF (sourcecode/GFM_VOF.cpp:8-325) and OGFM_VOF
+// (sourcecode/OGFM_VOF.cpp:8-274) visit the mixed cells of the real cells
+// plus a 3-cell ring, in row-major order, and overwrite both fluids' prims of
+// the visited cell while later cells read prims by bilinear samples: the
+// dependency rule of the Riemann GFM's loop (an earlier mixed cell in a
+// sample's corner supplies its new prims) with the warp-per-cell schedule.
+// ---------------------------------------------------------------------------
+enum { VOF_GFM = 0, VOF_OGFM = 1 };
+constexpr double VOF_ZEPS = 1e-8;
+constexpr int VOF_RING = 3;   // ghostrad of the reference's loops
+
+__device__ __forceinline__ double vlo(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double vhi(double a, double b) { return (b < a) ? a : b; }
+
+// area fraction of {c1 t + c2 s <= b} in the unit square (c1, c2 >= 0)
+__device__ double vof_area(double b, double c1, double c2) {
+  const double m1 = vlo(c1, c2), m2 = vhi(c1, c2);
+  if (b <= 0.0) return 0.0;
+  const double s = m1 + m2;
+  if (b >= s) return 1.0;
+  if (m1 == 0.0) return b / m2;
+  const double d = (2.0 * m1) * m2;
+  if (b < m1) return (b * b) / d;
+  if (b <= m2) return (b - 0.5 * m1) / m2;
+  const double r = s - b;
+  return 1.0 - (r * r) / d;
+}
+
+// the line constant with vof_area(b, m1, m2) = z (0 < z < 1, m1 <= m2, m2 > 0)
+__device__ double vof_line_constant(double z, double m1, double m2) {
+  if (m1 == 0.0) return z * m2;
+  const double v1 = m1 / (2.0 * m2);
+  const double d = (2.0 * m1) * m2;
+  if (z < v1) return sqrt(d * z);
+  if (z <= 1.0 - v1) return z * m2 + 0.5 * m1;
+  return (m1 + m2) - sqrt(d * (1.0 - z));
+}
+
+// PLIC reconstruction of the mixed cell c: in the unit cell with the axes
+// reflected where the normal component is negative, fluid 1 fills
+// {a xi + b eta <= beta}, a = |nx| dx, b = |ny| dy.
+struct VofPlic { double nx, ny, a, b, beta; };
+
+__device__ VofPlic vof_reconstruct(const GridP& P, const double* z, int64_t c) {
+  const int64_t w = P.pitch;
+  const double gx = ((z[c - w + 1] + 2.0 * z[c + 1]) + z[c + w + 1]) - ((z[c - w - 1] + 2.0 * z[c - 1]) + z[c + w - 1]);
+  const double gy = ((z[c + w - 1] + 2.0 * z[c + w]) + z[c + w + 1]) - ((z[c - w - 1] + 2.0 * z[c - w]) + z[c - w + 1]);
+  const double mx = -gx / P.dx, my = -gy / P.dy;
+  const double nn = sqrt(mx * mx + my * my);
+  VofPlic r;
+  if (nn > 0.0) { r.nx = mx / nn; r.ny = my / nn; }
+  else { r.nx = 1.0; r.ny = 0.0; }
+  r.a = fabs(r.nx) * P.dx;
+  r.b = fabs(r.ny) * P.dy;
+  r.beta = vof_line_constant(z[c], vlo(r.a, r.b), vhi(r.a, r.b));
+  return r;
+}
+
+// fluid-1 volume of cell c (fraction of the cell) inside the strip of width w
+// along axis dir touching the cell's high face (high) or its low face
+__device__ double vof_strip_fraction(const GridP& P, const double* z, int64_t c, int dir, bool high, double w) {
+  const double zc = z[c];
+  if (zc == 1.0) return w;
+  if (zc == 0.0) return 0.0;
+  const VofPlic r = vof_reconstruct(P, z, c);
+  const double n = dir == 0 ? r.nx : r.ny;
+  const double cd = dir == 0 ? r.a : r.b, co = dir == 0 ? r.b : r.a;
+  const bool refl = n < 0.0;
+  const double start = (high != refl) ? 1.0 - w : 0.0;
+  return w * vof_area(r.beta - cd * start, cd * w, co);
+}
+
+__device__ __forceinline__ bool vof_in_ring(const GridP& P, int i, int j) {
+  return i >= P.g - VOF_RING && i < P.Ny + P.g + VOF_RING && j >= P.g - VOF_RING && j < P.Nx + P.g + VOF_RING;
+}
+
+// Stage 1 of the VOF ghost fill: prims of both grids, the real fluid's
+// assert (z >= 0.5: fluid 1), the OGFM_VOF realcells boxes, the mixed cells
+// of the real cells plus the ring (mask, chunk counts) and, for each, its
+// reconstruction: nrm planes 0,1 = interface location, 2,3 = unit normal.
+struct VofPrimArgs {
+  GridP P;
+  const double* U1; const double* U2;
+  double* W1; double* W2;
+  const double* z;
+  double* nrm;
+  uint8_t* mask;
+  int* ifc_map;
+  int* chunk_count;
+  DevTime* D;
+  int ogfm;
+};
+
+__global__ void __launch_bounds__(CHUNK_T) k_vof_prims(VofPrimArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  __shared__ int s_cnt;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const int64_t n = (int64_t)P.nr * P.nc;
+  const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  uint32_t st = 0;
+  int cnt = 0;
+  int bb[8] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
+  for (int q = threadIdx.x; q < CHUNK; q += CHUNK_T) {
+    int64_t lin = base + q;
+    if (lin >= n) break;
+    int i, j;
+    linear_to_ij(P, lin, i, j);
+    const int64_t c = cidx(P, i, j);
+    const double zc = a.z[c];
+    bool ok1, ok2;
+    const V4 w1 = cons_to_prims_phys(P.g1, P.p1, load4(a.U1, P, c), &ok1);
+    const V4 w2 = cons_to_prims_phys(P.g2, P.p2, load4(a.U2, P, c), &ok2);
+    store4(a.W1, P, c, w1);
+    store4(a.W2, P, c, w2);
+    if (zc >= 0.5) {
+      if (!ok1) st |= ST_UNPHYSICAL;
+      bb[0] = min(bb[0], i - 2); bb[1] = max(bb[1], i + 2); bb[2] = min(bb[2], j - 2); bb[3] = max(bb[3], j + 2);
+    } else {
+      if (!ok2) st |= ST_UNPHYSICAL;
+      bb[4] = min(bb[4], i - 2); bb[5] = max(bb[5], i + 2); bb[6] = min(bb[6], j - 2); bb[7] = max(bb[7], j + 2);
+    }
+    uint8_t m = 0;
+    if (vof_in_ring(P, i, j) && 0.0 < zc && zc < 1.0) {
+      m = 1;
+      const VofPlic r = vof_reconstruct(P, a.z, c);
+      // midpoint of the PLIC segment
+      const double m1 = vlo(r.a, r.b), m2 = vhi(r.a, r.b), be = r.beta;
+      double u1, w1v, u2, w2v;
+      if (be < m1) { u1 = be / m1; w1v = 0.0; u2 = 0.0; w2v = be / m2; }
+      else if (be <= m2) { u1 = 0.0; w1v = be / m2; u2 = 1.0; w2v = (be - m1) / m2; }
+      else { u1 = 1.0; w1v = (be - m1) / m2; u2 = (be - m2) / m1; w2v = 1.0; }
+      const double um = 0.5 * (u1 + u2), wm = 0.5 * (w1v + w2v);
+      const bool swapped = r.b < r.a;
+      const double xr = swapped ? wm : um, er = swapped ? um : wm;
+      const double xi = (r.nx < 0.0) ? 1.0 - xr : xr;
+      const double eta = (r.ny < 0.0) ? 1.0 - er : er;
+      const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
+      const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
+      a.nrm[c] = ccx + (xi - 0.5) * P.dx;
+      a.nrm[c + P.plane] = ccy + (eta - 0.5) * P.dy;
+      a.nrm[c + 2 * P.plane] = r.nx;
+      a.nrm[c + 3 * P.plane] = r.ny;
+    }
+    a.mask[c] = m;
+    a.ifc_map[c] = -1;
+    cnt += m;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_cnt, cnt);
+  uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+  if ((threadIdx.x & 31) == 0 && wst) atomicOr(&a.D->status, wst);
+  if (a.ogfm) {
+    for (int q = 0; q < 8; q++) {
+      int v = bb[q];
+      if (q & 1) { for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o)); }
+      else { for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o)); }
+      if ((threadIdx.x & 31) == 0) {
+        if (q & 1) { if (v != INT_MIN) atomicMax(&a.D->rc[q], v); }
+        else { if (v != INT_MAX) atomicMin(&a.D->rc[q], v); }
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) a.chunk_count[blockIdx.x] = s_cnt;
+}
+
+// component kc of fluid f's prims at (i,j) as the sequential loop of cell
+// `lin` sees them: an earlier mixed cell supplies its new prims (out[4f+kc])
+__device__ __forceinline__ double vof_read1(const IfcArgs& a, int f, int i, int j, int kc, int64_t lin, bool& ok) {
+  const GridP& P = a.P;
+  const int64_t c = cidx(P, i, j);
+  const int64_t l2 = (int64_t)i * P.nc + j;
+  if (a.mask[c] && l2 < lin) {
+    const int p = a.ifc_map[c];
+    if (!ifc_wait(a, p)) { ok = false; return 0.0; }
+    return __ldcg(a.out + (int64_t)p * IFC_OUT + 4 * f + kc);
+  }
+  return (f == 0 ? a.W1 : a.W2)[c + kc * P.plane];
+}
+
+// The mixed-cell loop, one warp per cell in the lane layout of
+// k_interface_warp (lane = 16 s + 4 q + kc: probe side s, bilinear corner q,
+// component kc).  out (8 doubles): the cell's new prims of fluid 1 and 2;
+// mrp (8 doubles): MRPsoln1, MRPsoln2.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int n = a.D->n_ifc;
+  const int lane = threadIdx.x & 31;
+  const int s = lane >> 4, q = (lane >> 2) & 3, kc = lane & 3;
+  const bool isR = s == 1;
+  const Gas k = isR ? P.gas2 : P.gas1;
+  uint32_t st = 0;
+  int iters = 0;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(a.ticket, 1u);
+    t = __shfl_sync(FULL_MASK, t, 0);
+    if (t >= n) break;
+    const int64_t lin = a.list[t];
+    const int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
+    const int64_t c = cidx(P, i, j);
+    const double zc = a.phi[c];
+    const double lx = a.nrm[c], ly = a.nrm[c + P.plane];
+    const double nx = a.nrm[c + 2 * P.plane], ny = a.nrm[c + 3 * P.plane];
+    // get_interpolated_mixedRPstates_VOF (sourcecode/GFM_base.cpp:36-55):
+    // side 1 samples prims2 at loc + ds n, side 0 prims1 at loc - ds n
+    const double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
+    const double px = isR ? lx + ds * nx : lx - ds * nx;
+    const double py = isR ? ly + ds * ny : ly - ds * ny;
+    const double sx = (px - P.x0) * P.idx + (double)P.g - 0.5;
+    const double sy = (py - P.y0) * P.idy + (double)P.g - 0.5;
+    int j0 = (int)floor(sx), i0 = (int)floor(sy);
+    j0 = min(max(j0, 0), P.nc - 2);
+    i0 = min(max(i0, 0), P.nr - 2);
+    const double wa = sx - (double)j0, wb = sy - (double)i0;
+    const double fa = (q & 1) ? wa : 1.0 - wa;
+    const double fb = (q & 2) ? wb : 1.0 - wb;
+    bool ok = true;
+    const double gq = vof_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
+    const double pr = (fa * fb) * gq;
+    const double p1 = __shfl_down_sync(FULL_MASK, pr, 4);
+    const double p2 = __shfl_down_sync(FULL_MASK, pr, 8);
+    const double p3 = __shfl_down_sync(FULL_MASK, pr, 12);
+    const double v = ((pr + p1) + p2) + p3;   // lanes 16 s + kc
+    if (!__all_sync(FULL_MASK, ok)) {
+      st |= ST_SCHEDULE_LIMIT;
+      if (lane == 0) {
+        __threadfence();
+        ((volatile int*)a.done)[t] = 2;
+      }
+      continue;
+    }
+    double s0[4], s1[4];   // interfaceprims1 (side 0), interfaceprims2 (side 1)
+    for (int m = 0; m < 4; m++) {
+      s0[m] = __shfl_sync(FULL_MASK, v, m);
+      s1[m] = __shfl_sync(FULL_MASK, v, 16 + m);
+    }
+    const V4 w1 = load4(a.W1, P, c), w2 = load4(a.W2, P, c);
+    double o1[4], o2[4], m1v[4], m2v[4];
+    if (MODE == VOF_GFM) {
+      // the mixed Riemann problem in the normal frame (sourcecode/GFM_VOF.cpp:100-170)
+      const double* own = isR ? s1 : s0;
+      const double un = own[1] * nx + own[2] * ny;
+      const double tx = own[1] - un * nx, ty = own[2] - un * ny;
+      bool okp = true;
+      const V4 Us = prims_to_cons(k.g, k.pinf, V4{own[0], un, 0.0, c_lt(1e-6, own[3]) ? own[3] : 1e-6}, &okp);
+      if (!okp) st |= ST_UNPHYSICAL;
+      int it = 0, gt = 0;
+      const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it, a, nullptr, &gt);
+      if (lane == 0) iters += it;
+      if (c_isnan(m.p)) st |= ST_NAN;
+      const double orho = xside(m.rho_own), otx = xside(tx), oty = xside(ty);
+      const double rhoL = isR ? orho : m.rho_own, rhoR = isR ? m.rho_own : orho;
+      const double t1x = isR ? otx : tx, t1y = isR ? oty : ty;
+      const double t2x = isR ? tx : otx, t2y = isR ? ty : oty;
+      const double snx = m.u * nx, sny = m.u * ny;
+      double u1x, u1y, u2x, u2y;
+      if (a.slip) { u1x = snx + t1x; u1y = sny + t1y; u2x = snx + t2x; u2y = sny + t2y; }
+      else if (zc > 0.5) { u1x = snx + t1x; u1y = sny + t1y; u2x = snx + t1x; u2y = sny + t1y; }
+      else { u1x = snx + t2x; u1y = sny + t2y; u2x = snx + t2x; u2y = sny + t2y; }
+      m1v[0] = rhoL; m1v[1] = u1x; m1v[2] = u1y; m1v[3] = m.p;
+      m2v[0] = rhoR; m2v[1] = u2x; m2v[2] = u2y; m2v[3] = m.p;
+      if (zc > 0.5) {
+        o1[0] = eos_isentropic_extrapolation(P.g1, P.p1, rhoL, m.p, w1.d); o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
+        for (int e = 0; e < 4; e++) o2[e] = m2v[e];
+      } else {
+        o2[0] = eos_isentropic_extrapolation(P.g2, P.p2, rhoR, m.p, w2.d); o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
+        for (int e = 0; e < 4; e++) o1[e] = m1v[e];
+      }
+    } else {
+      // OGFM_VOF (sourcecode/OGFM_VOF.cpp:138-165): the interpolated states,
+      // the ghost fluid's density by isentropic extrapolation
+      for (int e = 0; e < 4; e++) { m1v[e] = s0[e]; m2v[e] = s1[e]; }
+      if (zc > 0.5) {
+        o1[0] = w1.a; o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
+        o2[0] = eos_isentropic_extrapolation(P.g2, P.p2, m2v[0], m2v[3], w1.d); o2[1] = w1.b; o2[2] = w1.c; o2[3] = w1.d;
+      } else {
+        o2[0] = w2.a; o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
+        o1[0] = eos_isentropic_extrapolation(P.g1, P.p1, m1v[0], m1v[3], w2.d); o1[1] = w2.b; o1[2] = w2.c; o1[3] = w2.d;
+      }
+    }
+    if (lane == 0) {
+      double* o = a.out + (int64_t)t * IFC_OUT;
+      double* r = mrp + (int64_t)t * 8;
+      for (int e = 0; e < 4; e++) { o[e] = o1[e]; o[4 + e] = o2[e]; r[e] = m1v[e]; r[4 + e] = m2v[e]; }
+      __threadfence();
+      ((volatile int*)a.done)[t] = 1;
+    }
+  }
+  uint32_t wst = __reduce_or_sync(FULL_MASK, st);
+  unsigned wit = __reduce_add_sync(FULL_MASK, (unsigned)iters);
+  if (lane == 0) {
+    if (wst) atomicOr(&a.D->status, wst);
+    if (wit) {
+      atomicAdd(&a.D->newton_iters, (unsigned long long)wit);
+      atomicAdd(&a.D->ifc_iters, (unsigned long long)wit);
+    }
+  }
+}
+
+// After the loop: the inverse-distance ghost states of the real cells within
+// the ring of a mixed cell (sourcecode/GFM_VOF.cpp:224-292,
+// sourcecode/OGFM_VOF.cpp:171-262), conserved grids, and the velocity field.
+struct VofGhostArgs {
+  GridP P;
+  const double* W1; const double* W2;
+  const double* z;
+  const uint8_t* mask;
+  const int* ifc_map;
+  const double* out;
+  const double* mrp;
+  double* U1; double* U2;
+  double* vel;
+  DevTime* D;
+};
+
+// sum over the mixed cells within the ring of (i,j), xinc-major as the reference
+__device__ V4 vof_invdist_average(const VofGhostArgs& a, int i, int j, int f) {
+  const GridP& P = a.P;
+  const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
+  const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
+  double sw = 0.0;
+  V4 sum = V4{0.0, 0.0, 0.0, 0.0};
+  for (int xinc = -VOF_RING; xinc <= VOF_RING; xinc++)
+    for (int yinc = -VOF_RING; yinc <= VOF_RING; yinc++) {
+      const int64_t c2 = cidx(P, i + yinc, j + xinc);
+      if (!a.mask[c2]) continue;
+      const double tx = P.x0 + ((double)(j + xinc - P.g) + 0.5) * P.dx;
+      const double ty = P.y0 + ((double)(i + yinc - P.g) + 0.5) * P.dy;
+      const double ddx = tx - ccx, ddy = ty - ccy;
+      const double w = 1.0 / sqrt(ddx * ddx + ddy * ddy);
+      sw += w;
+      const double* r = a.mrp + (int64_t)a.ifc_map[c2] * 8 + 4 * f;
+      sum = V4{sum.a + w * r[0], sum.b + w * r[1], sum.c + w * r[2], sum.d + w * r[3]};
+    }
+  return V4{sum.a / sw, sum.b / sw, sum.c / sw, sum.d / sw};
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_vof_ghost(VofGhostArgs a) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int64_t n = (int64_t)P.nr * P.nc;
+  uint32_t st = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    const int64_t c = cidx(P, i, j);
+    const double zc = a.z[c];
+    V4 p1 = load4(a.W1, P, c), p2 = load4(a.W2, P, c);
+    if (a.mask[c]) {
+      const double* o = a.out + (int64_t)a.ifc_map[c] * IFC_OUT;
+      p1 = V4{o[0], o[1], o[2], o[3]};
+      p2 = V4{o[4], o[5], o[6], o[7]};
+    }
+    const bool real = is_real(P, i, j);
+    const bool in_ring = vof_in_ring(P, i, j);
+    // the velocity field: the real fluid's prims after the loop (for OGFM_VOF
+    // stored in the loop, zero outside the ring; the ghost states below never
+    // change the real fluid's velocity)
+    double vx, vy;
+    if (MODE == VOF_OGFM && !in_ring) { vx = 0.0; vy = 0.0; }
+    else if (zc >= 0.5) { vx = p1.b; vy = p1.c; }
+    else { vx = p2.b; vy = p2.c; }
+    if (real && !a.mask[c] && (zc == 0.0 || zc == 1.0)) {
+      bool near = false;
+      for (int di = -VOF_RING; di <= VOF_RING && !near; di++)
+        for (int dj = -VOF_RING; dj <= VOF_RING; dj++)
+          if (a.mask[cidx(P, i + di, j + dj)]) { near = true; break; }
+      if (near) {
+        if (zc == 0.0) {   // flag 1: fluid 1 ghost state
+          const V4 s = vof_invdist_average(a, i, j, 0);
+          if (MODE == VOF_GFM) p1 = s;
+          else p1 = V4{eos_isentropic_extrapolation(P.g1, P.p1, s.a, s.d, p2.d), p2.b, p2.c, p2.d};
+        } else {           // flag 2: fluid 2 ghost state
+          const V4 s = vof_invdist_average(a, i, j, 1);
+          if (MODE == VOF_GFM) p2 = s;
+          else p2 = V4{eos_isentropic_extrapolation(P.g2, P.p2, s.a, s.d, p1.d), p1.b, p1.c, p1.d};
+        }
+      }
+    }
+    bool ok1 = true, ok2 = true;
+    const V4 u1 = prims_to_cons(P.g1, P.p1, p1, &ok1);
+    const V4 u2 = prims_to_cons(P.g2, P.p2, p2, &ok2);
+    if ((MODE == VOF_GFM || real) && (!ok1 || !ok2 || !is_physical_state(u1) || !is_physical_state(u2)))
+      st |= ST_UNPHYSICAL;
+    store4(a.U1, P, c, u1);
+    store4(a.U2, P, c, u2);
+    a.vel[c] = vx;
+    a.vel[c + P.plane] = vy;
+  }
+  uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+  if ((threadIdx.x & 31) == 0 && wst) atomicOr(&a.D->status, wst);
+}
+
+// One directional sweep of the VOF advection over every padded cell: a ghost
+// cell takes the update of its mirror / wrap source (the scalar BCs of phi).
+// second: 0 for the step's first sweep, 1 for its second; the direction
+// follows the step's parity (x first on even steps).
+__global__ void __launch_bounds__(256) k_vof_sweep(GridP P, const double* z, const double* z0, const double* vel,
+                                                    double* out, int second, const DevTime* D) {
+  if (!D->active) return;
+  const int first = (D->numsteps % 2 == 0) ? 0 : 1;
+  const int dir = second ? 1 - first : first;
+  const double dtdh = D->dt / (dir == 0 ? P.dx : P.dy);
+  const int64_t e = dir == 0 ? 1 : P.pitch;
+  GridP Q = P;
+  if (!P.periodic) { Q.bcL = Q.bcR = Q.bcB = Q.bcT = GFM_BC_TRANSMISSIVE; }
+  const int64_t n = (int64_t)P.nr * P.nc;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k / P.nc), j = (int)(k % P.nc);
+    const BCSrc sc = bc_source(Q, i, j);
+    const int64_t c = cidx(P, sc.i, sc.j);
+    const int64_t cl = c - e, ch = c + e;
+    const double uL = 0.5 * (vel[cl + dir * P.plane] + vel[c + dir * P.plane]);
+    const double uH = 0.5 * (vel[c + dir * P.plane] + vel[ch + dir * P.plane]);
+    const double sL = uL * dtdh, sH = uH * dtdh;
+    double FL = 0.0, FH = 0.0;
+    if (sL > 0.0) FL = vof_strip_fraction(P, z, cl, dir, true, sL);
+    else if (sL < 0.0) FL = -vof_strip_fraction(P, z, c, dir, false, -sL);
+    if (sH > 0.0) FH = vof_strip_fraction(P, z, c, dir, true, sH);
+    else if (sH < 0.0) FH = -vof_strip_fraction(P, z, ch, dir, false, -sH);
+    const double cw = (z0[c] > 0.5) ? 1.0 : 0.0;
+    double zn = z[c] - ((FH - cw * sH) - (FL - cw * sL));
+    if (zn < VOF_ZEPS) zn = 0.0;
+    else if (zn > 1.0 - VOF_ZEPS) zn = 1.0;
+    out[cidx(P, i, j)] = zn;
+  }
+}
+
 // Reset of the per-step interface bookkeeping.
 __global__ void k_ifc_reset(int* done, int cap, unsigned int* ticket, const DevTime* D) {
   if (!D->active) return;
@@ -1711,6 +2164,64 @@ void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream
   if (m->reinit_iters & 1) {
     k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, every); counted();
   }
+}
+
+// GFM_VOF / OGFM_VOF set_ghost_states: prims, mixed cells and their
+// reconstruction, the mixed-cell loop, ghost states + conserved grids +
+// velocity field, apply_BCs_euler on both grids.
+void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
+  const GridP& P = ctx->P;
+  cudaStream_t s = ctx->stream;
+  const bool og = m->gfm == GFM_OGFM_VOF;
+  VofPrimArgs pa;
+  pa.P = P;
+  pa.U1 = ctx->U[0]; pa.U2 = ctx->U[1];
+  pa.W1 = ctx->W[0]; pa.W2 = ctx->W[1];
+  pa.z = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
+  pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
+  pa.ogfm = og ? 1 : 0;
+  k_vof_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa); counted();
+  if (og) { k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted(); }
+  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
+                                              ctx->ifc_map, ctx->dtime); counted();
+  const int cap = P.nr * P.nc;
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime);
+  counted();
+  IfcArgs ia;
+  ia.P = P;
+  ia.W1 = ctx->W[0]; ia.W2 = ctx->W[1];
+  ia.phi = ctx->phi; ia.nrm = ctx->nrm; ia.mask = ctx->mask;
+  ia.list = ctx->ifc_list; ia.ifc_map = ctx->ifc_map;
+  ia.done = ctx->ifc_done; ia.out = ctx->ifc_out;
+  ia.ticket = (unsigned int*)(ctx->ifc_opp);
+  ia.D = ctx->dtime;
+  ia.slip = m->use_slip_BCs;
+  ia.mlp = nullptr; ia.cap_X = nullptr; ia.cap_Y = nullptr; ia.cap_count = nullptr; ia.cap = 0;
+  if (og) k_vof_chain<VOF_OGFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
+  else k_vof_chain<VOF_GFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
+  counted();
+  VofGhostArgs ga;
+  ga.P = P;
+  ga.W1 = ctx->W[0]; ga.W2 = ctx->W[1];
+  ga.z = ctx->phi; ga.mask = ctx->mask; ga.ifc_map = ctx->ifc_map;
+  ga.out = ctx->ifc_out; ga.mrp = ctx->ifc_mrp;
+  ga.U1 = ctx->U[0]; ga.U2 = ctx->U[1];
+  ga.vel = ctx->vel; ga.D = ctx->dtime;
+  const int gblocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  if (og) k_vof_ghost<VOF_OGFM><<<gblocks, 256, 0, s>>>(ga);
+  else k_vof_ghost<VOF_GFM><<<gblocks, 256, 0, s>>>(ga);
+  counted();
+  launch_bcs(ctx, 3);
+}
+
+// VOF update_interface_coupled: z0 := z, then two directional sweeps
+// z -> phi_a -> z on stream s
+void launch_vof_update(gfm_ctx* ctx, cudaStream_t s) {
+  const GridP& P = ctx->P;
+  const int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime, 0); counted();
+  k_vof_sweep<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->vel, ctx->phi_a, 0, ctx->dtime); counted();
+  k_vof_sweep<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi0, ctx->vel, ctx->phi, 1, ctx->dtime); counted();
 }
 
 void launch_end_step(gfm_ctx* ctx) {

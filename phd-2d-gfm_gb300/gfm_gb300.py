@@ -23,8 +23,10 @@ LIB_PATH = os.path.join(HERE, "lib", platform.machine(), "libgfm_gb300.so")
 
 BC = {"transmissive": 0, "reflective": 1, "periodic": 2}
 FS = {"Godunov": 0, "MUSCL": 1}
-GFM = {"OGFM": 0, "riemannGFM": 1, "realGFM": 2, "MGFM": 3}
-ITM = {"LS1": (1, 1), "LS5": (5, 1)}   # (advection order, reinitialise every k steps)
+GFM = {"OGFM": 0, "riemannGFM": 1, "realGFM": 2, "MGFM": 3, "VOFGFM": 4, "OGFMVOF": 5}
+# interface trackers: (advection order, reinitialise every k steps, tracker kind)
+ITM = {"LS1": (1, 1, 0), "LS5": (5, 1, 0), "PYVOF": (0, 0, 1)}
+ITM_LEVELSET, ITM_VOF = 0, 1
 
 ST_BITS = {
     1 << 0: "UNPHYSICAL_STATE",
@@ -54,7 +56,7 @@ class MethodDesc(ctypes.Structure):
     _fields_ = [("fs", ctypes.c_int), ("gfm", ctypes.c_int), ("ls_order", ctypes.c_int),
                 ("reinit_every", ctypes.c_int), ("reinit_iters", ctypes.c_int),
                 ("use_extension_vfield", ctypes.c_int), ("use_slip_BCs", ctypes.c_int),
-                ("CFL", ctypes.c_double), ("T", ctypes.c_double)]
+                ("CFL", ctypes.c_double), ("T", ctypes.c_double), ("itm", ctypes.c_int)]
 
 
 class GFMError(RuntimeError):
@@ -79,7 +81,7 @@ def lib():
         "gfm_ctx_destroy": [P],
         "gfm_set_stream": [P, V],
         "gfm_upload": [P, I, pd], "gfm_download": [P, I, pd],
-        "gfm_upload_phi": [P, pd], "gfm_download_phi": [P, pd],
+        "gfm_upload_phi": [P, pd], "gfm_download_phi": [P, pd], "gfm_download_velocity": [P, pd],
         "gfm_set_time": [P, D, I],
         "gfm_download_mask": [P, ctypes.POINTER(ctypes.c_uint8)],
         "gfm_get_time": [P, pd, ctypes.POINTER(I), pd],
@@ -87,7 +89,7 @@ def lib():
         "gfm_set_ghost_states": [P, ctypes.POINTER(MethodDesc)],
         "gfm_fs_update": [P, I, I],
         "gfm_ls_update": [P, ctypes.POINTER(MethodDesc)],
-        "gfm_apply_bcs": [P, I],
+        "gfm_apply_bcs": [P, I], "gfm_set_interface_tracker": [P, I],
         "gfm_step": [P, ctypes.POINTER(MethodDesc), I],
         "gfm_step_timed": [P, ctypes.POINTER(MethodDesc), I, pd],
         "gfm_set_overlap": [P, I],
@@ -118,6 +120,7 @@ def lib():
         "gfm_rs_mixed_batch": [I, D, D, D, D, V, V, V, V, V],
         "gfm_case_params": [ctypes.c_char_p, ctypes.c_char_p, I, I, ctypes.POINTER(GridDesc), pd],
         "gfm_case_init": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(GridDesc), pd, pd, pd],
+        "gfm_case_init_z": [ctypes.c_char_p, ctypes.POINTER(GridDesc), pd],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -171,10 +174,21 @@ def case_init(sim_type, test_case, desc):
     return U1, U2, phi
 
 
+def case_init_z(test_case, desc):
+    """Volume fraction of fluid 1 (nr, nc) of a two-fluid case: the initial
+    interface field of the VOF tracker (itm "PYVOF")."""
+    nr, nc = desc.shape
+    z = np.zeros((nr, nc))
+    _check(lib().gfm_case_init_z(test_case.encode(), ctypes.byref(desc), _dptr(z)),
+           "gfm_case_init_z(%s)" % test_case)
+    return z
+
+
 def method(fs="MUSCL", gfm="riemannGFM", itm="LS5", CFL=0.6, T=1.0, reinit_every=None, reinit_iters=5,
            use_extension_vfield=False, use_slip_BCs=False):
-    order, every = ITM[itm]
+    order, every, kind = ITM[itm]
     m = MethodDesc()
+    m.itm = kind
     m.fs = FS[fs]
     m.gfm = GFM[gfm]
     m.ls_order = order
@@ -266,6 +280,13 @@ class Context:
 
     def clear_status(self):
         _check(lib().gfm_clear_device_status(self._p), "gfm_clear_device_status")
+
+    def velocity(self):
+        """The velocity field (2, nr, nc) of the last ghost fill."""
+        nr, nc = self.desc.shape
+        vel = np.empty((2, nr, nc))
+        _check(lib().gfm_download_velocity(self._p, _dptr(vel)), "gfm_download_velocity")
+        return vel
 
     def stats(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
@@ -521,6 +542,8 @@ class sim_twofluid(sim_base):
     def run_sim(self, SF, stream=None):
         desc, T = case_params("twofluid", SF.test_case, SF.Nx, SF.Ny)
         U1, U2, phi = case_init("twofluid", SF.test_case, desc)
+        if ITM[SF.ITM][2] == ITM_VOF:   # the tracker's field is the volume fraction
+            phi = case_init_z(SF.test_case, desc)
         ctx = Context(desc, two_fluid=True, stream=stream)
         ctx.upload(U1, U2, phi)
         m = method(fs=SF.FS, gfm=SF.GFM, itm=SF.ITM, CFL=SF.CFL, T=T, reinit_every=SF.reinit_every,
