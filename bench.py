@@ -35,6 +35,11 @@ WORKLOADS = {
     "underwater_explosion": {"workload": "underwater_explosion_800x800_realGFM_MUSCL_LS5", "sim": "twofluid",
                              "test_case": "underwater_explosion_sg", "Nx": 800, "Ny": 800, "GFM": "realGFM",
                              "FS": "MUSCL", "ITM": "LS5", "CFL": 0.5, "reinit_every": 5, "run_steps": 1500},
+    # the same flow with the VOF tracker and GFM_VOF (a workload of the VOF
+    # ghost-fluid methods, not the headline configuration)
+    "shock_bubble_vof": {"workload": "shock_bubble_1000x400_VOFGFM_MUSCL_PYVOF", "sim": "twofluid",
+                         "test_case": "shock_bubble", "Nx": 1000, "Ny": 400, "GFM": "VOFGFM", "FS": "MUSCL",
+                         "ITM": "PYVOF", "CFL": 0.6, "reinit_every": 0, "run_steps": 2000},
     # CFL 0.4 as in the reference's settings files: at 0.8 the unsplit
     # MUSCL-Hancock update diverges at step 23 (oracle and GPU alike)
     "circular_explosion": {"workload": "circular_explosion_200x200_onefluid_MUSCL_CFL0.4", "sim": "onefluid",
@@ -172,6 +177,8 @@ def setup(W):
     import gfm_gb300 as g
     desc, T = g.case_params(W["sim"], W["test_case"], W["Nx"], W["Ny"])
     U1, U2, phi = g.case_init(W["sim"], W["test_case"], desc)
+    if W.get("ITM") == "PYVOF":   # the VOF tracker's field is the volume fraction
+        phi = g.case_init_z(W["test_case"], desc)
     if W["sim"] == "twofluid":
         m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T, reinit_every=W["reinit_every"])
     else:

@@ -16,7 +16,7 @@ using namespace gfm;
 std::atomic<long long> gfm::g_launches{0};
 
 // ---------------------------------------------------------------------------
-// SM partitions for the overlapped ghost fill: a 16-SM green context for the
+// SM partitions for the overlapped ghost fill: an 8-SM green context for the
 // interface chain and one for the remaining SMs, with one stream each,
 // created once per device.  The driver entry points are fetched through the
 // runtime, so the library does not link libcuda.  Without green-context
@@ -57,7 +57,9 @@ bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far) {
   CUdevResource res, grp[1], rem;
   if (pGetRes(d, &res, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return false;
   unsigned nb = 1;
-  if (pSplit(grp, &nb, &res, &rem, 0, 16) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
+  // 8 SMs for the chain: measured on the 1000x400 shock-bubble against 16,
+  // 24 and 32 (2.66 against 2.71, 2.79 and 2.89 ms per step)
+  if (pSplit(grp, &nb, &res, &rem, 0, 8) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
   CUdevResourceDesc d1, d2;
   if (pDesc(&d1, grp, 1) != CUDA_SUCCESS || pDesc(&d2, &rem, 1) != CUDA_SUCCESS) return false;
   CUgreenCtx g1, g2;

@@ -2089,7 +2089,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia);
-  const int chain_ctas = 16;   // 8 warps each: two chain warps per SM sub-partition
+  const int chain_ctas = 16;   // 8 warps each on the 8-SM partition: 4 chain warps per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   counted();
