@@ -120,6 +120,23 @@ def ncu_summary(workload):
     return out
 
 
+def step_summary(workload):
+    """key=value lines of the committed whole-step ncu summary on `workload`."""
+    p = os.path.join(ROOT, "profiles", "step_fp64_%s.md" % workload)
+    out = {}
+    if not os.path.exists(p):
+        return out
+    for line in open(p):
+        k, _, v = line.partition("=")
+        if not v or not k.strip().isidentifier() or line.startswith((" ", "|")):
+            continue
+        try:
+            out[k.strip()] = float(v.split()[0])
+        except (IndexError, ValueError):
+            pass
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -220,6 +237,8 @@ def run_gfm(args):
     prof = ncu_summary(args.workload)
     prof_step = int(prof.get("profiled_step", -1))
     flux_ms_prof = None
+    step_prof = step_summary(args.workload)
+    step_ms_prof = None
     launches0 = L.gfm_launch_count()
     if world > 1:
         import torch.distributed as tdist
@@ -236,6 +255,8 @@ def run_gfm(args):
             phases += ph
             if args.warmup + s == prof_step:   # the step of the profiled launch
                 flux_ms_prof = ph[2] + ph[8]
+            if args.warmup + s == int(step_prof.get("profiled_step", -1)):
+                step_ms_prof = float(ph[:5].sum())
         torch.cuda.synchronize()
     wall = time.time() - t_wall
     launches = L.gfm_launch_count() - launches0
@@ -268,6 +289,13 @@ def run_gfm(args):
                      "achieved_gflops": round(fl / (flux_ms_prof * 1e-3) / 1e9, 1),
                      "frac": round(fl / (flux_ms_prof * 1e-3) / 1e9 / fp64_peak.value, 4),
                      "pipe_active_frac_ncu": prof.get("fp64_pipe_active_frac")})
+    if "fp64_flops_per_cell_step" in step_prof and step_ms_prof:
+        # the whole step's FP64 work (ncu, all kernels of one step) over that
+        # step's time measured here
+        fs_ = step_prof["fp64_flops_per_cell_step"] * cells / (step_ms_prof * 1e-3) / 1e9
+        fp64["step"] = {"flops_per_cell": step_prof["fp64_flops_per_cell_step"],
+                        "step": int(step_prof["profiled_step"]), "ms_at_step": round(step_ms_prof, 5),
+                        "achieved_gflops": round(fs_, 1), "frac": round(fs_ / fp64_peak.value, 4)}
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 5), "traffic": prof.get("traffic_bytes_per_launch_full_size"),
             "kernel": "k_flux_update<MUSCL>", "peak_source": peak_kind, "bytes_per_cell": FLUX_BYTES_PER_CELL,

@@ -1403,7 +1403,7 @@ __global__ void __launch_bounds__(256) k_vof_ghost(VofGhostArgs a) {
     bool ok1 = true, ok2 = true;
     const V4 u1 = prims_to_cons(P.g1, P.p1, p1, &ok1);
     const V4 u2 = prims_to_cons(P.g2, P.p2, p2, &ok2);
-    if ((MODE == VOF_GFM || real) && (!ok1 || !ok2 || !is_physical_state(u1) || !is_physical_state(u2)))
+    if ((MODE == VOF_GFM || real) && (!ok1 || !ok2 || !is_physical_state_fast(u1) || !is_physical_state_fast(u2)))
       st |= ST_UNPHYSICAL;
     store4(a.U1, P, c, u1);
     store4(a.U2, P, c, u2);
@@ -1557,7 +1557,7 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
     bool ok1 = true, ok2 = true;
     V4 u1 = prims_to_cons(P.g1, P.p1, load4(a.C1, P, c), &ok1);
     V4 u2 = prims_to_cons(P.g2, P.p2, load4(a.C2, P, c), &ok2);
-    if (!ok1 || !ok2 || !is_physical_state(u1) || !is_physical_state(u2)) st |= ST_UNPHYSICAL;
+    if (!ok1 || !ok2 || !is_physical_state_fast(u1) || !is_physical_state_fast(u2)) st |= ST_UNPHYSICAL;
     store4(a.U1, P, c, u1);
     store4(a.U2, P, c, u2);
     if (a.vel_mode == 0) {
