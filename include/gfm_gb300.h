@@ -289,6 +289,39 @@ gfm_status_t gfm_get_interface_stats(gfm_ctx* ctx, int64_t* n_solves, int64_t* n
  * p 1e5) with a left-moving shock of Mach number `mach` at x = 0.9 width, a
  * bubble of fluid 1 (gamma_bubble, rho = rho_ratio, p 1e5) of radius
  * radius_frac x height at (0.7 width, height/2).  T is 1 (run by steps). */
+/* Output files of the reference's drivers (sim_twofluid::output,
+ * output_mass_error and the runtime file, sourcecode/sim_twofluid.cpp:163-331,
+ * 92-103; sim_onefluid::output, sourcecode/sim_onefluid.cpp:169-192), numbers
+ * printed as std::ostream prints them (%g).  Two-fluid: <base>-<n>-prims.dat,
+ * -ls.dat, -vfield.dat, -z.dat, -schlieren.dat and <base>-GDAerr.dat;
+ * one-fluid: <base>-<n>-prims.dat.
+ *   gfm_write_output_files   from HOST arrays (layouts of gfm_download; field =
+ *                            phi or z per itm, vel = 2 planes); no GPU involved
+ *   gfm_writer_*             the same files from a context's device state:
+ *                            gfm_writer_output stages the grids on the device
+ *                            in stream order and returns; a copy stream and a
+ *                            writer thread finish the files while the GPU
+ *                            keeps stepping.  gfm_writer_mass appends one
+ *                            masschange line (t, relative mass errors; masses
+ *                            reduced on the device, numsteps == 0 starts the
+ *                            file and sets the reference masses)
+ *   gfm_run_sim              the reference's time loop with these outputs:
+ *                            at the start, when t - lastoutput > T/output_freq
+ *                            (two-fluid) or numsteps % output_freq == 0
+ *                            (one-fluid), at the end; masschange every step */
+typedef struct gfm_writer gfm_writer;
+gfm_status_t gfm_write_output_files(const gfm_grid_desc* grid, const char* basename, int two_fluid, int itm,
+                                    int numsteps, const double* U1, const double* U2, const double* field,
+                                    const double* vel);
+gfm_status_t gfm_writer_create(gfm_ctx* ctx, const gfm_grid_desc* grid, const char* basename, gfm_writer** out);
+gfm_status_t gfm_writer_output(gfm_writer* w, int numsteps);
+gfm_status_t gfm_writer_mass(gfm_writer* w, int numsteps, double t);
+gfm_status_t gfm_writer_runtime(gfm_writer* w, double seconds);
+gfm_status_t gfm_writer_finish(gfm_writer* w);
+gfm_status_t gfm_writer_destroy(gfm_writer* w);
+gfm_status_t gfm_run_sim(gfm_ctx* ctx, const gfm_method_desc* m, const gfm_grid_desc* grid, const char* basename,
+                         int output_freq, int max_steps, double* seconds);
+
 /* volume fraction z of fluid 1 (one padded plane, layout of phi) of a named
  * two-fluid case, the initial field of the VOF interface tracker */
 gfm_status_t gfm_case_init_z(const char* test_case, const gfm_grid_desc* grid, double* z);

@@ -99,6 +99,13 @@ def twofluid_run(desc, m, U1, U2, phi, nsteps, t=0.0, numsteps=0):
             "n_interfacial": nifc.value}
 
 
+def fluid_mass(desc, interiorsign, U, phi):
+    """sim_twofluid::fluid_mass: sum of rho dx dy over real cells with interiorsign * phi > 0."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    phi = np.ascontiguousarray(phi, dtype=np.float64)
+    return lib().oracle_fluid_mass(ctypes.byref(desc), interiorsign, _p(U), _p(phi))
+
+
 def interfacial_mask(desc, phi):
     phi = np.ascontiguousarray(phi, dtype=np.float64)
     mask = np.zeros(phi.shape, dtype=np.uint8)

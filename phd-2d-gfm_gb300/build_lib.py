@@ -23,7 +23,8 @@ LIBDIR = os.path.join(HERE, "lib", MACHINE)
 ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_LIBDIR = os.path.join(ORACLE, "lib", MACHINE)
 
-CU_SOURCES = ["gfm_flux.cu", "gfm_step.cu", "gfm_api.cu", "gfm_noalloc.cu", "gfm_batch.cu", "gfm_mlp.cu"]
+CU_SOURCES = ["gfm_flux.cu", "gfm_step.cu", "gfm_api.cu", "gfm_noalloc.cu", "gfm_batch.cu", "gfm_mlp.cu",
+              "gfm_output.cu"]
 CPP_SOURCES = ["gfm_cases.cpp"]
 HEADERS = ["gfm_math.cuh", "gfm_internal.cuh", "gfm_tables.h", "gfm_mlp.cuh"]
 

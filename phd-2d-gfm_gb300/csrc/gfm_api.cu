@@ -148,6 +148,7 @@ gfm_status_t last_error() {
 }  // namespace
 
 gfm_status_t gfm::validate_method(gfm_ctx* ctx, const gfm_method_desc* m) { return check_method(ctx, m); }
+double* gfm::mass_scratch(gfm_ctx* ctx) { return extra(ctx).mass_part; }
 gfm_status_t gfm::launch_status() { return last_error(); }
 
 extern "C" {

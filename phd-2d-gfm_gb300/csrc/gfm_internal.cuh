@@ -172,6 +172,7 @@ const float* mlp_params(const struct gfm_mlp* m);   // the network's FP32 parame
 // nsteps iterations of the time loop on ctx's stream (gfm_step, gfm_step_timed)
 gfm_status_t run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
 gfm_status_t validate_method(gfm_ctx* ctx, const gfm_method_desc* m);
+double* mass_scratch(gfm_ctx* ctx);   // 256 + 1 doubles of the mass reduction
 gfm_status_t launch_status();   // GFM_ERR_CUDA (and a message) if a launch failed
 
 }  // namespace gfm

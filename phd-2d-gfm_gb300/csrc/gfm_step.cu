@@ -1754,14 +1754,14 @@ __global__ void __launch_bounds__(256) k_reinit_iter(GridP P, const double* cur,
 // fluid mass (sim_twofluid::fluid_mass, sourcecode/sim_twofluid.cpp:1803-1827):
 // fixed-order two-pass sum
 // ---------------------------------------------------------------------------
-__global__ void k_mass_partial(GridP P, const double* U, const double* phi, double sign, double* part) {
+__global__ void k_mass_partial(GridP P, const double* U, const double* phi, int vof, double sign, double* part) {
   __shared__ double sh[256];
   double acc = 0.0;
   const int64_t n = (int64_t)P.Nx * P.Ny;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     int i = (int)(k / P.Nx) + P.g, j = (int)(k % P.Nx) + P.g;
     int64_t c = cidx(P, i, j);
-    double ls = phi ? phi[c] : -1.0;
+    double ls = phi ? (vof ? 0.5 - phi[c] : phi[c]) : -1.0;   // get_sdf
     if (sign * ls > 0.0) acc += U[c] * P.dx * P.dy;
   }
   sh[threadIdx.x] = acc;
@@ -2233,7 +2233,9 @@ void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out) {
   const GridP& P = ctx->P;
   int nb = 256;
   k_mass_partial<<<nb, 256, 0, ctx->stream>>>(P, sign < 0.0 ? ctx->U[0] : ctx->U[ctx->two_fluid ? 1 : 0],
-                                               ctx->two_fluid ? ctx->phi : nullptr, sign, part); counted();
+                                               ctx->two_fluid ? ctx->phi : nullptr,
+                                               (ctx->two_fluid && ctx->itm == GFM_ITM_VOF) ? 1 : 0, sign, part);
+  counted();
   k_mass_final<<<1, 32, 0, ctx->stream>>>(part, nb, out); counted();
 }
 

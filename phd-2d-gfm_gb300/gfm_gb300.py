@@ -121,6 +121,8 @@ def lib():
         "gfm_case_params": [ctypes.c_char_p, ctypes.c_char_p, I, I, ctypes.POINTER(GridDesc), pd],
         "gfm_case_init": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(GridDesc), pd, pd, pd],
         "gfm_case_init_z": [ctypes.c_char_p, ctypes.POINTER(GridDesc), pd],
+        "gfm_write_output_files": [ctypes.POINTER(GridDesc), ctypes.c_char_p, I, I, I, pd, pd, pd, pd],
+        "gfm_run_sim": [P, ctypes.POINTER(MethodDesc), ctypes.POINTER(GridDesc), ctypes.c_char_p, I, I, pd],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -509,20 +511,51 @@ class GFM_settingsfile:
         return self
 
 
+# params.output_freq of set_sim_parameters (sourcecode/sim_twofluid.cpp:347,392,404;
+# sourcecode/sim_onefluid.cpp:102)
+OUTPUT_FREQ_TWOFLUID = {"GDA": 0, "shocked_helium_bubble": 2}
+OUTPUT_FREQ_ONEFLUID = 10 ** 9
+
+
 class sim_base:
     def run_sim(self, SF):
         raise NotImplementedError
+
+    @staticmethod
+    def _run_with_output(ctx, m, desc, SF, output_freq):
+        """gfm_run_sim: the reference's loop with its output files under
+        SF.basename; returns the loop's wall time in seconds."""
+        secs = ctypes.c_double(0.0)
+        nsteps = SF.nsteps if SF.nsteps > 0 else 0
+        _check(lib().gfm_run_sim(ctx._p, ctypes.byref(m), ctypes.byref(desc), SF.basename.encode(), int(output_freq),
+                                 int(nsteps), ctypes.byref(secs)), "gfm_run_sim")
+        return secs.value
+
+
+def write_output_files(desc, basename, numsteps, U1, U2=None, field=None, vel=None, itm="LS5"):
+    """The files of one output of sim_twofluid / sim_onefluid from host
+    arrays (gfm_write_output_files)."""
+    two = U2 is not None
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (U1, U2, field, vel)]
+    _check(lib().gfm_write_output_files(ctypes.byref(desc), basename.encode(), int(two), ITM[itm][2],
+                                        int(numsteps), *[_dptr(a) if a is not None else None for a in arrs]),
+           "gfm_write_output_files")
 
 
 class sim_onefluid(sim_base):
     """sourcecode/sim_onefluid.cpp:12-64 on the GPU."""
 
-    def run_sim(self, SF, stream=None):
+    def run_sim(self, SF, stream=None, output=False):
+        """output: write the reference's files under SF.basename (gfm_run_sim)."""
         desc, T = case_params("onefluid", SF.test_case, SF.Nx, SF.Ny)
         U1, _, _ = case_init("onefluid", SF.test_case, desc)
         ctx = Context(desc, two_fluid=False, stream=stream)
         ctx.upload(U1)
         m = method(fs=SF.FS, CFL=SF.CFL, T=T)
+        if output:
+            self.seconds = self._run_with_output(ctx, m, desc, SF, OUTPUT_FREQ_ONEFLUID)
+            self.ctx = ctx
+            return ctx
         nsteps = SF.nsteps if SF.nsteps > 0 else 10 ** 9
         done = 0
         while done < nsteps:
@@ -539,7 +572,8 @@ class sim_onefluid(sim_base):
 class sim_twofluid(sim_base):
     """sourcecode/sim_twofluid.cpp:27-103 on the GPU."""
 
-    def run_sim(self, SF, stream=None):
+    def run_sim(self, SF, stream=None, output=False):
+        """output: write the reference's files under SF.basename (gfm_run_sim)."""
         desc, T = case_params("twofluid", SF.test_case, SF.Nx, SF.Ny)
         U1, U2, phi = case_init("twofluid", SF.test_case, desc)
         if ITM[SF.ITM][2] == ITM_VOF:   # the tracker's field is the volume fraction
@@ -548,6 +582,11 @@ class sim_twofluid(sim_base):
         ctx.upload(U1, U2, phi)
         m = method(fs=SF.FS, gfm=SF.GFM, itm=SF.ITM, CFL=SF.CFL, T=T, reinit_every=SF.reinit_every,
                    reinit_iters=SF.reinit_iters)
+        if output:
+            freq = OUTPUT_FREQ_TWOFLUID.get(SF.test_case, 4)
+            self.seconds = self._run_with_output(ctx, m, desc, SF, freq)
+            self.ctx = ctx
+            return ctx
         nsteps = SF.nsteps if SF.nsteps > 0 else 10 ** 9
         done = 0
         while done < nsteps:
