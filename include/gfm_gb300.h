@@ -41,6 +41,7 @@ typedef int gfm_status_t;
 #define GFM_ERR_CUDA 2       /* a CUDA runtime call failed */
 #define GFM_ERR_NUMERIC 3    /* the device status word holds a numeric fault */
 #define GFM_ERR_UNSUPPORTED 4
+#define GFM_ERR_IO 5         /* a file could not be read or written, or is not a valid checkpoint */
 
 /* boundary conditions (sim_info BC_L/R/B/T strings) */
 #define GFM_BC_TRANSMISSIVE 0
@@ -321,6 +322,26 @@ gfm_status_t gfm_writer_finish(gfm_writer* w);
 gfm_status_t gfm_writer_destroy(gfm_writer* w);
 gfm_status_t gfm_run_sim(gfm_ctx* ctx, const gfm_method_desc* m, const gfm_grid_desc* grid, const char* basename,
                          int output_freq, int max_steps, double* seconds);
+
+/* Checkpoint / resume (no counterpart in the reference).  A checkpoint holds
+ * the grid description, t, the step count and the padded grids U1 (U2 and
+ * the interface field for two fluids): everything later steps read, so a run
+ * resumed from it continues bit for bit as the uninterrupted run would.
+ * Format (little-endian): "GFMCKPT1", u32 version 1, u32 two_fluid, the grid
+ * description field by field (i32 Nx, Ny, numGC, BC_L, BC_R, BC_B, BC_T; f64
+ * x0, y0, dx, dy, gamma1, pinf1, gamma2, pinf2), f64 t, i32 numsteps, i32 0,
+ * u64 plane count, the planes (rows of Nx + 2 numGC doubles), u64 FNV-1a hash
+ * of everything before it.
+ *   gfm_checkpoint_save / _load  a context's state (load: same grid, same
+ *                                fluid count; GFM_ERR_IO for a bad file)
+ *   gfm_checkpoint_write / _read host arrays; _read with NULL arrays returns
+ *                                the header only */
+gfm_status_t gfm_checkpoint_save(gfm_ctx* ctx, const char* path);
+gfm_status_t gfm_checkpoint_load(gfm_ctx* ctx, const char* path);
+gfm_status_t gfm_checkpoint_write(const char* path, const gfm_grid_desc* grid, int two_fluid, double t, int numsteps,
+                                  const double* U1, const double* U2, const double* phi);
+gfm_status_t gfm_checkpoint_read(const char* path, gfm_grid_desc* grid, int* two_fluid, double* t, int* numsteps,
+                                 double* U1, double* U2, double* phi);
 
 /* volume fraction z of fluid 1 (one padded plane, layout of phi) of a named
  * two-fluid case, the initial field of the VOF interface tracker */

@@ -504,3 +504,175 @@ gfm_status_t gfm_run_sim(gfm_ctx* ctx, const gfm_method_desc* m, const gfm_grid_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// checkpoint / resume
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr char CKPT_MAGIC[8] = {'G', 'F', 'M', 'C', 'K', 'P', 'T', '1'};
+constexpr uint32_t CKPT_VERSION = 1;
+
+struct Fnv {
+  uint64_t h = 0xcbf29ce484222325ull;
+  void add(const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t k = 0; k < n; k++) { h ^= b[k]; h *= 0x100000001b3ull; }
+  }
+};
+
+struct Out {
+  FILE* f;
+  Fnv fnv;
+  bool ok = true;
+  void put(const void* p, size_t n) {
+    if (ok && fwrite(p, 1, n, f) != n) ok = false;
+    fnv.add(p, n);
+  }
+  template <class T> void val(T v) { put(&v, sizeof(T)); }
+};
+
+struct In {
+  FILE* f;
+  Fnv fnv;
+  bool ok = true;
+  void get(void* p, size_t n) {
+    if (ok && fread(p, 1, n, f) != n) ok = false;
+    if (ok) fnv.add(p, n);
+  }
+  template <class T> T val() { T v{}; get(&v, sizeof(T)); return v; }
+};
+
+bool same_grid(const gfm_grid_desc& a, const gfm_grid_desc& b) {
+  return a.Nx == b.Nx && a.Ny == b.Ny && a.numGC == b.numGC && a.BC_L == b.BC_L && a.BC_R == b.BC_R &&
+         a.BC_B == b.BC_B && a.BC_T == b.BC_T && a.x0 == b.x0 && a.y0 == b.y0 && a.dx == b.dx && a.dy == b.dy &&
+         a.gamma1 == b.gamma1 && a.pinf1 == b.pinf1 && a.gamma2 == b.gamma2 && a.pinf2 == b.pinf2;
+}
+
+gfm_grid_desc desc_of(const gfm_ctx* ctx) {
+  const gfm::GridP& P = ctx->P;
+  gfm_grid_desc d;
+  memset(&d, 0, sizeof(d));
+  d.Nx = P.Nx; d.Ny = P.Ny; d.numGC = P.g;
+  d.x0 = P.x0; d.y0 = P.y0; d.dx = P.dx; d.dy = P.dy;
+  d.BC_L = P.bcL; d.BC_R = P.bcR; d.BC_B = P.bcB; d.BC_T = P.bcT;
+  d.gamma1 = P.g1; d.pinf1 = P.p1; d.gamma2 = P.g2; d.pinf2 = P.p2;
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+gfm_status_t gfm_checkpoint_write(const char* path, const gfm_grid_desc* d, int two_fluid, double t, int numsteps,
+                                  const double* U1, const double* U2, const double* phi) {
+  if (!path || !d || !U1 || (two_fluid && (!U2 || !phi)) || d->Nx < 1 || d->Ny < 1 || d->numGC < 1)
+    return GFM_ERR_ARG;
+  FILE* f = fopen(path, "wb");
+  if (!f) return GFM_ERR_IO;
+  Out o{f};
+  o.put(CKPT_MAGIC, 8);
+  o.val<uint32_t>(CKPT_VERSION);
+  o.val<uint32_t>(two_fluid ? 1u : 0u);
+  for (int v : {d->Nx, d->Ny, d->numGC, d->BC_L, d->BC_R, d->BC_B, d->BC_T}) o.val<int32_t>(v);
+  for (double v : {d->x0, d->y0, d->dx, d->dy, d->gamma1, d->pinf1, d->gamma2, d->pinf2}) o.val<double>(v);
+  o.val<double>(t);
+  o.val<int32_t>(numsteps);
+  o.val<int32_t>(0);
+  const size_t plane = (size_t)(d->Ny + 2 * d->numGC) * (d->Nx + 2 * d->numGC);
+  const uint64_t nplanes = two_fluid ? 9 : 4;
+  o.val<uint64_t>(nplanes);
+  o.put(U1, sizeof(double) * 4 * plane);
+  if (two_fluid) {
+    o.put(U2, sizeof(double) * 4 * plane);
+    o.put(phi, sizeof(double) * plane);
+  }
+  const uint64_t h = o.fnv.h;
+  if (o.ok && fwrite(&h, sizeof(h), 1, f) != 1) o.ok = false;
+  if (fclose(f) != 0) o.ok = false;
+  return o.ok ? GFM_OK : GFM_ERR_IO;
+}
+
+gfm_status_t gfm_checkpoint_read(const char* path, gfm_grid_desc* d, int* two_fluid, double* t, int* numsteps,
+                                 double* U1, double* U2, double* phi) {
+  if (!path || !d) return GFM_ERR_ARG;
+  FILE* f = fopen(path, "rb");
+  if (!f) return GFM_ERR_IO;
+  In in{f};
+  char magic[8];
+  in.get(magic, 8);
+  const uint32_t version = in.val<uint32_t>(), two = in.val<uint32_t>();
+  gfm_grid_desc g;
+  memset(&g, 0, sizeof(g));
+  g.Nx = in.val<int32_t>(); g.Ny = in.val<int32_t>(); g.numGC = in.val<int32_t>();
+  g.BC_L = in.val<int32_t>(); g.BC_R = in.val<int32_t>(); g.BC_B = in.val<int32_t>(); g.BC_T = in.val<int32_t>();
+  g.x0 = in.val<double>(); g.y0 = in.val<double>(); g.dx = in.val<double>(); g.dy = in.val<double>();
+  g.gamma1 = in.val<double>(); g.pinf1 = in.val<double>(); g.gamma2 = in.val<double>(); g.pinf2 = in.val<double>();
+  const double tt = in.val<double>();
+  const int32_t ns = in.val<int32_t>();
+  in.val<int32_t>();
+  const uint64_t nplanes = in.val<uint64_t>();
+  bool ok = in.ok && memcmp(magic, CKPT_MAGIC, 8) == 0 && version == CKPT_VERSION && two <= 1 &&
+            nplanes == (two ? 9u : 4u) && g.Nx > 0 && g.Ny > 0 && g.numGC > 0 && g.Nx < (1 << 20) &&
+            g.Ny < (1 << 20) && g.numGC < 64;
+  if (ok && (U1 || U2 || phi)) {
+    const size_t plane = (size_t)(g.Ny + 2 * g.numGC) * (g.Nx + 2 * g.numGC);
+    std::vector<double> buf(nplanes * plane);
+    in.get(buf.data(), sizeof(double) * buf.size());
+    uint64_t h = 0;
+    ok = in.ok && fread(&h, sizeof(h), 1, f) == 1 && h == in.fnv.h;
+    if (ok) {
+      if (U1) memcpy(U1, buf.data(), sizeof(double) * 4 * plane);
+      if (two && U2) memcpy(U2, buf.data() + 4 * plane, sizeof(double) * 4 * plane);
+      if (two && phi) memcpy(phi, buf.data() + 8 * plane, sizeof(double) * plane);
+    }
+  }
+  fclose(f);
+  if (!ok) return GFM_ERR_IO;
+  *d = g;
+  if (two_fluid) *two_fluid = (int)two;
+  if (t) *t = tt;
+  if (numsteps) *numsteps = ns;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_checkpoint_save(gfm_ctx* ctx, const char* path) {
+  if (!ctx || !path) return GFM_ERR_ARG;
+  const gfm_grid_desc d = desc_of(ctx);
+  const size_t plane = (size_t)ctx->P.nr * ctx->P.nc;
+  std::vector<double> U1(4 * plane), U2, phi;
+  gfm_status_t r = gfm_download(ctx, 1, U1.data());
+  if (r == GFM_OK && ctx->two_fluid) {
+    U2.resize(4 * plane);
+    phi.resize(plane);
+    r = gfm_download(ctx, 2, U2.data());
+    if (r == GFM_OK) r = gfm_download_phi(ctx, phi.data());
+  }
+  double t = 0.0, dt = 0.0;
+  int n = 0;
+  if (r == GFM_OK) r = gfm_get_time(ctx, &t, &n, &dt);
+  if (r != GFM_OK) return r;
+  return gfm_checkpoint_write(path, &d, ctx->two_fluid, t, n, U1.data(), ctx->two_fluid ? U2.data() : nullptr,
+                              ctx->two_fluid ? phi.data() : nullptr);
+}
+
+gfm_status_t gfm_checkpoint_load(gfm_ctx* ctx, const char* path) {
+  if (!ctx || !path) return GFM_ERR_ARG;
+  gfm_grid_desc d;
+  int two = 0, n = 0;
+  double t = 0.0;
+  gfm_status_t r = gfm_checkpoint_read(path, &d, &two, &t, &n, nullptr, nullptr, nullptr);
+  if (r != GFM_OK) return r;
+  if (!same_grid(d, desc_of(ctx)) || two != ctx->two_fluid) return GFM_ERR_ARG;
+  const size_t plane = (size_t)ctx->P.nr * ctx->P.nc;
+  std::vector<double> U1(4 * plane), U2(two ? 4 * plane : 0), phi(two ? plane : 0);
+  r = gfm_checkpoint_read(path, &d, &two, &t, &n, U1.data(), two ? U2.data() : nullptr, two ? phi.data() : nullptr);
+  if (r != GFM_OK) return r;
+  r = gfm_upload(ctx, 1, U1.data());
+  if (r == GFM_OK && two) r = gfm_upload(ctx, 2, U2.data());
+  if (r == GFM_OK && two) r = gfm_upload_phi(ctx, phi.data());
+  if (r == GFM_OK) r = gfm_set_time(ctx, t, n);
+  return r;
+}
+
+}  // extern "C"

@@ -123,6 +123,10 @@ def lib():
         "gfm_case_init_z": [ctypes.c_char_p, ctypes.POINTER(GridDesc), pd],
         "gfm_write_output_files": [ctypes.POINTER(GridDesc), ctypes.c_char_p, I, I, I, pd, pd, pd, pd],
         "gfm_run_sim": [P, ctypes.POINTER(MethodDesc), ctypes.POINTER(GridDesc), ctypes.c_char_p, I, I, pd],
+        "gfm_checkpoint_save": [P, ctypes.c_char_p], "gfm_checkpoint_load": [P, ctypes.c_char_p],
+        "gfm_checkpoint_write": [ctypes.c_char_p, ctypes.POINTER(GridDesc), I, D, I, pd, pd, pd],
+        "gfm_checkpoint_read": [ctypes.c_char_p, ctypes.POINTER(GridDesc), ctypes.POINTER(I), pd, ctypes.POINTER(I),
+                                pd, pd, pd],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -282,6 +286,14 @@ class Context:
 
     def clear_status(self):
         _check(lib().gfm_clear_device_status(self._p), "gfm_clear_device_status")
+
+    def save_checkpoint(self, path):
+        """gfm_checkpoint_save: grids, interface field, t and step count."""
+        _check(lib().gfm_checkpoint_save(self._p, str(path).encode()), "gfm_checkpoint_save")
+
+    def load_checkpoint(self, path):
+        """gfm_checkpoint_load: the state of a checkpoint of the same grid."""
+        _check(lib().gfm_checkpoint_load(self._p, str(path).encode()), "gfm_checkpoint_load")
 
     def velocity(self):
         """The velocity field (2, nr, nc) of the last ghost fill."""
@@ -530,6 +542,33 @@ class sim_base:
         _check(lib().gfm_run_sim(ctx._p, ctypes.byref(m), ctypes.byref(desc), SF.basename.encode(), int(output_freq),
                                  int(nsteps), ctypes.byref(secs)), "gfm_run_sim")
         return secs.value
+
+
+def checkpoint_write(path, desc, t, numsteps, U1, U2=None, phi=None):
+    """gfm_checkpoint_write from host arrays."""
+    two = U2 is not None
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (U1, U2, phi)]
+    _check(lib().gfm_checkpoint_write(str(path).encode(), ctypes.byref(desc), int(two), float(t), int(numsteps),
+                                      *[_dptr(a) if a is not None else None for a in arrs]),
+           "gfm_checkpoint_write")
+
+
+def checkpoint_read(path):
+    """gfm_checkpoint_read: (desc, t, numsteps, U1, U2 or None, phi or None)."""
+    d = GridDesc()
+    two, ns = ctypes.c_int(0), ctypes.c_int(0)
+    t = ctypes.c_double(0.0)
+    L = lib()
+    _check(L.gfm_checkpoint_read(str(path).encode(), ctypes.byref(d), ctypes.byref(two), ctypes.byref(t),
+                                 ctypes.byref(ns), None, None, None), "gfm_checkpoint_read")
+    nr, nc = d.shape
+    U1 = np.empty((4, nr, nc))
+    U2 = np.empty((4, nr, nc)) if two.value else None
+    phi = np.empty((nr, nc)) if two.value else None
+    _check(L.gfm_checkpoint_read(str(path).encode(), ctypes.byref(d), ctypes.byref(two), ctypes.byref(t),
+                                 ctypes.byref(ns), _dptr(U1), _dptr(U2) if U2 is not None else None,
+                                 _dptr(phi) if phi is not None else None), "gfm_checkpoint_read")
+    return d, t.value, ns.value, U1, U2, phi
 
 
 def write_output_files(desc, basename, numsteps, U1, U2=None, field=None, vel=None, itm="LS5"):
