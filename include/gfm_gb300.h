@@ -353,6 +353,15 @@ typedef struct {
 gfm_status_t gfm_case_shock_bubble(const gfm_bubble_params* p, int Nx, int Ny, gfm_grid_desc* grid, double* T);
 gfm_status_t gfm_case_init_shock_bubble(const gfm_bubble_params* p, const gfm_grid_desc* grid, double* U1,
                                         double* U2, double* phi);
+/* its volume fraction of fluid 1 (10x10 sub-sampled area fractions) */
+gfm_status_t gfm_case_init_shock_bubble_z(const gfm_bubble_params* p, const gfm_grid_desc* grid, double* z);
+/* Initial conditions written on the device into a context's grids (and phi,
+ * or z for itm = GFM_ITM_VOF), time and step count reset: no host set-up or
+ * upload.  Bit-identical to gfm_case_init / _z / gfm_case_init_shock_bubble,
+ * except GDA's Gaussian density (exp from this library on the device, from
+ * the C library on the host: within 1 ulp). */
+gfm_status_t gfm_case_init_device(gfm_ctx* ctx, const char* sim_type, const char* test_case, int itm);
+gfm_status_t gfm_case_init_shock_bubble_device(gfm_ctx* ctx, const gfm_bubble_params* p, int itm);
 
 /* One-fluid time steps for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library.

@@ -13,9 +13,10 @@
 #include <cstring>
 #include <string>
 #include <vector>
-#include "gfm_math.cuh"
+#include "gfm_cases.cuh"
 #include "../../include/gfm_gb300.h"
 
+using gfm::CaseSpec;
 using gfm::V4;
 
 namespace {
@@ -81,21 +82,6 @@ void host_bcs(const gfm_grid_desc* d, double* U) {
     }
 }
 
-// fraction of 10x10 sub-samples of cell (i,j) within radius R of (cx, cy)
-double area_fraction(const Geo& G, int i, int j, double cx, double cy, double R) {
-  const int N = 10;
-  int inside = 0;
-  double delx = G.dx / N, dely = G.dy / N;
-  double blx = G.ccx(j) - 0.5 * G.dx, bly = G.ccy(i) - 0.5 * G.dy;
-  for (int a = 0; a < N; a++)
-    for (int b = 0; b < N; b++) {
-      double sx = blx + (a + 0.5) * delx - cx;
-      double sy = bly + (b + 0.5) * dely - cy;
-      if (std::sqrt(sx * sx + sy * sy) <= R) inside++;
-    }
-  return double(inside) / (N * N);
-}
-
 void base_desc(gfm_grid_desc* d, int Nx, int Ny, int g) {
   memset(d, 0, sizeof(*d));
   d->Nx = Nx; d->Ny = Ny; d->numGC = g;
@@ -115,7 +101,128 @@ void post_shock(double g, double M, double rho1, double p1, double& rho2, double
   u2 = -W * (1.0 - rho1 / rho2);
 }
 
+gfm::CaseGeo case_geo(const Geo& G) {
+  gfm::CaseGeo C;
+  C.Nx = G.Nx; C.Ny = G.Ny; C.g = G.g; C.nr = G.nr; C.nc = G.nc;
+  C.x0 = G.x0; C.y0 = G.y0; C.dx = G.dx; C.dy = G.dy;
+  return C;
+}
+
+// every padded cell from the case's spec, then apply_BCs_euler on the grids
+void fill_case(const CaseSpec& cs, const gfm_grid_desc* d, bool two, double* U1, double* U2, double* phi, double* z) {
+  Geo G = geo_of(d);
+  const gfm::CaseGeo C = case_geo(G);
+  for (int i = 0; i < G.nr; i++)
+    for (int j = 0; j < G.nc; j++) {
+      V4 u1, u2 = V4{0.0, 0.0, 0.0, 0.0};
+      double ph = 0.0, zz = 0.0;
+      gfm::case_cell(cs, C, i, j, z != nullptr, u1, u2, ph, zz);
+      put(G, U1, i, j, u1);
+      if (two) {
+        put(G, U2, i, j, u2);
+        phi[(size_t)i * G.nc + j] = ph;
+        if (z) z[(size_t)i * G.nc + j] = zz;
+      }
+    }
+  host_bcs(d, U1);
+  if (two) host_bcs(d, U2);
+}
+
 }  // namespace
+
+namespace gfm {
+
+// The parameters of a named case (set_sim_ICs, sourcecode/sim_twofluid.cpp:599-1799,
+// sourcecode/sim_onefluid.cpp:196-449, and the workloads of this build).
+bool make_case_spec(const char* sim_type, const char* test_case, const gfm_grid_desc* d, CaseSpec* out) {
+  std::string st(sim_type), tc(test_case);
+  const double g1 = d->gamma1, q1 = d->pinf1, g2 = d->gamma2, q2 = d->pinf2;
+  CaseSpec c;
+  memset(&c, 0, sizeof(c));
+  c.g1 = g1; c.q1 = q1; c.g2 = g2; c.q2 = q2;
+  c.xsplit = INFINITY;
+  if (st == "onefluid") {
+    bool ydir = tc.size() > 2 && tc.substr(tc.size() - 2) == "_y";
+    c.kind = gfm::CASE_PLANAR;
+    c.pa = ydir ? 0.0 : 1.0; c.pb = ydir ? 1.0 : 0.0; c.pc = 0.5;
+    if (tc == "TTC1_x" || tc == "TTC1_y") { c.L = p2c(g1, q1, 1.0, 0, 0, 1.0); c.R = p2c(g1, q1, 0.125, 0, 0, 0.1); }
+    else if (tc == "TTC2_x") { c.L = p2c(g1, q1, 1.0, -2.0, 0, 0.4); c.R = p2c(g1, q1, 1.0, 2.0, 0, 0.4); }
+    else if (tc == "TTC2_y") { c.L = p2c(g1, q1, 1.0, 0, -2.0, 0.4); c.R = p2c(g1, q1, 1.0, 0, 2.0, 0.4); }
+    else if (tc == "TTC3_x" || tc == "TTC3_y") { c.L = p2c(g1, q1, 1.0, 0, 0, 1000.0); c.R = p2c(g1, q1, 1.0, 0, 0, 0.01); }
+    else if (tc == "TTC4_x" || tc == "TTC4_y") { c.L = p2c(g1, q1, 1.0, 0, 0, 0.1); c.R = p2c(g1, q1, 1.0, 0, 0, 100.0); }
+    else if (tc == "TTC5_x") {
+      c.L = p2c(g1, q1, 5.99924, 19.5975, 0, 460.894); c.R = p2c(g1, q1, 5.99242, -6.19633, 0, 46.0950);
+    } else if (tc == "TTC5_y") {
+      c.L = p2c(g1, q1, 5.99924, 0, 19.5975, 460.894); c.R = p2c(g1, q1, 5.99242, 0, -6.19633, 46.0950);
+    } else if (tc == "circularexplosion") {
+      // sourcecode/sim_onefluid.cpp:359-415: primitives blended by area fraction
+      c.kind = gfm::CASE_BLEND_CIRCLE;
+      c.L = V4{1.0, 0.0, 0.0, 1.0}; c.R = V4{0.125, 0.0, 0.0, 0.1};
+      c.cx = 1.0; c.cy = 1.0; c.r = 0.4;
+    } else {
+      return false;
+    }
+    *out = c;
+    return true;
+  }
+  if (st != "twofluid") return false;
+  c.kind = gfm::CASE_CIRCLE;
+  if (tc == "circularexplosion") {
+    c.s1 = p2c(g1, q1, 1.0, 0, 0, 1.0); c.s2a = c.s2b = p2c(g2, q2, 0.125, 0, 0, 0.1);
+    c.cx = 1.0; c.cy = 1.0; c.r = 0.4;
+  } else if (tc == "ST1_x") {
+    c.kind = gfm::CASE_PLANE_X; c.c = 0.5;
+    c.s1 = p2c(g1, q1, 1.0, 0, 0, 100000.0); c.s2a = c.s2b = p2c(g2, q2, 0.125, 0, 0, 10000.0);
+  } else if (tc == "ST2_y") {
+    c.kind = gfm::CASE_PLANE_Y; c.c = 0.7;
+    c.s1 = p2c(g1, q1, 1000.0, 0, 0, 1000000000.0); c.s2a = c.s2b = p2c(g2, q2, 50.0, 0, 0, 100000.0);
+  } else if (tc == "GDA") {
+    c.kind = gfm::CASE_GDA;
+  } else if (tc == "shocked_helium_bubble") {
+    c.s1 = p2c(g1, q1, 0.138, 0, 0, 1.0);
+    c.s2a = p2c(g2, q2, 1.0, 0, 0, 1.0); c.s2b = p2c(g2, q2, 1.3764, -0.394, 0, 1.5698); c.xsplit = 225.0;
+    c.cx = 175.0; c.cy = 44.5; c.r = 25.0;
+  } else if (tc == "shocked_R22_bubble") {
+    c.s1 = p2c(g1, q1, 3.863, 0, 0, 1.01325e5);
+    c.s2a = p2c(g2, q2, 1.225, 0, 0, 1.01325e5); c.s2b = p2c(g2, q2, 1.686, -113.5, 0, 1.59e5); c.xsplit = 0.275;
+    c.cx = 0.225; c.cy = 0.0445; c.r = 0.025;
+  } else if (tc == "shock_bubble") {
+    // light-gas bubble (fluid 1) hit by a Mach 1.22 shock in air (fluid 2)
+    double rho2, u2, p2;
+    post_shock(g2, 1.22, 1.0, 1e5, rho2, u2, p2);
+    c.s1 = p2c(g1, q1, 0.182, 0, 0, 1e5);
+    c.s2a = p2c(g2, q2, 1.0, 0, 0, 1e5); c.s2b = p2c(g2, q2, rho2, u2, 0, p2); c.xsplit = 0.225;
+    c.cx = 0.175; c.cy = 0.0445; c.r = 0.025;
+  } else if (tc == "underwater_explosion_sg") {
+    // high-pressure air bubble (fluid 1) in stiffened-gas water (fluid 2)
+    c.s1 = p2c(g1, q1, 1270.0, 0, 0, 8.29e8); c.s2a = c.s2b = p2c(g2, q2, 1000.0, 0, 0, 1e5);
+    c.cx = 0.0; c.cy = 0.0; c.r = 0.2;
+  } else {
+    return false;
+  }
+  *out = c;
+  return true;
+}
+
+// Shock-bubble family of the batched workload (gfm_case_shock_bubble's grids)
+bool make_bubble_spec(const gfm_bubble_params* p, const gfm_grid_desc* d, CaseSpec* out) {
+  CaseSpec c;
+  memset(&c, 0, sizeof(c));
+  const double W = d->dx * d->Nx, H = d->dy * d->Ny;
+  double rho2, u2, p2;
+  post_shock(d->gamma2, p->mach, 1.0, 1e5, rho2, u2, p2);
+  c.kind = gfm::CASE_CIRCLE;
+  c.g1 = d->gamma1; c.q1 = d->pinf1; c.g2 = d->gamma2; c.q2 = d->pinf2;
+  c.s1 = p2c(d->gamma1, d->pinf1, p->rho_ratio, 0, 0, 1e5);
+  c.s2a = p2c(d->gamma2, d->pinf2, 1.0, 0, 0, 1e5);
+  c.s2b = p2c(d->gamma2, d->pinf2, rho2, u2, 0, p2);
+  c.xsplit = 0.9 * W;
+  c.cx = 0.7 * W; c.cy = 0.5 * H; c.r = p->radius_frac * H;
+  *out = c;
+  return true;
+}
+
+}  // namespace gfm
 
 extern "C" {
 
@@ -169,110 +276,11 @@ gfm_status_t gfm_case_params(const char* sim_type, const char* test_case, int Nx
 gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gfm_grid_desc* d, double* U1,
                            double* U2, double* phi) {
   if (!sim_type || !test_case || !d || !U1) return GFM_ERR_ARG;
-  std::string st(sim_type), tc(test_case);
-  Geo G = geo_of(d);
-  const double g1 = d->gamma1, q1 = d->pinf1, g2 = d->gamma2, q2 = d->pinf2;
-  if (st == "onefluid") {
-    auto planar = [&](V4 Lst, V4 Rst, double a, double b, double c) {
-      for (int i = 0; i < G.nr; i++)
-        for (int j = 0; j < G.nc; j++) put(G, U1, i, j, (G.ccx(j) * a + G.ccy(i) * b <= c) ? Lst : Rst);
-    };
-    bool ydir = tc.size() > 2 && tc.substr(tc.size() - 2) == "_y";
-    double a = ydir ? 0.0 : 1.0, b = ydir ? 1.0 : 0.0;
-    if (tc == "TTC1_x" || tc == "TTC1_y") planar(p2c(g1, q1, 1.0, 0, 0, 1.0), p2c(g1, q1, 0.125, 0, 0, 0.1), a, b, 0.5);
-    else if (tc == "TTC2_x") planar(p2c(g1, q1, 1.0, -2.0, 0, 0.4), p2c(g1, q1, 1.0, 2.0, 0, 0.4), 1.0, 0.0, 0.5);
-    else if (tc == "TTC2_y") planar(p2c(g1, q1, 1.0, 0, -2.0, 0.4), p2c(g1, q1, 1.0, 0, 2.0, 0.4), 0.0, 1.0, 0.5);
-    else if (tc == "TTC3_x" || tc == "TTC3_y")
-      planar(p2c(g1, q1, 1.0, 0, 0, 1000.0), p2c(g1, q1, 1.0, 0, 0, 0.01), a, b, 0.5);
-    else if (tc == "TTC4_x" || tc == "TTC4_y")
-      planar(p2c(g1, q1, 1.0, 0, 0, 0.1), p2c(g1, q1, 1.0, 0, 0, 100.0), a, b, 0.5);
-    else if (tc == "TTC5_x")
-      planar(p2c(g1, q1, 5.99924, 19.5975, 0, 460.894), p2c(g1, q1, 5.99242, -6.19633, 0, 46.0950), 1.0, 0.0, 0.5);
-    else if (tc == "TTC5_y")
-      planar(p2c(g1, q1, 5.99924, 0, 19.5975, 460.894), p2c(g1, q1, 5.99242, 0, -6.19633, 46.0950), 0.0, 1.0, 0.5);
-    else if (tc == "circularexplosion") {
-      // sourcecode/sim_onefluid.cpp:359-415
-      const double L[4] = {1.0, 0.0, 0.0, 1.0}, R[4] = {0.125, 0.0, 0.0, 0.1};
-      for (int i = 0; i < G.nr; i++)
-        for (int j = 0; j < G.nc; j++) {
-          double frac = area_fraction(G, i, j, 1.0, 1.0, 0.4);
-          double W[4];
-          for (int k = 0; k < 4; k++) W[k] = frac * L[k] + (1.0 - frac) * R[k];
-          put(G, U1, i, j, p2c(g1, q1, W[0], W[1], W[2], W[3]));
-        }
-    } else {
-      return GFM_ERR_ARG;
-    }
-    host_bcs(d, U1);
-    return GFM_OK;
-  }
-  if (st != "twofluid" || !U2 || !phi) return GFM_ERR_ARG;
-  auto fill = [&](auto&& f) {
-    for (int i = 0; i < G.nr; i++)
-      for (int j = 0; j < G.nc; j++) {
-        V4 s1, s2;
-        double ls;
-        f(i, j, G.ccx(j), G.ccy(i), s1, s2, ls);
-        put(G, U1, i, j, s1);
-        put(G, U2, i, j, s2);
-        phi[(size_t)i * G.nc + j] = ls;
-      }
-  };
-  if (tc == "circularexplosion") {
-    V4 Ls = p2c(g1, q1, 1.0, 0, 0, 1.0), Rs = p2c(g2, q2, 0.125, 0, 0, 0.1);
-    fill([&](int, int, double x, double y, V4& a, V4& b, double& ls) {
-      ls = std::sqrt((x - 1.0) * (x - 1.0) + (y - 1.0) * (y - 1.0)) - 0.4;
-      a = Ls; b = Rs;
-    });
-  } else if (tc == "ST1_x") {
-    V4 Ls = p2c(g1, q1, 1.0, 0, 0, 100000.0), Rs = p2c(g2, q2, 0.125, 0, 0, 10000.0);
-    fill([&](int, int, double x, double, V4& a, V4& b, double& ls) { ls = x - 0.5; a = Ls; b = Rs; });
-  } else if (tc == "ST2_y") {
-    V4 Ls = p2c(g1, q1, 1000.0, 0, 0, 1000000000.0), Rs = p2c(g2, q2, 50.0, 0, 0, 100000.0);
-    fill([&](int, int, double, double y, V4& a, V4& b, double& ls) { ls = y - 0.7; a = Ls; b = Rs; });
-  } else if (tc == "GDA") {
-    fill([&](int, int, double x, double y, V4& a, V4& b, double& ls) {
-      double r2 = (x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5);
-      V4 s = p2c(g1, q1, 1.0 + 1000.0 * std::exp(-r2 / (2.0 * 0.1 * 0.1)), 1.0, 1.0, 0.0001);
-      a = s; b = s; ls = -1.0;
-    });
-  } else if (tc == "shocked_helium_bubble") {
-    V4 he = p2c(g1, q1, 0.138, 0, 0, 1.0);
-    V4 Ls = p2c(g2, q2, 1.3764, -0.394, 0, 1.5698), Rs = p2c(g2, q2, 1.0, 0, 0, 1.0);
-    fill([&](int, int, double x, double y, V4& a, V4& b, double& ls) {
-      b = (x < 225.0) ? Rs : Ls;
-      a = he;
-      ls = std::sqrt((x - 175.0) * (x - 175.0) + (y - 44.5) * (y - 44.5)) - 25.0;
-    });
-  } else if (tc == "shocked_R22_bubble") {
-    V4 r22 = p2c(g1, q1, 3.863, 0, 0, 1.01325e5);
-    V4 Ls = p2c(g2, q2, 1.686, -113.5, 0, 1.59e5), Rs = p2c(g2, q2, 1.225, 0, 0, 1.01325e5);
-    fill([&](int, int, double x, double y, V4& a, V4& b, double& ls) {
-      b = (x < 0.275) ? Rs : Ls;
-      a = r22;
-      ls = std::sqrt((x - 0.225) * (x - 0.225) + (y - 0.0445) * (y - 0.0445)) - 0.025;
-    });
-  } else if (tc == "shock_bubble") {
-    double rho2, u2, p2;
-    post_shock(g2, 1.22, 1.0, 1e5, rho2, u2, p2);
-    V4 bub = p2c(g1, q1, 0.182, 0, 0, 1e5);
-    V4 pre = p2c(g2, q2, 1.0, 0, 0, 1e5), post = p2c(g2, q2, rho2, u2, 0, p2);
-    fill([&](int, int, double x, double y, V4& a, V4& b, double& ls) {
-      b = (x < 0.225) ? pre : post;
-      a = bub;
-      ls = std::sqrt((x - 0.175) * (x - 0.175) + (y - 0.0445) * (y - 0.0445)) - 0.025;
-    });
-  } else if (tc == "underwater_explosion_sg") {
-    V4 air = p2c(g1, q1, 1270.0, 0, 0, 8.29e8), water = p2c(g2, q2, 1000.0, 0, 0, 1e5);
-    fill([&](int, int, double x, double y, V4& a, V4& b, double& ls) {
-      a = air; b = water;
-      ls = std::sqrt(x * x + y * y) - 0.2;
-    });
-  } else {
-    return GFM_ERR_ARG;
-  }
-  host_bcs(d, U1);
-  host_bcs(d, U2);
+  CaseSpec cs;
+  if (!gfm::make_case_spec(sim_type, test_case, d, &cs)) return GFM_ERR_ARG;
+  const bool two = std::string(sim_type) == "twofluid";
+  if (two && (!U2 || !phi)) return GFM_ERR_ARG;
+  fill_case(cs, d, two, U1, U2, phi, nullptr);
   return GFM_OK;
 }
 
@@ -282,23 +290,16 @@ gfm_status_t gfm_case_init(const char* sim_type, const char* test_case, const gf
 // the planar tubes, :697,731; z = 1 for GDA, :769).
 gfm_status_t gfm_case_init_z(const char* test_case, const gfm_grid_desc* d, double* z) {
   if (!test_case || !d || !z) return GFM_ERR_ARG;
-  std::string tc(test_case);
+  CaseSpec cs;
+  if (!gfm::make_case_spec("twofluid", test_case, d, &cs)) return GFM_ERR_ARG;
   Geo G = geo_of(d);
-  auto clip01 = [](double v) { return std::min(1.0, std::max(0.0, v)); };
+  const gfm::CaseGeo C = case_geo(G);
   for (int i = 0; i < G.nr; i++)
     for (int j = 0; j < G.nc; j++) {
-      const double x = G.ccx(j), y = G.ccy(i);
-      double v;
-      if (tc == "circularexplosion") v = area_fraction(G, i, j, 1.0, 1.0, 0.4);
-      else if (tc == "ST1_x") v = clip01((0.5 - x + 0.5 * G.dx) / G.dx);
-      else if (tc == "ST2_y") v = clip01((0.7 - y + 0.5 * G.dy) / G.dy);
-      else if (tc == "GDA") v = 1.0;
-      else if (tc == "shocked_helium_bubble") v = area_fraction(G, i, j, 175.0, 44.5, 25.0);
-      else if (tc == "shocked_R22_bubble") v = area_fraction(G, i, j, 0.225, 0.0445, 0.025);
-      else if (tc == "shock_bubble") v = area_fraction(G, i, j, 0.175, 0.0445, 0.025);
-      else if (tc == "underwater_explosion_sg") v = area_fraction(G, i, j, 0.0, 0.0, 0.2);
-      else return GFM_ERR_ARG;
-      z[(size_t)i * G.nc + j] = v;
+      V4 u1, u2;
+      double ph, zz;
+      gfm::case_cell(cs, C, i, j, true, u1, u2, ph, zz);
+      z[(size_t)i * G.nc + j] = zz;
     }
   return GFM_OK;
 }
@@ -326,22 +327,25 @@ gfm_status_t gfm_case_shock_bubble(const gfm_bubble_params* p, int Nx, int Ny, g
 gfm_status_t gfm_case_init_shock_bubble(const gfm_bubble_params* p, const gfm_grid_desc* d, double* U1, double* U2,
                                         double* phi) {
   if (!p || !d || !U1 || !U2 || !phi) return GFM_ERR_ARG;
+  CaseSpec cs;
+  if (!gfm::make_bubble_spec(p, d, &cs)) return GFM_ERR_ARG;
+  fill_case(cs, d, true, U1, U2, phi, nullptr);
+  return GFM_OK;
+}
+
+gfm_status_t gfm_case_init_shock_bubble_z(const gfm_bubble_params* p, const gfm_grid_desc* d, double* z) {
+  if (!p || !d || !z) return GFM_ERR_ARG;
+  CaseSpec cs;
+  if (!gfm::make_bubble_spec(p, d, &cs)) return GFM_ERR_ARG;
   Geo G = geo_of(d);
-  const double W = d->dx * d->Nx, H = d->dy * d->Ny;
-  const double xc = 0.7 * W, yc = 0.5 * H, r = p->radius_frac * H, xs = 0.9 * W;
-  double rho2, u2, p2;
-  post_shock(d->gamma2, p->mach, 1.0, 1e5, rho2, u2, p2);
-  const V4 bub = p2c(d->gamma1, d->pinf1, p->rho_ratio, 0, 0, 1e5);
-  const V4 pre = p2c(d->gamma2, d->pinf2, 1.0, 0, 0, 1e5), post = p2c(d->gamma2, d->pinf2, rho2, u2, 0, p2);
+  const gfm::CaseGeo C = case_geo(G);
   for (int i = 0; i < G.nr; i++)
     for (int j = 0; j < G.nc; j++) {
-      const double x = G.ccx(j), y = G.ccy(i);
-      put(G, U1, i, j, bub);
-      put(G, U2, i, j, (x < xs) ? pre : post);
-      phi[(size_t)i * G.nc + j] = std::sqrt((x - xc) * (x - xc) + (y - yc) * (y - yc)) - r;
+      V4 u1, u2;
+      double ph, zz;
+      gfm::case_cell(cs, C, i, j, true, u1, u2, ph, zz);
+      z[(size_t)i * G.nc + j] = zz;
     }
-  host_bcs(d, U1);
-  host_bcs(d, U2);
   return GFM_OK;
 }
 

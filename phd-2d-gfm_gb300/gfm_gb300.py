@@ -121,6 +121,9 @@ def lib():
         "gfm_case_params": [ctypes.c_char_p, ctypes.c_char_p, I, I, ctypes.POINTER(GridDesc), pd],
         "gfm_case_init": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(GridDesc), pd, pd, pd],
         "gfm_case_init_z": [ctypes.c_char_p, ctypes.POINTER(GridDesc), pd],
+        "gfm_case_init_shock_bubble_z": [V, ctypes.POINTER(GridDesc), pd],
+        "gfm_case_init_device": [P, ctypes.c_char_p, ctypes.c_char_p, I],
+        "gfm_case_init_shock_bubble_device": [P, V, I],
         "gfm_write_output_files": [ctypes.POINTER(GridDesc), ctypes.c_char_p, I, I, I, pd, pd, pd, pd],
         "gfm_run_sim": [P, ctypes.POINTER(MethodDesc), ctypes.POINTER(GridDesc), ctypes.c_char_p, I, I, pd],
         "gfm_checkpoint_save": [P, ctypes.c_char_p], "gfm_checkpoint_load": [P, ctypes.c_char_p],
@@ -287,6 +290,16 @@ class Context:
     def clear_status(self):
         _check(lib().gfm_clear_device_status(self._p), "gfm_clear_device_status")
 
+    def init_device(self, sim_type, test_case, itm="LS5"):
+        """The named case's initial state generated on the device (gfm_case_init_device)."""
+        _check(lib().gfm_case_init_device(self._p, sim_type.encode(), test_case.encode(), ITM[itm][2]),
+               "gfm_case_init_device")
+
+    def init_shock_bubble_device(self, params, itm="LS5"):
+        """A shock-bubble family member generated on the device."""
+        _check(lib().gfm_case_init_shock_bubble_device(self._p, ctypes.byref(params), ITM[itm][2]),
+               "gfm_case_init_shock_bubble_device")
+
     def save_checkpoint(self, path):
         """gfm_checkpoint_save: grids, interface field, t and step count."""
         _check(lib().gfm_checkpoint_save(self._p, str(path).encode()), "gfm_checkpoint_save")
@@ -411,6 +424,16 @@ def shock_bubble_case(Nx, Ny, mach, gamma_bubble, rho_ratio, radius_frac):
     _check(lib().gfm_case_init_shock_bubble(ctypes.byref(p), ctypes.byref(d), _dptr(U1), _dptr(U2), _dptr(phi)),
            "gfm_case_init_shock_bubble")
     return d, T.value, U1, U2, phi
+
+
+def shock_bubble_case_z(d, mach, gamma_bubble, rho_ratio, radius_frac):
+    """The family member's volume fraction of fluid 1 (gfm_case_init_shock_bubble_z)."""
+    p = BubbleParams(mach, gamma_bubble, rho_ratio, radius_frac)
+    nr, nc = d.shape
+    z = np.empty((nr, nc))
+    _check(lib().gfm_case_init_shock_bubble_z(ctypes.byref(p), ctypes.byref(d), _dptr(z)),
+           "gfm_case_init_shock_bubble_z")
+    return z
 
 
 # ---------------------------------------------------------------------------
