@@ -322,16 +322,12 @@ def run_gfm(args):
         n_e2e = args.steps if args.e2e_steps < 0 else min(args.e2e_steps, args.steps)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        up = (pd(hU1), pd(hU2), pd(hphi)) if two else (pd(hU1), None, None)
         for s in range(n_e2e):
-            L.gfm_upload(ctx._p, 1, pd(hU1))
-            if two:
-                L.gfm_upload(ctx._p, 2, pd(hU2))
-                L.gfm_upload_phi(ctx._p, pd(hphi))
+            # the whole state in and out through the C ABI every step
+            L.gfm_upload_state(ctx._p, *up)
             L.gfm_step(ctx._p, ctypes.byref(m), 1)
-            L.gfm_download(ctx._p, 1, pd(hU1))
-            if two:
-                L.gfm_download(ctx._p, 2, pd(hU2))
-                L.gfm_download_phi(ctx._p, pd(hphi))
+            L.gfm_download_state(ctx._p, *up)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
         args.e2e_steps = n_e2e
@@ -561,14 +557,10 @@ def run_batch(args):
         t0 = time.perf_counter()
         for _ in range(n_e2e):
             for ctx, (h1, h2, hp) in zip(b.instances, pinned):
-                L.gfm_upload(ctx._p, 1, pd(h1))
-                L.gfm_upload(ctx._p, 2, pd(h2))
-                L.gfm_upload_phi(ctx._p, pd(hp))
+                L.gfm_upload_state(ctx._p, pd(h1), pd(h2), pd(hp))
             b.step(m, 1, graph=True)
             for ctx, (h1, h2, hp) in zip(b.instances, pinned):
-                L.gfm_download(ctx._p, 1, pd(h1))
-                L.gfm_download(ctx._p, 2, pd(h2))
-                L.gfm_download_phi(ctx._p, pd(hp))
+                L.gfm_download_state(ctx._p, pd(h1), pd(h2), pd(hp))
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         nbytes = sum(sum(a.nbytes for a in arrs) for arrs in pinned)

@@ -106,6 +106,9 @@ gfm_status_t gfm_upload(gfm_ctx* ctx, int fluid, const double* U);
 gfm_status_t gfm_download(gfm_ctx* ctx, int fluid, double* U);
 gfm_status_t gfm_upload_phi(gfm_ctx* ctx, const double* phi);
 gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi);
+/* all fields at once (U1, and U2 and phi for two fluids), one synchronisation */
+gfm_status_t gfm_upload_state(gfm_ctx* ctx, const double* U1, const double* U2, const double* phi);
+gfm_status_t gfm_download_state(gfm_ctx* ctx, double* U1, double* U2, double* phi);
 
 /* the velocity field of the last ghost fill (GFM_base::vfield, handed to the
  * interface tracker): 2 planes (u, v), layout of phi */

@@ -302,17 +302,23 @@ gfm_status_t gfm_set_stream(gfm_ctx* ctx, void* s) {
   return GFM_OK;
 }
 
-static gfm_status_t copy_grid(gfm_ctx* ctx, double* dev, const double* host_src, double* host_dst, int planes) {
+// consecutive planes of a field are one pitched 2D region (plane = nr x pitch):
+// one copy moves them all
+static gfm_status_t enqueue_grid(gfm_ctx* ctx, double* dev, const double* host_src, double* host_dst, int planes) {
   const GridP& P = ctx->P;
-  size_t wb = sizeof(double) * (size_t)P.nc;
-  for (int k = 0; k < planes; k++) {
-    if (host_src)
-      CK(cudaMemcpy2DAsync(dev + k * P.plane, sizeof(double) * P.pitch, host_src + (size_t)k * P.nr * P.nc, wb, wb,
-                           P.nr, cudaMemcpyHostToDevice, ctx->stream));
-    else
-      CK(cudaMemcpy2DAsync(host_dst + (size_t)k * P.nr * P.nc, wb, dev + k * P.plane, sizeof(double) * P.pitch, wb,
-                           P.nr, cudaMemcpyDeviceToHost, ctx->stream));
-  }
+  const size_t wb = sizeof(double) * (size_t)P.nc;
+  if (host_src)
+    CK(cudaMemcpy2DAsync(dev, sizeof(double) * P.pitch, host_src, wb, wb, (size_t)planes * P.nr,
+                         cudaMemcpyHostToDevice, ctx->stream));
+  else
+    CK(cudaMemcpy2DAsync(host_dst, wb, dev, sizeof(double) * P.pitch, wb, (size_t)planes * P.nr,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+  return GFM_OK;
+}
+
+static gfm_status_t copy_grid(gfm_ctx* ctx, double* dev, const double* host_src, double* host_dst, int planes) {
+  gfm_status_t r = enqueue_grid(ctx, dev, host_src, host_dst, planes);
+  if (r != GFM_OK) return r;
   CK(cudaStreamSynchronize(ctx->stream));
   return GFM_OK;
 }
@@ -332,6 +338,26 @@ gfm_status_t gfm_upload_phi(gfm_ctx* ctx, const double* phi) {
 gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi) {
   if (!ctx || !phi || !ctx->two_fluid) return GFM_ERR_ARG;
   return copy_grid(ctx, ctx->phi, nullptr, phi, 1);
+}
+
+gfm_status_t gfm_upload_state(gfm_ctx* ctx, const double* U1, const double* U2, const double* phi) {
+  if (!ctx || !U1 || (ctx->two_fluid && (!U2 || !phi))) return GFM_ERR_ARG;
+  gfm_status_t r = enqueue_grid(ctx, ctx->U[0], U1, nullptr, 4);
+  if (r == GFM_OK && ctx->two_fluid) r = enqueue_grid(ctx, ctx->U[1], U2, nullptr, 4);
+  if (r == GFM_OK && ctx->two_fluid) r = enqueue_grid(ctx, ctx->phi, phi, nullptr, 1);
+  if (r != GFM_OK) return r;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFM_OK;
+}
+
+gfm_status_t gfm_download_state(gfm_ctx* ctx, double* U1, double* U2, double* phi) {
+  if (!ctx || !U1 || (ctx->two_fluid && (!U2 || !phi))) return GFM_ERR_ARG;
+  gfm_status_t r = enqueue_grid(ctx, ctx->U[0], nullptr, U1, 4);
+  if (r == GFM_OK && ctx->two_fluid) r = enqueue_grid(ctx, ctx->U[1], nullptr, U2, 4);
+  if (r == GFM_OK && ctx->two_fluid) r = enqueue_grid(ctx, ctx->phi, nullptr, phi, 1);
+  if (r != GFM_OK) return r;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFM_OK;
 }
 
 gfm_status_t gfm_download_velocity(gfm_ctx* ctx, double* vel) {

@@ -74,3 +74,23 @@ def test_device_initialised_run_matches():
     b.close()
     for x, y in zip(ra, rb):
         assert np.array_equal(x, y)
+
+
+def test_state_upload_download_in_one_call():
+    """gfm_upload_state / gfm_download_state move the same bytes as the
+    per-field calls."""
+    import ctypes
+    d, T = g.case_params("twofluid", "shock_bubble", 57, 23)
+    U1, U2, phi = g.case_init("twofluid", "shock_bubble", d)
+    L = g.lib()
+    pd = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))   # noqa: E731
+    ctx = g.Context(d, two_fluid=True)
+    assert L.gfm_upload_state(ctx._p, pd(U1), pd(U2), pd(phi)) == 0
+    V1, V2, ph = ctx.download()
+    assert np.array_equal(V1, U1) and np.array_equal(V2, U2) and np.array_equal(ph, phi)
+    ctx.step(g.method(T=T), 3)
+    W1, W2, wp = np.empty_like(U1), np.empty_like(U2), np.empty_like(phi)
+    assert L.gfm_download_state(ctx._p, pd(W1), pd(W2), pd(wp)) == 0
+    X1, X2, xp = ctx.download()
+    ctx.close()
+    assert np.array_equal(W1, X1) and np.array_equal(W2, X2) and np.array_equal(wp, xp)
