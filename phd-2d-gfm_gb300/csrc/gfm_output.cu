@@ -320,6 +320,13 @@ gfm_status_t gfm_writer_output(gfm_writer* w, int numsteps) {
     s->busy = true;
   }
   w->next_slot = (w->next_slot + 1) % gfm_writer::NSLOT;
+  auto fail = [&]() {   // release the slot: nothing was queued for it
+    std::lock_guard<std::mutex> lk(w->mu);
+    s->busy = false;
+    w->failed = true;
+    w->cv.notify_all();
+    return GFM_ERR_CUDA;
+  };
   const gfm::GridP& P = w->ctx->P;
   const double* src[4];
   size_t planes[4];
@@ -330,17 +337,16 @@ gfm_status_t gfm_writer_output(gfm_writer* w, int numsteps) {
     if (!src[a]) continue;
     if (cudaMemcpyAsync(s->dev + off * P.plane, src[a], sizeof(double) * planes[a] * P.plane,
                         cudaMemcpyDeviceToDevice, w->ctx->stream) != cudaSuccess)
-      return GFM_ERR_CUDA;
+      return fail();
     off += planes[a];
   }
-  if (cudaEventRecord(s->staged, w->ctx->stream) != cudaSuccess) return GFM_ERR_CUDA;
-  if (cudaStreamWaitEvent(w->copy, s->staged, 0) != cudaSuccess) return GFM_ERR_CUDA;
+  if (cudaEventRecord(s->staged, w->ctx->stream) != cudaSuccess) return fail();
+  if (cudaStreamWaitEvent(w->copy, s->staged, 0) != cudaSuccess) return fail();
   const size_t wb = sizeof(double) * (size_t)P.nc;
-  for (size_t k = 0; k < off; k++)
-    if (cudaMemcpy2DAsync(s->host + k * w->G.plane(), wb, s->dev + k * P.plane, sizeof(double) * P.pitch, wb, P.nr,
-                          cudaMemcpyDeviceToHost, w->copy) != cudaSuccess)
-      return GFM_ERR_CUDA;
-  if (cudaEventRecord(s->copied, w->copy) != cudaSuccess) return GFM_ERR_CUDA;
+  if (cudaMemcpy2DAsync(s->host, wb, s->dev, sizeof(double) * P.pitch, wb, off * P.nr, cudaMemcpyDeviceToHost,
+                        w->copy) != cudaSuccess)
+    return fail();
+  if (cudaEventRecord(s->copied, w->copy) != cudaSuccess) return fail();
   const int itm = w->ctx->itm;
   push(w, [w, s, numsteps, itm]() {
     bool ok = cudaEventSynchronize(s->copied) == cudaSuccess;
@@ -373,14 +379,21 @@ gfm_status_t gfm_writer_mass(gfm_writer* w, int numsteps, double t) {
     w->mass_busy[k] = true;
   }
   w->next_mass = (k + 1) % gfm_writer::NMASS;
+  auto fail = [&]() {
+    std::lock_guard<std::mutex> lk(w->mu);
+    w->mass_busy[k] = false;
+    w->failed = true;
+    w->cv.notify_all();
+    return GFM_ERR_CUDA;
+  };
   gfm_ctx* c = w->ctx;
   double* part = gfm::mass_scratch(c);
   gfm::launch_mass(c, -1.0, part, w->mass_dev + 2 * k);
   gfm::launch_mass(c, 1.0, part, w->mass_dev + 2 * k + 1);
   if (cudaMemcpyAsync(w->mass_host + 2 * k, w->mass_dev + 2 * k, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                       c->stream) != cudaSuccess)
-    return GFM_ERR_CUDA;
-  if (cudaEventRecord(w->mass_ev[k], c->stream) != cudaSuccess) return GFM_ERR_CUDA;
+    return fail();
+  if (cudaEventRecord(w->mass_ev[k], c->stream) != cudaSuccess) return fail();
   push(w, [w, k, numsteps, t]() {
     bool ok = cudaEventSynchronize(w->mass_ev[k]) == cudaSuccess;
     const double m1 = w->mass_host[2 * k], m2 = w->mass_host[2 * k + 1];
