@@ -243,6 +243,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_chain, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_far, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_far_final, cudaEventDisableTiming);
     for (int q = 0; q < 6; q++)
       if (e == cudaSuccess) e = cudaEventCreate(&ctx->tev[q]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s_ls, cudaStreamNonBlocking);
@@ -277,10 +278,10 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
     for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cell); cudaFree(ctx->tile_near);
   cudaFree(ctx->band_list); cudaFree(ctx->near_list); cudaFree(ctx->list_n);
-  cudaFree(ctx->stage);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_chain) cudaEventDestroy(ctx->ev_chain);
   if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);
+  if (ctx->ev_far_final) cudaEventDestroy(ctx->ev_far_final);
   for (int q = 0; q < 6; q++)
     if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
   if (ctx->s_ls) {
@@ -341,26 +342,12 @@ gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi) {
   return copy_grid(ctx, ctx->phi, nullptr, phi, 1);
 }
 
-// Host-to-device copies into pitched rows run slower than contiguous ones
-// (135 against 206 GB/s measured on GB300 for the 1000x400 state): the state
-// goes to a packed device buffer in one copy per field and is spread into the
-// pitched planes on the device.
 gfm_status_t gfm_upload_state(gfm_ctx* ctx, const double* U1, const double* U2, const double* phi) {
   if (!ctx || !U1 || (ctx->two_fluid && (!U2 || !phi))) return GFM_ERR_ARG;
-  const GridP& P = ctx->P;
-  const size_t plane = (size_t)P.nr * P.nc, wb = sizeof(double) * (size_t)P.nc;
-  if (!ctx->stage) CK(cudaMalloc(&ctx->stage, sizeof(double) * 9 * plane));
-  const double* src[3] = {U1, U2, phi};
-  double* dst[3] = {ctx->U[0], ctx->U[1], ctx->phi};
-  const int planes[3] = {4, 4, 1};
-  size_t off = 0;
-  for (int a = 0; a < (ctx->two_fluid ? 3 : 1); a++) {
-    double* st = ctx->stage + off * plane;
-    CK(cudaMemcpyAsync(st, src[a], sizeof(double) * planes[a] * plane, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpy2DAsync(dst[a], sizeof(double) * P.pitch, st, wb, wb, (size_t)planes[a] * P.nr,
-                         cudaMemcpyDeviceToDevice, ctx->stream));
-    off += planes[a];
-  }
+  gfm_status_t r = enqueue_grid(ctx, ctx->U[0], U1, nullptr, 4);
+  if (r == GFM_OK && ctx->two_fluid) r = enqueue_grid(ctx, ctx->U[1], U2, nullptr, 4);
+  if (r == GFM_OK && ctx->two_fluid) r = enqueue_grid(ctx, ctx->phi, phi, nullptr, 1);
+  if (r != GFM_OK) return r;
   CK(cudaStreamSynchronize(ctx->stream));
   return GFM_OK;
 }
@@ -516,6 +503,7 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
         launch_ghost_fill_overlapped(ctx, m);
         fork_level_set();
         launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->stream);
+        cudaStreamWaitEvent(ctx->stream, ctx->ev_far, 0);   // the far tiles' flux update
         mark(3);
       } else {
         if (vof) launch_ghost_fill_vof(ctx, m);

@@ -88,10 +88,10 @@ struct gfm_ctx {
   int* band_list;         // cells (ghost cells included) whose source is a band cell
   int* near_list;         // cells whose source is a near cell
   int* list_n;            // 2 counts: band_list, near_list
-  double* stage;          // contiguous staging of uploads (9 packed planes), allocated on first use
   int* tile_near;         // per flux tile: its region holds a near cell
   cudaStream_t s_chain, s_far;
   cudaEvent_t ev_fork, ev_chain, ev_far;
+  cudaEvent_t ev_far_final;   // far cells' conserved grids and velocities written
   cudaEvent_t tev[6];     // timing events of the overlapped schedule (gfm_step_timed)
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist

@@ -2110,6 +2110,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* fin[2] = {src1, src2};
     finalize_sel(ctx, fin, 1, ctx->s_far);
   }
+  cudaEventRecord(ctx->ev_far_final, ctx->s_far);
   if (ctx->timing) cudaEventRecord(ctx->tev[5], ctx->s_far);
   launch_fs_update_sel(ctx, m->fs, 3, TILES_FAR, ctx->s_far);
   cudaEventRecord(ctx->ev_far, ctx->s_far);
@@ -2132,9 +2133,13 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     finalize_sel(ctx, fin, 2, s);
   }
   if (ctx->timing) cudaEventRecord(ctx->tev[3], s);
-  cudaStreamWaitEvent(s, ctx->ev_far, 0);
+  // The near tiles read far cells too, and the level set reads the far cells'
+  // velocities: both wait for the far cells' conversion, not for the far
+  // tiles' flux update, which writes only its own tiles of Unew.
+  cudaStreamWaitEvent(s, ctx->ev_far_final, 0);
   if (ctx->timing) cudaEventRecord(ctx->tev[4], s);
-  // the caller launches the flux update of the near tiles
+  // the caller forks the level set, launches the flux update of the near
+  // tiles and then waits for ev_far
 }
 
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
