@@ -228,6 +228,8 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->ifc_done, sizeof(int) * cap);
     alloc((void**)&ctx->ifc_out, sizeof(double) * 8 * cap);
     alloc((void**)&ctx->ifc_mrp, sizeof(double) * 8 * cap);
+    alloc((void**)&ctx->probe_ij, sizeof(int) * 4 * cap);
+    alloc((void**)&ctx->probe_w, sizeof(double) * 8 * cap);
     ctx->n_chunks = (int)(((int64_t)P.nr * P.nc + 2047) / 2048);
     alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)ctx->n_chunks);
     for (int b = 0; b < 2; b++)
@@ -274,6 +276,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->nrm); cudaFree(ctx->vel); cudaFree(ctx->vel_t);
   cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
   cudaFree(ctx->ifc_out); cudaFree(ctx->ifc_mrp); cudaFree(ctx->chunk_count);
+  cudaFree(ctx->probe_ij); cudaFree(ctx->probe_w);
   for (int b = 0; b < 2; b++)
     for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cell); cudaFree(ctx->tile_near);

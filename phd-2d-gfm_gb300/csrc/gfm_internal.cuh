@@ -74,6 +74,8 @@ struct gfm_ctx {
   int* ifc_pred;     // 8 per interface
   double* ifc_out;   // 8 per interface: star state (4), extension velocity (2), rho* other side, spare
   double* ifc_mrp;   // 8 per mixed cell of the VOF loop: MRPsoln1, MRPsoln2
+  int* probe_ij;     // Riemann GFM: per interfacial cell and side, the bilinear probe's cell (i0, j0)
+  double* probe_w;   // and its 4 weights
   int itm;           // interface tracker of the last method used (GFM_ITM_*)
   int* ifc_opp;      // real GFM: opposite cell
   gfm::DevTime* dtime;

@@ -501,6 +501,10 @@ struct IfcArgs {
   float* cap_Y;
   int* cap_count;
   int cap;
+  // probe geometry of the Riemann GFM's cells from k_ifc_probes (or null):
+  // per list entry and side, the bilinear cell (i0, j0) and the 4 weights
+  const int* probe_ij;
+  const double* probe_w;
 };
 
 __device__ __forceinline__ bool ifc_wait(const IfcArgs& a, int p) {
@@ -838,6 +842,65 @@ struct IfcCell {
   V4 Us;
 };
 
+// The bilinear probe of side R (isR: interface point + ds n, sampling fluid
+// 2) or L (- ds n, fluid 1) of interfacial cell c = (i,j): the lower-left
+// cell (i0, j0) and the fractional offsets (wa, wb)
+// (get_interpolated_mixedRPstates, sourcecode/GFM_base.cpp:4-33, and the
+// project's bilinear interpolation).
+__device__ __forceinline__ void ifc_probe(const IfcArgs& a, int64_t c, int i, int j, double lsval, double nx,
+                                          double ny, bool isR, int& i0, int& j0, double& wa, double& wb) {
+  const GridP& P = a.P;
+  const double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
+  const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
+  const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
+  const double gx = a.nrm[c], gy = a.nrm[c + P.plane];
+  const double nm = a.nrm[c + 4 * P.plane];
+  double lv = lsval;
+  if (fabs(lv) > ds) lv = copysign(ds, lv);
+  double hx = nx, hy = ny;
+  if (nm < 1e-12) { hx = gx / nm; hy = gy / nm; }
+  const double ilx = ccx - lv * hx, ily = ccy - lv * hy;
+  const double dsx = ds * hx, dsy = ds * hy;
+  const double px = ilx + (isR ? dsx : -dsx);
+  const double py = ily + (isR ? dsy : -dsy);
+  const double sx = (px - P.x0) * P.idx + (double)P.g - 0.5;
+  const double sy = (py - P.y0) * P.idy + (double)P.g - 0.5;
+  j0 = (int)floor(sx);
+  i0 = (int)floor(sy);
+  j0 = min(max(j0, 0), P.nc - 2);
+  i0 = min(max(i0, 0), P.nr - 2);
+  wa = sx - (double)j0;
+  wb = sy - (double)i0;
+}
+
+// The probes of every interfacial cell ahead of the interface loop: they
+// depend on phi and its normals only, so computing them here in parallel
+// takes their FP64 instructions off the loop's dependency chain.
+__global__ void __launch_bounds__(256) k_ifc_probes(IfcArgs a, int* probe_ij, double* probe_w) {
+  const GridP& P = a.P;
+  if (!a.D->active) return;
+  const int n = a.D->n_ifc;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * n; q += gridDim.x * blockDim.x) {
+    const int t = q >> 1, s = q & 1;
+    const int64_t lin = a.list[t];
+    const int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
+    const int64_t c = cidx(P, i, j);
+    double nx, ny;
+    unit_normal(a.nrm, P, c, nx, ny);
+    int i0, j0;
+    double wa, wb;
+    ifc_probe(a, c, i, j, a.phi[c], nx, ny, s == 1, i0, j0, wa, wb);
+    probe_ij[4 * (int64_t)t + 2 * s] = i0;
+    probe_ij[4 * (int64_t)t + 2 * s + 1] = j0;
+    double* w = probe_w + 8 * (int64_t)t + 4 * s;
+    for (int e = 0; e < 4; e++) {
+      const double fa = (e & 1) ? wa : 1.0 - wa;
+      const double fb = (e & 2) ? wb : 1.0 - wb;
+      w[e] = fa * fb;
+    }
+  }
+}
+
 template <int MODE>
 __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k, uint32_t& st, IfcCell& cell) {
   const GridP& P = a.P;
@@ -898,31 +961,23 @@ __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k,
       else v = ifc_read1(a, s, iopp, jopp, kc, lin, ok);
     }
   } else {
-    // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33)
-    const double ds = 1.0 * (P.dy < P.dx ? P.dy : P.dx);
-    const double ccx = P.x0 + ((double)(j - P.g) + 0.5) * P.dx;
-    const double ccy = P.y0 + ((double)(i - P.g) + 0.5) * P.dy;
-    const double gx = a.nrm[c], gy = a.nrm[c + P.plane];
-    const double nm = a.nrm[c + 4 * P.plane];
-    double lv = lsval;
-    if (fabs(lv) > ds) lv = copysign(ds, lv);
-    double hx = nx, hy = ny;
-    if (nm < 1e-12) { hx = gx / nm; hy = gy / nm; }
-    const double ilx = ccx - lv * hx, ily = ccy - lv * hy;
-    // probe of side s: interface point + ds n (side 1) or - ds n (side 0)
-    const double dsx = ds * hx, dsy = ds * hy;
-    const double px = ilx + (isR ? dsx : -dsx);
-    const double py = ily + (isR ? dsy : -dsy);
-    const double sx = (px - P.x0) * P.idx + (double)P.g - 0.5;
-    const double sy = (py - P.y0) * P.idy + (double)P.g - 0.5;
-    int j0 = (int)floor(sx), i0 = (int)floor(sy);
-    j0 = min(max(j0, 0), P.nc - 2);
-    i0 = min(max(i0, 0), P.nr - 2);
-    const double wa = sx - (double)j0, wb = sy - (double)i0;
-    const double fa = (q & 1) ? wa : 1.0 - wa;
-    const double fb = (q & 2) ? wb : 1.0 - wb;
+    // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33); the
+    // probe geometry depends on phi only and comes from k_ifc_probes when set
+    int i0, j0;
+    double w;
+    if (a.probe_ij) {
+      i0 = __ldg(a.probe_ij + 4 * (int64_t)t + 2 * s);
+      j0 = __ldg(a.probe_ij + 4 * (int64_t)t + 2 * s + 1);
+      w = __ldg(a.probe_w + 8 * (int64_t)t + 4 * s + q);
+    } else {
+      double wa, wb;
+      ifc_probe(a, c, i, j, lsval, nx, ny, isR, i0, j0, wa, wb);
+      const double fa = (q & 1) ? wa : 1.0 - wa;
+      const double fb = (q & 2) ? wb : 1.0 - wb;
+      w = fa * fb;
+    }
     const double g = ifc_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
-    const double pr = (fa * fb) * g;
+    const double pr = w * g;
     const double p1 = __shfl_down_sync(FULL_MASK, pr, 4);
     const double p2 = __shfl_down_sync(FULL_MASK, pr, 8);
     const double p3 = __shfl_down_sync(FULL_MASK, pr, 12);
@@ -1894,6 +1949,11 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia);
+  ia.probe_ij = nullptr; ia.probe_w = nullptr;
+  if (variant == GFM_RIEMANN) {
+    k_ifc_probes<<<152, 256, 0, s>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
+    ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w;
+  }
   int iblocks = 152;   // 4 warps per CTA: one chain warp per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
   else if (variant == GFM_REAL) k_interface_warp<IFC_REAL><<<iblocks, 128, 0, s>>>(ia);
@@ -2089,6 +2149,11 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia);
+  ia.probe_ij = nullptr; ia.probe_w = nullptr;
+  if (variant == GFM_RIEMANN) {
+    k_ifc_probes<<<16, 256, 0, ctx->s_chain>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
+    ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w;
+  }
   const int chain_ctas = 16;   // 8 warps each on the 8-SM partition: 4 chain warps per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
@@ -2202,6 +2267,7 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.D = ctx->dtime;
   ia.slip = m->use_slip_BCs;
   ia.mlp = nullptr; ia.cap_X = nullptr; ia.cap_Y = nullptr; ia.cap_count = nullptr; ia.cap = 0;
+  ia.probe_ij = nullptr; ia.probe_w = nullptr;
   if (og) k_vof_chain<VOF_OGFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
   else k_vof_chain<VOF_GFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
   counted();
