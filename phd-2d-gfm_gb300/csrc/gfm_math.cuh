@@ -522,6 +522,29 @@ GFM_HD void rs_prefun(const RSSide& K, const Gas& k, double p, double* f, double
   }
 }
 
+// rs_prefun with the two branches' divisions (1/(pb + B) of the shock,
+// pw/prat of the rarefaction) issued as one: when lanes of a warp take
+// different branches the division runs once for all of them.  Every value
+// comes from the same operations as in rs_prefun.
+GFM_HD void rs_prefun_merged(const RSSide& K, const Gas& k, double p, double* f, double* fd) {
+  const double pb = p + k.pinf;
+  const bool shock = c_gt(p, K.p);
+  double pw = 0.0, prat = 1.0;
+  if (!shock) {
+    prat = pb * K.ipb;
+    pw = gfm_pow(prat, k.G1);
+  }
+  const double q = (shock ? 1.0 : pw) / (shock ? pb + K.BK : prat);
+  if (shock) {
+    const double qrt = sqrt(K.AK * q);
+    *f = (p - K.p) * qrt;
+    *fd = (1.0 - 0.5 * ((p - K.p) * q)) * qrt;
+  } else {
+    *f = K.G4c * (pw - 1.0);
+    *fd = K.irc * q;
+  }
+}
+
 struct RSStar {
   double p, u;        // P_STAR, S_STAR
   int iters;

@@ -507,15 +507,27 @@ struct IfcArgs {
   const double* probe_w;
 };
 
+// Completion flags of the interface loop: the writer publishes a cell's
+// outputs with a release store of its flag, readers poll it with acquire
+// loads (tightly at first, then with a short sleep), so a dependant sees the
+// outputs as soon as the flag does, without a full fence on either side.
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ bool ifc_wait(const IfcArgs& a, int p) {
-  volatile int* d = a.done;
   long long spins = 0;
-  while (d[p] == 0) {
+  int v;
+  while ((v = ld_acquire(a.done + p)) == 0) {
     if (++spins > IFC_SPIN_LIMIT) return false;
-    __nanosleep(64);
+    if (spins > 512) __nanosleep(64);
   }
-  __threadfence();
-  return d[p] == 1;
+  return v == 1;
 }
 
 __device__ __forceinline__ V4 ifc_out4(const IfcArgs& a, int p) {
@@ -653,8 +665,7 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
     double* o = a.out + (int64_t)k * IFC_OUT;
     if (!ok) {
       st |= ST_SCHEDULE_LIMIT;
-      __threadfence();
-      ((volatile int*)a.done)[k] = 2;
+      st_release(a.done + k, 2);
       continue;
     }
     // mixed Riemann problem in the normal frame (e.g. GFM_riemann.cpp:76-122)
@@ -688,8 +699,7 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
       else { o[0] = m.rho_star_R; o[1] = snx + t2x; o[2] = sny + t2y; o[3] = m.p_star; }
       o[4] = snx; o[5] = sny;
     }
-    __threadfence();
-    ((volatile int*)a.done)[k] = 1;
+    st_release(a.done + k, 1);
   }
   uint32_t wst = __reduce_or_sync(0xffffffffu, st);
   unsigned wit = __reduce_add_sync(0xffffffffu, (unsigned)iters);
@@ -748,8 +758,15 @@ struct PairStar { double p, u, rho_own; bool trivial; };
 __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const Gas& kL, const Gas& kR, const V4& Uown,
                                                   uint32_t* status, int* iters, const IfcArgs& a, float* hbuf,
                                                   int* proposed) {
-  bool ok;
-  V4 Wp = cons_to_prims_phys(k.g, k.pinf, Uown, &ok);
+  // cons_to_prims_phys with its three quotients by rho (rho u, rho v, E) in
+  // one: lane kc of each group of four divides component kc + 1 (E twice)
+  const int lane = threadIdx.x & 31, grp = lane & ~3, kq = lane & 3;
+  const Recip Rr = recip(Uown.a);
+  const double qv = rdiv(kq == 0 ? Uown.b : (kq == 1 ? Uown.c : Uown.d), Rr);
+  const double uq = __shfl_sync(FULL_MASK, qv, grp), vq = __shfl_sync(FULL_MASK, qv, grp + 1);
+  const double eq = __shfl_sync(FULL_MASK, qv, grp + 2) - 0.5 * (uq * uq + vq * vq);
+  const bool ok = c_ge0(Uown.a) && c_ge0(eq);
+  const V4 Wp = V4{Uown.a, uq, vq, eos_pressure(k.g, k.pinf, eq, Uown.a)};
   if (!ok) *status |= ST_UNPHYSICAL;
   RSSide S = rs_side(Wp.a, Wp.b, Wp.d, k);
   const double ou = xside(S.u), op = xside(S.p);
@@ -761,7 +778,18 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
     return r;
   }
   r.trivial = false;
-  rs_side_consts(S, k);
+  {
+    // rs_side_consts with its two reciprocals (1/rho, 1/pb) in one division:
+    // even lanes divide by rho, odd lanes by pb, and exchange
+    const double y = 1.0 / ((lane & 1) ? S.pb : S.rho);
+    const double irho = __shfl_sync(FULL_MASK, y, lane & ~1), ipb = __shfl_sync(FULL_MASK, y, lane | 1);
+    S.ipb = ipb;
+    S.c = sqrt(k.g * S.pb * irho);
+    S.AK = k.G5 * irho;
+    S.BK = k.G6 * S.pb;
+    S.G4c = k.G4 * S.c;
+    S.irc = S.c * S.ipb * k.IG;
+  }
   const double orho = xside(S.rho), oc = xside(S.c), oG4c = xside(S.G4c), opb = xside(S.pb);
   const double rhoL = isR ? orho : S.rho, rhoR = isR ? S.rho : orho;
   const double cL = isR ? oc : S.c, cR = isR ? S.c : oc;
@@ -799,7 +827,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   int it = 0;
   for (;;) {
     double f, fd;
-    rs_prefun(S, k, pold, &f, &fd);
+    rs_prefun_merged(S, k, pold, &f, &fd);   // the halves often take different branches
     const double of = xside(f), ofd = xside(fd);
     fL = isR ? of : f;
     fR = isR ? f : of;
@@ -1022,8 +1050,7 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
     if (!ifc_front<MODE>(a, t, k, st, cell)) {
       st |= ST_SCHEDULE_LIMIT;
       if (lane == 0) {
-        __threadfence();
-        ((volatile int*)a.done)[t] = 2;
+        st_release(a.done + t, 2);
       }
       continue;
     }
@@ -1036,8 +1063,7 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
       const double snx = m.u * cell.nx, sny = m.u * cell.ny;
       o[0] = m.rho_own; o[1] = snx + cell.tx; o[2] = sny + cell.ty; o[3] = m.p;
       o[4] = snx; o[5] = sny;
-      __threadfence();
-      ((volatile int*)a.done)[t] = 1;
+      st_release(a.done + t, 1);
     }
   }
   uint32_t wst = __reduce_or_sync(FULL_MASK, st);
@@ -1302,8 +1328,7 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
     if (!__all_sync(FULL_MASK, ok)) {
       st |= ST_SCHEDULE_LIMIT;
       if (lane == 0) {
-        __threadfence();
-        ((volatile int*)a.done)[t] = 2;
+        st_release(a.done + t, 2);
       }
       continue;
     }
@@ -1360,8 +1385,7 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       double* o = a.out + (int64_t)t * IFC_OUT;
       double* r = mrp + (int64_t)t * 8;
       for (int e = 0; e < 4; e++) { o[e] = o1[e]; o[4 + e] = o2[e]; r[e] = m1v[e]; r[4 + e] = m2v[e]; }
-      __threadfence();
-      ((volatile int*)a.done)[t] = 1;
+      st_release(a.done + t, 1);
     }
   }
   uint32_t wst = __reduce_or_sync(FULL_MASK, st);
