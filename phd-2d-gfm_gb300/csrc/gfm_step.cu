@@ -1410,6 +1410,7 @@ struct VofGhostArgs {
   const int* ifc_map;
   const double* out;
   const double* mrp;
+  const uint8_t* near_cell;   // real cells within the ring of a mixed cell
   double* U1; double* U2;
   double* vel;
   DevTime* D;
@@ -1463,11 +1464,7 @@ __global__ void __launch_bounds__(256) k_vof_ghost(VofGhostArgs a) {
     else if (zc >= 0.5) { vx = p1.b; vy = p1.c; }
     else { vx = p2.b; vy = p2.c; }
     if (real && !a.mask[c] && (zc == 0.0 || zc == 1.0)) {
-      bool near = false;
-      for (int di = -VOF_RING; di <= VOF_RING && !near; di++)
-        for (int dj = -VOF_RING; dj <= VOF_RING; dj++)
-          if (a.mask[cidx(P, i + di, j + dj)]) { near = true; break; }
-      if (near) {
+      if (a.near_cell[c]) {
         if (zc == 0.0) {   // flag 1: fluid 1 ghost state
           const V4 s = vof_invdist_average(a, i, j, 0);
           if (MODE == VOF_GFM) p1 = s;
@@ -2281,6 +2278,11 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   const int cap = P.nr * P.nc;
   k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime);
   counted();
+  // the real cells flagged 1 or 2 by the loop: within the ring of a mixed cell
+  cudaMemsetAsync(ctx->near_cell, 0, (size_t)P.plane, s);
+  k_near_mark<<<grid_blocks((int64_t)P.Nx * P.Ny, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->near_cell,
+                                                                      VOF_RING);
+  counted();
   IfcArgs ia;
   ia.P = P;
   ia.W1 = ctx->W[0]; ia.W2 = ctx->W[1];
@@ -2300,6 +2302,7 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   ga.W1 = ctx->W[0]; ga.W2 = ctx->W[1];
   ga.z = ctx->phi; ga.mask = ctx->mask; ga.ifc_map = ctx->ifc_map;
   ga.out = ctx->ifc_out; ga.mrp = ctx->ifc_mrp;
+  ga.near_cell = ctx->near_cell;
   ga.U1 = ctx->U[0]; ga.U2 = ctx->U[1];
   ga.vel = ctx->vel; ga.D = ctx->dtime;
   const int gblocks = grid_blocks((int64_t)P.nr * P.nc, 256);

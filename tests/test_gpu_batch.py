@@ -69,3 +69,29 @@ def test_batch_graph_after_single_calls():
     for k, (d, T, U1, U2, phi) in enumerate(cases):
         ref = orc.twofluid_run(d, m, U1, U2, phi, 19)
         assert np.array_equal(outs[k][0], ref["U1"]) and np.array_equal(outs[k][2], ref["phi"])
+
+
+def test_batch_vof_graph_matches_single():
+    """GFM_VOF with the VOF tracker through the recorded graph: the sweep
+    order of the advection follows the step number on the device, so every
+    replay is right; each instance ends as it would alone, states generated
+    on the device."""
+    import ctypes
+    m = g.method(gfm="VOFGFM", itm="PYVOF", CFL=0.5, T=1.0)
+    params = [g.BubbleParams(*p[2:]) for p in MEMBERS]
+    descs = [g.shock_bubble_case(*p)[0] for p in MEMBERS]
+    b = g.Batch(descs, two_fluid=True)
+    for ctx, p in zip(b.instances, params):
+        ctx.init_shock_bubble_device(p, itm="PYVOF")
+    b.step(m, 17, graph=True)
+    b.synchronize()
+    outs = [ctx.download() for ctx in b.instances]
+    b.close()
+    for k, (d, p) in enumerate(zip(descs, params)):
+        single = g.Context(d, two_fluid=True)
+        single.init_shock_bubble_device(p, itm="PYVOF")
+        single.step(m, 17)
+        S = single.download()
+        single.close()
+        for a, c in zip(outs[k], S):
+            assert np.array_equal(a, c), "VOF instance %d differs from its single run" % k
