@@ -7,6 +7,7 @@
 
 namespace gfm {
 void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter);
+void launch_step_begin(gfm_ctx* ctx, double CFL, double T, bool ogfm);
 void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream_t s);
 void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out);
 }  // namespace gfm
@@ -248,7 +249,12 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_far_final, cudaEventDisableTiming);
     for (int q = 0; q < 6; q++)
       if (e == cudaSuccess) e = cudaEventCreate(&ctx->tev[q]);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s_ls, cudaStreamNonBlocking);
+    int prio_lo = 0, prio_hi = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->s_ls, cudaStreamNonBlocking, prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->s_near, cudaStreamNonBlocking, prio_hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_near, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_phi_free, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_done, cudaEventDisableTiming);
     if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
@@ -293,6 +299,12 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   }
   if (ctx->ev_ls_fork) cudaEventDestroy(ctx->ev_ls_fork);
   if (ctx->ev_ls_done) cudaEventDestroy(ctx->ev_ls_done);
+  if (ctx->s_near) {
+    cudaStreamSynchronize(ctx->s_near);
+    cudaStreamDestroy(ctx->s_near);
+  }
+  if (ctx->ev_near) cudaEventDestroy(ctx->ev_near);
+  if (ctx->ev_phi_free) cudaEventDestroy(ctx->ev_phi_free);
   cudaFree(ctx->dtime);
   cudaFree(extra(ctx).counters);
   cudaFree(extra(ctx).mass_part);
@@ -474,7 +486,15 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
   for (int s = 0; s < nsteps; s++) {
     bool ogfm = ctx->two_fluid && (m->gfm == GFM_OGFM || m->gfm == GFM_OGFM_VOF);
     mark(0);
-    launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
+    if (ctx->two_fluid && !vof) {
+      // the CFL reduction runs inside the ghost fill's conversion (k_prims),
+      // which reads the same grids; only the flux and level-set updates read dt
+      ctx->cfl_counter = extra(ctx).counters;
+      launch_step_begin(ctx, m->CFL, m->T, ogfm);
+    } else {
+      ctx->cfl_counter = nullptr;
+      launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
+    }
     mark(1);
     if (ctx->two_fluid) {
       overlapped = !vof && !m->use_extension_vfield &&
@@ -483,6 +503,14 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
       // The level-set update reads phi and the velocity field of the ghost
       // fill and writes only level-set buffers: it runs on its own stream
       // beside the flux update (which reads and writes the fluid grids).
+      auto reinit = [&]() {
+        if (m->reinit_every > 0 && m->reinit_iters > 0) {
+          if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
+            launch_reinit(ctx, m, m->reinit_every, ctx->s_ls);
+          else if ((ctx->steps_done_host + 1) % m->reinit_every == 0)
+            launch_reinit(ctx, m, 0, ctx->s_ls);
+        }
+      };
       auto fork_level_set = [&]() {
         cudaEventRecord(ctx->ev_ls_fork, ctx->stream);
         cudaStreamWaitEvent(ctx->s_ls, ctx->ev_ls_fork, 0);
@@ -492,20 +520,26 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
           return;
         }
         launch_ls_update(ctx, m, ctx->s_ls);
-        if (m->reinit_every > 0 && m->reinit_iters > 0) {
-          if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
-            launch_reinit(ctx, m, m->reinit_every, ctx->s_ls);
-          else if ((ctx->steps_done_host + 1) % m->reinit_every == 0)
-            launch_reinit(ctx, m, 0, ctx->s_ls);
-        }
+        reinit();
         cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
       };
       if (overlapped) {
         // ghost fill and flux update interleaved across SM partitions; the
         // flux phase here is the update of the tiles near the interface
         launch_ghost_fill_overlapped(ctx, m);
-        fork_level_set();
-        launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->stream);
+        // The level set's advection stages read phi and the velocity field,
+        // complete once the chain has written its cells' velocities; its
+        // writes of phi (copy, reinitialisation) wait for the ghost fill's
+        // last read of phi.
+        cudaStreamWaitEvent(ctx->s_ls, ctx->ev_chain, 0);
+        launch_ls_stages(ctx, m, ctx->s_ls);
+        cudaStreamWaitEvent(ctx->s_ls, ctx->ev_phi_free, 0);
+        launch_ls_copy(ctx, ctx->s_ls);
+        reinit();
+        cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
+        launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->s_near);
+        cudaEventRecord(ctx->ev_near, ctx->s_near);
+        cudaStreamWaitEvent(ctx->stream, ctx->ev_near, 0);
         cudaStreamWaitEvent(ctx->stream, ctx->ev_far, 0);   // the far tiles' flux update
         mark(3);
       } else {
@@ -549,6 +583,7 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
       }
     }
   }
+  ctx->cfl_counter = nullptr;
   if (phase_ms)
     for (int q = 0; q < 6; q++) cudaEventDestroy(ev[q]);
   return r;

@@ -38,7 +38,7 @@ struct FluxSmem {
   double fs[4][4][SR][SC];      // [face L,R,B,T][component][r][c]
   double fx[4][TY][TX + 1];
   double fy[4][TY + 1][TX];
-  double qd[4][NXF + NYF];      // queued faces: uR, pR, utL, utR (rhoL, uL, pL, rhoR sit in the flux slot)
+  double qd[6][NXF + NYF];      // queued faces: uR, pR, utL, utR, irhoL, irhoR (rhoL, uL, pL, rhoR sit in the flux slot)
   unsigned short qid[NXF + NYF];
 };
 
@@ -261,6 +261,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
         s.qid[e] = (unsigned short)k;
         slot[0] = d.rhoL; slot[cs] = d.uL; slot[2 * cs] = d.pL; slot[3 * cs] = d.rhoR;
         s.qd[0][k] = d.uR; s.qd[1][k] = d.pR; s.qd[2][k] = d.utL; s.qd[3][k] = d.utR;
+        s.qd[4][k] = d.irhoL; s.qd[5][k] = d.irhoR;
       }
     }
     __syncthreads();
@@ -274,6 +275,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
       FaceData d;
       d.rhoL = slot[0]; d.uL = slot[cs]; d.pL = slot[2 * cs]; d.rhoR = slot[3 * cs];
       d.uR = s.qd[0][k]; d.pR = s.qd[1][k]; d.utL = s.qd[2][k]; d.utR = s.qd[3][k];
+      d.irhoL = s.qd[4][k]; d.irhoR = s.qd[5][k];
       V4 f = rs_face_finish(xdir, gas, d, &st, &iters);
       slot[0] = f.a; slot[cs] = f.b; slot[2 * cs] = f.c; slot[3 * cs] = f.d;
     }

@@ -98,14 +98,22 @@ struct gfm_ctx {
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist
   int overlap;            // GFM_OVERLAP_* mode (gfm_set_overlap)
-  cudaStream_t s_ls;      // level-set update beside the flux update
+  cudaStream_t s_ls;      // level-set update beside the flux update (highest priority)
   cudaEvent_t ev_ls_fork, ev_ls_done;
+  // overlapped schedule: the work after the interface chain (near-field
+  // extrapolation and flux update) on a highest-priority stream, so that its
+  // CTAs take the SMs that the far field's flux update frees
+  cudaStream_t s_near;
+  cudaEvent_t ev_near, ev_phi_free;
   struct gfm_mlp* mlp;    // learned proposal for the interface solves (gfm_set_mlp), or null
   float* cap_X;           // capture of gated interface problems (gfm_capture_interface_problems), or null
   float* cap_Y;
   int* cap_count;
   int cap;
   int graph_mode;         // launches are being recorded into a CUDA graph
+  // the step's CFL reduction runs inside the ghost fill's conversion (k_prims)
+  // with this last-block counter; null when a separate k_cfl computes dt
+  unsigned int* cfl_counter;
 };
 
 namespace gfm {
@@ -167,6 +175,8 @@ void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
+void launch_ls_stages(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
+void launch_ls_copy(gfm_ctx* ctx, cudaStream_t s);
 void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_vof_update(gfm_ctx* ctx, cudaStream_t s);
 void launch_end_step(gfm_ctx* ctx);

@@ -413,9 +413,10 @@ GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
 }
 // conserved_to_primitives together with is_physical_state of the same state:
 // both compute u, v and e with the same operations, done here once.
-GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys) {
+GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys, Recip* Rout = nullptr) {
   double rho = U.a;
   const Recip R = recip(rho);
+  if (Rout) *Rout = R;
   double u = rdiv(U.b, R);
   double v = rdiv(U.c, R);
   double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
@@ -483,6 +484,8 @@ struct RSSide {
   double ipb;         // 1 / pb
   double G4c;         // G4 c
   double irc;         // 1 / (rho c)
+  double irho;        // 1 / rho when the caller has it (has_irho), else filled in by rs_side_consts
+  bool has_irho;
 };
 
 // The state itself; the constants that only iteration and wave sampling use
@@ -492,12 +495,21 @@ GFM_HD RSSide rs_side(double rho, double u, double p, const Gas& k) {
   s.rho = rho; s.u = u; s.p = p;
   s.pb = p + k.pinf;
   s.c = 0.0; s.AK = 0.0; s.BK = 0.0; s.ipb = 0.0; s.G4c = 0.0; s.irc = 0.0;
+  s.irho = 0.0; s.has_irho = false;
+  return s;
+}
+// the same with 1/rho already formed (the correctly rounded quotient, as
+// rs_side_consts would form it)
+GFM_HD RSSide rs_side_r(double rho, double irho, double u, double p, const Gas& k) {
+  RSSide s = rs_side(rho, u, p, k);
+  s.irho = irho;
+  s.has_irho = true;
   return s;
 }
 // Two divisions and one square root per side (1/rho, 1/pb, c); A = G5/rho and
 // 1/(rho c) = c / (g pb) follow by multiplication.
 GFM_HD void rs_side_consts(RSSide& s, const Gas& k) {
-  double irho = 1.0 / s.rho;
+  double irho = s.has_irho ? s.irho : 1.0 / s.rho;
   s.ipb = 1.0 / s.pb;
   s.c = sqrt(k.g * s.pb * irho);
   s.AK = k.G5 * irho;
@@ -705,24 +717,27 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
 //                  and their tangential velocities; returns rs_solve's
 //                  no-wave test (equal u_n and p)
 //   rs_face_finish the solve, the sample at x/t = 0 and the flux.
-struct FaceData { double rhoL, uL, pL, rhoR, uR, pR, utL, utR; };
+// irhoL, irhoR: the conversions' reciprocals 1/rho, which the solve reuses
+struct FaceData { double rhoL, uL, pL, rhoR, uR, pR, utL, utR, irhoL, irhoR; };
 
 GFM_HD bool rs_face_front(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status,
                           FaceData& d) {
   bool okL, okR;
-  V4 Lp = cons_to_prims_phys(k.g, k.pinf, UL, &okL);
-  V4 Rp = cons_to_prims_phys(k.g, k.pinf, UR, &okR);
+  Recip RL, RR;
+  V4 Lp = cons_to_prims_phys(k.g, k.pinf, UL, &okL, &RL);
+  V4 Rp = cons_to_prims_phys(k.g, k.pinf, UR, &okR, &RR);
   if (!okL || !okR) *status |= ST_UNPHYSICAL;
   d.rhoL = Lp.a; d.uL = paralleltox ? Lp.b : Lp.c; d.pL = Lp.d;
   d.rhoR = Rp.a; d.uR = paralleltox ? Rp.b : Rp.c; d.pR = Rp.d;
+  d.irhoL = RL.y; d.irhoR = RR.y;
   d.utL = paralleltox ? Lp.c : Lp.b;
   d.utR = paralleltox ? Rp.c : Rp.b;
   return c_eq(d.uL, d.uR) && c_eq(d.pL, d.pR);
 }
 
 GFM_HD V4 rs_face_finish(bool paralleltox, const Gas& k, const FaceData& d, uint32_t* status, int* iters) {
-  RSSide L = rs_side(d.rhoL, d.uL, d.pL, k);
-  RSSide R = rs_side(d.rhoR, d.uR, d.pR, k);
+  RSSide L = rs_side_r(d.rhoL, d.irhoL, d.uL, d.pL, k);
+  RSSide R = rs_side_r(d.rhoR, d.irhoR, d.uR, d.pR, k);
   RSStar st = rs_solve(L, k, R, k);
   *status |= st.status;
   *iters += st.iters;

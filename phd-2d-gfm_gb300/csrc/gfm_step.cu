@@ -22,8 +22,10 @@ constexpr int CHUNK_T = 512;
 // ---------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double dmax_std(double a, double b) { return (a < b) ? b : a; }  // std::max
-__device__ __forceinline__ double dmin_std(double a, double b) { return (b < a) ? b : a; }  // std::min
+// std::max and std::min, NaN semantics included, with the comparison on the
+// integer pipe (c_lt): the FP64 pipe bounds the kernels that use them
+__device__ __forceinline__ double dmax_std(double a, double b) { return c_lt(a, b) ? b : a; }
+__device__ __forceinline__ double dmin_std(double a, double b) { return c_lt(b, a) ? b : a; }
 
 // Normal planes (k_prims): 0,1 raw central-difference gradient of phi,
 // 2,3 unit normal with the reference's fallback to (1,0) below 1e-12
@@ -131,6 +133,47 @@ __global__ void __launch_bounds__(256) k_cfl(CflArgs a) {
   }
 }
 
+// The start-of-step flags of k_cfl for the two-fluid steps whose CFL
+// reduction runs inside the ghost fill's conversion (k_prims): nothing before
+// the flux and level-set updates reads dt, so dt may follow the conversion.
+__global__ void k_step_begin(GridP P, DevTime* D, double CFL, double T, int ogfm) {
+  if (!(D->t < T)) {
+    D->active = 0;
+    return;
+  }
+  D->T = T;
+  D->CFL = (D->numsteps < 5) ? ((0.2 < CFL) ? 0.2 : CFL) : CFL;   // std::min(CFL, 0.2)
+  D->active = 1;
+  const int g = P.g;
+  for (int f = 0; f < 2; f++) {
+    if (ogfm) {
+      D->rc[4 * f + 0] = g + P.Ny; D->rc[4 * f + 1] = g; D->rc[4 * f + 2] = g + P.Nx; D->rc[4 * f + 3] = g;
+    } else {
+      D->rc[4 * f + 0] = g; D->rc[4 * f + 1] = g + P.Ny; D->rc[4 * f + 2] = g; D->rc[4 * f + 3] = g + P.Nx;
+    }
+  }
+  D->newton_iters = 0ull;
+  D->ifc_iters = 0ull;
+  D->ifc_gated = 0;
+}
+
+// dt from the reduced maxima, by the last CTA of a fused reduction (the same
+// operations as the last CTA of k_cfl)
+__device__ void cfl_dt_from_max(const GridP& P, DevTime* D, unsigned int* counter) {
+  __threadfence();
+  const double maxu = __longlong_as_double((long long)atomicAdd(&D->maxu_bits, 0ull));
+  const double maxv = __longlong_as_double((long long)atomicAdd(&D->maxv_bits, 0ull));
+  const double cfl = D->CFL;
+  const double dx_u = P.dx / maxu, dy_v = P.dy / maxv;
+  double dt = cfl * ((dy_v < dx_u) ? dy_v : dx_u);
+  if (D->t + dt > D->T) dt = D->T - D->t;
+  if (!(dt > 0.0)) D->status |= ST_DT_NONPOSITIVE;
+  D->dt = dt;
+  D->maxu_bits = 0ull;
+  D->maxv_bits = 0ull;
+  *counter = 0u;
+}
+
 __global__ void k_end_step(DevTime* D) {
   if (D->active) {
     D->t += D->dt;
@@ -154,6 +197,10 @@ void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int
   int blocks = (int)((n + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
   k_cfl<<<blocks, 256, 0, ctx->stream>>>(a); counted();
+}
+
+void launch_step_begin(gfm_ctx* ctx, double CFL, double T, bool ogfm) {
+  k_step_begin<<<1, 1, 0, ctx->stream>>>(ctx->P, ctx->dtime, CFL, T, ogfm ? 1 : 0); counted();
 }
 
 // ---------------------------------------------------------------------------
@@ -232,6 +279,8 @@ struct PrimArgs {
   int* chunk_count;
   DevTime* D;
   int check_both;             // 1: assert both grids (OGFM, RGFM); 0: the phi-selected one
+  unsigned int* cfl_counter;  // non-null: also the step's CFL reduction and dt (k_cfl's)
+  double* vel;                // non-null: the real cells' velocity field (overlapped schedule)
 };
 
 __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
@@ -245,6 +294,7 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
   const Recip r2dx = recip(2.0 * P.dx), r2dy = recip(2.0 * P.dy);   // central-difference divisors
   uint32_t st = 0;
   int cnt = 0;
+  double mu = 0.0, mv = 0.0;   // CFL maxima over the real cells (k_cfl's)
   for (int q = threadIdx.x; q < CHUNK; q += CHUNK_T) {
     int64_t lin = base + q;
     if (lin >= n) break;
@@ -255,16 +305,41 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
     double ph = a.phi[c];
     // conversion and is_physical_state of the same state share their operations
     bool ok1, ok2;
-    V4 w1 = cons_to_prims_phys(P.g1, P.p1, u1, &ok1);
-    V4 w2 = cons_to_prims_phys(P.g2, P.p2, u2, &ok2);
+    Recip R1, R2;
+    V4 w1 = cons_to_prims_phys(P.g1, P.p1, u1, &ok1, &R1);
+    V4 w2 = cons_to_prims_phys(P.g2, P.p2, u2, &ok2, &R2);
     if (a.check_both) {
       if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
     } else {
-      if (!(ph <= 0.0 ? ok1 : ok2)) st |= ST_UNPHYSICAL;
+      if (!(c_le0(ph) ? ok1 : ok2)) st |= ST_UNPHYSICAL;
+    }
+    if (a.cfl_counter && is_real(P, i, j)) {
+      // k_cfl's wave speeds from this conversion: the fluid with phi < 0 is
+      // fluid 1, u = (rho u)/rho and p are the values just computed, and for
+      // rho > 0 the quotient |rho u| / rho is |u| (round-to-nearest is
+      // symmetric), otherwise it is formed as k_cfl forms it
+      const bool f1 = c_lt0(ph);
+      const V4& u = f1 ? u1 : u2;
+      const V4& w = f1 ? w1 : w2;
+      const Recip& R = f1 ? R1 : R2;
+      const double cs = eos_soundspeed_r(f1 ? P.g1 : P.g2, f1 ? P.p1 : P.p2, w.d, R);
+      const bool pos = c_gt0(u.a);
+      const double xu = (pos ? fabs(w.b) : rdiv(fabs(u.b), R)) + cs;
+      const double xv = (pos ? fabs(w.c) : rdiv(fabs(u.c), R)) + cs;
+      mu = dmax_std(mu, xu);   // NaN never replaces the running max (std::max semantics)
+      mv = dmax_std(mv, xv);
     }
     store4(a.W1, P, c, w1);
     store4(a.W2, P, c, w2);
     if (a.Wc1) { store4(a.Wc1, P, c, w1); store4(a.Wc2, P, c, w2); }
+    if (a.vel && is_real(P, i, j)) {
+      // the velocity field of a real cell is its real fluid's velocity after
+      // the ghost fill, which changes only the real fluid of interfacial cells
+      // (k_ifc_vel) and the other fluid of every cell: these are its values
+      const V4& w = c_le0(ph) ? w1 : w2;
+      a.vel[c] = w.b;
+      a.vel[c + P.plane] = w.c;
+    }
     double gx = 0.0, gy = 0.0;
     if (i >= 1 && i < P.nr - 1 && j >= 1 && j < P.nc - 1) {
       gx = rdiv(a.phi[c + 1] - a.phi[c - 1], r2dx);
@@ -274,7 +349,7 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
     // fallback (sourcecode/GFM_riemann.cpp:58-68), once per step
     double nn = sqrt(gx * gx + gy * gy);
     double ux = 1.0, uy = 0.0;
-    if (!(nn < 1e-12)) {
+    if (!c_lt(nn, 1e-12)) {
       const Recip rn = recip(nn);
       ux = rdiv(gx, rn);
       uy = rdiv(gy, rn);
@@ -286,9 +361,9 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
     a.nrm[c + 4 * P.plane] = nn;
     uint8_t m = 0;
     if (is_real(P, i, j)) {
-      bool s = ph <= 0.0;
-      m = ((a.phi[c - 1] <= 0.0) != s || (a.phi[c + 1] <= 0.0) != s || (a.phi[c - P.pitch] <= 0.0) != s ||
-           (a.phi[c + P.pitch] <= 0.0) != s) ? 1 : 0;
+      bool s = c_le0(ph);
+      m = (c_le0(a.phi[c - 1]) != s || c_le0(a.phi[c + 1]) != s || c_le0(a.phi[c - P.pitch]) != s ||
+           c_le0(a.phi[c + P.pitch]) != s) ? 1 : 0;
     }
     a.mask[c] = m;
     a.ifc_map[c] = -1;
@@ -300,6 +375,28 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
   if ((threadIdx.x & 31) == 0 && wst) atomicOr(&a.D->status, wst);
   __syncthreads();
   if (threadIdx.x == 0) a.chunk_count[blockIdx.x] = s_cnt;
+  if (a.cfl_counter) {
+    __shared__ double s_u[CHUNK_T / 32], s_v[CHUNK_T / 32];
+    __shared__ bool s_last;
+    for (int o = 16; o > 0; o >>= 1) {
+      mu = dmax_std(mu, __shfl_xor_sync(0xffffffffu, mu, o));
+      mv = dmax_std(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { s_u[w] = mu; s_v[w] = mv; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int q = 1; q < CHUNK_T / 32; q++) { mu = dmax_std(mu, s_u[q]); mv = dmax_std(mv, s_v[q]); }
+      // positive doubles order as their bit patterns
+      atomicMax(&a.D->maxu_bits, (unsigned long long)__double_as_longlong(mu));
+      atomicMax(&a.D->maxv_bits, (unsigned long long)__double_as_longlong(mv));
+      __threadfence();
+      const unsigned int prev = atomicAdd(a.cfl_counter, 1u);
+      s_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) cfl_dt_from_max(P, a.D, a.cfl_counter);
+  }
 }
 
 // Stage 2: ordered compaction of the interfacial cells (row-major order).
@@ -1571,6 +1668,22 @@ __global__ void k_ifc_scatter(ScatterArgs a) {
   }
 }
 
+// Velocity field of the interfacial cells after the Riemann / real GFM loop:
+// the star state it wrote into the cell's real fluid (the rest of the real
+// cells' field comes from the conversion, k_prims with a velocity plane).
+__global__ void k_ifc_vel(GridP P, const int* list, const double* out, double* vel, const DevTime* D) {
+  if (!D->active) return;
+  const int n = D->n_ifc;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int i, j;
+    linear_to_ij(P, list[k], i, j);
+    const int64_t c = cidx(P, i, j);
+    const double* o = out + (int64_t)k * IFC_OUT;
+    vel[c] = o[1];
+    vel[c + P.plane] = o[2];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // End of the ghost fill: primitives -> conserved on the whole padded grid,
 // velocity field (real fluid's velocity per cell), and for the original GFM
@@ -1611,7 +1724,7 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
       const bool nr = a.near_cell[cidx(P, s.i, s.j)] != 0;
       if ((a.sel == 2) != nr) continue;
     }
-    bool f1 = a.phi[c] <= 0.0;
+    bool f1 = c_le0(a.phi[c]);
     if (a.ogfm) {
       V4 w1 = load4(a.W1, P, c), w2 = load4(a.W2, P, c);
       if (is_real(P, i, j)) {
@@ -1640,6 +1753,12 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
       const double* V = f1 ? a.V1 : a.V2;
       a.vel[c] = V[c + P.plane];
       a.vel[c + P.plane] = V[c + 2 * P.plane];
+    } else if (a.vel_mode == 3) {   // ghost cells only (k_prims and k_ifc_vel write the real cells)
+      if (!is_real(P, i, j)) {
+        const double* V = f1 ? a.V1 : a.V2;
+        a.vel[c] = V[c + P.plane];
+        a.vel[c + P.plane] = V[c + 2 * P.plane];
+      }
     } else if (a.vel_mode == 1) {
       double vx = 0.0, vy = 0.0;
       if (a.mask[c]) { const double* V = f1 ? a.V1 : a.V2; vx = V[c + P.plane]; vy = V[c + 2 * P.plane]; }
@@ -1726,7 +1845,7 @@ __global__ void __launch_bounds__(256) k_ext_vel(GridP P, const double* S, doubl
 // Ghost cells: mirror (or periodic) copies, computed by their own threads.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double houc5(double a, const double* f, int64_t c, int64_t st, double inv60h) {
-  if (a >= 0.0)
+  if (c_ge0(a))
     return (-2.0 * f[c - 3 * st] + 15.0 * f[c - 2 * st] - 60.0 * f[c - st] + 20.0 * f[c] + 30.0 * f[c + st] -
             3.0 * f[c + 2 * st]) * inv60h;
   return (3.0 * f[c - 2 * st] - 30.0 * f[c - st] - 20.0 * f[c] + 60.0 * f[c + st] - 15.0 * f[c + 2 * st] +
@@ -1750,8 +1869,8 @@ __global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, cons
     double u = vel[c], v = vel[c + P.plane];
     double fx, fy;
     if (ORDER == 1) {
-      fx = (u >= 0.0) ? (X[c] - X[c - 1]) * idx : (X[c + 1] - X[c]) * idx;
-      fy = (v >= 0.0) ? (X[c] - X[c - P.pitch]) * idy : (X[c + P.pitch] - X[c]) * idy;
+      fx = c_ge0(u) ? (X[c] - X[c - 1]) * idx : (X[c + 1] - X[c]) * idx;
+      fy = c_ge0(v) ? (X[c] - X[c - P.pitch]) * idy : (X[c + P.pitch] - X[c]) * idy;
     } else {
       fx = houc5(u, X, c, 1, i60x);
       fy = houc5(v, X, c, P.pitch, i60y);
@@ -1812,7 +1931,7 @@ __global__ void __launch_bounds__(256) k_reinit_iter(GridP P, const double* cur,
     double cc = (f - cur[c - P.pitch]) * idy;
     double d = (cur[c + P.pitch] - f) * idy;
     double gx, gy;
-    if (sg > 0.0) {
+    if (c_gt0(sg)) {
       double ap = dmax_std(a, 0.0), bm = dmin_std(b, 0.0), cp = dmax_std(cc, 0.0), dm = dmin_std(d, 0.0);
       gx = dmax_std(ap * ap, bm * bm);
       gy = dmax_std(cp * cp, dm * dm);
@@ -1930,6 +2049,8 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
   pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
   pa.check_both = (variant == GFM_OGFM || variant == GFM_RIEMANN) ? 1 : 0;
+  pa.cfl_counter = ctx->cfl_counter;
+  pa.vel = nullptr;   // k_finalize writes the velocity field
   k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa); counted();
   k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
                                               ctx->ifc_map, ctx->dtime); counted();
@@ -2106,7 +2227,7 @@ static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStr
   f.U1 = ctx->U[0]; f.U2 = ctx->U[1];
   f.vel = ctx->vel; f.D = ctx->dtime;
   f.ogfm = 0;
-  f.vel_mode = 0;
+  f.vel_mode = 3;   // ghost cells: k_prims and k_ifc_vel write the real cells' velocities
   f.near_cell = ctx->near_cell;
   f.sel = sel;
   f.list = (sel == 2) ? ctx->near_list : nullptr;
@@ -2128,6 +2249,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
   pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
   pa.check_both = (variant == GFM_RIEMANN) ? 1 : 0;
+  pa.cfl_counter = ctx->cfl_counter;
+  pa.vel = ctx->vel;  // real cells' velocity field, for a level set that starts after the chain
   k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa);
   counted();
   k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
@@ -2179,6 +2302,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   counted();
+  k_ifc_vel<<<chain_ctas, 256, 0, ctx->s_chain>>>(P, ctx->ifc_list, ctx->ifc_out, ctx->vel, ctx->dtime);
+  counted();
   cudaEventRecord(ctx->ev_chain, ctx->s_chain);
   if (ctx->timing) cudaEventRecord(ctx->tev[1], ctx->s_chain);
 
@@ -2202,9 +2327,11 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   cudaEventRecord(ctx->ev_far, ctx->s_far);
   if (ctx->timing) cudaEventRecord(ctx->tev[2], ctx->s_far);
 
-  // after the chain: the true extrapolation (the loop's writes overlaid on the
-  // first sweep's reads), conserved grids of near cells, flux update of near tiles
-  cudaStreamWaitEvent(s, ctx->ev_chain, 0);
+  // after the chain, on the highest-priority stream: the true extrapolation
+  // (the loop's writes overlaid on the first sweep's reads), conserved grids
+  // of near cells, flux update of near tiles
+  cudaStream_t sn = ctx->s_near;
+  cudaStreamWaitEvent(sn, ctx->ev_chain, 0);
   {
     double* bufA[2] = {ctx->Wt[0], ctx->Wt[1]};
     double* bufB[2] = {ctx->Wc[0], ctx->Wc[1]};
@@ -2212,23 +2339,26 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = (it & 1) ? bufB : bufA;
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, s, ctx->band_list, ctx->list_n);
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, sn, ctx->band_list, ctx->list_n);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
-    finalize_sel(ctx, fin, 2, s);
+    finalize_sel(ctx, fin, 2, sn);
   }
-  if (ctx->timing) cudaEventRecord(ctx->tev[3], s);
-  // The near tiles read far cells too, and the level set reads the far cells'
-  // velocities: both wait for the far cells' conversion, not for the far
-  // tiles' flux update, which writes only its own tiles of Unew.
-  cudaStreamWaitEvent(s, ctx->ev_far_final, 0);
-  if (ctx->timing) cudaEventRecord(ctx->tev[4], s);
-  // the caller forks the level set, launches the flux update of the near
-  // tiles and then waits for ev_far
+  if (ctx->timing) cudaEventRecord(ctx->tev[3], sn);
+  // The near tiles read far cells too: they wait for the far cells'
+  // conversion, not for the far tiles' flux update, which writes only its own
+  // tiles of Unew.  From here on nothing in the ghost fill reads phi.
+  cudaStreamWaitEvent(sn, ctx->ev_far_final, 0);
+  cudaEventRecord(ctx->ev_phi_free, sn);
+  if (ctx->timing) cudaEventRecord(ctx->tev[4], sn);
+  // the caller issues the level set and the flux update of the near tiles
+  // (on s_near) and joins s_near and the far stream back into ctx->stream
 }
 
-void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
+// the advection stages read phi and the velocity field and write phi_a /
+// phi_b; the copy writes the result into phi
+void launch_ls_stages(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
   const GridP& P = ctx->P;
   int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
   if (m->ls_order == 1) {
@@ -2238,7 +2368,17 @@ void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
     k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime); counted();
     k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
   }
-  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0); counted();
+}
+
+void launch_ls_copy(gfm_ctx* ctx, cudaStream_t s) {
+  const GridP& P = ctx->P;
+  k_copy_plane<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0);
+  counted();
+}
+
+void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
+  launch_ls_stages(ctx, m, s);
+  launch_ls_copy(ctx, s);
 }
 
 // reinitialisation: iterations alternate phi -> phi_a -> phi ...; an odd
