@@ -236,10 +236,10 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     for (int b = 0; b < 2; b++)
       for (int f = 0; f < 2; f++) alloc((void**)&ctx->S[b][f], 4 * plane_b);
     alloc((void**)&ctx->near_cell, (size_t)P.plane);
-    alloc((void**)&ctx->band_cell, (size_t)P.plane);
-    alloc((void**)&ctx->band_list, (size_t)P.nr * P.nc * sizeof(int));
-    alloc((void**)&ctx->near_list, (size_t)P.nr * P.nc * sizeof(int));
-    alloc((void**)&ctx->list_n, 2 * sizeof(int));
+    alloc((void**)&ctx->band_cls, sizeof(int) * (size_t)P.plane);
+    ctx->band_stride = (int64_t)P.nr * P.nc;
+    alloc((void**)&ctx->band_list, 6 * (size_t)ctx->band_stride * sizeof(int));
+    alloc((void**)&ctx->list_n, 8 * sizeof(int));
     alloc((void**)&ctx->tile_near, sizeof(int) * (size_t)flux_tiles_x(P) * flux_tiles_y(P));
     int dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
@@ -251,10 +251,14 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
       if (e == cudaSuccess) e = cudaEventCreate(&ctx->tev[q]);
     int prio_lo = 0, prio_hi = 0;
     if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->s_ls, cudaStreamNonBlocking, prio_hi);
+    // the near-field work after the interface chain is on the critical path:
+    // the level set (which fills gaps beside it) ranks one level below
+    const int prio_ls = (prio_hi < prio_lo) ? prio_hi + 1 : prio_hi;
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->s_ls, cudaStreamNonBlocking, prio_ls);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->s_near, cudaStreamNonBlocking, prio_hi);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_near, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_phi_free, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_lists, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_done, cudaEventDisableTiming);
     if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
@@ -285,8 +289,8 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->probe_ij); cudaFree(ctx->probe_w);
   for (int b = 0; b < 2; b++)
     for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
-  cudaFree(ctx->near_cell); cudaFree(ctx->band_cell); cudaFree(ctx->tile_near);
-  cudaFree(ctx->band_list); cudaFree(ctx->near_list); cudaFree(ctx->list_n);
+  cudaFree(ctx->near_cell); cudaFree(ctx->band_cls); cudaFree(ctx->tile_near);
+  cudaFree(ctx->band_list); cudaFree(ctx->list_n);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_chain) cudaEventDestroy(ctx->ev_chain);
   if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);
@@ -305,6 +309,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   }
   if (ctx->ev_near) cudaEventDestroy(ctx->ev_near);
   if (ctx->ev_phi_free) cudaEventDestroy(ctx->ev_phi_free);
+  if (ctx->ev_lists) cudaEventDestroy(ctx->ev_lists);
   cudaFree(ctx->dtime);
   cudaFree(extra(ctx).counters);
   cudaFree(extra(ctx).mass_part);

@@ -86,10 +86,11 @@ struct gfm_ctx {
   // the rest (see launch_ghost_fill_overlapped)
   double* S[2][2];        // speculative extrapolation ping-pong [buffer][fluid]
   uint8_t* near_cell;     // real cells within 6 (Chebyshev) of an interfacial cell
-  uint8_t* band_cell;     // real cells within 12: those the exact extrapolation writes
-  int* band_list;         // cells (ghost cells included) whose source is a band cell
-  int* near_list;         // cells whose source is a near cell
-  int* list_n;            // 2 counts: band_list, near_list
+  int* band_cls;          // real cells within 11: 12 - the distance (the exact extrapolation's band)
+  int* band_list;         // 6 segments of band_stride entries: the cells (ghost cells included, by
+                          // their source) at distance <= 6 (segment 0), 7, 8, 9, 10, 11
+  int64_t band_stride;
+  int* list_n;            // the 6 segments' counts
   int* tile_near;         // per flux tile: its region holds a near cell
   cudaStream_t s_chain, s_far;
   cudaEvent_t ev_fork, ev_chain, ev_far;
@@ -98,13 +99,14 @@ struct gfm_ctx {
   int timing;
   int overlap_ok;         // SM partitions (or two side streams) exist
   int overlap;            // GFM_OVERLAP_* mode (gfm_set_overlap)
-  cudaStream_t s_ls;      // level-set update beside the flux update (highest priority)
+  cudaStream_t s_ls;      // level-set update beside the flux update (second-highest priority)
   cudaEvent_t ev_ls_fork, ev_ls_done;
   // overlapped schedule: the work after the interface chain (near-field
   // extrapolation and flux update) on a highest-priority stream, so that its
   // CTAs take the SMs that the far field's flux update frees
   cudaStream_t s_near;
   cudaEvent_t ev_near, ev_phi_free;
+  cudaEvent_t ev_lists;   // band lists, near cells and flux-tile flags written (far stream)
   struct gfm_mlp* mlp;    // learned proposal for the interface solves (gfm_set_mlp), or null
   float* cap_X;           // capture of gated interface problems (gfm_capture_interface_problems), or null
   float* cap_Y;

@@ -591,8 +591,8 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   const Gas kA = rfirst ? kR : kL, kB = rfirst ? kL : kR;
   for (;;) {
     double fA, fAd, fB, fBd;
-    rs_prefun(A, kA, pold, &fA, &fAd);
-    rs_prefun(B, kB, pold, &fB, &fBd);
+    rs_prefun_merged(A, kA, pold, &fA, &fAd);   // lanes of a warp may take different branches
+    rs_prefun_merged(B, kB, pold, &fB, &fBd);
     fL = rfirst ? fB : fA; fLd = rfirst ? fBd : fAd;
     fR = rfirst ? fA : fB; fRd = rfirst ? fAd : fBd;
     p = pold - (fL + fR + udiff) / (fLd + fRd);
@@ -659,6 +659,14 @@ GFM_HD double rs_rho_star(const RSSide& K, const Gas& k, double pstar) {
 }
 
 // Toro's SAMPLE at speed S; returns (rho, u, p).
+//
+// The side K that S falls on (left of the contact: L) is selected first and
+// one code path serves both sides, with the sign of each wave speed term taken
+// from the side: a warp whose lanes sample different sides issues the FP64
+// work once, not once per side.  Every value comes from the same operations
+// as Toro's four branches (a - b is formed as a + (-b), which is the same
+// IEEE operation), and a rarefaction's star density shares the logarithm of
+// (p* + pinf)/(p_K + pinf) with the tail speed (gfm_pow is exp(y log x)).
 struct RS1D { double rho, u, p; };
 GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, const RSStar& st,
                       double S) {
@@ -668,45 +676,44 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
     else { w.rho = R.rho; w.u = R.u; w.p = R.p; }
     return w;
   }
-  if (c_le(S, st.u)) {  // left of contact
-    if (c_le(st.p, L.p)) {  // left rarefaction
-      double shl = L.u - L.c;
-      if (c_le(S, shl)) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
-      double cml = L.c * gfm_pow((st.p + kL.pinf) * L.ipb, kL.G1);
-      double stl = st.u - cml;
-      if (c_gt(S, stl)) { w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w; }
-      double c = kL.G5 * (L.c + kL.G7 * (L.u - S));
-      double cr = c / L.c;
-      w.rho = L.rho * gfm_pow(cr, kL.G4);
-      w.u = kL.G5 * (L.c + kL.G7 * L.u + S);
-      w.p = L.pb * gfm_pow(cr, kL.G3) - kL.pinf;
-      return w;
-    } else {  // left shock
-      double pml = (st.p + kL.pinf) * L.ipb;
-      double sl = L.u - L.c * sqrt(kL.G2 * pml + kL.G1);
-      if (c_le(S, sl)) { w.rho = L.rho; w.u = L.u; w.p = L.p; return w; }
-      w.rho = rs_rho_star(L, kL, st.p); w.u = st.u; w.p = st.p; return w;
-    }
-  } else {  // right of contact
-    if (c_gt(st.p, R.p)) {  // right shock
-      double pmr = (st.p + kR.pinf) * R.ipb;
-      double sr = R.u + R.c * sqrt(kR.G2 * pmr + kR.G1);
-      if (c_ge(S, sr)) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
-      w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w;
-    } else {  // right rarefaction
-      double shr = R.u + R.c;
-      if (c_ge(S, shr)) { w.rho = R.rho; w.u = R.u; w.p = R.p; return w; }
-      double cmr = R.c * gfm_pow((st.p + kR.pinf) * R.ipb, kR.G1);
-      double str = st.u + cmr;
-      if (c_le(S, str)) { w.rho = rs_rho_star(R, kR, st.p); w.u = st.u; w.p = st.p; return w; }
-      double c = kR.G5 * (R.c - kR.G7 * (R.u - S));
-      double cr = c / R.c;
-      w.rho = R.rho * gfm_pow(cr, kR.G4);
-      w.u = kR.G5 * (-R.c + kR.G7 * R.u + S);
-      w.p = R.pb * gfm_pow(cr, kR.G3) - kR.pinf;
-      return w;
-    }
+  const bool left = c_le(S, st.u);
+  const double Krho = left ? L.rho : R.rho, Ku = left ? L.u : R.u, Kp = left ? L.p : R.p;
+  const double Kpb = left ? L.pb : R.pb, Kc = left ? L.c : R.c, Kipb = left ? L.ipb : R.ipb;
+  const double pinf = left ? kL.pinf : kR.pinf, G1 = left ? kL.G1 : kR.G1, G2 = left ? kL.G2 : kR.G2;
+  const double G3 = left ? kL.G3 : kR.G3, G4 = left ? kL.G4 : kR.G4, G5 = left ? kL.G5 : kR.G5;
+  const double G6 = left ? kL.G6 : kR.G6, G7 = left ? kL.G7 : kR.G7, IG = left ? kL.IG : kR.IG;
+  // left: rarefaction when p* <= p_L; right: shock when p* > p_R
+  const bool shock = left ? !c_le(st.p, L.p) : c_gt(st.p, R.p);
+  const double pr = (st.p + pinf) * Kipb;
+  if (shock) {
+    const double q = Kc * sqrt(G2 * pr + G1);
+    const double sK = Ku + (left ? -q : q);   // shock speed
+    if (left ? c_le(S, sK) : c_ge(S, sK)) { w.rho = Krho; w.u = Ku; w.p = Kp; return w; }
+    // rs_rho_star behind the K wave
+    w.rho = c_gt(st.p, Kp) ? Krho * ((pr + G6) / (pr * G6 + 1.0)) : Krho * gfm_pow(pr, IG);
+    w.u = st.u; w.p = st.p;
+    return w;
   }
+  const double hK = Ku + (left ? -Kc : Kc);   // rarefaction head
+  if (left ? c_le(S, hK) : c_ge(S, hK)) { w.rho = Krho; w.u = Ku; w.p = Kp; return w; }
+  const bool zero = (as_bits(pr) & GFM_MAG_BITS) == 0;
+  const double lpr = zero ? 0.0 : gfm_log(pr);
+  const double cm = Kc * (zero ? gfm_pow(pr, G1) : gfm_exp(G1 * lpr));
+  const double tK = st.u + (left ? -cm : cm);   // rarefaction tail
+  if (left ? c_gt(S, tK) : c_le(S, tK)) {
+    // rs_rho_star of a rarefaction (p* <= p_K here, or NaN on the right)
+    w.rho = Krho * (zero ? gfm_pow(pr, IG) : gfm_exp(IG * lpr));
+    w.u = st.u; w.p = st.p;
+    return w;
+  }
+  // inside the fan
+  const double t = G7 * (Ku - S);
+  const double c = G5 * (Kc + (left ? t : -t));
+  const double cr = c / Kc;
+  w.rho = Krho * gfm_pow(cr, G4);
+  w.u = G5 * ((left ? Kc : -Kc) + G7 * Ku + S);
+  w.p = Kpb * gfm_pow(cr, G3) - pinf;
+  return w;
 }
 
 // pure_RS_exact::solve_RP (sourcecode/pure_RS_exact.cpp:9-73): flux of the

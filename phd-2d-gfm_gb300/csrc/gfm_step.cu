@@ -448,6 +448,18 @@ __global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mas
 // ---------------------------------------------------------------------------
 constexpr int IFC_OUT = 8;   // doubles of interface output per interfacial cell
 
+// Overlapped ghost fill: the cells within NEAR_RADIUS (Chebyshev) of an
+// interfacial cell depend on the interface loop through the six sweeps of
+// extrapolate_vector (one cell per sweep).  The exact extrapolation after the
+// loop writes, in sweep k = 1..6, the cells within BAND_RADIUS - k + 1 of an
+// interfacial cell: its reads one cell further out come from sweep k - 1
+// (sweep 1 reads the pre-loop primitives, exact everywhere), so sweep k is
+// exact where it writes and sweep 6 is exact on the near cells.  The band's
+// cells are listed in BAND_CLASSES segments by distance (k_band_lists).
+constexpr int NEAR_RADIUS = 6;
+constexpr int BAND_RADIUS = 11;
+constexpr int BAND_CLASSES = BAND_RADIUS - NEAR_RADIUS + 1;
+
 struct ExtrapArgs {
   GridP P;
   const double* S1; const double* S2;   // grid1/grid2 of this iteration
@@ -465,10 +477,14 @@ struct ExtrapArgs {
   // band: only cells whose boundary-condition source is marked are written
   // (the others keep the buffer's earlier values), or null for every cell
   const uint8_t* band;
-  // list: the cells to write (linear indices over the padded rows, count in
-  // *list_n), or null for every cell; a list replaces the band test
+  // list: the cells to write (linear indices over the padded rows), or null
+  // for every cell; a list replaces the band test.  It is `nclass`
+  // consecutive segments of `list_stride` entries, segment q holding
+  // list_n[q] cells.
   const int* list;
   const int* list_n;
+  int nclass;
+  int64_t list_stride;
   // (0.5 min(dx, dy)) / dx and / dy, formed once on the host
   double cdx, cdy;
 };
@@ -517,8 +533,14 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
   if (a.list) {
-    const int n = *a.list_n;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) extrap_cell(a, a.list[q]);
+    int cnt[BAND_CLASSES];
+    int n = 0;
+    for (int q = 0; q < a.nclass; q++) { cnt[q] = a.list_n[q]; n += cnt[q]; }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+      int q = 0, r = e;
+      while (r >= cnt[q]) { r -= cnt[q]; q++; }
+      extrap_cell(a, a.list[(int64_t)q * a.list_stride + r]);
+    }
     return;
   }
   const int64_t n = (int64_t)P.nr * P.nc;
@@ -527,36 +549,38 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
 }
 
 // The cells (over the padded rows, ghost cells included) whose
-// boundary-condition source is marked in `band`, and in `near`, appended to
-// band_list and near_list; counts in n2[0] and n2[1] (zeroed by the caller).
-// Order within a list is free: a sweep writes each listed cell from reads of
-// the previous buffer only.
-__global__ void k_band_lists(GridP P, const uint8_t* band, const uint8_t* near_cell, int* band_list, int* near_list,
-                             int* n2, const DevTime* D) {
+// boundary-condition source lies within BAND_RADIUS (Chebyshev) of an
+// interfacial cell, appended to the segment of their source's distance d:
+// segment 0 for d <= NEAR_RADIUS, segment d - NEAR_RADIUS beyond (counts in
+// n6[0..5], zeroed by the caller).  cls[c] = BAND_RADIUS + 1 - d of a real
+// cell c (k_band_mark), 0 beyond the band.  Also the near-cell mask of the
+// real cells (d <= NEAR_RADIUS).  Order within a segment is free: a sweep
+// writes each listed cell from reads of the previous buffer only.
+__global__ void k_band_lists(GridP P, const int* cls, uint8_t* near_cell, int* band_list, int64_t stride, int* n6,
+                             const DevTime* D) {
   if (!D->active) return;
   const int64_t n = (int64_t)P.nr * P.nc;
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = base + lane;
-    bool inb = false, inn = false;
+    int q = -1;
     if (k < n) {
-      BCSrc s = bc_source(P, (int)(k / P.nc), (int)(k % P.nc));
-      const int64_t c = cidx(P, s.i, s.j);
-      inb = band[c] != 0;
-      inn = near_cell[c] != 0;
+      const int i = (int)(k / P.nc), j = (int)(k % P.nc);
+      BCSrc s = bc_source(P, i, j);
+      const int v = cls[cidx(P, s.i, s.j)];
+      if (v > 0) q = (v >= BAND_RADIUS + 1 - NEAR_RADIUS) ? 0 : BAND_RADIUS + 1 - NEAR_RADIUS - v;
+      if (is_real(P, i, j)) near_cell[cidx(P, i, j)] = (v >= BAND_RADIUS + 1 - NEAR_RADIUS) ? 1 : 0;
     }
-    const unsigned mb = __ballot_sync(0xffffffffu, inb), mn = __ballot_sync(0xffffffffu, inn);
-    int ob = 0, on = 0;
-    if (lane == 0) {
-      if (mb) ob = atomicAdd(&n2[0], __popc(mb));
-      if (mn) on = atomicAdd(&n2[1], __popc(mn));
-    }
-    ob = __shfl_sync(0xffffffffu, ob, 0);
-    on = __shfl_sync(0xffffffffu, on, 0);
     const unsigned below = (1u << lane) - 1u;
-    if (inb) band_list[ob + __popc(mb & below)] = (int)k;
-    if (inn) near_list[on + __popc(mn & below)] = (int)k;
+    for (int c = 0; c < BAND_CLASSES; c++) {
+      const unsigned m = __ballot_sync(0xffffffffu, q == c);
+      if (!m) continue;
+      int o = 0;
+      if (lane == 0) o = atomicAdd(&n6[c], __popc(m));
+      o = __shfl_sync(0xffffffffu, o, 0);
+      if (q == c) band_list[(int64_t)c * stride + o + __popc(m & below)] = (int)k;
+    }
   }
 }
 
@@ -2007,6 +2031,7 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.ov_out = nullptr; e.ov_map = nullptr; e.overlay = 0;
     e.band = nullptr;
     e.list = nullptr; e.list_n = nullptr;
+    e.nclass = 0; e.list_stride = 0;
     extrap_coeffs(P, e);
     k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
@@ -2147,12 +2172,6 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
 // sequential schedule: every value is computed from the same inputs by the
 // same kernels.
 // ---------------------------------------------------------------------------
-constexpr int NEAR_RADIUS = 6;
-// The exact extrapolation after the loop writes only cells within BAND_RADIUS
-// of an interfacial cell.  Cells outside read stale values at the band's
-// edge, and a sweep carries a value one cell, so after the six sweeps the
-// values within 12 - 5 = 7 cells are exact, which covers the near cells.
-constexpr int BAND_RADIUS = 12;
 
 // marks the real cells within `radius` (Chebyshev) of an interfacial cell
 __global__ void k_near_mark(GridP P, const int* list, const DevTime* D, uint8_t* near_cell, int radius) {
@@ -2173,6 +2192,31 @@ __global__ void k_near_mark(GridP P, const int* list, const DevTime* D, uint8_t*
       continue;
     }
     near_cell[cidx(P, i, j)] = 1;
+  }
+}
+
+// cls[c] = max over interfacial cells of radius + 1 - (Chebyshev distance to
+// the real cell c), for the cells within `radius` (cls zeroed by the caller)
+__global__ void k_band_mark(GridP P, const int* list, const DevTime* D, int* cls, int radius) {
+  if (!D->active) return;
+  const int n = D->n_ifc;
+  const int side = 2 * radius + 1;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)n * side * side;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int k = (int)(q / (side * side));
+    int r = (int)(q % (side * side));
+    int64_t lin = list[k];
+    const int di = r / side - radius, dj = r % side - radius;
+    int i = (int)(lin / P.nc) + di;
+    int j = (int)(lin % P.nc) + dj;
+    if (P.periodic) {
+      i = ((i - P.g) % P.Ny + P.Ny) % P.Ny + P.g;
+      j = ((j - P.g) % P.Nx + P.Nx) % P.Nx + P.g;
+    } else if (!is_real(P, i, j)) {
+      continue;
+    }
+    const int d = max(abs(di), abs(dj));
+    atomicMax(&cls[cidx(P, i, j)], radius + 1 - d);
   }
 }
 
@@ -2197,7 +2241,7 @@ __global__ void k_tile_flags(GridP P, const uint8_t* near_cell, int* tile_near, 
 }
 
 static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, double* D1, double* D2, bool overlay,
-                         cudaStream_t s, const int* list, const int* list_n) {
+                         cudaStream_t s, const int* list, const int* list_n, int nclass) {
   const GridP& P = ctx->P;
   ExtrapArgs e;
   e.P = P;
@@ -2209,6 +2253,8 @@ static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, doubl
   e.overlay = overlay ? 1 : 0;
   e.band = nullptr;
   e.list = list; e.list_n = list_n;
+  e.nclass = nclass;
+  e.list_stride = ctx->band_stride;
   extrap_coeffs(P, e);
   // a listed sweep covers the band around the interface: a few percent of the grid
   const int blocks = list ? 2 * 152 : grid_blocks((int64_t)P.nr * P.nc, 256);
@@ -2230,8 +2276,8 @@ static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStr
   f.vel_mode = 3;   // ghost cells: k_prims and k_ifc_vel write the real cells' velocities
   f.near_cell = ctx->near_cell;
   f.sel = sel;
-  f.list = (sel == 2) ? ctx->near_list : nullptr;
-  f.list_n = (sel == 2) ? ctx->list_n + 1 : nullptr;
+  f.list = (sel == 2) ? ctx->band_list : nullptr;   // segment 0: the cells whose source is near
+  f.list_n = (sel == 2) ? ctx->list_n : nullptr;
   k_finalize<<<(sel == 2) ? 2 * 152 : grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(f);
   counted();
 }
@@ -2256,27 +2302,30 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
                                               ctx->ifc_map, ctx->dtime);
   counted();
-  // near field: cells within NEAR_RADIUS of an interfacial cell, and tiles reading them
-  cudaMemsetAsync(ctx->near_cell, 0, (size_t)P.plane, s);
-  cudaMemsetAsync(ctx->band_cell, 0, (size_t)P.plane, s);
   const int cap = P.Nx * P.Ny;
-  k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->near_cell,
-                                                              NEAR_RADIUS);
-  k_near_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, s>>>(P, ctx->ifc_list, ctx->dtime, ctx->band_cell,
-                                                              BAND_RADIUS);
-  counted(2);
-  cudaMemsetAsync(ctx->list_n, 0, 2 * sizeof(int), s);
-  k_band_lists<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(P, ctx->band_cell, ctx->near_cell,
-                                                                      ctx->band_list, ctx->near_list, ctx->list_n,
-                                                                      ctx->dtime);
-  counted();
-  const int ntx = flux_tiles_x(P), nty = flux_tiles_y(P);
-  k_tile_flags<<<(ntx * nty + 7) / 8, 256, 0, s>>>(P, ctx->near_cell, ctx->tile_near, ntx, nty, ctx->dtime);
-  counted();
   // extrapolate_vector(2) before the Riemann GFM's interface loop
   if (variant == GFM_RIEMANN) run_extrap(ctx, 2, false);
   cudaEventRecord(ctx->ev_fork, s);
   if (ctx->timing) cudaEventRecord(ctx->tev[0], s);
+
+  // far partition, first: the band around the interface (distance classes,
+  // lists), the near cells and the flux tiles that read them; the interface
+  // loop does not need them, the far field and the near path after the loop do
+  cudaStream_t sf = ctx->s_far;
+  cudaStreamWaitEvent(sf, ctx->ev_fork, 0);
+  cudaMemsetAsync(ctx->band_cls, 0, sizeof(int) * (size_t)P.plane, sf);
+  k_band_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, sf>>>(P, ctx->ifc_list, ctx->dtime, ctx->band_cls,
+                                                               BAND_RADIUS);
+  counted();
+  cudaMemsetAsync(ctx->list_n, 0, BAND_CLASSES * sizeof(int), sf);
+  k_band_lists<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, sf>>>(P, ctx->band_cls, ctx->near_cell,
+                                                                       ctx->band_list, ctx->band_stride,
+                                                                       ctx->list_n, ctx->dtime);
+  counted();
+  const int ntx = flux_tiles_x(P), nty = flux_tiles_y(P);
+  k_tile_flags<<<(ntx * nty + 7) / 8, 256, 0, sf>>>(P, ctx->near_cell, ctx->tile_near, ntx, nty, ctx->dtime);
+  counted();
+  cudaEventRecord(ctx->ev_lists, sf);
 
   // chain partition: the interface loop
   cudaStreamWaitEvent(ctx->s_chain, ctx->ev_fork, 0);
@@ -2309,13 +2358,12 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
 
   // far partition: extrapolation without the interface loop's writes,
   // conserved grids of far cells, flux update of far tiles
-  cudaStreamWaitEvent(ctx->s_far, ctx->ev_fork, 0);
   {
     const double* src1 = ctx->W[0];
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = ctx->S[it & 1];
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr, nullptr);
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr, nullptr, 0);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
@@ -2332,6 +2380,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   // of near cells, flux update of near tiles
   cudaStream_t sn = ctx->s_near;
   cudaStreamWaitEvent(sn, ctx->ev_chain, 0);
+  cudaStreamWaitEvent(sn, ctx->ev_lists, 0);
   {
     double* bufA[2] = {ctx->Wt[0], ctx->Wt[1]};
     double* bufB[2] = {ctx->Wc[0], ctx->Wc[1]};
@@ -2339,7 +2388,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = (it & 1) ? bufB : bufA;
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, sn, ctx->band_list, ctx->list_n);
+      // sweep it + 1 writes the cells within BAND_RADIUS - it: segments 0 .. BAND_CLASSES - 1 - it
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, sn, ctx->band_list, ctx->list_n, BAND_CLASSES - it);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
