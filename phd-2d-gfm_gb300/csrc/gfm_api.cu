@@ -204,6 +204,14 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->Unew[f], 4 * plane_b);
   }
   alloc((void**)&ctx->dtime, sizeof(DevTime));
+  {
+    int sms = 0, cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur) != cudaSuccess || sms < 1)
+      sms = 152;
+    ctx->num_sms = sms;
+    ctx->far_sms = sms > 16 ? sms - 8 : sms;   // the far partition of the overlapped ghost fill
+  }
   CtxExtra& X = extra(ctx);
   alloc((void**)&X.counters, 64);
   alloc((void**)&X.mass_part, sizeof(double) * 260);
@@ -231,8 +239,15 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->ifc_mrp, sizeof(double) * 8 * cap);
     alloc((void**)&ctx->probe_ij, sizeof(int) * 4 * cap);
     alloc((void**)&ctx->probe_w, sizeof(double) * 8 * cap);
-    ctx->n_chunks = (int)(((int64_t)P.nr * P.nc + 2047) / 2048);
-    alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)ctx->n_chunks);
+    // chunks of at least 2048 cells (the count array's size), enough of them
+    // for one CTA per SM on large grids (the chunked kernels run one CTA per SM)
+    const int sms = ctx->num_sms;
+    const int64_t ncell = (int64_t)P.nr * P.nc;
+    int64_t chunk = ((ncell + sms - 1) / sms + 511) / 512 * 512;
+    if (chunk < 2048) chunk = 2048;
+    ctx->chunk = (int)chunk;
+    ctx->n_chunks = (int)((ncell + chunk - 1) / chunk);
+    alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)((ncell + 2047) / 2048));
     for (int b = 0; b < 2; b++)
       for (int f = 0; f < 2; f++) alloc((void**)&ctx->S[b][f], 4 * plane_b);
     alloc((void**)&ctx->near_cell, (size_t)P.plane);
@@ -264,6 +279,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
     ctx->overlap = ctx->overlap_ok ? GFM_OVERLAP_AUTO : GFM_OVERLAP_OFF;
   }
+  if (e == cudaSuccess) prepare_kernels();   // kernel attributes and occupancies, before any capture
   if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_dtime, sizeof(DevTime));
   if (e != cudaSuccess) {
     fprintf(stderr, "gfm: allocation failed: %s\n", cudaGetErrorString(e));

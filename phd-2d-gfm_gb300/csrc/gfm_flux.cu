@@ -328,6 +328,7 @@ void prepare_kernels() {
     cudaFuncSetAttribute(k_flux_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem());
     cudaFuncSetAttribute(k_flux_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem());
   });
+  prepare_step_kernels();
 }
 
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {

@@ -69,6 +69,9 @@ struct gfm_ctx {
   int* ifc_list;     // interfacial cells in row-major order
   int* chunk_count;  // per-CTA counts of the compaction
   int n_chunks;
+  int chunk;         // cells per CTA of the chunked kernels (k_prims, k_vof_prims, k_compact)
+  int num_sms;       // SMs of the device, and of the far partition of the overlapped ghost fill
+  int far_sms;
   // per-interface work arrays (capacity = Nx*Ny)
   int* ifc_done;
   int* ifc_pred;     // 8 per interface
@@ -183,6 +186,7 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_vof_update(gfm_ctx* ctx, cudaStream_t s);
 void launch_end_step(gfm_ctx* ctx);
 void prepare_kernels();
+void prepare_step_kernels();   // occupancy of the grid-stride kernels (gfm_step.cu)
 const float* mlp_params(const struct gfm_mlp* m);   // the network's FP32 parameters (device)
 // nsteps iterations of the time loop on ctx's stream (gfm_step, gfm_step_timed)
 gfm_status_t run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);

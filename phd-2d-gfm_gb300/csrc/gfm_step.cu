@@ -11,13 +11,55 @@
 // ghost-layer cells itself: a ghost cell is a mirrored real cell, so its
 // thread evaluates that real cell's update and applies the reflective signs.
 #include "gfm_internal.cuh"
+#include <mutex>
+#include <unordered_map>
 #include "gfm_mlp.cuh"
 #include <climits>
 
 namespace gfm {
 
-constexpr int CHUNK = 2048;      // cells per CTA in the 1D full-grid kernels
+// Cells per CTA of the chunked full-grid kernels (k_prims, k_vof_prims,
+// k_compact): gfm_ctx::chunk, a multiple of CHUNK_T of at least 2048, sized
+// so that the chunks make one wave of one CTA per SM on large grids.
 constexpr int CHUNK_T = 512;
+
+static int grid_blocks(int64_t n, int per) {
+  int64_t b = (n + per - 1) / per;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// Blocks of a grid-stride kernel of `threads` threads for one full wave on
+// `sms` SMs: its resident CTAs per SM (queried once per kernel) times the
+// SMs, capped by the cells to cover.  Every SM then takes the same share of
+// the cells, where a grid of one CTA per 256 cells leaves a partial last wave
+// on some SMs while the others idle.
+static int wave_blocks(const void* kernel, int threads, int sms, int64_t n) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> occ;
+  int per = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = occ.find(kernel);
+    if (it != occ.end()) {
+      per = it->second;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0) != cudaSuccess || per < 1) {
+        cudaGetLastError();
+        per = 1;
+      }
+      occ[kernel] = per;
+    }
+  }
+  if (sms < 1) sms = 152;
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)per * sms;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+static int64_t padded_cells(const GridP& P) { return (int64_t)P.nr * P.nc; }
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -242,9 +284,7 @@ __global__ void k_commit_u(GridP P, const double* Unew, double* U, int bcs, cons
 }
 
 void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs) {
-  int64_t n = (int64_t)ctx->P.nr * ctx->P.nc;
-  int blocks = (int)((n + 255) / 256);
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  const int blocks = wave_blocks((const void*)k_commit_u, 256, ctx->num_sms, padded_cells(ctx->P));
   for (int f = 0; f < 2; f++)
     if (fluid_mask & (1 << f)) {
       k_commit_u<<<blocks, 256, 0, ctx->stream>>>(ctx->P, ctx->Unew[f], ctx->U[f], bcs ? 1 : 0, ctx->dtime);
@@ -277,6 +317,7 @@ struct PrimArgs {
   uint8_t* mask;
   int* ifc_map;
   int* chunk_count;
+  int chunk;                  // cells per CTA
   DevTime* D;
   int check_both;             // 1: assert both grids (OGFM, RGFM); 0: the phi-selected one
   unsigned int* cfl_counter;  // non-null: also the step's CFL reduction and dt (k_cfl's)
@@ -290,12 +331,12 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
   if (threadIdx.x == 0) s_cnt = 0;
   __syncthreads();
   const int64_t n = (int64_t)P.nr * P.nc;
-  const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  const int64_t base = (int64_t)blockIdx.x * a.chunk;
   const Recip r2dx = recip(2.0 * P.dx), r2dy = recip(2.0 * P.dy);   // central-difference divisors
   uint32_t st = 0;
   int cnt = 0;
   double mu = 0.0, mv = 0.0;   // CFL maxima over the real cells (k_cfl's)
-  for (int q = threadIdx.x; q < CHUNK; q += CHUNK_T) {
+  for (int q = threadIdx.x; q < a.chunk; q += CHUNK_T) {
     int64_t lin = base + q;
     if (lin >= n) break;
     int i, j;
@@ -401,7 +442,8 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
 
 // Stage 2: ordered compaction of the interfacial cells (row-major order).
 __global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mask, const int* chunk_count,
-                                                     int n_chunks, int* list, int* ifc_map, DevTime* D) {
+                                                     int n_chunks, int chunk, int* list, int* ifc_map,
+                                                     DevTime* D) {
   if (!D->active) return;
   __shared__ int s_off;
   __shared__ int s_warp[CHUNK_T / 32];
@@ -415,10 +457,10 @@ __global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mas
   int off = s_off;
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) D->n_ifc = off + chunk_count[blockIdx.x];
   const int64_t n = (int64_t)P.nr * P.nc;
-  const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  const int64_t base = (int64_t)blockIdx.x * chunk;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // cells base + it*CHUNK_T + tid, in order of it then tid
-  for (int it = 0; it < CHUNK / CHUNK_T; it++) {
+  for (int it = 0; it < chunk / CHUNK_T; it++) {
     int64_t lin = base + (int64_t)it * CHUNK_T + threadIdx.x;
     int m = 0;
     int i = 0, j = 0;
@@ -1307,6 +1349,7 @@ struct VofPrimArgs {
   uint8_t* mask;
   int* ifc_map;
   int* chunk_count;
+  int chunk;                  // cells per CTA
   DevTime* D;
   int ogfm;
 };
@@ -1318,11 +1361,11 @@ __global__ void __launch_bounds__(CHUNK_T) k_vof_prims(VofPrimArgs a) {
   if (threadIdx.x == 0) s_cnt = 0;
   __syncthreads();
   const int64_t n = (int64_t)P.nr * P.nc;
-  const int64_t base = (int64_t)blockIdx.x * CHUNK;
+  const int64_t base = (int64_t)blockIdx.x * a.chunk;
   uint32_t st = 0;
   int cnt = 0;
   int bb[8] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
-  for (int q = threadIdx.x; q < CHUNK; q += CHUNK_T) {
+  for (int q = threadIdx.x; q < a.chunk; q += CHUNK_T) {
     int64_t lin = base + q;
     if (lin >= n) break;
     int i, j;
@@ -2003,12 +2046,6 @@ __global__ void k_mass_final(const double* part, int nb, double* out) {
 // ---------------------------------------------------------------------------
 // host orchestration
 // ---------------------------------------------------------------------------
-static int grid_blocks(int64_t n, int per) {
-  int64_t b = (n + per - 1) / per;
-  if (b > 152 * 16) b = 152 * 16;
-  if (b < 1) b = 1;
-  return (int)b;
-}
 
 // the sweep's coefficients dt/dx, dt/dy with dt = 0.5 min(dx, dy), correctly
 // rounded here exactly as a device division would round them
@@ -2020,7 +2057,7 @@ static void extrap_coeffs(const GridP& P, ExtrapArgs& e) {
 
 static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
   const GridP& P = ctx->P;
-  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  const int blocks = wave_blocks((const void*)k_extrap, 256, ctx->num_sms, padded_cells(P));
   for (int it = 0; it < N; it++) {
     ExtrapArgs e;
     e.P = P;
@@ -2072,15 +2109,15 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   pa.Wc1 = modified ? ctx->Wc[0] : nullptr;
   pa.Wc2 = modified ? ctx->Wc[1] : nullptr;
   pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
-  pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
+  pa.chunk_count = ctx->chunk_count; pa.chunk = ctx->chunk; pa.D = ctx->dtime;
   pa.check_both = (variant == GFM_OGFM || variant == GFM_RIEMANN) ? 1 : 0;
   pa.cfl_counter = ctx->cfl_counter;
   pa.vel = nullptr;   // k_finalize writes the velocity field
   k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa); counted();
-  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
+  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->chunk, ctx->ifc_list,
                                               ctx->ifc_map, ctx->dtime); counted();
   const bool ext = m->use_extension_vfield != 0;
-  int fblocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  const int fblocks = wave_blocks((const void*)k_finalize, 256, ctx->num_sms, padded_cells(P));
   if (variant == GFM_OGFM) {
     run_extrap(ctx, 6, false);
     FinalArgs f;
@@ -2257,7 +2294,7 @@ static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, doubl
   e.list_stride = ctx->band_stride;
   extrap_coeffs(P, e);
   // a listed sweep covers the band around the interface: a few percent of the grid
-  const int blocks = list ? 2 * 152 : grid_blocks((int64_t)P.nr * P.nc, 256);
+  const int blocks = list ? 2 * 152 : wave_blocks((const void*)k_extrap, 256, ctx->far_sms, padded_cells(P));
   k_extrap<<<blocks, 256, 0, s>>>(e);
   counted();
 }
@@ -2278,7 +2315,8 @@ static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStr
   f.sel = sel;
   f.list = (sel == 2) ? ctx->band_list : nullptr;   // segment 0: the cells whose source is near
   f.list_n = (sel == 2) ? ctx->list_n : nullptr;
-  k_finalize<<<(sel == 2) ? 2 * 152 : grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(f);
+  k_finalize<<<(sel == 2) ? 2 * 152 : wave_blocks((const void*)k_finalize, 256, ctx->far_sms, padded_cells(P)), 256, 0,
+               s>>>(f);
   counted();
 }
 
@@ -2293,13 +2331,13 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   pa.W1 = ctx->W[0]; pa.W2 = ctx->W[1];
   pa.Wc1 = nullptr; pa.Wc2 = nullptr;
   pa.phi = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
-  pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
+  pa.chunk_count = ctx->chunk_count; pa.chunk = ctx->chunk; pa.D = ctx->dtime;
   pa.check_both = (variant == GFM_RIEMANN) ? 1 : 0;
   pa.cfl_counter = ctx->cfl_counter;
   pa.vel = ctx->vel;  // real cells' velocity field, for a level set that starts after the chain
   k_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa);
   counted();
-  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
+  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->chunk, ctx->ifc_list,
                                               ctx->ifc_map, ctx->dtime);
   counted();
   const int cap = P.Nx * P.Ny;
@@ -2410,7 +2448,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
 // phi_b; the copy writes the result into phi
 void launch_ls_stages(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
   const GridP& P = ctx->P;
-  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
+  // the stage kernels have one occupancy
+  const int blocks = wave_blocks((const void*)k_ls_stage<5, 1>, 256, ctx->num_sms, padded_cells(P));
   if (m->ls_order == 1) {
     k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
   } else {
@@ -2422,7 +2461,8 @@ void launch_ls_stages(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
 
 void launch_ls_copy(gfm_ctx* ctx, cudaStream_t s) {
   const GridP& P = ctx->P;
-  k_copy_plane<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0);
+  k_copy_plane<<<wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, padded_cells(P)), 256, 0, s>>>(
+      P, ctx->phi_a, ctx->phi, ctx->dtime, 0);
   counted();
 }
 
@@ -2435,16 +2475,33 @@ void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
 // count ends with a copy back, so phi stays the one buffer holding the level set
 void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream_t s) {
   const GridP& P = ctx->P;
-  int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
-  k_reinit_sign<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime, every); counted();
+  const int64_t n = padded_cells(P);
+  k_reinit_sign<<<wave_blocks((const void*)k_reinit_sign, 256, ctx->num_sms, n), 256, 0, s>>>(P, ctx->phi, ctx->phi0,
+                                                                                             ctx->dtime, every);
+  counted();
+  const int blocks = wave_blocks((const void*)k_reinit_iter, 256, ctx->num_sms, n);
   for (int it = 0; it < m->reinit_iters; it++) {
     const double* src = (it & 1) ? ctx->phi_a : ctx->phi;
     double* dst = (it & 1) ? ctx->phi : ctx->phi_a;
     k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime, every); counted();
   }
   if (m->reinit_iters & 1) {
-    k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, every); counted();
+    k_copy_plane<<<wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, n), 256, 0, s>>>(P, ctx->phi_a, ctx->phi,
+                                                                                           ctx->dtime, every);
+    counted();
   }
+}
+
+// Occupancy queries of the grid-stride kernels, made once before any launch
+// (and so before any stream capture records one)
+void prepare_step_kernels() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const void* ks[] = {(const void*)k_commit_u, (const void*)k_extrap, (const void*)k_finalize,
+                        (const void*)k_ls_stage<5, 1>, (const void*)k_copy_plane, (const void*)k_reinit_sign,
+                        (const void*)k_reinit_iter};
+    for (const void* k : ks) wave_blocks(k, 256, 1, 1);
+  });
 }
 
 // GFM_VOF / OGFM_VOF set_ghost_states: prims, mixed cells and their
@@ -2459,11 +2516,11 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   pa.U1 = ctx->U[0]; pa.U2 = ctx->U[1];
   pa.W1 = ctx->W[0]; pa.W2 = ctx->W[1];
   pa.z = ctx->phi; pa.nrm = ctx->nrm; pa.mask = ctx->mask; pa.ifc_map = ctx->ifc_map;
-  pa.chunk_count = ctx->chunk_count; pa.D = ctx->dtime;
+  pa.chunk_count = ctx->chunk_count; pa.chunk = ctx->chunk; pa.D = ctx->dtime;
   pa.ogfm = og ? 1 : 0;
   k_vof_prims<<<ctx->n_chunks, CHUNK_T, 0, s>>>(pa); counted();
   if (og) { k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted(); }
-  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->ifc_list,
+  k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->chunk, ctx->ifc_list,
                                               ctx->ifc_map, ctx->dtime); counted();
   const int cap = P.nr * P.nc;
   k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime);
