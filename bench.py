@@ -324,8 +324,10 @@ def run_gfm(args):
         t0 = time.perf_counter()
         up = (pd(hU1), pd(hU2), pd(hphi)) if two else (pd(hU1), None, None)
         for s in range(n_e2e):
-            # the whole state in and out through the C ABI every step
-            L.gfm_upload_state(ctx._p, *up)
+            # the whole state in and out through the C ABI every step (the
+            # upload is ordered before the step on the context's stream; the
+            # download synchronises)
+            L.gfm_upload_state_async(ctx._p, *up)
             L.gfm_step(ctx._p, ctypes.byref(m), 1)
             L.gfm_download_state(ctx._p, *up)
         torch.cuda.synchronize()
@@ -557,7 +559,7 @@ def run_batch(args):
         t0 = time.perf_counter()
         for _ in range(n_e2e):
             for ctx, (h1, h2, hp) in zip(b.instances, pinned):
-                L.gfm_upload_state(ctx._p, pd(h1), pd(h2), pd(hp))
+                L.gfm_upload_state_async(ctx._p, pd(h1), pd(h2), pd(hp))
             b.step(m, 1, graph=True)
             for ctx, (h1, h2, hp) in zip(b.instances, pinned):
                 L.gfm_download_state(ctx._p, pd(h1), pd(h2), pd(hp))

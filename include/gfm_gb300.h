@@ -109,6 +109,11 @@ gfm_status_t gfm_download_phi(gfm_ctx* ctx, double* phi);
 /* all fields at once (U1, and U2 and phi for two fluids), one synchronisation */
 gfm_status_t gfm_upload_state(gfm_ctx* ctx, const double* U1, const double* U2, const double* phi);
 gfm_status_t gfm_download_state(gfm_ctx* ctx, double* U1, double* U2, double* phi);
+/* gfm_upload_state without the synchronisation: the copies are ordered on the
+ * context's stream before the calls that follow (a step, a download), and the
+ * host buffers must stay unchanged until a later synchronising call on the
+ * context (gfm_download_state, gfm_get_time) has returned */
+gfm_status_t gfm_upload_state_async(gfm_ctx* ctx, const double* U1, const double* U2, const double* phi);
 
 /* the velocity field of the last ghost fill (GFM_base::vfield, handed to the
  * interface tracker): 2 planes (u, v), layout of phi */

@@ -72,6 +72,8 @@ struct gfm_ctx {
   int chunk;         // cells per CTA of the chunked kernels (k_prims, k_vof_prims, k_compact)
   int num_sms;       // SMs of the device, and of the far partition of the overlapped ghost fill
   int far_sms;
+  double* stage;     // packed (unpitched) copy of the whole state: 4, 4 and 1 planes of nr x nc
+                     // (gfm_upload_state / gfm_download_state)
   // per-interface work arrays (capacity = Nx*Ny)
   int* ifc_done;
   int* ifc_pred;     // 8 per interface

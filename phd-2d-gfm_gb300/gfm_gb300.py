@@ -83,6 +83,7 @@ def lib():
         "gfm_upload": [P, I, pd], "gfm_download": [P, I, pd],
         "gfm_upload_phi": [P, pd], "gfm_download_phi": [P, pd], "gfm_download_velocity": [P, pd],
         "gfm_upload_state": [P, pd, pd, pd], "gfm_download_state": [P, pd, pd, pd],
+        "gfm_upload_state_async": [P, pd, pd, pd],
         "gfm_set_time": [P, D, I],
         "gfm_download_mask": [P, ctypes.POINTER(ctypes.c_uint8)],
         "gfm_get_time": [P, pd, ctypes.POINTER(I), pd],

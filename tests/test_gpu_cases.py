@@ -88,6 +88,14 @@ def test_state_upload_download_in_one_call():
     assert L.gfm_upload_state(ctx._p, pd(U1), pd(U2), pd(phi)) == 0
     V1, V2, ph = ctx.download()
     assert np.array_equal(V1, U1) and np.array_equal(V2, U2) and np.array_equal(ph, phi)
+    # the asynchronous form, completed by the synchronising download
+    Z1, Z2, zp = np.zeros_like(U1), np.zeros_like(U2), np.zeros_like(phi)
+    assert L.gfm_upload_state_async(ctx._p, pd(Z1), pd(Z2), pd(zp)) == 0
+    assert L.gfm_download_state(ctx._p, pd(V1), pd(V2), pd(ph)) == 0
+    assert not V1.any() and not V2.any() and not ph.any()
+    assert L.gfm_upload_state_async(ctx._p, pd(U1), pd(U2), pd(phi)) == 0
+    assert L.gfm_download_state(ctx._p, pd(V1), pd(V2), pd(ph)) == 0
+    assert np.array_equal(V1, U1) and np.array_equal(V2, U2) and np.array_equal(ph, phi)
     ctx.step(g.method(T=T), 3)
     W1, W2, wp = np.empty_like(U1), np.empty_like(U2), np.empty_like(phi)
     assert L.gfm_download_state(ctx._p, pd(W1), pd(W2), pd(wp)) == 0
