@@ -250,12 +250,12 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     ctx->chunk = (int)chunk;
     ctx->n_chunks = (int)((ncell + chunk - 1) / chunk);
     alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)((ncell + 2047) / 2048));
-    for (int b = 0; b < 2; b++)
-      for (int f = 0; f < 2; f++) alloc((void**)&ctx->S[b][f], 4 * plane_b);
+    for (int b = 0; b < 6; b++)
+      for (int f = 0; f < 2; f++) alloc((void**)&ctx->SF[b][f], 4 * plane_b);
     alloc((void**)&ctx->near_cell, (size_t)P.plane);
     alloc((void**)&ctx->band_cls, sizeof(int) * (size_t)P.plane);
     ctx->band_stride = (int64_t)P.nr * P.nc;
-    alloc((void**)&ctx->band_list, 6 * (size_t)ctx->band_stride * sizeof(int));
+    alloc((void**)&ctx->band_list, 7 * (size_t)ctx->band_stride * sizeof(int));
     alloc((void**)&ctx->list_n, 8 * sizeof(int));
     alloc((void**)&ctx->tile_near, sizeof(int) * (size_t)flux_tiles_x(P) * flux_tiles_y(P));
     int dev = 0;
@@ -305,8 +305,8 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
   cudaFree(ctx->ifc_out); cudaFree(ctx->ifc_mrp); cudaFree(ctx->chunk_count);
   cudaFree(ctx->probe_ij); cudaFree(ctx->probe_w);
-  for (int b = 0; b < 2; b++)
-    for (int f = 0; f < 2; f++) cudaFree(ctx->S[b][f]);
+  for (int b = 0; b < 6; b++)
+    for (int f = 0; f < 2; f++) cudaFree(ctx->SF[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cls); cudaFree(ctx->tile_near);
   cudaFree(ctx->band_list); cudaFree(ctx->list_n);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);

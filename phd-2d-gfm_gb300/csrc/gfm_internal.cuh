@@ -89,13 +89,13 @@ struct gfm_ctx {
   // overlapped ghost fill (Riemann and real GFM): the interface chain runs on
   // a small SM partition while the far field is extrapolated and updated on
   // the rest (see launch_ghost_fill_overlapped)
-  double* S[2][2];        // speculative extrapolation ping-pong [buffer][fluid]
+  double* SF[6][2];       // the far field's six extrapolation sweeps [sweep][fluid]
   uint8_t* near_cell;     // real cells within 6 (Chebyshev) of an interfacial cell
-  int* band_cls;          // real cells within 11: 12 - the distance (the exact extrapolation's band)
-  int* band_list;         // 6 segments of band_stride entries: the cells (ghost cells included, by
-                          // their source) at distance <= 6 (segment 0), 7, 8, 9, 10, 11
+  int* band_cls;          // cells within 6: 7 - the distance (ghost cells: their source's), else 0
+  int* band_list;         // 7 segments of band_stride entries: the cells (ghost cells included, by
+                          // their source) at distance 0, 1, ..., 6
   int64_t band_stride;
-  int* list_n;            // the 6 segments' counts
+  int* list_n;            // the 7 segments' counts
   int* tile_near;         // per flux tile: its region holds a near cell
   cudaStream_t s_chain, s_far;
   cudaEvent_t ev_fork, ev_chain, ev_far;

@@ -490,17 +490,24 @@ __global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mas
 // ---------------------------------------------------------------------------
 constexpr int IFC_OUT = 8;   // doubles of interface output per interfacial cell
 
-// Overlapped ghost fill: the cells within NEAR_RADIUS (Chebyshev) of an
-// interfacial cell depend on the interface loop through the six sweeps of
-// extrapolate_vector (one cell per sweep).  The exact extrapolation after the
-// loop writes, in sweep k = 1..6, the cells within BAND_RADIUS - k + 1 of an
-// interfacial cell: its reads one cell further out come from sweep k - 1
-// (sweep 1 reads the pre-loop primitives, exact everywhere), so sweep k is
-// exact where it writes and sweep 6 is exact on the near cells.  The band's
-// cells are listed in BAND_CLASSES segments by distance (k_band_lists).
+// Overlapped ghost fill: the interface loop changes only the real fluid of
+// interfacial cells, and a sweep of extrapolate_vector reads a cell and its
+// four neighbours, so after sweep k its values differ from those of the same
+// sweeps without the loop's results (the far field's, computed beside the
+// loop) only within k cells (Chebyshev) of an interfacial cell.  The exact
+// extrapolation after the loop therefore writes, in sweep k = 1..6, the cells
+// within k: it reads the previous exact sweep inside that band and the far
+// field's previous sweep outside, and sweep 6 gives the cells within
+// NEAR_RADIUS.  The band's cells are listed in BAND_CLASSES segments by
+// distance 0..NEAR_RADIUS (k_band_lists).
 constexpr int NEAR_RADIUS = 6;
-constexpr int BAND_RADIUS = 11;
-constexpr int BAND_CLASSES = BAND_RADIUS - NEAR_RADIUS + 1;
+constexpr int BAND_CLASSES = NEAR_RADIUS + 1;
+// CTAs of the listed kernels after the loop (exact sweeps, near conversion):
+// the band holds a few thousand to ten thousand cells, and these kernels run
+// while the far field's flux update fills the other SMs, so a grid that fits
+// in one wave on the loop's own 8 SMs starts at once, where one of 2 CTAs per
+// SM queued several waves of nearly empty CTAs behind each other
+constexpr int NEAR_CTAS = 40;
 
 struct ExtrapArgs {
   GridP P;
@@ -527,6 +534,11 @@ struct ExtrapArgs {
   const int* list_n;
   int nclass;
   int64_t list_stride;
+  // exact sweep k >= 2 after the loop: F1/F2 the far field's sweep k - 1,
+  // read where cls[c] < near_min (outside the band of sweep k - 1), or null
+  const double* F1; const double* F2;
+  const int* cls;
+  int near_min;
   // (0.5 min(dx, dy)) / dx and / dy, formed once on the host
   double cdx, cdy;
 };
@@ -536,6 +548,7 @@ __device__ __forceinline__ V4 ex_rd(const ExtrapArgs& a, int f, int64_t c) {
     const double* o = a.ov_out + (int64_t)a.ov_map[c] * IFC_OUT;
     return V4{o[0], o[1], o[2], o[3]};
   }
+  if (a.F1 && a.cls[c] < a.near_min) return load4(f == 0 ? a.F1 : a.F2, a.P, c);
   return load4(f == 0 ? a.S1 : a.S2, a.P, c);
 }
 
@@ -591,14 +604,14 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
 }
 
 // The cells (over the padded rows, ghost cells included) whose
-// boundary-condition source lies within BAND_RADIUS (Chebyshev) of an
-// interfacial cell, appended to the segment of their source's distance d:
-// segment 0 for d <= NEAR_RADIUS, segment d - NEAR_RADIUS beyond (counts in
-// n6[0..5], zeroed by the caller).  cls[c] = BAND_RADIUS + 1 - d of a real
-// cell c (k_band_mark), 0 beyond the band.  Also the near-cell mask of the
-// real cells (d <= NEAR_RADIUS).  Order within a segment is free: a sweep
-// writes each listed cell from reads of the previous buffer only.
-__global__ void k_band_lists(GridP P, const int* cls, uint8_t* near_cell, int* band_list, int64_t stride, int* n6,
+// boundary-condition source lies within NEAR_RADIUS (Chebyshev) of an
+// interfacial cell, appended to the segment of their source's distance d
+// (counts in nseg[0..NEAR_RADIUS], zeroed by the caller).  cls[c] =
+// NEAR_RADIUS + 1 - d of a real cell c (k_band_mark), 0 beyond; the ghost
+// cells' entries are set here to their source's.  Also the near-cell mask of
+// the real cells.  Order within a segment is free: a sweep writes each listed
+// cell from reads of the previous buffers only.
+__global__ void k_band_lists(GridP P, int* cls, uint8_t* near_cell, int* band_list, int64_t stride, int* nseg,
                              const DevTime* D) {
   if (!D->active) return;
   const int64_t n = (int64_t)P.nr * P.nc;
@@ -610,16 +623,17 @@ __global__ void k_band_lists(GridP P, const int* cls, uint8_t* near_cell, int* b
     if (k < n) {
       const int i = (int)(k / P.nc), j = (int)(k % P.nc);
       BCSrc s = bc_source(P, i, j);
-      const int v = cls[cidx(P, s.i, s.j)];
-      if (v > 0) q = (v >= BAND_RADIUS + 1 - NEAR_RADIUS) ? 0 : BAND_RADIUS + 1 - NEAR_RADIUS - v;
-      if (is_real(P, i, j)) near_cell[cidx(P, i, j)] = (v >= BAND_RADIUS + 1 - NEAR_RADIUS) ? 1 : 0;
+      const int v = cls[cidx(P, s.i, s.j)];   // a real cell: k_band_mark's value
+      if (v > 0) q = NEAR_RADIUS + 1 - v;
+      if (is_real(P, i, j)) near_cell[cidx(P, i, j)] = (v > 0) ? 1 : 0;
+      else cls[cidx(P, i, j)] = v;
     }
     const unsigned below = (1u << lane) - 1u;
     for (int c = 0; c < BAND_CLASSES; c++) {
       const unsigned m = __ballot_sync(0xffffffffu, q == c);
       if (!m) continue;
       int o = 0;
-      if (lane == 0) o = atomicAdd(&n6[c], __popc(m));
+      if (lane == 0) o = atomicAdd(&nseg[c], __popc(m));
       o = __shfl_sync(0xffffffffu, o, 0);
       if (q == c) band_list[(int64_t)c * stride + o + __popc(m & below)] = (int)k;
     }
@@ -1771,19 +1785,32 @@ struct FinalArgs {
   int vel_mode;   // 0: real-fluid velocity, 1: extension seeds (OGFM interfacial), 2: leave vel alone
   const uint8_t* near_cell;
   int sel;        // 0: every cell, 1: cells far from the interface, 2: near cells
-  // the near cells as a list (count in *list_n) for sel 2, or null
+  // the near cells as BAND_CLASSES list segments of list_stride entries
+  // (counts in list_n[]) for sel 2, or null
   const int* list;
   const int* list_n;
+  int64_t list_stride;
 };
 
 __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
-  const int64_t n = a.list ? (int64_t)*a.list_n : (int64_t)P.nr * P.nc;
+  int cnt[BAND_CLASSES];
+  int64_t n = (int64_t)P.nr * P.nc;
+  if (a.list) {
+    n = 0;
+    for (int q = 0; q < BAND_CLASSES; q++) { cnt[q] = a.list_n[q]; n += cnt[q]; }
+  }
   uint32_t st = 0;
   int bb[8] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = a.list ? (int64_t)a.list[q] : q;
+    int64_t k = q;
+    if (a.list) {
+      int sg = 0;
+      int64_t r = q;
+      while (r >= cnt[sg]) { r -= cnt[sg]; sg++; }
+      k = a.list[(int64_t)sg * a.list_stride + r];
+    }
     int i = (int)(k / P.nc), j = (int)(k % P.nc);
     int64_t c = cidx(P, i, j);
     if (a.sel && !a.list) {   // a ghost cell is near when its boundary-condition source is
@@ -2069,6 +2096,7 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.band = nullptr;
     e.list = nullptr; e.list_n = nullptr;
     e.nclass = 0; e.list_stride = 0;
+    e.F1 = nullptr; e.F2 = nullptr; e.cls = nullptr; e.near_min = 0;
     extrap_coeffs(P, e);
     k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
@@ -2131,7 +2159,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
     f.ogfm = 1;
     f.vel_mode = ext ? 1 : 0;
     f.near_cell = nullptr;
-    f.list = nullptr; f.list_n = nullptr;
+    f.list = nullptr; f.list_n = nullptr; f.list_stride = 0;
     f.sel = 0;
     k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
     k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted();
@@ -2188,7 +2216,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   f.ogfm = 0;
   f.vel_mode = ext ? 2 : 0;
   f.near_cell = nullptr;
-  f.list = nullptr; f.list_n = nullptr;
+  f.list = nullptr; f.list_n = nullptr; f.list_stride = 0;
   f.sel = 0;
   k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
   if (ext) run_ext_vfield(ctx, 20);
@@ -2278,7 +2306,8 @@ __global__ void k_tile_flags(GridP P, const uint8_t* near_cell, int* tile_near, 
 }
 
 static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, double* D1, double* D2, bool overlay,
-                         cudaStream_t s, const int* list, const int* list_n, int nclass) {
+                         cudaStream_t s, const int* list, const int* list_n, int nclass,
+                         const double* const* far = nullptr, int near_min = 0) {
   const GridP& P = ctx->P;
   ExtrapArgs e;
   e.P = P;
@@ -2292,9 +2321,12 @@ static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, doubl
   e.list = list; e.list_n = list_n;
   e.nclass = nclass;
   e.list_stride = ctx->band_stride;
+  e.F1 = far ? far[0] : nullptr; e.F2 = far ? far[1] : nullptr;
+  e.cls = ctx->band_cls;
+  e.near_min = near_min;
   extrap_coeffs(P, e);
   // a listed sweep covers the band around the interface: a few percent of the grid
-  const int blocks = list ? 2 * 152 : wave_blocks((const void*)k_extrap, 256, ctx->far_sms, padded_cells(P));
+  const int blocks = list ? NEAR_CTAS : wave_blocks((const void*)k_extrap, 256, ctx->far_sms, padded_cells(P));
   k_extrap<<<blocks, 256, 0, s>>>(e);
   counted();
 }
@@ -2313,9 +2345,10 @@ static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStr
   f.vel_mode = 3;   // ghost cells: k_prims and k_ifc_vel write the real cells' velocities
   f.near_cell = ctx->near_cell;
   f.sel = sel;
-  f.list = (sel == 2) ? ctx->band_list : nullptr;   // segment 0: the cells whose source is near
+  f.list = (sel == 2) ? ctx->band_list : nullptr;   // every segment: the cells whose source is near
   f.list_n = (sel == 2) ? ctx->list_n : nullptr;
-  k_finalize<<<(sel == 2) ? 2 * 152 : wave_blocks((const void*)k_finalize, 256, ctx->far_sms, padded_cells(P)), 256, 0,
+  f.list_stride = ctx->band_stride;
+  k_finalize<<<(sel == 2) ? NEAR_CTAS : wave_blocks((const void*)k_finalize, 256, ctx->far_sms, padded_cells(P)), 256, 0,
                s>>>(f);
   counted();
 }
@@ -2353,7 +2386,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   cudaStreamWaitEvent(sf, ctx->ev_fork, 0);
   cudaMemsetAsync(ctx->band_cls, 0, sizeof(int) * (size_t)P.plane, sf);
   k_band_mark<<<grid_blocks((int64_t)cap, 256), 256, 0, sf>>>(P, ctx->ifc_list, ctx->dtime, ctx->band_cls,
-                                                               BAND_RADIUS);
+                                                               NEAR_RADIUS);
   counted();
   cudaMemsetAsync(ctx->list_n, 0, BAND_CLASSES * sizeof(int), sf);
   k_band_lists<<<grid_blocks((int64_t)P.nr * P.nc, 256), 256, 0, sf>>>(P, ctx->band_cls, ctx->near_cell,
@@ -2399,8 +2432,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   {
     const double* src1 = ctx->W[0];
     const double* src2 = ctx->W[1];
-    for (int it = 0; it < 6; it++) {
-      double** dst = ctx->S[it & 1];
+    for (int it = 0; it < 6; it++) {   // each sweep into its own buffer: the exact sweeps read them
+      double** dst = ctx->SF[it];
       extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr, nullptr, 0);
       src1 = dst[0]; src2 = dst[1];
     }
@@ -2418,7 +2451,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   // of near cells, flux update of near tiles
   cudaStream_t sn = ctx->s_near;
   cudaStreamWaitEvent(sn, ctx->ev_chain, 0);
-  cudaStreamWaitEvent(sn, ctx->ev_lists, 0);
+  cudaStreamWaitEvent(sn, ctx->ev_far_final, 0);   // band lists and the far field's sweeps
   {
     double* bufA[2] = {ctx->Wt[0], ctx->Wt[1]};
     double* bufB[2] = {ctx->Wc[0], ctx->Wc[1]};
@@ -2426,18 +2459,22 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     const double* src2 = ctx->W[1];
     for (int it = 0; it < 6; it++) {
       double** dst = (it & 1) ? bufB : bufA;
-      // sweep it + 1 writes the cells within BAND_RADIUS - it: segments 0 .. BAND_CLASSES - 1 - it
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, sn, ctx->band_list, ctx->list_n, BAND_CLASSES - it);
+      // sweep k = it + 1 writes the cells within k of an interfacial cell
+      // (segments 0..k); sweep 1 reads the pre-loop primitives with the loop's
+      // writes overlaid, sweep k > 1 the exact sweep k - 1 within k - 1
+      // (cls >= NEAR_RADIUS + 2 - k) and the far field's sweep k - 1 beyond
+      const double* far[2] = {it ? ctx->SF[it - 1][0] : nullptr, it ? ctx->SF[it - 1][1] : nullptr};
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, sn, ctx->band_list, ctx->list_n, it + 2,
+                   it ? far : nullptr, NEAR_RADIUS + 1 - it);
       src1 = dst[0]; src2 = dst[1];
     }
     const double* fin[2] = {src1, src2};
     finalize_sel(ctx, fin, 2, sn);
   }
   if (ctx->timing) cudaEventRecord(ctx->tev[3], sn);
-  // The near tiles read far cells too: they wait for the far cells'
-  // conversion, not for the far tiles' flux update, which writes only its own
-  // tiles of Unew.  From here on nothing in the ghost fill reads phi.
-  cudaStreamWaitEvent(sn, ctx->ev_far_final, 0);
+  // The near tiles read far cells too: the far cells' conversion is done (the
+  // far tiles' flux update writes only its own tiles of Unew).  From here on
+  // nothing in the ghost fill reads phi.
   cudaEventRecord(ctx->ev_phi_free, sn);
   if (ctx->timing) cudaEventRecord(ctx->tev[4], sn);
   // the caller issues the level set and the flux update of the near tiles
