@@ -35,6 +35,7 @@ constexpr int NYF = (TY + 1) * TX;
 
 struct FluxSmem {
   double w[4][WR][WC];          // primitives (MUSCL) or conserved (Godunov)
+  double irho[WR][WC];          // MUSCL: 1/rho of the conversion, reused by the cell's face states
   double fs[4][4][SR][SC];      // [face L,R,B,T][component][r][c]
   double fx[4][TY][TX + 1];
   double fy[4][TY + 1][TX];
@@ -80,9 +81,9 @@ __device__ __forceinline__ V4 B_times(double s, const V4& W, double irho, double
 // extrapolated values (:199-210), first physicality fallback (:213-247) and
 // the half-step evolution with both quasilinear matrices (:250-272).
 // out = evolved L, R, B, T face states of the cell.
-__device__ __forceinline__ void cell_face_states(const V4& W, const V4& Ww, const V4& We, const V4& Ws,
-                                                 const V4& Wn, double gam, double pinf, double sx, double sy,
-                                                 V4 out[4]) {
+__device__ __forceinline__ void cell_face_states(const V4& W, double irho_W, const V4& Ww, const V4& We,
+                                                 const V4& Ws, const V4& Wn, double gam, double pinf, double sx,
+                                                 double sy, V4 out[4]) {
   V4 dxL = v4sub(W, Ww), dxR = v4sub(We, W);
   V4 dyL = v4sub(W, Ws), dyR = v4sub(Wn, W);
   V4 sxv = V4{minmod(dxL.a, dxR.a), minmod(dxL.b, dxR.b), minmod(dxL.c, dxR.c), minmod(dxL.d, dxR.d)};
@@ -93,7 +94,10 @@ __device__ __forceinline__ void cell_face_states(const V4& W, const V4& Ww, cons
   V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
   if (!is_physical_primitives_fast(gam, pinf, L) || !is_physical_primitives_fast(gam, pinf, R)) { L = W; R = W; }
   if (!is_physical_primitives_fast(gam, pinf, B) || !is_physical_primitives_fast(gam, pinf, T)) { B = W; T = W; }
-  const Recip Rr = recip(W.a);
+  // 1/rho from the cell's conversion (the correctly rounded quotient, as
+  // recip(W.a) would form it)
+  Recip Rr;
+  Rr.b = W.a; Rr.y = irho_W; Rr.fast = mid_range(W.a);
   double cs = eos_soundspeed_r(gam, pinf, W.d, Rr);
   double irho = Rr.y, rcc = W.a * cs * cs;   // irho = 1.0 / W.a
   V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
@@ -188,7 +192,13 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
     V4 u = load4(U, P, cidx(P, i, j));
     same = same && as_bits(u.a) == as_bits(u00.a) && as_bits(u.b) == as_bits(u00.b) &&
            as_bits(u.c) == as_bits(u00.c) && as_bits(u.d) == as_bits(u00.d);
-    V4 w = MUSCL ? cons_to_prims(gam, pinf, u) : u;
+    V4 w = u;
+    if (MUSCL) {
+      bool phys;
+      Recip R;
+      w = cons_to_prims_phys(gam, pinf, u, &phys, &R);   // cons_to_prims, and its 1/rho
+      s.irho[r][c] = R.y;
+    }
     s.w[0][r][c] = w.a; s.w[1][r][c] = w.b; s.w[2][r][c] = w.c; s.w[3][r][c] = w.d;
   }
   // Uniform region: every cell of the tile and its halo has the same state,
@@ -203,7 +213,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
       int itx = 0, ity = 0;
       if (MUSCL) {
         V4 fs[4];
-        cell_face_states(W, W, W, W, W, gam, pinf, sx, sy, fs);
+        cell_face_states(W, s.irho[2][2], W, W, W, W, gam, pinf, sx, sy, fs);
         fx = muscl_face_flux(true, fs[0], fs[1], W, W, gas, &st, &itx);
         fy = muscl_face_flux(false, fs[2], fs[3], W, W, gas, &st, &ity);
       } else {
@@ -221,8 +231,8 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
       for (int k = tid; k < SR * SC; k += NT) {
         int r = k / SC, c = k % SC;       // cell (i0-1+r, j0-1+c) = w[r+1][c+1]
         V4 fs[4];
-        cell_face_states(sW(s, r + 1, c + 1), sW(s, r + 1, c), sW(s, r + 1, c + 2), sW(s, r, c + 1),
-                         sW(s, r + 2, c + 1), gam, pinf, sx, sy, fs);
+        cell_face_states(sW(s, r + 1, c + 1), s.irho[r + 1][c + 1], sW(s, r + 1, c), sW(s, r + 1, c + 2),
+                         sW(s, r, c + 1), sW(s, r + 2, c + 1), gam, pinf, sx, sy, fs);
         for (int f = 0; f < 4; f++) putFS(s, f, r, c, fs[f]);
       }
       __syncthreads();
