@@ -9,7 +9,6 @@
 namespace gfm {
 void launch_cfl_impl(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int* counter);
 void launch_step_begin(gfm_ctx* ctx, double CFL, double T, bool ogfm);
-void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream_t s);
 void launch_mass(gfm_ctx* ctx, double sign, double* part, double* out);
 }  // namespace gfm
 
@@ -250,7 +249,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     ctx->chunk = (int)chunk;
     ctx->n_chunks = (int)((ncell + chunk - 1) / chunk);
     alloc((void**)&ctx->chunk_count, sizeof(int) * (size_t)((ncell + 2047) / 2048));
-    for (int b = 0; b < 6; b++)
+    for (int b = 0; b < 5; b++)
       for (int f = 0; f < 2; f++) alloc((void**)&ctx->SF[b][f], 4 * plane_b);
     alloc((void**)&ctx->near_cell, (size_t)P.plane);
     alloc((void**)&ctx->band_cls, sizeof(int) * (size_t)P.plane);
@@ -305,7 +304,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
   cudaFree(ctx->ifc_out); cudaFree(ctx->ifc_mrp); cudaFree(ctx->chunk_count);
   cudaFree(ctx->probe_ij); cudaFree(ctx->probe_w);
-  for (int b = 0; b < 6; b++)
+  for (int b = 0; b < 5; b++)
     for (int f = 0; f < 2; f++) cudaFree(ctx->SF[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cls); cudaFree(ctx->tile_near);
   cudaFree(ctx->band_list); cudaFree(ctx->list_n);
@@ -591,14 +590,6 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
       // The level-set update reads phi and the velocity field of the ghost
       // fill and writes only level-set buffers: it runs on its own stream
       // beside the flux update (which reads and writes the fluid grids).
-      auto reinit = [&]() {
-        if (m->reinit_every > 0 && m->reinit_iters > 0) {
-          if (ctx->graph_mode)   // recorded into a graph: the device picks the steps
-            launch_reinit(ctx, m, m->reinit_every, ctx->s_ls);
-          else if ((ctx->steps_done_host + 1) % m->reinit_every == 0)
-            launch_reinit(ctx, m, 0, ctx->s_ls);
-        }
-      };
       auto fork_level_set = [&]() {
         cudaEventRecord(ctx->ev_ls_fork, ctx->stream);
         cudaStreamWaitEvent(ctx->s_ls, ctx->ev_ls_fork, 0);
@@ -607,8 +598,7 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
           cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
           return;
         }
-        launch_ls_update(ctx, m, ctx->s_ls);
-        reinit();
+        launch_level_set(ctx, m, ctx->s_ls, 3);   // a graph's steps decide the reinitialisation on the device
         cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
       };
       if (overlapped) {
@@ -620,10 +610,9 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
         // writes of phi (copy, reinitialisation) wait for the ghost fill's
         // last read of phi.
         cudaStreamWaitEvent(ctx->s_ls, ctx->ev_chain, 0);
-        launch_ls_stages(ctx, m, ctx->s_ls);
+        launch_level_set(ctx, m, ctx->s_ls, 1);
         cudaStreamWaitEvent(ctx->s_ls, ctx->ev_phi_free, 0);
-        launch_ls_copy(ctx, ctx->s_ls);
-        reinit();
+        launch_level_set(ctx, m, ctx->s_ls, 2);
         cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
         launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->s_near);
         cudaEventRecord(ctx->ev_near, ctx->s_near);

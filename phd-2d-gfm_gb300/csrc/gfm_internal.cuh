@@ -89,7 +89,7 @@ struct gfm_ctx {
   // overlapped ghost fill (Riemann and real GFM): the interface chain runs on
   // a small SM partition while the far field is extrapolated and updated on
   // the rest (see launch_ghost_fill_overlapped)
-  double* SF[6][2];       // the far field's six extrapolation sweeps [sweep][fluid]
+  double* SF[5][2];       // the far field's first five extrapolation sweeps [sweep][fluid]
   uint8_t* near_cell;     // real cells within 6 (Chebyshev) of an interfacial cell
   int* band_cls;          // cells within 6: 7 - the distance (ghost cells: their source's), else 0
   int* band_list;         // 7 segments of band_stride entries: the cells (ghost cells included, by
@@ -182,8 +182,9 @@ void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
-void launch_ls_stages(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
-void launch_ls_copy(gfm_ctx* ctx, cudaStream_t s);
+// the step's level set: parts 1 the advection stages, 2 phi := the result
+// (or the reinitialisation from it), 3 both
+void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts);
 void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_vof_update(gfm_ctx* ctx, cudaStream_t s);
 void launch_end_step(gfm_ctx* ctx);

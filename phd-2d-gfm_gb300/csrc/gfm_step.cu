@@ -517,6 +517,7 @@ struct ExtrapArgs {
   const double* nrm;
   const uint8_t* mask;
   const DevTime* D;
+  DevTime* Dw;                          // status word of the fused conversion
   int mgfm;
   // overlay: the interface loop's writes (star state into the real fluid of
   // each interfacial cell) applied on the fly to the source reads
@@ -539,6 +540,16 @@ struct ExtrapArgs {
   const double* F1; const double* F2;
   const int* cls;
   int near_min;
+  // the conversion back to conserved grids fused into the overlapped
+  // schedule's last sweeps (k_finalize's work for these cells): fsel 0 none,
+  // 1 the cells whose boundary-condition source is not near (fnear), 2 every
+  // written cell; fU1/fU2 the conserved grids, fvel the velocity field of the
+  // ghost cells; store_w 0 skips the store of the primitives (D1/D2)
+  int fsel;
+  const uint8_t* fnear;
+  double* fU1; double* fU2;
+  double* fvel;
+  int store_w;
   // (0.5 min(dx, dy)) / dx and / dy, formed once on the host
   double cdx, cdy;
 };
@@ -552,12 +563,13 @@ __device__ __forceinline__ V4 ex_rd(const ExtrapArgs& a, int f, int64_t c) {
   return load4(f == 0 ? a.S1 : a.S2, a.P, c);
 }
 
-__device__ __forceinline__ void extrap_cell(const ExtrapArgs& a, int64_t k) {
+template <bool FUSE>
+__device__ __forceinline__ uint32_t extrap_cell(const ExtrapArgs& a, int64_t k) {
   const GridP& P = a.P;
   int i = (int)(k / P.nc), j = (int)(k % P.nc);
   BCSrc s = bc_source(P, i, j);
   int64_t c = cidx(P, s.i, s.j);
-  if (a.band && !a.band[c]) return;
+  if (a.band && !a.band[c]) return 0u;
   V4 v1 = ex_rd(a, 0, c), v2 = ex_rd(a, 1, c);
   bool skip = a.mgfm && a.mask[c];
   if (!skip) {
@@ -580,13 +592,36 @@ __device__ __forceinline__ void extrap_cell(const ExtrapArgs& a, int64_t k) {
   if (s.flipu) { v1.b = -v1.b; v2.b = -v2.b; }
   if (s.flipv) { v1.c = -v1.c; v2.c = -v2.c; }
   int64_t o = cidx(P, i, j);
-  store4(a.D1, P, o, v1);
-  store4(a.D2, P, o, v2);
+  if (!FUSE || a.store_w) {
+    store4(a.D1, P, o, v1);
+    store4(a.D2, P, o, v2);
+  }
+  uint32_t st = 0u;
+  if (FUSE && (a.fsel == 2 || (a.fsel == 1 && !a.fnear[c]))) {
+    // k_finalize's conversion of these cells (Riemann / real GFM), with the
+    // velocity field of the ghost cells
+    bool ok1 = true, ok2 = true;
+    const V4 u1 = prims_to_cons(P.g1, P.p1, v1, &ok1);
+    const V4 u2 = prims_to_cons(P.g2, P.p2, v2, &ok2);
+    if (!ok1 || !ok2 || !is_physical_state_fast(u1) || !is_physical_state_fast(u2)) st |= ST_UNPHYSICAL;
+    store4(a.fU1, P, o, u1);
+    store4(a.fU2, P, o, u2);
+    if (!is_real(P, i, j)) {   // the real cells' velocities come from k_prims and k_ifc_vel
+      const V4& V = c_le0(a.phi[o]) ? v1 : v2;
+      a.fvel[o] = V.b;
+      a.fvel[o + P.plane] = V.c;
+    }
+  }
+  return st;
 }
 
+// FUSE: the sweep may carry the fused conversion (a separate instance, so
+// that the plain sweeps keep their lower register count)
+template <bool FUSE>
 __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
+  uint32_t st = 0u;
   if (a.list) {
     int cnt[BAND_CLASSES];
     int n = 0;
@@ -594,13 +629,17 @@ __global__ void __launch_bounds__(256) k_extrap(ExtrapArgs a) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
       int q = 0, r = e;
       while (r >= cnt[q]) { r -= cnt[q]; q++; }
-      extrap_cell(a, a.list[(int64_t)q * a.list_stride + r]);
+      st |= extrap_cell<FUSE>(a, a.list[(int64_t)q * a.list_stride + r]);
     }
-    return;
+  } else {
+    const int64_t n = (int64_t)P.nr * P.nc;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+      st |= extrap_cell<FUSE>(a, k);
   }
-  const int64_t n = (int64_t)P.nr * P.nc;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    extrap_cell(a, k);
+  if (FUSE && a.fsel) {
+    const uint32_t wst = __reduce_or_sync(0xffffffffu, st);
+    if ((threadIdx.x & 31) == 0 && wst) atomicOr(&a.Dw->status, wst);
+  }
 }
 
 // The cells (over the padded rows, ghost cells included) whose
@@ -1783,41 +1822,17 @@ struct FinalArgs {
   DevTime* D;
   int ogfm;
   int vel_mode;   // 0: real-fluid velocity, 1: extension seeds (OGFM interfacial), 2: leave vel alone
-  const uint8_t* near_cell;
-  int sel;        // 0: every cell, 1: cells far from the interface, 2: near cells
-  // the near cells as BAND_CLASSES list segments of list_stride entries
-  // (counts in list_n[]) for sel 2, or null
-  const int* list;
-  const int* list_n;
-  int64_t list_stride;
 };
 
 __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
-  int cnt[BAND_CLASSES];
-  int64_t n = (int64_t)P.nr * P.nc;
-  if (a.list) {
-    n = 0;
-    for (int q = 0; q < BAND_CLASSES; q++) { cnt[q] = a.list_n[q]; n += cnt[q]; }
-  }
+  const int64_t n = (int64_t)P.nr * P.nc;
   uint32_t st = 0;
   int bb[8] = {INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN, INT_MAX, INT_MIN};
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-    int64_t k = q;
-    if (a.list) {
-      int sg = 0;
-      int64_t r = q;
-      while (r >= cnt[sg]) { r -= cnt[sg]; sg++; }
-      k = a.list[(int64_t)sg * a.list_stride + r];
-    }
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     int i = (int)(k / P.nc), j = (int)(k % P.nc);
     int64_t c = cidx(P, i, j);
-    if (a.sel && !a.list) {   // a ghost cell is near when its boundary-condition source is
-      BCSrc s = bc_source(P, i, j);
-      const bool nr = a.near_cell[cidx(P, s.i, s.j)] != 0;
-      if ((a.sel == 2) != nr) continue;
-    }
     bool f1 = c_le0(a.phi[c]);
     if (a.ogfm) {
       V4 w1 = load4(a.W1, P, c), w2 = load4(a.W2, P, c);
@@ -1847,12 +1862,6 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a) {
       const double* V = f1 ? a.V1 : a.V2;
       a.vel[c] = V[c + P.plane];
       a.vel[c + P.plane] = V[c + 2 * P.plane];
-    } else if (a.vel_mode == 3) {   // ghost cells only (k_prims and k_ifc_vel write the real cells)
-      if (!is_real(P, i, j)) {
-        const double* V = f1 ? a.V1 : a.V2;
-        a.vel[c] = V[c + P.plane];
-        a.vel[c + P.plane] = V[c + 2 * P.plane];
-      }
     } else if (a.vel_mode == 1) {
       double vx = 0.0, vy = 0.0;
       if (a.mask[c]) { const double* V = f1 ? a.V1 : a.V2; vx = V[c + P.plane]; vy = V[c + 2 * P.plane]; }
@@ -1946,11 +1955,23 @@ __device__ __forceinline__ double houc5(double a, const double* f, int64_t c, in
           2.0 * f[c + 3 * st]) * inv60h;
 }
 
+// every > 1: part of a reinitialisation that runs only on steps whose number
+// (counting from 1) is a multiple of `every`, decided on the device so that a
+// captured step graph replays correctly on every step
+__device__ __forceinline__ bool reinit_skipped(const DevTime* D, int every) {
+  return every > 1 && (D->numsteps + 1) % every != 0;
+}
+
+// S non-null (the last stage of a step that reinitialises, unless
+// reinit_skipped(D, every)): also the reinitialisation's sign function
+// S = r / sqrt(r^2 + h^2) of the new value r, k_reinit_iter's S
 template <int ORDER, int STAGE>
 __global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, const double* phi, double* out,
-                                                  const double* vel, const DevTime* D) {
+                                                  const double* vel, const DevTime* D, double* S, int every) {
   if (!D->active) return;
   const double dt = D->dt;
+  const bool sign = S != nullptr && !reinit_skipped(D, every);
+  const double h = dmin_std(P.dx, P.dy);
   const int64_t n = (int64_t)P.nr * P.nc;
   GridP Q = P;
   if (!P.periodic) { Q.bcL = Q.bcR = Q.bcB = Q.bcT = GFM_BC_TRANSMISSIVE; }
@@ -1975,33 +1996,15 @@ __global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, cons
     else if (STAGE == 2) r = 0.75 * phi[c] + 0.25 * (X[c] + dt * L);
     else r = (1.0 / 3.0) * phi[c] + (2.0 / 3.0) * (X[c] + dt * L);
     out[cidx(P, i, j)] = r;
+    if (sign) S[cidx(P, i, j)] = r / sqrt(r * r + h * h);
   }
 }
 
-// every > 1: part of a reinitialisation that runs only on steps whose number
-// (counting from 1) is a multiple of `every`, decided on the device so that a
-// captured step graph replays correctly on every step
-__device__ __forceinline__ bool reinit_skipped(const DevTime* D, int every) {
-  return every > 1 && (D->numsteps + 1) % every != 0;
-}
-
-__global__ void k_copy_plane(GridP P, const double* src, double* dst, const DevTime* D, int every) {
-  if (!D->active || reinit_skipped(D, every)) return;
+// invert 0: skipped on the steps reinit_skipped(D, every) names; invert 1: on the others
+__global__ void k_copy_plane(GridP P, const double* src, double* dst, const DevTime* D, int every, int invert) {
+  if (!D->active || reinit_skipped(D, every) != (invert != 0)) return;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < P.plane; k += (int64_t)gridDim.x * blockDim.x)
     dst[k] = src[k];
-}
-
-// S(phi0) = phi0 / sqrt(phi0^2 + h^2), cached for the reinitialisation
-__global__ void k_reinit_sign(GridP P, const double* phi, double* S, const DevTime* D, int every) {
-  if (!D->active || reinit_skipped(D, every)) return;
-  const int64_t n = (int64_t)P.nr * P.nc;
-  const double h = dmin_std(P.dx, P.dy);
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    int i = (int)(k / P.nc), j = (int)(k % P.nc);
-    int64_t c = cidx(P, i, j);
-    double p0 = phi[c];
-    S[c] = p0 / sqrt(p0 * p0 + h * h);
-  }
 }
 
 // one Sussman-Smereka-Osher iteration with Godunov upwinding
@@ -2084,7 +2087,7 @@ static void extrap_coeffs(const GridP& P, ExtrapArgs& e) {
 
 static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
   const GridP& P = ctx->P;
-  const int blocks = wave_blocks((const void*)k_extrap, 256, ctx->num_sms, padded_cells(P));
+  const int blocks = wave_blocks((const void*)k_extrap<false>, 256, ctx->num_sms, padded_cells(P));
   for (int it = 0; it < N; it++) {
     ExtrapArgs e;
     e.P = P;
@@ -2097,8 +2100,10 @@ static void run_extrap(gfm_ctx* ctx, int N, bool mgfm) {
     e.list = nullptr; e.list_n = nullptr;
     e.nclass = 0; e.list_stride = 0;
     e.F1 = nullptr; e.F2 = nullptr; e.cls = nullptr; e.near_min = 0;
+    e.Dw = ctx->dtime; e.fsel = 0; e.fnear = nullptr; e.fU1 = nullptr; e.fU2 = nullptr; e.fvel = nullptr;
+    e.store_w = 1;
     extrap_coeffs(P, e);
-    k_extrap<<<blocks, 256, 0, ctx->stream>>>(e); counted();
+    k_extrap<false><<<blocks, 256, 0, ctx->stream>>>(e); counted();
     for (int f = 0; f < 2; f++) { double* t = ctx->W[f]; ctx->W[f] = ctx->Wt[f]; ctx->Wt[f] = t; }
   }
 }
@@ -2158,9 +2163,6 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
     f.vel = ctx->vel; f.D = ctx->dtime;
     f.ogfm = 1;
     f.vel_mode = ext ? 1 : 0;
-    f.near_cell = nullptr;
-    f.list = nullptr; f.list_n = nullptr; f.list_stride = 0;
-    f.sel = 0;
     k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
     k_rc_clamp<<<1, 1, 0, s>>>(P, ctx->dtime); counted();
     if (ext) run_ext_vfield(ctx, 20);
@@ -2215,9 +2217,6 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   f.vel = ctx->vel; f.D = ctx->dtime;
   f.ogfm = 0;
   f.vel_mode = ext ? 2 : 0;
-  f.near_cell = nullptr;
-  f.list = nullptr; f.list_n = nullptr; f.list_stride = 0;
-  f.sel = 0;
   k_finalize<<<fblocks, 256, 0, s>>>(f); counted();
   if (ext) run_ext_vfield(ctx, 20);
 }
@@ -2305,9 +2304,12 @@ __global__ void k_tile_flags(GridP P, const uint8_t* near_cell, int* tile_near, 
   if (lane == 0) tile_near[warp] = any ? 1 : 0;
 }
 
+// one sweep of the overlapped schedule; fsel != 0 fuses k_finalize's
+// conversion of the sweep's results (1: far cells, 2: the listed near cells),
+// which are then not stored as primitives
 static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, double* D1, double* D2, bool overlay,
                          cudaStream_t s, const int* list, const int* list_n, int nclass,
-                         const double* const* far = nullptr, int near_min = 0) {
+                         const double* const* far = nullptr, int near_min = 0, int fsel = 0) {
   const GridP& P = ctx->P;
   ExtrapArgs e;
   e.P = P;
@@ -2324,34 +2326,24 @@ static void extrap_sweep(gfm_ctx* ctx, const double* S1, const double* S2, doubl
   e.F1 = far ? far[0] : nullptr; e.F2 = far ? far[1] : nullptr;
   e.cls = ctx->band_cls;
   e.near_min = near_min;
+  e.Dw = ctx->dtime;
+  e.fsel = fsel;
+  e.fnear = ctx->near_cell;
+  e.fU1 = ctx->U[0]; e.fU2 = ctx->U[1];
+  e.fvel = ctx->vel;
+  e.store_w = fsel ? 0 : 1;
   extrap_coeffs(P, e);
   // a listed sweep covers the band around the interface: a few percent of the grid
-  const int blocks = list ? NEAR_CTAS : wave_blocks((const void*)k_extrap, 256, ctx->far_sms, padded_cells(P));
-  k_extrap<<<blocks, 256, 0, s>>>(e);
+  if (fsel) {
+    const int blocks = list ? NEAR_CTAS : wave_blocks((const void*)k_extrap<true>, 256, ctx->far_sms, padded_cells(P));
+    k_extrap<true><<<blocks, 256, 0, s>>>(e);
+  } else {
+    const int blocks = list ? NEAR_CTAS : wave_blocks((const void*)k_extrap<false>, 256, ctx->far_sms, padded_cells(P));
+    k_extrap<false><<<blocks, 256, 0, s>>>(e);
+  }
   counted();
 }
 
-static void finalize_sel(gfm_ctx* ctx, const double* const* Wf, int sel, cudaStream_t s) {
-  const GridP& P = ctx->P;
-  FinalArgs f;
-  f.P = P;
-  f.W1 = const_cast<double*>(Wf[0]); f.W2 = const_cast<double*>(Wf[1]);
-  f.C1 = Wf[0]; f.C2 = Wf[1];
-  f.V1 = Wf[0]; f.V2 = Wf[1];
-  f.mask = ctx->mask; f.phi = ctx->phi;
-  f.U1 = ctx->U[0]; f.U2 = ctx->U[1];
-  f.vel = ctx->vel; f.D = ctx->dtime;
-  f.ogfm = 0;
-  f.vel_mode = 3;   // ghost cells: k_prims and k_ifc_vel write the real cells' velocities
-  f.near_cell = ctx->near_cell;
-  f.sel = sel;
-  f.list = (sel == 2) ? ctx->band_list : nullptr;   // every segment: the cells whose source is near
-  f.list_n = (sel == 2) ? ctx->list_n : nullptr;
-  f.list_stride = ctx->band_stride;
-  k_finalize<<<(sel == 2) ? NEAR_CTAS : wave_blocks((const void*)k_finalize, 256, ctx->far_sms, padded_cells(P)), 256, 0,
-               s>>>(f);
-  counted();
-}
 
 void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   const GridP& P = ctx->P;
@@ -2432,13 +2424,14 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   {
     const double* src1 = ctx->W[0];
     const double* src2 = ctx->W[1];
-    for (int it = 0; it < 6; it++) {   // each sweep into its own buffer: the exact sweeps read them
-      double** dst = ctx->SF[it];
-      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr, nullptr, 0);
+    // each of the first five sweeps into its own buffer (the exact sweeps
+    // read them); the sixth converts the far cells to conserved grids
+    for (int it = 0; it < 6; it++) {
+      double** dst = ctx->SF[it < 5 ? it : 4];   // not written by the sixth
+      extrap_sweep(ctx, src1, src2, dst[0], dst[1], false, ctx->s_far, nullptr, nullptr, 0, nullptr, 0,
+                   it == 5 ? 1 : 0);
       src1 = dst[0]; src2 = dst[1];
     }
-    const double* fin[2] = {src1, src2};
-    finalize_sel(ctx, fin, 1, ctx->s_far);
   }
   cudaEventRecord(ctx->ev_far_final, ctx->s_far);
   if (ctx->timing) cudaEventRecord(ctx->tev[5], ctx->s_far);
@@ -2463,13 +2456,12 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
       // (segments 0..k); sweep 1 reads the pre-loop primitives with the loop's
       // writes overlaid, sweep k > 1 the exact sweep k - 1 within k - 1
       // (cls >= NEAR_RADIUS + 2 - k) and the far field's sweep k - 1 beyond
+      // the sixth converts the near cells to conserved grids
       const double* far[2] = {it ? ctx->SF[it - 1][0] : nullptr, it ? ctx->SF[it - 1][1] : nullptr};
       extrap_sweep(ctx, src1, src2, dst[0], dst[1], it == 0, sn, ctx->band_list, ctx->list_n, it + 2,
-                   it ? far : nullptr, NEAR_RADIUS + 1 - it);
+                   it ? far : nullptr, NEAR_RADIUS + 1 - it, it == 5 ? 2 : 0);
       src1 = dst[0]; src2 = dst[1];
     }
-    const double* fin[2] = {src1, src2};
-    finalize_sel(ctx, fin, 2, sn);
   }
   if (ctx->timing) cudaEventRecord(ctx->tev[3], sn);
   // The near tiles read far cells too: the far cells' conversion is done (the
@@ -2481,52 +2473,77 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   // (on s_near) and joins s_near and the far stream back into ctx->stream
 }
 
-// the advection stages read phi and the velocity field and write phi_a /
-// phi_b; the copy writes the result into phi
-void launch_ls_stages(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
-  const GridP& P = ctx->P;
-  // the stage kernels have one occupancy
-  const int blocks = wave_blocks((const void*)k_ls_stage<5, 1>, 256, ctx->num_sms, padded_cells(P));
-  if (m->ls_order == 1) {
-    k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
-  } else {
-    k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
-    k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime); counted();
-    k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime); counted();
-  }
+// The level set of one step: the advection stages (part 1) read phi and the
+// velocity field and write phi_a / phi_b, the last of them, on a step that
+// reinitialises, also the sign function S; then (part 2) phi := phi_a, or on
+// a reinitialisation step the Sussman iterations starting from phi_a
+// (phi_a -> phi -> phi_a ...; an even count ends with a copy into phi).
+// every: -1 no reinitialisation this step, 0 one this step (decided on the
+// host), k >= 1 decided on the device (a step recorded into a graph).
+static int ls_reinit_every(const gfm_ctx* ctx, const gfm_method_desc* m) {
+  if (m->reinit_every <= 0 || m->reinit_iters <= 0) return -1;
+  if (ctx->graph_mode) return m->reinit_every;
+  return ((ctx->steps_done_host + 1) % m->reinit_every == 0) ? 0 : -1;
 }
 
-void launch_ls_copy(gfm_ctx* ctx, cudaStream_t s) {
-  const GridP& P = ctx->P;
-  k_copy_plane<<<wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, padded_cells(P)), 256, 0, s>>>(
-      P, ctx->phi_a, ctx->phi, ctx->dtime, 0);
-  counted();
-}
-
-void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
-  launch_ls_stages(ctx, m, s);
-  launch_ls_copy(ctx, s);
-}
-
-// reinitialisation: iterations alternate phi -> phi_a -> phi ...; an odd
-// count ends with a copy back, so phi stays the one buffer holding the level set
-void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream_t s) {
+void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts) {
   const GridP& P = ctx->P;
   const int64_t n = padded_cells(P);
-  k_reinit_sign<<<wave_blocks((const void*)k_reinit_sign, 256, ctx->num_sms, n), 256, 0, s>>>(P, ctx->phi, ctx->phi0,
-                                                                                             ctx->dtime, every);
-  counted();
-  const int blocks = wave_blocks((const void*)k_reinit_iter, 256, ctx->num_sms, n);
-  for (int it = 0; it < m->reinit_iters; it++) {
-    const double* src = (it & 1) ? ctx->phi_a : ctx->phi;
-    double* dst = (it & 1) ? ctx->phi : ctx->phi_a;
-    k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime, every); counted();
+  const int every = ls_reinit_every(ctx, m);
+  double* S = every >= 0 ? ctx->phi0 : nullptr;
+  const int ev = every > 0 ? every : 0;
+  if (parts & 1) {
+    // the stage kernels have one occupancy
+    const int blocks = wave_blocks((const void*)k_ls_stage<5, 1>, 256, ctx->num_sms, n);
+    if (m->ls_order == 1) {
+      k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, S, ev);
+      counted();
+    } else {
+      k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
+      k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime, nullptr, 0);
+      k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, S, ev);
+      counted(3);
+    }
   }
-  if (m->reinit_iters & 1) {
-    k_copy_plane<<<wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, n), 256, 0, s>>>(P, ctx->phi_a, ctx->phi,
-                                                                                           ctx->dtime, every);
+  if (parts & 2) {
+    const int cblocks = wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, n);
+    // phi := phi_a on the steps without a reinitialisation
+    if (every < 0) {
+      k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0, 0); counted();
+    } else if (every > 1) {
+      k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, every, 1); counted();
+    }
+    if (every >= 0) {
+      const int blocks = wave_blocks((const void*)k_reinit_iter, 256, ctx->num_sms, n);
+      for (int it = 0; it < m->reinit_iters; it++) {
+        const double* src = (it & 1) ? ctx->phi : ctx->phi_a;
+        double* dst = (it & 1) ? ctx->phi_a : ctx->phi;
+        k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime, ev); counted();
+      }
+      if (!(m->reinit_iters & 1)) {
+        k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, ev, 0); counted();
+      }
+    }
+  }
+}
+
+// the advection alone (gfm_ls_update): stages, then phi := phi_a
+void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
+  const GridP& P = ctx->P;
+  const int64_t n = padded_cells(P);
+  const int blocks = wave_blocks((const void*)k_ls_stage<5, 1>, 256, ctx->num_sms, n);
+  if (m->ls_order == 1) {
+    k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
     counted();
+  } else {
+    k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
+    k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime, nullptr, 0);
+    k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
+    counted(3);
   }
+  k_copy_plane<<<wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, n), 256, 0, s>>>(P, ctx->phi_a, ctx->phi,
+                                                                                           ctx->dtime, 0, 0);
+  counted();
 }
 
 // Occupancy queries of the grid-stride kernels, made once before any launch
@@ -2534,9 +2551,9 @@ void launch_reinit(gfm_ctx* ctx, const gfm_method_desc* m, int every, cudaStream
 void prepare_step_kernels() {
   static std::once_flag once;
   std::call_once(once, [] {
-    const void* ks[] = {(const void*)k_commit_u, (const void*)k_extrap, (const void*)k_finalize,
-                        (const void*)k_ls_stage<5, 1>, (const void*)k_copy_plane, (const void*)k_reinit_sign,
-                        (const void*)k_reinit_iter};
+    const void* ks[] = {(const void*)k_commit_u, (const void*)k_extrap<false>, (const void*)k_extrap<true>,
+                        (const void*)k_finalize,
+                        (const void*)k_ls_stage<5, 1>, (const void*)k_copy_plane, (const void*)k_reinit_iter};
     for (const void* k : ks) wave_blocks(k, 256, 1, 1);
   });
 }
@@ -2601,7 +2618,7 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
 void launch_vof_update(gfm_ctx* ctx, cudaStream_t s) {
   const GridP& P = ctx->P;
   const int blocks = grid_blocks((int64_t)P.nr * P.nc, 256);
-  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime, 0); counted();
+  k_copy_plane<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->dtime, 0, 0); counted();
   k_vof_sweep<<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi0, ctx->vel, ctx->phi_a, 0, ctx->dtime); counted();
   k_vof_sweep<<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi0, ctx->vel, ctx->phi, 1, ctx->dtime); counted();
 }
