@@ -502,11 +502,10 @@ constexpr int IFC_OUT = 8;   // doubles of interface output per interfacial cell
 // distance 0..NEAR_RADIUS (k_band_lists).
 constexpr int NEAR_RADIUS = 6;
 constexpr int BAND_CLASSES = NEAR_RADIUS + 1;
-// CTAs of the listed kernels after the loop (exact sweeps, near conversion):
-// the band holds a few thousand to ten thousand cells, and these kernels run
-// while the far field's flux update fills the other SMs, so a grid that fits
-// in one wave on the loop's own 8 SMs starts at once, where one of 2 CTAs per
-// SM queued several waves of nearly empty CTAs behind each other
+// CTAs of the listed sweeps after the loop: the band holds a few thousand to
+// about ten thousand cells, about one per thread of 40 CTAs of 256 threads
+// (one wave on the loop's own 8 SMs, which these kernels share with the
+// level set while the far field's flux update fills the other SMs)
 constexpr int NEAR_CTAS = 40;
 
 struct ExtrapArgs {
