@@ -68,6 +68,8 @@ static int64_t padded_cells(const GridP& P) { return (int64_t)P.nr * P.nc; }
 // integer pipe (c_lt): the FP64 pipe bounds the kernels that use them
 __device__ __forceinline__ double dmax_std(double a, double b) { return c_lt(a, b) ? b : a; }
 __device__ __forceinline__ double dmin_std(double a, double b) { return c_lt(b, a) ? b : a; }
+// |x| by clearing the sign bit (an integer operation)
+__device__ __forceinline__ double fabs_bits(double x) { return from_bits(as_bits(x) & GFM_MAG_BITS); }
 
 // Normal planes (k_prims): 0,1 raw central-difference gradient of phi,
 // 2,3 unit normal with the reference's fallback to (1,0) below 1e-12
@@ -2026,16 +2028,21 @@ __global__ void __launch_bounds__(256) k_reinit_iter(GridP P, const double* cur,
     double b = (cur[c + 1] - f) * idx;
     double cc = (f - cur[c - P.pitch]) * idy;
     double d = (cur[c + P.pitch] - f) * idy;
-    double gx, gy;
+    // Godunov's upwind gradient: gx = max(x1^2, x2^2) with (x1, x2) = (max(a,0),
+    // min(b,0)) where sg > 0, (min(a,0), max(b,0)) elsewhere (gy alike).  The
+    // larger square is the square of the larger magnitude (rounding is
+    // monotonic; equal squares are the same double, and a NaN operand keeps
+    // max()'s choice of its first argument), so the candidates are compared
+    // on the integer pipe and one square is formed per direction.
+    double x1, x2, y1, y2;
     if (c_gt0(sg)) {
-      double ap = dmax_std(a, 0.0), bm = dmin_std(b, 0.0), cp = dmax_std(cc, 0.0), dm = dmin_std(d, 0.0);
-      gx = dmax_std(ap * ap, bm * bm);
-      gy = dmax_std(cp * cp, dm * dm);
+      x1 = dmax_std(a, 0.0); x2 = dmin_std(b, 0.0); y1 = dmax_std(cc, 0.0); y2 = dmin_std(d, 0.0);
     } else {
-      double am = dmin_std(a, 0.0), bp = dmax_std(b, 0.0), cm = dmin_std(cc, 0.0), dp = dmax_std(d, 0.0);
-      gx = dmax_std(am * am, bp * bp);
-      gy = dmax_std(cm * cm, dp * dp);
+      x1 = dmin_std(a, 0.0); x2 = dmax_std(b, 0.0); y1 = dmin_std(cc, 0.0); y2 = dmax_std(d, 0.0);
     }
+    const double mx = c_lt(fabs_bits(x1), fabs_bits(x2)) ? x2 : x1;
+    const double my = c_lt(fabs_bits(y1), fabs_bits(y2)) ? y2 : y1;
+    const double gx = mx * mx, gy = my * my;
     double G = sqrt(gx + gy) - 1.0;
     out[cidx(P, i, j)] = f - dtau * sg * G;
   }
