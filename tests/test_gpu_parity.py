@@ -143,7 +143,9 @@ def test_determinism():
                                                      ("shocked_helium_bubble", 64, 20, "riemannGFM", False),
                                                      ("ST1_x", 64, 32, "riemannGFM", False),
                                                      ("ST2_y", 32, 64, "riemannGFM", False),
-                                                     ("ST1_x", 32, 32, "riemannGFM", True)])
+                                                     ("ST1_x", 32, 32, "riemannGFM", True),
+                                                     # no interfacial cell: empty band, near pass idle
+                                                     ("GDA", 32, 32, "riemannGFM", False)])
 def test_overlapped_schedule_matches_sequential(case, Nx, Ny, gfm, periodic):
     """The SM-partitioned schedule (interface loop beside the far-field
     update, the exact extrapolation on a band that grows by one cell per
