@@ -207,22 +207,22 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   const bool uniform = __syncthreads_and(same) != 0;
 
   if (uniform) {
-    if (tid == 0) {
+    // lane 0 forms the x faces' flux and lane 1 the y faces', side by side
+    // in one instruction stream (both form the cell's face states)
+    if (tid < 2) {
+      const bool xd = tid == 0;
       V4 W = sW(s, 2, 2);
-      V4 fx, fy;
-      int itx = 0, ity = 0;
+      V4 f;
+      int it = 0;
       if (MUSCL) {
         V4 fs[4];
         cell_face_states(W, s.irho[2][2], W, W, W, W, gam, pinf, sx, sy, fs);
-        fx = muscl_face_flux(true, fs[0], fs[1], W, W, gas, &st, &itx);
-        fy = muscl_face_flux(false, fs[2], fs[3], W, W, gas, &st, &ity);
+        f = muscl_face_flux(xd, xd ? fs[0] : fs[2], xd ? fs[1] : fs[3], W, W, gas, &st, &it);
       } else {
-        fx = pure_rs_flux(true, gas, W, W, &st, &itx);
-        fy = pure_rs_flux(false, gas, W, W, &st, &ity);
+        f = pure_rs_flux(xd, gas, W, W, &st, &it);
       }
-      iters = itx * NXF + ity * NYF;
-      s_uniform_flux[0] = fx;
-      s_uniform_flux[1] = fy;
+      iters = it * (xd ? NXF : NYF);
+      s_uniform_flux[tid] = f;
     }
     __syncthreads();
   } else {
