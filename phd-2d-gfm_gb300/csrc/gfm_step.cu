@@ -1948,12 +1948,17 @@ __global__ void __launch_bounds__(256) k_ext_vel(GridP P, const double* S, doubl
 //   L(f) = -(u f_x + v f_y) with the cell-centred velocity field
 // Ghost cells: mirror (or periodic) copies, computed by their own threads.
 // ---------------------------------------------------------------------------
+// HOUC5 derivative: a >= 0 uses (-2, 15, -60, 20, 30, -3) on f[c-3..c+2],
+// a < 0 (3, -30, -20, 60, -15, 2) on f[c-2..c+3], each summed left to right
+// as written.  Subtracting b*x is adding (-b)*x (the same IEEE operations), so
+// both branches are one sum with coefficients and offset chosen per lane: a
+// warp whose lanes upwind in different directions issues it once.
 __device__ __forceinline__ double houc5(double a, const double* f, int64_t c, int64_t st, double inv60h) {
-  if (c_ge0(a))
-    return (-2.0 * f[c - 3 * st] + 15.0 * f[c - 2 * st] - 60.0 * f[c - st] + 20.0 * f[c] + 30.0 * f[c + st] -
-            3.0 * f[c + 2 * st]) * inv60h;
-  return (3.0 * f[c - 2 * st] - 30.0 * f[c - st] - 20.0 * f[c] + 60.0 * f[c + st] - 15.0 * f[c + 2 * st] +
-          2.0 * f[c + 3 * st]) * inv60h;
+  const bool up = c_ge0(a);
+  const double k0 = up ? -2.0 : 3.0, k1 = up ? 15.0 : -30.0, k2 = up ? -60.0 : -20.0;
+  const double k3 = up ? 20.0 : 60.0, k4 = up ? 30.0 : -15.0, k5 = up ? -3.0 : 2.0;
+  const double* g = f + c + (up ? -3 : -2) * st;
+  return (k0 * g[0] + k1 * g[st] + k2 * g[2 * st] + k3 * g[3 * st] + k4 * g[4 * st] + k5 * g[5 * st]) * inv60h;
 }
 
 // every > 1: part of a reinitialisation that runs only on steps whose number
