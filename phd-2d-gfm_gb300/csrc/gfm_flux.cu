@@ -12,10 +12,11 @@
 //            reference recomputes these per face (as cell C, L or B); each
 //            cell's values do not depend on which face asks for them.
 //   phase 3  per face: the second fallback, primitives -> conserved, and the
-//            exact Riemann flux (pure_RS_exact::solve_RP).  Faces whose data
-//            hold no waves are finished at once; the others are queued and
-//            solved by consecutive threads afterwards, so that the Newton
-//            iterations run with few idle lanes.
+//            exact Riemann flux (pure_RS_exact::solve_RP).  Up to the
+//            no-wave test the faces run one per thread; then the faces with
+//            waves and those without are queued apart and finished by
+//            consecutive threads, so that the Newton iterations run with few
+//            idle lanes and no warp runs both kinds.
 //   phase 4  per cell: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn, the
 //            accumulation order of the reference's face loop (:290-292).
 #include "gfm_internal.cuh"
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FluxSmem& s = *reinterpret_cast<FluxSmem*>(smem_raw);
   __shared__ V4 s_uniform_flux[2];
-  __shared__ int s_nq;   // queued faces (phase 3)
+  __shared__ int s_nq, s_nt;   // queued faces with waves and without (phase 3)
   const GridP& P = a.P;
   const int fluid = a.fluid_base + blockIdx.z;
   const double* __restrict__ U = a.U[blockIdx.z];
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   // whole region holds one bit pattern
   const int64_t c00 = cidx(P, min(max(i0 - 2, 0), P.nr - 1), min(max(j0 - 2, 0), P.nc - 1));
   const V4 u00 = load4(U, P, c00);
-  if (tid == 0) s_nq = 0;
+  if (tid == 0) { s_nq = 0; s_nt = 0; }
   bool same = true;
   for (int k = tid; k < WR * WC; k += NT) {
     int r = k / WC, c = k % WC;
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
       __syncthreads();
     }
     // phase 3a: x faces (TY rows x TX+1) then y faces (TY+1 rows x TX) up to
-    // the no-wave test; those without waves are finished, the others queued
+    // the no-wave test, then queued by kind
     //   x face (fr, fc): between cells (i0+fr, j0+fc-1) and (i0+fr, j0+fc)
     //   y face (fr, fc): between cells (i0+fr-1, j0+fc) and (i0+fr, j0+fc)
     // Flux slot of face k, component m: fx[m] (flat) + k, or fy[m] + k - NXF.
@@ -263,22 +264,19 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
       const bool nowave = rs_face_front(xdir, gas, UL, UR, &st, d);
       double* slot = xdir ? &s.fx[0][0][0] + k : &s.fy[0][0][0] + (k - NXF);
       const int cs = xdir ? NXF : NYF;
-      if (nowave) {
-        V4 f = rs_face_finish(xdir, gas, d, &st, &iters);
-        slot[0] = f.a; slot[cs] = f.b; slot[2 * cs] = f.c; slot[3 * cs] = f.d;
-      } else {
-        const int e = atomicAdd(&s_nq, 1);
-        s.qid[e] = (unsigned short)k;
-        slot[0] = d.rhoL; slot[cs] = d.uL; slot[2 * cs] = d.pL; slot[3 * cs] = d.rhoR;
-        s.qd[0][k] = d.uR; s.qd[1][k] = d.pR; s.qd[2][k] = d.utL; s.qd[3][k] = d.utR;
-        s.qd[4][k] = d.irhoL; s.qd[5][k] = d.irhoR;
-      }
+      // every face is queued, those with waves from the front and those
+      // without from the back, so that phase 3b runs each kind in whole warps
+      const int e = nowave ? NXF + NYF - 1 - atomicAdd(&s_nt, 1) : atomicAdd(&s_nq, 1);
+      s.qid[e] = (unsigned short)k;
+      slot[0] = d.rhoL; slot[cs] = d.uL; slot[2 * cs] = d.pL; slot[3 * cs] = d.rhoR;
+      s.qd[0][k] = d.uR; s.qd[1][k] = d.pR; s.qd[2][k] = d.utL; s.qd[3][k] = d.utR;
+      s.qd[4][k] = d.irhoL; s.qd[5][k] = d.irhoR;
     }
     __syncthreads();
-    // phase 3b: the queued faces
-    const int nq = s_nq;
-    for (int e = tid; e < nq; e += NT) {
-      const int k = s.qid[e];
+    // phase 3b: the queued faces, those with waves first
+    const int nq = s_nq, nt = s_nt;
+    for (int e = tid; e < nq + nt; e += NT) {
+      const int k = s.qid[e < nq ? e : NXF + NYF - nt + (e - nq)];
       const bool xdir = k < NXF;
       double* slot = xdir ? &s.fx[0][0][0] + k : &s.fy[0][0][0] + (k - NXF);
       const int cs = xdir ? NXF : NYF;
