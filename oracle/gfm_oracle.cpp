@@ -1,7 +1,7 @@
 // TEST INFRASTRUCTURE: the CPU oracle of the two-fluid ghost-fluid Euler step.
 //
 // Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may load
-// this library, and only as the checker / CPU baseline.  It is never on the
+// this library, and only as the test reference / CPU baseline.  It is never on the
 // product path.
 //
 // A single-threaded C++ restatement of murraycutforth/PhD-2D-GFM's hot path,

@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE: ctypes binding of the CPU oracle (liboracle.so).
 
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may use
-this module, and only as the checker or the timed CPU baseline.
+this module, and only as the test reference or the timed CPU baseline.
 
 PARITY UNPINNED: the reference cannot be built in this environment and ships
 no golden vectors; the oracle restates its code (see gfm_oracle.cpp).

@@ -133,7 +133,7 @@ void fill_case(const CaseSpec& cs, const gfm_grid_desc* d, bool two, double* U1,
 namespace gfm {
 
 // The parameters of a named case (set_sim_ICs, sourcecode/sim_twofluid.cpp:599-1799,
-// sourcecode/sim_onefluid.cpp:196-449, and the workloads of this build).
+// sourcecode/sim_onefluid.cpp:196-449, and the benchmark workloads).
 bool make_case_spec(const char* sim_type, const char* test_case, const gfm_grid_desc* d, CaseSpec* out) {
   std::string st(sim_type), tc(test_case);
   const double g1 = d->gamma1, q1 = d->pinf1, g2 = d->gamma2, q2 = d->pinf2;

@@ -14,7 +14,7 @@
 // waves); elsewhere the two-shock guess is already within about 1e-6 and is
 // kept.  Newton's method then runs from the proposal exactly as from any
 // other guess, so the converged p* meets the same tolerance and the exact
-// solver stays the judge.
+// solver has the last word.
 #pragma once
 
 #include "gfm_math.cuh"

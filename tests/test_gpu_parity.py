@@ -2,7 +2,7 @@
 
 Both follow the same operation order with no contracted multiply-adds, so
 the expected difference is zero; the bar written into the asserts is the
-spec tolerance, relative L1 <= 1e-10 per conserved field over real
+required tolerance, relative L1 <= 1e-10 per conserved field over real
 cells (and for phi), with interfacial masks bit-exact.
 """
 import numpy as np
