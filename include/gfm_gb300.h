@@ -170,6 +170,23 @@ gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
 #define GFM_OVERLAP_AUTO 2
 gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int mode);
 
+/* Newton iteration limit of the context's exact Riemann solves (flux update
+ * and interface solves; default 60).  A solve that reaches it stops there
+ * and sets GFM_ST_NEWTON_NO_CONVERGE: the reference has no limit of its own
+ * (its solver is an absent library), so this is the device-side stand-in for
+ * a solve that does not converge. */
+gfm_status_t gfm_set_newton_limit(gfm_ctx* ctx, int max_iterations);
+
+/* Bounded waits of the interface loop (Riemann, real and VOF GFMs): each
+ * wait for an earlier cell's result polls its completion flag at most
+ * spin_limit times (0: the default, about a second) and then gives up,
+ * abandons its own cell and sets GFM_ST_SCHEDULE_LIMIT; the kernel returns
+ * and the context stays usable.  withheld_entry (>= 0) is a failure-detection
+ * hook for tests: that entry of the interface list (row-major order) is
+ * neither solved nor published, so its dependants' waits run out (-1: none,
+ * the default).  The step's results are not valid after a withheld entry. */
+gfm_status_t gfm_set_interface_wait(gfm_ctx* ctx, int64_t spin_limit, int withheld_entry);
+
 /* number of kernels this library has launched since it was loaded */
 int64_t gfm_launch_count(void);
 
@@ -378,12 +395,15 @@ gfm_status_t gfm_case_init_shock_bubble_device(gfm_ctx* ctx, const gfm_bubble_pa
  * start-up).  This entry point advances the caller's DEVICE grid U (layout as
  * above, unpitched) in place by up to nsteps steps of sim_onefluid's loop
  * (sourcecode/sim_onefluid.cpp:40-54); t and numsteps are in/out, status
- * receives the GFM_ST_* bits.  It calls no cudaMalloc/cudaFree: its scratch
- * is a built-in 16 MiB device array, which limits the grid to
+ * receives the GFM_ST_* bits.  The grid description is checked as by
+ * gfm_ctx_create (GFM_ERR_ARG otherwise).  It calls no cudaMalloc/cudaFree:
+ * its scratch is a built-in 16 MiB device array, which limits the grid to
  * GFM_NOALLOC_MAX_CELLS padded cells ((Nx+2 numGC)(Ny+2 numGC)); larger
- * grids are rejected with GFM_ERR_ARG.  The first call on each device looks
- * up the array's address and should come before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race. */
+ * grids are rejected with GFM_ERR_ARG.  It works in the CUDA context current
+ * on the calling thread; the first call in each context (once per device
+ * with the runtime's primary context) looks up the array's device address
+ * and should come before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race. */
 #define GFM_NOALLOC_MAX_CELLS 524272
 gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* grid, const gfm_method_desc* m, double* U, int nsteps,
                                        double* t, int* numsteps, uint32_t* status, void* cuda_stream);

@@ -714,6 +714,20 @@ gfm_status_t gfm_set_overlap(gfm_ctx* ctx, int mode) {
   return GFM_OK;
 }
 
+gfm_status_t gfm_set_newton_limit(gfm_ctx* ctx, int max_iterations) {
+  if (!ctx || max_iterations < 1 || max_iterations > 1000) return GFM_ERR_ARG;
+  ctx->P.gas1.maxit = max_iterations;
+  ctx->P.gas2.maxit = max_iterations;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_set_interface_wait(gfm_ctx* ctx, int64_t spin_limit, int withheld_entry) {
+  if (!ctx || spin_limit < 0 || withheld_entry < -1) return GFM_ERR_ARG;
+  ctx->ifc_spin_limit = (long long)spin_limit;
+  ctx->ifc_withhold = withheld_entry + 1;
+  return GFM_OK;
+}
+
 // FP64 peak: 8 independent FMA chains per thread, 8 CTAs of 256 per SM.
 __global__ void k_fp64_peak(double* out, int iters, double a, double b) {
   double x[8];

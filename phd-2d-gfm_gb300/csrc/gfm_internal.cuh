@@ -83,6 +83,8 @@ struct gfm_ctx {
   double* probe_w;   // and its 4 weights
   int itm;           // interface tracker of the last method used (GFM_ITM_*)
   int* ifc_opp;      // real GFM: opposite cell
+  long long ifc_spin_limit;  // polls before an interface-loop wait gives up (0: the default)
+  int ifc_withhold;  // test hook: 1 + the interface-list entry left unsolved (0: none)
   gfm::DevTime* dtime;
   gfm::DevTime* h_dtime;  // pinned host mirror
   int steps_done_host;

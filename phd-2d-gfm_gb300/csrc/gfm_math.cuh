@@ -457,9 +457,13 @@ GFM_HD V4 prims_to_cons(double g, double pinf, const V4& W, bool* ok) {
 // |f''/f'| <= 3.5/(p + pinf), so a step that small leaves the new iterate
 // within about 2e-14 (relative) of the root.
 // ---------------------------------------------------------------------------
+#define GFM_RS_TOL 1e-7
+#define GFM_RS_MAXIT 60
+
 struct Gas {
   double g, pinf;
   double G1, G2, G3, G4, G5, G6, G7, IG;
+  int maxit;   // Newton iteration limit of the exact solves with this material
 };
 
 GFM_HD Gas make_gas(double g, double pinf) {
@@ -473,6 +477,7 @@ GFM_HD Gas make_gas(double g, double pinf) {
   k.G6 = (g - 1.0) / (g + 1.0);
   k.G7 = (g - 1.0) / 2.0;
   k.IG = 1.0 / g;
+  k.maxit = GFM_RS_MAXIT;
   return k;
 }
 
@@ -564,8 +569,6 @@ struct RSStar {
   bool trivial;       // equal u and p: no waves, W_L | W_R across the contact
 };
 
-#define GFM_RS_TOL 1e-7
-#define GFM_RS_MAXIT 60
 
 // Newton-Raphson on p* (Toro's STARPU) from the initial guess p0, then u*
 // from the last pressure-function evaluation taken to p* along its tangent.
@@ -602,7 +605,7 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
     dp = p - pold;
     pold = p;
     if (conv) break;
-    if (it >= GFM_RS_MAXIT) { s.status |= ST_NEWTON_NO_CONVERGE; break; }
+    if (it >= kL.maxit) { s.status |= ST_NEWTON_NO_CONVERGE; break; }
   }
   s.p = p;
   // the pressure functions carried from the last evaluation point to p along

@@ -9,14 +9,21 @@
 // CFL reduction words) lives in the file-scope array below, which every GPU
 // that loads this library holds until the process exits.
 //
-// Set-up: the first call on each device looks up the array's device address
-// with cudaGetSymbolAddress, with that device current (host code may not use
-// the array's name as a device address).  Make that first call before any
-// stream capture.  Calls share the array and it keeps the last call's
-// contents, so every call re-initialises what must start at zero; calls that
-// overlap on the GPU (different streams, or different host threads on the
-// same device) race on it.
+// Set-up: host code may not use the array's name as a device address.  The
+// first call in each CUDA context (normally once per device: the runtime's
+// primary context) looks up the array's device address with
+// cudaGetSymbolAddress, with that context current, and keeps it under the
+// context's unique id.  A __device__ array has its own address in every
+// context that loads the module, so a caller that makes its own contexts with
+// the driver API, or that resets the device (a new primary context), gets a
+// fresh look-up there.  Make that first call before any stream capture.
+// Calls share the array and it keeps the last call's contents, so every call
+// re-initialises what must start at zero; calls that overlap on the GPU
+// (different streams, or different host threads on the same device) race on
+// it.
 #include "gfm_internal.cuh"
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cstdio>
 #include <mutex>
 
@@ -30,8 +37,60 @@ constexpr size_t NOALLOC_HEADER = 512;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 static_assert(sizeof(DevTime) <= 256, "time record must fit its slot");
 
+// The array's address per CUDA context, keyed by the context's unique id
+// (cuCtxGetId: ids are never reused within a process, unlike context
+// handles).  Driver entry points come through the runtime, so the library
+// links no driver library.
 static std::mutex g_noalloc_mutex;
-static void* g_noalloc_ptr[128];
+struct NoallocSlot { unsigned long long ctx_id; void* ptr; };
+static NoallocSlot g_noalloc_slots[64];
+static int g_noalloc_nslots = 0;
+
+static bool current_context_id(unsigned long long* id) {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    looked_up = true;
+  }
+  if (!get_current || !get_id) return false;
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS;
+}
+
+// Device address of the scratch array in the current context; nullptr and
+// a message on failure.  Called with g_noalloc_mutex held.
+static void* scratch_address() {
+  unsigned long long id = 0;
+  if (current_context_id(&id))
+    for (int k = 0; k < g_noalloc_nslots; k++)
+      if (g_noalloc_slots[k].ctx_id == id) return g_noalloc_slots[k].ptr;
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    fprintf(stderr, "gfm_onefluid_step_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+    return nullptr;
+  }
+  // The look-up has made the runtime's context current if none was: its id
+  // is read now.  Kept when a slot is free; otherwise looked up again on the
+  // next call (the look-up allocates nothing).
+  if (current_context_id(&id) && g_noalloc_nslots < 64) g_noalloc_slots[g_noalloc_nslots++] = NoallocSlot{id, p};
+  return p;
+}
+
+static bool valid_bc_kind(int b) {
+  return b == GFM_BC_TRANSMISSIVE || b == GFM_BC_REFLECTIVE || b == GFM_BC_PERIODIC;
+}
 
 __global__ void k_noalloc_init(DevTime* D, unsigned int* counters, double t, int numsteps, GridP P) {
   D->t = t;
@@ -59,7 +118,11 @@ extern "C" gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* d, const 
                                                   int nsteps, double* t, int* numsteps, uint32_t* status,
                                                   void* stream) {
   if (!d || !m || !U || !t || !numsteps || nsteps < 0) return GFM_ERR_ARG;
-  if (d->Nx < d->numGC || d->Ny < d->numGC || d->numGC < 2 || !(d->dx > 0.0) || !(d->dy > 0.0)) return GFM_ERR_ARG;
+  // the grid checks of gfm_ctx_create
+  if (d->Nx < 1 || d->Ny < 1 || d->numGC < 2 || d->numGC > 64) return GFM_ERR_ARG;
+  if (d->Nx < d->numGC || d->Ny < d->numGC || !(d->dx > 0.0) || !(d->dy > 0.0)) return GFM_ERR_ARG;
+  if (!valid_bc_kind(d->BC_L) || !valid_bc_kind(d->BC_R) || !valid_bc_kind(d->BC_B) || !valid_bc_kind(d->BC_T))
+    return GFM_ERR_ARG;
   if (m->fs != GFM_FS_GODUNOV && m->fs != GFM_FS_MUSCL) return GFM_ERR_ARG;
   if (!(m->CFL > 0.0) || !(d->gamma1 > 1.0)) return GFM_ERR_ARG;
   bool per = d->BC_L == GFM_BC_PERIODIC || d->BC_R == GFM_BC_PERIODIC || d->BC_B == GFM_BC_PERIODIC ||
@@ -76,22 +139,16 @@ extern "C" gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* d, const 
             (long long)cells, (int)GFM_NOALLOC_MAX_CELLS);
     return GFM_ERR_ARG;
   }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return GFM_ERR_CUDA;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GFM_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    return GFM_ERR_CUDA;
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        fprintf(stderr, "gfm_onefluid_step_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
-        return GFM_ERR_CUDA;
-      }
-      g_noalloc_ptr[dev] = p;
-    }
-    base = g_noalloc_ptr[dev];
+    base = scratch_address();
   }
+  if (!base) return GFM_ERR_CUDA;
   // a context on the host stack pointing at the caller's grid and the scratch
   gfm_ctx ctx;
   memset(&ctx, 0, sizeof(ctx));
@@ -108,6 +165,7 @@ extern "C" gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* d, const 
   P.gas2 = P.gas1;
   P.periodic = allper;
   ctx.two_fluid = 0;
+  ctx.num_sms = sms;   // grid sizes of the grid-stride kernels, as in gfm_ctx_create
   ctx.stream = static_cast<cudaStream_t>(stream);
   ctx.U[0] = U;
   unsigned char* b = static_cast<unsigned char*>(base);

@@ -697,8 +697,10 @@ __global__ void k_band_lists(GridP P, int* cls, uint8_t* near_cell, int* band_li
 //
 // Cells are claimed in list (row-major) order through a ticket counter, so
 // every predecessor was claimed before its dependant by a running thread: the
-// lowest unfinished cell can always proceed.  Waits are bounded; a wait that
-// runs out sets ST_SCHEDULE_LIMIT and the thread abandons its cell.
+// lowest unfinished cell can always proceed.  Waits are bounded (IfcArgs::
+// spin_limit polls, IFC_SPIN_LIMIT by default: about a second); a wait that
+// runs out sets ST_SCHEDULE_LIMIT and the thread abandons its cell, which its
+// own dependants see at once.
 // ---------------------------------------------------------------------------
 enum { IFC_RIEMANN = 0, IFC_REAL = 1, IFC_MODIFIED = 2 };
 constexpr long long IFC_SPIN_LIMIT = 1ll << 24;
@@ -722,6 +724,8 @@ struct IfcArgs {
   // per list entry and side, the bilinear cell (i0, j0) and the 4 weights
   const int* probe_ij;
   const double* probe_w;
+  long long spin_limit;   // polls of a completion flag before a wait gives up
+  int withhold;           // test hook: this list entry is never solved or published (-1: none)
 };
 
 // Completion flags of the interface loop: the writer publishes a cell's
@@ -741,7 +745,7 @@ __device__ __forceinline__ bool ifc_wait(const IfcArgs& a, int p) {
   long long spins = 0;
   int v;
   while ((v = ld_acquire(a.done + p)) == 0) {
-    if (++spins > IFC_SPIN_LIMIT) return false;
+    if (++spins > a.spin_limit) return false;
     if (spins > 512) __nanosleep(64);
   }
   return v == 1;
@@ -812,7 +816,7 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
     if (lane == 0) k = (int)atomicAdd(a.ticket, 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
     if (k >= n) break;
-    if (lane != 0) continue;
+    if (lane != 0 || k == a.withhold) continue;
     int64_t lin = a.list[k];
     int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
     int64_t c = cidx(P, i, j);
@@ -1057,13 +1061,13 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
     dp = p - pold;
     pold = p;
     if (conv) break;
-    if (it >= GFM_RS_MAXIT) { *status |= ST_NEWTON_NO_CONVERGE; break; }
+    if (it >= kL.maxit) { *status |= ST_NEWTON_NO_CONVERGE; break; }
   }
   r.p = p;
   r.u = 0.5 * (uL + uR + (fR + fRd * dp) - (fL + fLd * dp));
   r.rho_own = rs_rho_star(S, k, p);
   *iters += it;
-  if (gated && a.cap_X && (threadIdx.x & 31) == 0 && it < GFM_RS_MAXIT && !c_le(G4cL + G4cR, udiff)) {
+  if (gated && a.cap_X && (threadIdx.x & 31) == 0 && it < kL.maxit && !c_le(G4cL + G4cR, udiff)) {
     const double y = gfm_log((p + pinf_min) / (pts + pinf_min));
     if (fabs(y) < 30.0) {
       const int slot = atomicAdd(a.cap_count, 1);
@@ -1263,6 +1267,7 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
     if (lane == 0) t = (int)atomicAdd(a.ticket, 1u);
     t = __shfl_sync(FULL_MASK, t, 0);
     if (t >= n) break;
+    if (t == a.withhold) continue;
     IfcCell cell;
     if (!ifc_front<MODE>(a, t, k, st, cell)) {
       st |= ST_SCHEDULE_LIMIT;
@@ -1517,6 +1522,7 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
     if (lane == 0) t = (int)atomicAdd(a.ticket, 1u);
     t = __shfl_sync(FULL_MASK, t, 0);
     if (t >= n) break;
+    if (t == a.withhold) continue;
     const int64_t lin = a.list[t];
     const int i = (int)(lin / P.nc), j = (int)(lin % P.nc);
     const int64_t c = cidx(P, i, j);
@@ -2192,6 +2198,8 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.done = ctx->ifc_done; ia.out = ctx->ifc_out;
   ia.ticket = (unsigned int*)(ctx->ifc_opp);
   ia.D = ctx->dtime;
+  ia.spin_limit = ctx->ifc_spin_limit > 0 ? ctx->ifc_spin_limit : IFC_SPIN_LIMIT;
+  ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia);
   ia.probe_ij = nullptr; ia.probe_w = nullptr;
@@ -2414,6 +2422,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.done = ctx->ifc_done; ia.out = ctx->ifc_out;
   ia.ticket = (unsigned int*)(ctx->ifc_opp);
   ia.D = ctx->dtime;
+  ia.spin_limit = ctx->ifc_spin_limit > 0 ? ctx->ifc_spin_limit : IFC_SPIN_LIMIT;
+  ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia);
   ia.probe_ij = nullptr; ia.probe_w = nullptr;
@@ -2603,6 +2613,8 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.done = ctx->ifc_done; ia.out = ctx->ifc_out;
   ia.ticket = (unsigned int*)(ctx->ifc_opp);
   ia.D = ctx->dtime;
+  ia.spin_limit = ctx->ifc_spin_limit > 0 ? ctx->ifc_spin_limit : IFC_SPIN_LIMIT;
+  ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
   ia.mlp = nullptr; ia.cap_X = nullptr; ia.cap_Y = nullptr; ia.cap_count = nullptr; ia.cap = 0;
   ia.probe_ij = nullptr; ia.probe_w = nullptr;

@@ -95,6 +95,8 @@ def lib():
         "gfm_step": [P, ctypes.POINTER(MethodDesc), I],
         "gfm_step_timed": [P, ctypes.POINTER(MethodDesc), I, pd],
         "gfm_set_overlap": [P, I],
+        "gfm_set_newton_limit": [P, I],
+        "gfm_set_interface_wait": [P, ctypes.c_int64, I],
         "gfm_fp64_peak": [pd, V],
         "gfm_batch_create": [ctypes.POINTER(GridDesc), I, I, ctypes.POINTER(P)],
         "gfm_batch_destroy": [P], "gfm_batch_instance": [P, I, ctypes.POINTER(P)],
@@ -333,6 +335,17 @@ class Context:
             return False
         _check(rc, "gfm_set_overlap")
         return True
+
+    def set_newton_limit(self, max_iterations):
+        """Newton iteration limit of the exact Riemann solves (default 60);
+        a solve that reaches it sets GFM_ST_NEWTON_NO_CONVERGE."""
+        _check(lib().gfm_set_newton_limit(self._p, int(max_iterations)), "gfm_set_newton_limit")
+
+    def set_interface_wait(self, spin_limit=0, withheld_entry=-1):
+        """Polls before an interface-loop wait gives up (0: default), and the
+        failure-detection test hook: an interface-list entry left unsolved."""
+        _check(lib().gfm_set_interface_wait(self._p, int(spin_limit), int(withheld_entry)),
+               "gfm_set_interface_wait")
 
     def step_timed(self, m, nsteps=1):
         """gfm_step with per-phase device times; returns GFM_NPHASES (9)
