@@ -126,6 +126,12 @@ gfm_status_t gfm_download_mask(gfm_ctx* ctx, uint8_t* mask);
 /* time state kept on the device: t, step count, last dt */
 gfm_status_t gfm_set_time(gfm_ctx* ctx, double t, int numsteps);
 gfm_status_t gfm_get_time(gfm_ctx* ctx, double* t, int* numsteps, double* dt);
+/* realcells1 and realcells2 of the last step (BBrange imin, imax, jmin,
+ * jmax each; sourcecode/sim_twofluid.cpp:43-44): the cells each flux update
+ * covers.  OGFM and OGFM_VOF shrink them to the real cells of their fluid
+ * plus a margin (sourcecode/GFM_original.cpp:47-128); the other methods keep
+ * the whole grid. */
+gfm_status_t gfm_get_realcells(gfm_ctx* ctx, int* boxes);
 
 /* One sub-step each, stream-ordered, dt kept on the device. */
 gfm_status_t gfm_compute_dt(gfm_ctx* ctx, double CFL, double T);

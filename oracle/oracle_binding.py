@@ -113,6 +113,13 @@ def interfacial_mask(desc, phi):
     return mask
 
 
+def last_realcells():
+    """realcells1 and realcells2 of the last two-fluid step, each (imin, imax, jmin, jmax)."""
+    rc = (ctypes.c_int * 8)()
+    lib().oracle_last_realcells(rc)
+    return tuple(rc[:4]), tuple(rc[4:])
+
+
 def status():
     return lib().oracle_status()
 

@@ -156,6 +156,7 @@ inline double isentropic_extrapolation(double gamma, double pinf, double rho1, d
 // the root.  Initial guess: PVRS (Toro eq. 4.47); the mixed (two-material)
 // solve refines it by the two-shock approximation (TSRS, Toro eq. 9.42) with
 // the shock constants taken at max(PVRS, floor).
+namespace omath {
 class exact_rs_stiffenedgas {
  public:
   struct Gas {
@@ -319,3 +320,4 @@ class exact_rs_stiffenedgas {
     out[2] = SR.pb * omath::pow(cr, KR.G3) - KR.pinf;
   }
 };
+}  // namespace omath

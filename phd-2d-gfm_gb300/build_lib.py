@@ -2,6 +2,9 @@
 
     libgfm_gb300.so   CUDA kernels + C ABI + host test-case set-up, sm_103a only
     liboracle.so      the CPU oracle (test infrastructure), built beside it
+    oracle/_ref/gfm_ref  the reference checker (test infrastructure): the
+                      reference's own sources compiled by oracle/build_ref.py,
+                      only where those sources are present
 
 Translation units compile in parallel.  The FP64 arithmetic of kernels and
 oracle must agree bit for bit, so every compile disables contraction of
@@ -85,16 +88,26 @@ def build_oracle(verbose=False):
     os.makedirs(ORACLE_LIBDIR, exist_ok=True)
     out = os.path.join(ORACLE_LIBDIR, "liboracle.so")
     srcs = [os.path.join(ORACLE, "gfm_oracle.cpp")]
-    deps = srcs + [os.path.join(ORACLE, "oracle_math.hpp"), os.path.join(CSRC, "gfm_tables.h"),
+    deps = srcs + [os.path.join(ORACLE, "oracle_math.hpp"), os.path.join(ORACLE, "oracle_itm.hpp"),
+                   os.path.join(CSRC, "gfm_tables.h"),
                    os.path.join(ROOT, "include", "gfm_gb300.h")]
     if _newer(out, deps):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"] + srcs + ["-o", out])
     return out
 
 
+def build_reference_checker(verbose=False):
+    """oracle/_ref/gfm_ref when the reference's sources are present, else None."""
+    if ORACLE not in sys.path:
+        sys.path.insert(0, ORACLE)
+    import build_ref
+    return build_ref.build(verbose)
+
+
 def build_all(verbose=False):
     lib = build_library(verbose)
     orc = build_oracle(verbose)
+    build_reference_checker(verbose)
     return lib, orc
 
 

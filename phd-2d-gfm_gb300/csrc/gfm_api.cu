@@ -494,6 +494,14 @@ gfm_status_t gfm_set_time(gfm_ctx* ctx, double t, int numsteps) {
   return GFM_OK;
 }
 
+gfm_status_t gfm_get_realcells(gfm_ctx* ctx, int* boxes) {
+  if (!ctx || !boxes) return GFM_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int q = 0; q < 8; q++) boxes[q] = ctx->h_dtime->rc[q];
+  return GFM_OK;
+}
+
 gfm_status_t gfm_get_time(gfm_ctx* ctx, double* t, int* numsteps, double* dt) {
   if (!ctx) return GFM_ERR_ARG;
   CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));

@@ -87,6 +87,7 @@ def lib():
         "gfm_set_time": [P, D, I],
         "gfm_download_mask": [P, ctypes.POINTER(ctypes.c_uint8)],
         "gfm_get_time": [P, pd, ctypes.POINTER(I), pd],
+        "gfm_get_realcells": [P, ctypes.POINTER(I)],
         "gfm_compute_dt": [P, D, D],
         "gfm_set_ghost_states": [P, ctypes.POINTER(MethodDesc)],
         "gfm_fs_update": [P, I, I],
@@ -285,6 +286,12 @@ class Context:
         dt = ctypes.c_double()
         _check(lib().gfm_get_time(self._p, ctypes.byref(t), ctypes.byref(n), ctypes.byref(dt)), "gfm_get_time")
         return t.value, n.value, dt.value
+
+    def realcells(self):
+        """(realcells1, realcells2) of the last step, each (imin, imax, jmin, jmax)."""
+        rc = (ctypes.c_int * 8)()
+        _check(lib().gfm_get_realcells(self._p, rc), "gfm_get_realcells")
+        return tuple(rc[:4]), tuple(rc[4:])
 
     def status(self):
         s = ctypes.c_uint32()
