@@ -396,18 +396,35 @@ def cpu_baseline(W, desc, m, start, seconds):
                       % (done, W["workload"], n, el)}
 
 
+def setup_oracle(W):
+    """The workload's initial state from the oracle's own restatement of its
+    initial conditions: the reference arm loads nothing of the library."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_binding as orc
+    import gfm_gb300 as g   # the C-ABI struct layouts and method table only: no library is loaded
+    desc, T, U1, U2, phi = orc.case_setup(W["sim"], W["test_case"], W["Nx"], W["Ny"])
+    if W["sim"] == "twofluid":
+        m = g.method(fs=W["FS"], gfm=W["GFM"], itm=W["ITM"], CFL=W["CFL"], T=T, reinit_every=W["reinit_every"])
+    else:
+        m = g.method(fs=W["FS"], CFL=W["CFL"], T=T)
+    return desc, T, U1, U2, phi, m
+
+
 def run_reference(args):
-    """--impl reference: the CPU oracle (the reference itself cannot be built
-    here) on this host's cores: one independent run per core, aggregate."""
+    """--impl reference: the CPU oracle on this host's cores, one independent
+    run per core, aggregate.  The oracle is pinned bit for bit to the
+    reference's own code (tests/test_oracle_vs_reference.py), which cannot be
+    built on this host (its external libraries are absent; the checker that
+    compiles its sources against the oracle's stand-ins is x86 test
+    infrastructure).  Nothing of the GPU library is loaded here."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     import multiprocessing as mp
-    import gfm_gb300 as g
     if args.workload == "batch64":
         return run_reference_batch(args)
     W = WORKLOADS[args.workload]
-    desc, T, U1, U2, phi, m = setup(W)
+    desc, T, U1, U2, phi, m = setup_oracle(W)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_binding as orc
     if W["sim"] == "twofluid":
@@ -441,9 +458,12 @@ def run_reference(args):
 
 
 def _oracle_member(spec, nsteps, seconds):
-    """One oracle process on one batch member from its initial state."""
-    import gfm_gb300 as g
-    d, T, U1, U2, phi = g.shock_bubble_case(*spec)
+    """One oracle process on one batch member from its initial state (the
+    oracle's own initial conditions; nothing of the GPU library)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_binding as orc
+    import gfm_gb300 as g   # struct layouts and method table only: no library is loaded
+    d, T, U1, U2, phi = orc.bubble_setup(*spec)
     m = g.method(gfm="riemannGFM", CFL=0.6, T=1.0)
     done, el = _oracle_steps(_fields(d), _fields(m), U1, U2, phi, nsteps, 0.0, 0, seconds)
     return d.Nx * d.Ny * done, el

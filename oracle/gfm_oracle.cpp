@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../include/gfm_gb300.h"
@@ -1109,6 +1110,63 @@ void phi_to(const sim_info& p, const griddoubletype& g, double* f) {
 // ============================================================================
 // C ABI of the oracle (loaded with ctypes by the tests)
 // ============================================================================
+// ----------------------------------------------------------------------------
+// Initial conditions of the timed workloads, restated here so that the CPU
+// baseline needs nothing of the library: the one-fluid circular explosion
+// (sourcecode/sim_onefluid.cpp:359-415: primitives blended by the 10x10
+// sub-sampled area fraction of the circle) and the two-fluid shock-bubble and
+// underwater explosion, built as the reference's set_sim_ICs builds its
+// bubble cases (sourcecode/sim_twofluid.cpp:774-859): every padded cell from
+// its centre, fluid 1 uniform, fluid 2 with a planar shock, phi = distance
+// to the centre - radius; then apply_BCs_euler on the grids.
+// ----------------------------------------------------------------------------
+// Rankine-Hugoniot state behind a shock of Mach M running into (rho1, p1) at
+// rest towards -x
+void post_shock_state(double g, double M, double rho1, double p1, double& rho2, double& u2, double& p2) {
+  const double M2 = M * M;
+  p2 = p1 * (1.0 + 2.0 * g / (g + 1.0) * (M2 - 1.0));
+  rho2 = rho1 * ((g + 1.0) * M2 / ((g - 1.0) * M2 + 2.0));
+  const double W = M * std::sqrt(g * p1 / rho1);
+  u2 = -W * (1.0 - rho1 / rho2);
+}
+
+struct BubbleIC {
+  vec4type s1, s2_left, s2_right;   // conserved states; fluid 2 splits at x = xsplit
+  double xsplit, cx, cy, r;
+};
+
+void fill_bubble(const gfm_grid_desc* d, const BubbleIC& b, double* U1, double* U2, double* phi) {
+  sim_info params = make_params(d);
+  const int nr = params.Ny + 2 * params.numGC, nc = params.Nx + 2 * params.numGC;
+  grideuler2type g1(nr, std::vector<vec4type>(nc)), g2 = g1;
+  griddoubletype ls(nr, std::vector<double>(nc));
+  for (int i = 0; i < nr; i++)
+    for (int j = 0; j < nc; j++) {
+      const vec2 cc = params.cellcentre_coord(i, j);
+      g1[i][j] = b.s1;
+      g2[i][j] = (cc[0] < b.xsplit) ? b.s2_left : b.s2_right;
+      ls[i][j] = std::sqrt((cc[0] - b.cx) * (cc[0] - b.cx) + (cc[1] - b.cy) * (cc[1] - b.cy)) - b.r;
+    }
+  apply_BCs_euler(params, g1);
+  apply_BCs_euler(params, g2);
+  to_soa(params, g1, U1);
+  to_soa(params, g2, U2);
+  phi_to(params, ls, phi);
+}
+
+void base_grid(gfm_grid_desc* d, int Nx, int Ny, int g) {
+  std::memset(d, 0, sizeof(*d));
+  d->Nx = Nx; d->Ny = Ny; d->numGC = g;
+  d->x0 = 0.0; d->y0 = 0.0;
+  d->dx = 1.0 / Nx; d->dy = 1.0 / Ny;
+  d->BC_L = d->BC_R = d->BC_B = d->BC_T = GFM_BC_TRANSMISSIVE;
+  d->gamma1 = 1.4; d->gamma2 = 1.4; d->pinf1 = 0.0; d->pinf2 = 0.0;
+}
+
+vec4type p2c(double g, double pinf, double rho, double u, double v, double p) {
+  return misc::primitives_to_conserved(g, pinf, vec4type{rho, u, v, p});
+}
+
 extern "C" {
 
 uint32_t oracle_status(void) { return g_status; }
@@ -1297,6 +1355,118 @@ double oracle_fluid_mass(const gfm_grid_desc* d, double interiorsign, const doub
       if (interiorsign * lsval > 0.0) total += U[static_cast<size_t>(i) * nc + j] * params.dx * params.dy;
     }
   return total;
+}
+
+// Grid description and end time of a timed workload (onefluid
+// circularexplosion; twofluid shock_bubble, underwater_explosion_sg);
+// -1 for any other name.
+int oracle_case_params(const char* sim_type, const char* test_case, int Nx, int Ny, gfm_grid_desc* d, double* T) {
+  const std::string st(sim_type), tc(test_case);
+  if (st == "onefluid" && tc == "circularexplosion") {
+    base_grid(d, Nx, Ny, 2);   // sourcecode/sim_onefluid.cpp:96-146
+    d->gamma2 = 0.0;
+    d->dx = 2.0 / Nx; d->dy = 2.0 / Ny;
+    *T = 0.25;
+    return 0;
+  }
+  if (st != "twofluid") return -1;
+  base_grid(d, Nx, Ny, 8);     // sourcecode/sim_twofluid.cpp:336-360
+  if (tc == "shock_bubble") {
+    // 0.25 x 0.089, light-gas bubble (gamma 1.648) in air, walls top and bottom
+    d->gamma1 = 1.648; d->dx = 0.25 / Nx; d->dy = 0.089 / Ny;
+    d->BC_T = d->BC_B = GFM_BC_REFLECTIVE;
+    *T = 1.0;
+    return 0;
+  }
+  if (tc == "underwater_explosion_sg") {
+    // [-1,1]^2, air bubble in stiffened-gas water (gamma 4.4, pinf 6e8)
+    d->gamma2 = 4.4; d->pinf2 = 6e8;
+    d->x0 = -1.0; d->y0 = -1.0; d->dx = 2.0 / Nx; d->dy = 2.0 / Ny;
+    *T = 1.0;
+    return 0;
+  }
+  return -1;
+}
+
+// Initial state of a timed workload into SoA planes (U2, phi unused for one fluid).
+int oracle_case_init(const char* sim_type, const char* test_case, const gfm_grid_desc* d, double* U1, double* U2,
+                     double* phi) {
+  const std::string st(sim_type), tc(test_case);
+  if (st == "onefluid" && tc == "circularexplosion") {
+    sim_info params = make_params(d);
+    const int nr = params.Ny + 2 * params.numGC, nc = params.Nx + 2 * params.numGC;
+    grideuler2type grid(nr, std::vector<vec4type>(nc));
+    const vec4type L = {1.0, 0.0, 0.0, 1.0}, R = {0.125, 0.0, 0.0, 0.1};
+    const double cx = 1.0, cy = 1.0, rad = 0.4;
+    const int N = 10;
+    for (int i = 0; i < nr; i++)
+      for (int j = 0; j < nc; j++) {
+        const vec2 cc = params.cellcentre_coord(i, j);
+        const double delx = params.dx / N, dely = params.dy / N;
+        const double blx = cc[0] - 0.5 * params.dx, bly = cc[1] - 0.5 * params.dy;
+        int inside = 0;
+        for (int a = 0; a < N; a++)
+          for (int b = 0; b < N; b++) {
+            const double sx = blx + (a + 0.5) * delx - cx, sy = bly + (b + 0.5) * dely - cy;
+            if (std::sqrt(sx * sx + sy * sy) <= rad) inside++;
+          }
+        const double frac = double(inside) / (N * N);
+        vec4type W;
+        for (int k = 0; k < 4; k++) W[k] = frac * L[k] + (1.0 - frac) * R[k];
+        grid[i][j] = misc::primitives_to_conserved(d->gamma1, d->pinf1, W);
+      }
+    apply_BCs_euler(params, grid);
+    to_soa(params, grid, U1);
+    return 0;
+  }
+  if (st != "twofluid") return -1;
+  BubbleIC b;
+  if (tc == "shock_bubble") {
+    double rho2, u2, p2;
+    post_shock_state(d->gamma2, 1.22, 1.0, 1e5, rho2, u2, p2);
+    b.s1 = p2c(d->gamma1, d->pinf1, 0.182, 0, 0, 1e5);
+    b.s2_left = p2c(d->gamma2, d->pinf2, 1.0, 0, 0, 1e5);
+    b.s2_right = p2c(d->gamma2, d->pinf2, rho2, u2, 0, p2);
+    b.xsplit = 0.225; b.cx = 0.175; b.cy = 0.0445; b.r = 0.025;
+  } else if (tc == "underwater_explosion_sg") {
+    b.s1 = p2c(d->gamma1, d->pinf1, 1270.0, 0, 0, 8.29e8);
+    b.s2_left = b.s2_right = p2c(d->gamma2, d->pinf2, 1000.0, 0, 0, 1e5);
+    b.xsplit = INFINITY; b.cx = 0.0; b.cy = 0.0; b.r = 0.2;
+  } else {
+    return -1;
+  }
+  fill_bubble(d, b, U1, U2, phi);
+  return 0;
+}
+
+// The batched workload's shock-bubble family: the 1000 x 400 geometry on any
+// grid (width 0.25, square cells, walls top and bottom), bubble of fluid 1
+// (gamma_bubble, rho = rho_ratio, p 1e5) of radius radius_frac x height at
+// (0.7 width, height / 2), shock of Mach `mach` in air from x = 0.9 width.
+int oracle_bubble_case(double mach, double gamma_bubble, double rho_ratio, double radius_frac, int Nx, int Ny,
+                       gfm_grid_desc* d, double* T) {
+  base_grid(d, Nx, Ny, 8);
+  d->dx = 0.25 / Nx; d->dy = d->dx;
+  d->BC_B = d->BC_T = GFM_BC_REFLECTIVE;
+  d->gamma1 = gamma_bubble;
+  *T = 1.0;
+  (void)mach; (void)rho_ratio; (void)radius_frac;
+  return 0;
+}
+
+int oracle_bubble_init(double mach, double gamma_bubble, double rho_ratio, double radius_frac, const gfm_grid_desc* d,
+                       double* U1, double* U2, double* phi) {
+  (void)gamma_bubble;
+  const double W = d->dx * d->Nx, H = d->dy * d->Ny;
+  double rho2, u2, p2;
+  post_shock_state(d->gamma2, mach, 1.0, 1e5, rho2, u2, p2);
+  BubbleIC b;
+  b.s1 = p2c(d->gamma1, d->pinf1, rho_ratio, 0, 0, 1e5);
+  b.s2_left = p2c(d->gamma2, d->pinf2, 1.0, 0, 0, 1e5);
+  b.s2_right = p2c(d->gamma2, d->pinf2, rho2, u2, 0, p2);
+  b.xsplit = 0.9 * W; b.cx = 0.7 * W; b.cy = 0.5 * H; b.r = radius_frac * H;
+  fill_bubble(d, b, U1, U2, phi);
+  return 0;
 }
 
 }  // extern "C"

@@ -52,6 +52,10 @@ def lib():
     L.oracle_interfacial_mask.argtypes = [ctypes.POINTER(GridDesc), pd, ctypes.POINTER(ctypes.c_uint8)]
     L.oracle_fluid_mass.argtypes = [ctypes.POINTER(GridDesc), D, pd, pd]
     L.oracle_fluid_mass.restype = D
+    L.oracle_case_params.argtypes = [ctypes.c_char_p, ctypes.c_char_p, I, I, ctypes.POINTER(GridDesc), pd]
+    L.oracle_case_init.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(GridDesc), pd, pd, pd]
+    L.oracle_bubble_case.argtypes = [D, D, D, D, I, I, ctypes.POINTER(GridDesc), pd]
+    L.oracle_bubble_init.argtypes = [D, D, D, D, ctypes.POINTER(GridDesc), pd, pd, pd]
     _lib = L
     return L
 
@@ -97,6 +101,35 @@ def twofluid_run(desc, m, U1, U2, phi, nsteps, t=0.0, numsteps=0):
                                       ctypes.byref(tt), ctypes.byref(ns), _p(vel), ctypes.byref(nifc))
     return {"U1": U1, "U2": U2, "phi": phi, "vel": vel, "t": tt.value, "numsteps": ns.value, "taken": taken,
             "n_interfacial": nifc.value}
+
+
+def case_setup(sim_type, test_case, Nx, Ny):
+    """(desc, T, U1, U2, phi) of a timed workload from the oracle's own
+    restatement of its initial conditions (U2, phi None for one fluid)."""
+    desc = GridDesc()
+    T = ctypes.c_double()
+    if lib().oracle_case_params(sim_type.encode(), test_case.encode(), Nx, Ny, ctypes.byref(desc), ctypes.byref(T)):
+        raise ValueError("no oracle initial condition for %s %s" % (sim_type, test_case))
+    nr, nc = desc.Ny + 2 * desc.numGC, desc.Nx + 2 * desc.numGC
+    U1 = np.zeros((4, nr, nc))
+    if sim_type == "onefluid":
+        lib().oracle_case_init(sim_type.encode(), test_case.encode(), ctypes.byref(desc), _p(U1), None, None)
+        return desc, T.value, U1, None, None
+    U2 = np.zeros((4, nr, nc))
+    phi = np.zeros((nr, nc))
+    lib().oracle_case_init(sim_type.encode(), test_case.encode(), ctypes.byref(desc), _p(U1), _p(U2), _p(phi))
+    return desc, T.value, U1, U2, phi
+
+
+def bubble_setup(Nx, Ny, mach, gamma_bubble, rho_ratio, radius_frac):
+    """(desc, T, U1, U2, phi) of a member of the batched shock-bubble family."""
+    desc = GridDesc()
+    T = ctypes.c_double()
+    lib().oracle_bubble_case(mach, gamma_bubble, rho_ratio, radius_frac, Nx, Ny, ctypes.byref(desc), ctypes.byref(T))
+    nr, nc = desc.Ny + 2 * desc.numGC, desc.Nx + 2 * desc.numGC
+    U1, U2, phi = np.zeros((4, nr, nc)), np.zeros((4, nr, nc)), np.zeros((nr, nc))
+    lib().oracle_bubble_init(mach, gamma_bubble, rho_ratio, radius_frac, ctypes.byref(desc), _p(U1), _p(U2), _p(phi))
+    return desc, T.value, U1, U2, phi
 
 
 def fluid_mass(desc, interiorsign, U, phi):

@@ -92,7 +92,7 @@ def build_oracle(verbose=False):
                    os.path.join(CSRC, "gfm_tables.h"),
                    os.path.join(ROOT, "include", "gfm_gb300.h")]
     if _newer(out, deps):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"] + srcs + ["-o", out])
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"] + srcs + ["-o", out])
     return out
 
 
