@@ -133,12 +133,31 @@ gfm_status_t gfm_get_time(gfm_ctx* ctx, double* t, int* numsteps, double* dt);
  * the whole grid. */
 gfm_status_t gfm_get_realcells(gfm_ctx* ctx, int* boxes);
 
-/* One sub-step each, stream-ordered, dt kept on the device. */
+/* One sub-step each, stream-ordered, dt kept on the device.
+ *   gfm_compute_dt       the CFL step (with the ramp min(CFL, 0.2) while the
+ *                        step count is below 5, sourcecode/sim_twofluid.cpp:66)
+ *   gfm_set_ghost_states the ghost fill of the method (mask, interface solves,
+ *                        extrapolation, velocity field; OGFM's realcells)
+ *   gfm_fs_update        one fluid's flux update over its realcells box, no BCs
+ *   gfm_ls_update        the interface tracker's update_interface_coupled: level
+ *                        set advection, then the reinitialisation on the steps
+ *                        that take one ((step count + 1) % reinit_every == 0,
+ *                        the step count of gfm_set_time); VOF advection
+ *   gfm_apply_bcs        apply_BCs_euler on one fluid
+ *   gfm_set_step         dt (>= 0) and, if realcells is not NULL, the realcells
+ *                        boxes (8 ints: realcells1 then realcells2, each imin,
+ *                        imax, jmin, jmax; within the grid less a 2-cell rim) of
+ *                        the sub-steps that follow, as the reference passes them
+ *                        to pure_fluid_update (headers/FS_base.hpp:23-32)
+ *   gfm_upload_velocity  the velocity field the tracker advects with (2 planes
+ *                        u, v in the layout of phi), GFM_base::vfield */
 gfm_status_t gfm_compute_dt(gfm_ctx* ctx, double CFL, double T);
 gfm_status_t gfm_set_ghost_states(gfm_ctx* ctx, const gfm_method_desc* m);
 gfm_status_t gfm_fs_update(gfm_ctx* ctx, int fs, int fluid);
 gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m);
 gfm_status_t gfm_apply_bcs(gfm_ctx* ctx, int fluid);
+gfm_status_t gfm_set_step(gfm_ctx* ctx, double dt, const int* realcells);
+gfm_status_t gfm_upload_velocity(gfm_ctx* ctx, const double* vel);
 /* The interface field's kind for gfm_compute_dt before any call that takes a
  * method (gfm_set_ghost_states, gfm_ls_update and gfm_step record it): with
  * GFM_ITM_VOF, phi holds z and fluid 1 is where 0.5 - z < 0. */

@@ -28,7 +28,7 @@ ORACLE_LIBDIR = os.path.join(ORACLE, "lib", MACHINE)
 
 CU_SOURCES = ["gfm_flux.cu", "gfm_step.cu", "gfm_api.cu", "gfm_noalloc.cu", "gfm_batch.cu", "gfm_mlp.cu",
               "gfm_output.cu", "gfm_cases_dev.cu"]
-CPP_SOURCES = ["gfm_cases.cpp"]
+CPP_SOURCES = ["gfm_cases.cpp", "gfm_classes.cpp"]
 HEADERS = ["gfm_math.cuh", "gfm_internal.cuh", "gfm_tables.h", "gfm_mlp.cuh", "gfm_cases.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -61,8 +61,10 @@ def build_library(verbose=False):
     """Compile libgfm_gb300.so; returns its path."""
     os.makedirs(os.path.join(LIBDIR, "obj"), exist_ok=True)
     out = os.path.join(LIBDIR, "libgfm_gb300.so")
-    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "gfm_gb300.h")]
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "gfm_gb300.h"),
+                                                       os.path.join(ROOT, "include", "gfm_gb300.hpp")]
     nvcc = _nvcc()
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
     jobs, objs = [], []
     for src in CU_SOURCES + CPP_SOURCES:
         s = os.path.join(CSRC, src)
@@ -73,7 +75,7 @@ def build_library(verbose=False):
         if src.endswith(".cu"):
             jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
         else:
-            jobs.append(["g++"] + CXX_FLAGS + ["-c", s, "-o", o])
+            jobs.append(["g++"] + CXX_FLAGS + ["-I", cuda_inc, "-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for log in ex.map(_run, jobs):
             if verbose and log:

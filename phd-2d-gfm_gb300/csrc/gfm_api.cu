@@ -148,6 +148,17 @@ gfm_status_t last_error() {
 
 }  // namespace
 
+// the empty realcells boxes (imin = g + Ny > imax = g, jmin = g + Nx > jmax = g)
+// that the original and OGFM_VOF ghost fills grow
+__global__ void k_rc_empty(GridP P, DevTime* D) {
+  for (int f = 0; f < 2; f++) {
+    D->rc[4 * f + 0] = P.g + P.Ny;
+    D->rc[4 * f + 1] = P.g;
+    D->rc[4 * f + 2] = P.g + P.Nx;
+    D->rc[4 * f + 3] = P.g;
+  }
+}
+
 gfm_status_t gfm::validate_method(gfm_ctx* ctx, const gfm_method_desc* m) { return check_method(ctx, m); }
 double* gfm::mass_scratch(gfm_ctx* ctx) { return extra(ctx).mass_part; }
 gfm_status_t gfm::launch_status() { return last_error(); }
@@ -469,6 +480,30 @@ gfm_status_t gfm_download_velocity(gfm_ctx* ctx, double* vel) {
   return copy_grid(ctx, ctx->vel, nullptr, vel, 2);
 }
 
+gfm_status_t gfm_upload_velocity(gfm_ctx* ctx, const double* vel) {
+  if (!ctx || !vel || !ctx->two_fluid) return GFM_ERR_ARG;
+  return copy_grid(ctx, ctx->vel, vel, nullptr, 2);
+}
+
+gfm_status_t gfm_set_step(gfm_ctx* ctx, double dt, const int* realcells) {
+  if (!ctx || !(dt >= 0.0)) return GFM_ERR_ARG;
+  const GridP& P = ctx->P;
+  if (realcells)
+    for (int f = 0; f < 2; f++) {
+      const int* r = realcells + 4 * f;
+      if (r[0] < 2 || r[1] > P.Ny + 2 * P.g - 2 || r[0] > r[1] || r[2] < 2 || r[3] > P.Nx + 2 * P.g - 2 || r[2] > r[3])
+        return GFM_ERR_ARG;
+    }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost));
+  ctx->h_dtime->dt = dt;
+  ctx->h_dtime->active = 1;
+  if (realcells)
+    for (int q = 0; q < 8; q++) ctx->h_dtime->rc[q] = realcells[q];
+  CK(cudaMemcpy(ctx->dtime, ctx->h_dtime, sizeof(DevTime), cudaMemcpyHostToDevice));
+  return GFM_OK;
+}
+
 gfm_status_t gfm_download_mask(gfm_ctx* ctx, uint8_t* mask) {
   if (!ctx || !mask || !ctx->two_fluid) return GFM_ERR_ARG;
   const GridP& P = ctx->P;
@@ -525,6 +560,13 @@ gfm_status_t gfm_set_ghost_states(gfm_ctx* ctx, const gfm_method_desc* m) {
   // the ticket of the interface solve
   ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
   ctx->itm = m->itm;
+  // GFM_original and OGFM_VOF start their realcells boxes empty and grow
+  // them over their fluid's cells (sourcecode/GFM_original.cpp:47-55; in a
+  // whole step the step's first kernel does this)
+  if (m->gfm == GFM_OGFM || m->gfm == GFM_OGFM_VOF) {
+    k_rc_empty<<<1, 1, 0, ctx->stream>>>(ctx->P, ctx->dtime);
+    counted();
+  }
   if (m->itm == GFM_ITM_VOF) launch_ghost_fill_vof(ctx, m);
   else launch_ghost_fill(ctx, m);
   return last_error();
@@ -551,7 +593,7 @@ gfm_status_t gfm_ls_update(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (r != GFM_OK) return r;
   ctx->itm = m->itm;
   if (m->itm == GFM_ITM_VOF) launch_vof_update(ctx, ctx->stream);
-  else launch_ls_update(ctx, m, ctx->stream);
+  else launch_level_set(ctx, m, ctx->stream, 3);   // advection, then the reinitialisation schedule
   return last_error();
 }
 

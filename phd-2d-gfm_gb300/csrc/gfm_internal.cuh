@@ -183,7 +183,6 @@ void launch_bcs(gfm_ctx* ctx, int fluid_mask);
 void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);
 void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
-void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s);
 // the step's level set: parts 1 the advection stages, 2 phi := the result
 // (or the reinitialisation from it), 3 both
 void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts);

@@ -2548,25 +2548,6 @@ void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, in
   }
 }
 
-// the advection alone (gfm_ls_update): stages, then phi := phi_a
-void launch_ls_update(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s) {
-  const GridP& P = ctx->P;
-  const int64_t n = padded_cells(P);
-  const int blocks = wave_blocks((const void*)k_ls_stage<5, 1>, 256, ctx->num_sms, n);
-  if (m->ls_order == 1) {
-    k_ls_stage<1, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
-    counted();
-  } else {
-    k_ls_stage<5, 1><<<blocks, 256, 0, s>>>(P, ctx->phi, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
-    k_ls_stage<5, 2><<<blocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->phi_b, ctx->vel, ctx->dtime, nullptr, 0);
-    k_ls_stage<5, 3><<<blocks, 256, 0, s>>>(P, ctx->phi_b, ctx->phi, ctx->phi_a, ctx->vel, ctx->dtime, nullptr, 0);
-    counted(3);
-  }
-  k_copy_plane<<<wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, n), 256, 0, s>>>(P, ctx->phi_a, ctx->phi,
-                                                                                           ctx->dtime, 0, 0);
-  counted();
-}
-
 // Occupancy queries of the grid-stride kernels, made once before any launch
 // (and so before any stream capture records one)
 void prepare_step_kernels() {
