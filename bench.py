@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--overlap", default="auto", choices=["auto", "on", "off"],
                     help="ghost-fill schedule (gfm_set_overlap); results are identical")
+    ap.add_argument("--no-batched-learned", dest="batched_learned", action="store_false",
+                    help="skip the batched / learned-proposal block of the default line")
     return ap.parse_args()
 
 
@@ -350,6 +352,8 @@ def run_gfm(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(W, desc, m, e2e_start, args.cpu_seconds)
     ctx.close()
+    if rank == 0 and world == 1 and args.batched_learned:
+        line["batched_learned"] = batched_learned_block(args)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -513,6 +517,94 @@ def batch_members(n=64, seed=BATCH_SEED):
         out.append((nx, ny, rng.uniform(1.1, 3.0), rng.uniform(1.09, 1.67), float(np.exp(rng.uniform(np.log(0.1),
                     np.log(10.0)))), rng.uniform(0.1, 0.3)))
     return out
+
+
+def batched_learned_block(args):
+    """The metric's second half on the batched workload: the 64 instances of
+    the seeded shock-bubble family stepped (1) one after another with the
+    plain guess, (2) together through the recorded step graph with the plain
+    guess, and (3) together with the learned star-pressure proposal (weights
+    from phd-2d-gfm_gb300/data/pstar_mlp.f32, trained by train_pstar.py),
+    each for the same steps from the same state after the warm-up; the
+    Newton iterations per interface solve of (2) and (3) and the largest
+    relative L1 difference of their end fields (real cells, per field)."""
+    import numpy as np
+    import torch
+    import gfm_gb300 as g
+    import train_pstar
+    K = max(1, min(args.steps, 20))
+    spec = batch_members()
+    cases = [g.shock_bubble_case(*p) for p in spec]
+    m = g.method(gfm="riemannGFM", CFL=0.6, T=1.0)
+    mlp = train_pstar.load()
+    weights = "phd-2d-gfm_gb300/data/pstar_mlp.f32 (train_pstar.py)"
+    if mlp is None:   # no saved weights: a short training run here
+        n = 1 << 20
+        X = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+        Y = torch.empty(n, dtype=torch.float32, device="cuda")
+        got = g.mlp_generate(21, n, X.data_ptr(), Y.data_ptr())
+        mlp = g.MLP(seed=5)
+        mlp.train(X.data_ptr(), Y.data_ptr(), got, epochs=10, batch=4096, lr=2e-3)
+        weights = "trained in this run (%d synthetic problems, 10 epochs)" % got
+    descs = [c[0] for c in cases]
+    bp = g.Batch(descs, two_fluid=True)
+    bl = g.Batch(descs, two_fluid=True)
+    for ctx in bl.instances:
+        ctx.set_mlp(mlp)
+    for ctx, (d, T, U1, U2, phi) in zip(bp.instances, cases):
+        ctx.upload(U1, U2, phi)
+    bp.step(m, args.warmup, graph=True)
+    bp.synchronize()
+    start = [ctx.download() + ctx.time()[:2] for ctx in bp.instances]
+    cells = sum(d.Nx * d.Ny for d in descs)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(b, graph):
+        for ctx, st in zip(b.instances, start):
+            ctx.upload(st[0], st[1], st[2], t=st[3], numsteps=st[4])
+        torch.cuda.synchronize()
+        flush.zero_()
+        stream = torch.cuda.current_stream()
+        import ctypes
+        g.lib().gfm_batch_set_stream(b._p, ctypes.c_void_p(stream.cuda_stream))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(m, K, graph=graph)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        tot = [ctx.interface_totals() for ctx in b.instances]
+        solves = sum(x["solves"] for x in tot)
+        iters = sum(x["newton_iters"] for x in tot)
+        return {"value": cells * K / (ms * 1e-3), "ms_per_step": ms / K, "interface_solves": solves,
+                "newton_per_interface_solve": iters / max(1, solves),
+                "from_proposal": sum(x["proposed"] for x in tot),
+                "device_status_nonzero": int(sum(1 for ctx in b.instances if ctx.status()))}
+
+    seq = timed(bp, False)
+    plain = timed(bp, True)
+    outp = [ctx.download() for ctx in bp.instances]
+    learned = timed(bl, True)
+    outl = [ctx.download() for ctx in bl.instances]
+    rel = 0.0
+    identical = True
+    for (d, *_), a3, b3 in zip(cases, outl, outp):
+        gc = d.numGC
+        for a, b in zip(a3, b3):
+            ra, rb = a[..., gc:-gc, gc:-gc], b[..., gc:-gc, gc:-gc]
+            rel = max(rel, float(np.abs(ra - rb).sum() / max(np.abs(rb).sum(), 1e-300)))
+            identical = identical and np.array_equal(a, b)
+    bp.close()
+    bl.close()
+    mlp.close()
+    return {"workload": "batch64_shock_bubble_riemannGFM", "instances": len(spec), "cells": cells, "steps": K,
+            "warmup": args.warmup, "seed": BATCH_SEED, "weights": weights,
+            "plain_sequential": seq, "batched_plain": plain, "batched_learned": learned,
+            "batched_learned_over_plain_sequential": learned["value"] / seq["value"],
+            "batched_plain_over_plain_sequential": plain["value"] / seq["value"],
+            "max_rel_l1_learned_vs_plain": rel, "learned_bit_identical_to_plain": identical,
+            "l2": "inputs larger than L2 (%.1f GB of state); 512 MiB flush before each timed run"
+                  % (cells * 9 * 8 / 1e9)}
 
 
 def run_batch(args):

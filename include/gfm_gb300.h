@@ -294,7 +294,10 @@ gfm_status_t gfm_batch_synchronize(gfm_batch* b);
  *   gfm_mlp_train             Adam over shuffled minibatches, cosine learning
  *                             rate; loss_per_epoch (host, epochs floats) or NULL
  *   gfm_mlp_infer             DEVICE X[n][10] -> out[n]: FP32 on CUDA cores
- *                             (tensor_cores = 0) or BF16 tensor cores (1)
+ *                             (tensor_cores = 0), BF16 tensor cores with
+ *                             tcgen05 over tiles of 128 problems (1), or the
+ *                             interface loop's warp-level path, one problem per
+ *                             warp with mma.sync BF16 tiles (2); FP32 accumulation
  *   gfm_rs_mixed_batch_learned  gfm_rs_mixed_batch with the proposal (use_net =
  *                             1) or the two-shock guess (0); iters[n] receives
  *                             each solve's Newton iteration count */
@@ -317,9 +320,11 @@ gfm_status_t gfm_rs_mixed_batch_learned(gfm_mlp* m, int n, double gammaL, double
 /* The context's interface solves (Riemann and real GFM) start Newton's
  * method from the learned proposal where it applies (NULL: the two-shock
  * guess everywhere, the default).  Each warp of the interface loop evaluates
- * the network in FP32 on its cell's actual states (one problem at a time, on
- * the loop's latency-bound critical path).  The network is read at each step
- * (training it between steps takes effect).  Results differ from the default
+ * the network on the tensor cores on its cell's actual states (one problem at
+ * a time, on the loop's latency-bound critical path: BF16 mma.sync tiles with
+ * FP32 accumulation, the activations kept in the lanes that feed the next
+ * layer).  The network is read at each step (training it between steps takes
+ * effect).  Results differ from the default
  * only within the Newton tolerance (p* within about 2e-14); they are not
  * bit-identical to the oracle. */
 gfm_status_t gfm_set_mlp(gfm_ctx* ctx, gfm_mlp* mlp);
@@ -333,6 +338,10 @@ gfm_status_t gfm_capture_interface_problems(gfm_ctx* ctx, float* X, float* Y, in
 /* Interface solves of the last step: count, Newton iterations, and how many
  * started from the learned proposal. */
 gfm_status_t gfm_get_interface_stats(gfm_ctx* ctx, int64_t* n_solves, int64_t* newton_iters, int64_t* n_proposed);
+/* The same summed over the steps of gfm_step (and of batched steps) since the
+ * context's last gfm_set_time or state upload: read once after a run, a
+ * recorded graph included. */
+gfm_status_t gfm_get_interface_totals(gfm_ctx* ctx, int64_t* n_solves, int64_t* newton_iters, int64_t* n_proposed);
 
 /* Shock-bubble family of the batched workload: the 1000x400 shock-bubble's
  * geometry on any grid (width 0.25, square cells, height 0.25 Ny/Nx,

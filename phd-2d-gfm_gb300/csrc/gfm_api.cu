@@ -520,6 +520,7 @@ gfm_status_t gfm_set_time(gfm_ctx* ctx, double t, int numsteps) {
   ctx->h_dtime->t = t;
   ctx->h_dtime->numsteps = numsteps;
   ctx->h_dtime->active = 0;
+  ctx->h_dtime->ifc_solves_total = ctx->h_dtime->ifc_iters_total = ctx->h_dtime->ifc_gated_total = 0ull;
   const GridP& P = ctx->P;
   int full[4] = {P.g, P.g + P.Ny, P.g, P.g + P.Nx};
   for (int f = 0; f < 2; f++)
@@ -754,6 +755,16 @@ gfm_status_t gfm_get_interface_stats(gfm_ctx* ctx, int64_t* n_solves, int64_t* n
   if (n_solves) *n_solves = ctx->h_dtime->n_ifc;
   if (newton_iters) *newton_iters = (int64_t)ctx->h_dtime->ifc_iters;
   if (n_proposed) *n_proposed = ctx->h_dtime->ifc_gated;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_get_interface_totals(gfm_ctx* ctx, int64_t* n_solves, int64_t* newton_iters, int64_t* n_proposed) {
+  if (!ctx) return GFM_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_dtime, ctx->dtime, sizeof(DevTime), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (n_solves) *n_solves = (int64_t)ctx->h_dtime->ifc_solves_total;
+  if (newton_iters) *newton_iters = (int64_t)ctx->h_dtime->ifc_iters_total;
+  if (n_proposed) *n_proposed = (int64_t)ctx->h_dtime->ifc_gated_total;
   return GFM_OK;
 }
 

@@ -41,6 +41,8 @@ struct DevTime {
   unsigned long long newton_iters;
   unsigned long long ifc_iters;   // Newton iterations of the interface solves (Riemann, real GFM)
   int ifc_gated;                  // interface solves started from the learned proposal
+  // the same three summed over the steps since the last gfm_set_time
+  unsigned long long ifc_solves_total, ifc_iters_total, ifc_gated_total;
   int rc[8];               // realcells1 (imin,imax,jmin,jmax), realcells2
 };
 
@@ -192,6 +194,8 @@ void launch_end_step(gfm_ctx* ctx);
 void prepare_kernels();
 void prepare_step_kernels();   // occupancy of the grid-stride kernels (gfm_step.cu)
 const float* mlp_params(const struct gfm_mlp* m);   // the network's FP32 parameters (device)
+const uint32_t* mlp_frag(const struct gfm_mlp* m);  // its B fragments for mlp_forward_warp_tc (device)
+void launch_mlp_frag_pack(const struct gfm_mlp* m, cudaStream_t s);   // refresh them from the parameters
 // nsteps iterations of the time loop on ctx's stream (gfm_step, gfm_step_timed)
 gfm_status_t run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
 gfm_status_t validate_method(gfm_ctx* ctx, const gfm_method_desc* m);

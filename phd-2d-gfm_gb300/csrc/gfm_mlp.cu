@@ -239,6 +239,40 @@ __global__ void k_mlp_infer_f32(const float* P, const float* X, int n, float* ou
 }
 
 // ---------------------------------------------------------------------------
+// Warp-level tensor-core inference (mlp_forward_warp_tc, the interface
+// loop's path): its B fragments, and a batch kernel of one warp per problem
+// that runs the same function for tests and measurements.
+// ---------------------------------------------------------------------------
+__global__ void k_mlp_frag_pack(const float* __restrict__ P, uint32_t* __restrict__ frag) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= MLP_FRAG_WORDS) return;
+  const int tile = w >> 6, lane = (w >> 1) & 31, half = w & 1;
+  int layer, ks, t;
+  if (tile < 8) { layer = 0; ks = 0; t = tile; }
+  else if (tile < 40) { layer = 1; ks = (tile - 8) >> 3; t = (tile - 8) & 7; }
+  else { layer = 2; ks = (tile - 40) >> 3; t = (tile - 40) & 7; }
+  const int n = 8 * t + (lane >> 2);
+  const int k = 16 * ks + 2 * (lane & 3) + 8 * half;
+  const int base = layer == 0 ? MLP_W1 : (layer == 1 ? MLP_W2 : MLP_W3);
+  const int kmax = layer == 0 ? MLP_IN : MLP_H;
+  const float lo = k < kmax ? P[base + k * MLP_H + n] : 0.0f;
+  const float hi = k + 1 < kmax ? P[base + (k + 1) * MLP_H + n] : 0.0f;
+  frag[w] = mlp_bf16x2(lo, hi);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_infer_warp_tc(const uint32_t* frag, const float* P, const float* X,
+                                                           int n, float* out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int q = warp; q < n; q += nwarps) {
+    float x[MLP_IN];
+    for (int k = 0; k < MLP_IN; k++) x[k] = X[(int64_t)q * MLP_IN + k];
+    const float y = mlp_forward_warp_tc(frag, P, x);
+    if ((threadIdx.x & 31) == 0) out[q] = y;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // BF16 inference on the tensor cores.
 //
 // One CTA of 128 threads per tile of 128 problems (thread t = row t).  Each
@@ -529,6 +563,7 @@ struct gfm_mlp {
   float* M;          // Adam moments
   float* V;
   uint16_t* pack;    // BF16 weights in the tensor-core layout
+  uint32_t* frag;    // BF16 B fragments of the warp-level tensor-core path (mlp_forward_warp_tc)
   int* err;
   int adam_steps;
   bool pack_stale;
@@ -579,6 +614,14 @@ size_t tc_smem() { return sizeof(TcSmem); }
 }  // namespace
 
 const float* gfm::mlp_params(const gfm_mlp* m) { return m->P; }
+const uint32_t* gfm::mlp_frag(const gfm_mlp* m) { return m->frag; }
+
+// Stream-ordered, so a step recorded into a graph packs the network as it
+// is when the step runs.
+void gfm::launch_mlp_frag_pack(const gfm_mlp* m, cudaStream_t s) {
+  k_mlp_frag_pack<<<(MLP_FRAG_WORDS + 255) / 256, 256, 0, s>>>(m->P, m->frag);
+  counted();
+}
 
 extern "C" {
 
@@ -593,6 +636,7 @@ gfm_status_t gfm_mlp_create(uint64_t seed, gfm_mlp** out) {
   if (e == cudaSuccess) e = cudaMalloc(&m->M, sizeof(float) * MLP_NPARAM);
   if (e == cudaSuccess) e = cudaMalloc(&m->V, sizeof(float) * MLP_NPARAM);
   if (e == cudaSuccess) e = cudaMalloc(&m->pack, sizeof(uint16_t) * TC_PACK_ELEMS);
+  if (e == cudaSuccess) e = cudaMalloc(&m->frag, sizeof(uint32_t) * MLP_FRAG_WORDS);
   if (e == cudaSuccess) e = cudaMalloc(&m->err, sizeof(int));
   if (e != cudaSuccess) {
     gfm_mlp_destroy(m);
@@ -620,7 +664,8 @@ gfm_status_t gfm_mlp_create(uint64_t seed, gfm_mlp** out) {
 
 gfm_status_t gfm_mlp_destroy(gfm_mlp* m) {
   if (!m) return GFM_OK;
-  cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->pack); cudaFree(m->err);
+  cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->pack); cudaFree(m->frag);
+  cudaFree(m->err);
   delete m;
   return GFM_OK;
 }
@@ -750,6 +795,16 @@ gfm_status_t gfm_mlp_infer(gfm_mlp* m, const float* X, int n, float* out, int te
     k_mlp_infer_f32<<<(n + 127) / 128, 128, sm, s>>>(m->P, X, n, out);
     counted();
     return ck(cudaGetLastError(), "k_mlp_infer_f32");
+  }
+  if (tensor_cores == 2) {   // the interface loop's warp-level path, one warp per problem
+    launch_mlp_frag_pack(m, s);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = (n + 3) / 4 < sms * 16 ? (n + 3) / 4 : sms * 16;
+    k_mlp_infer_warp_tc<<<blocks, 128, 0, s>>>(m->frag, m->P, X, n, out);
+    counted();
+    return ck(cudaGetLastError(), "k_mlp_infer_warp_tc");
   }
   if (m->pack_stale) {
     gfm_status_t r = repack(m, s);

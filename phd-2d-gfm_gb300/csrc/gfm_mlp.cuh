@@ -19,6 +19,10 @@
 
 #include "gfm_math.cuh"
 
+#if defined(__CUDACC__)
+#include <cuda_bf16.h>
+#endif
+
 namespace gfm {
 
 constexpr int MLP_IN = 10;
@@ -89,35 +93,92 @@ GFM_HD double mlp_apply(const GuessInfo& g, float y) {
 __host__ __device__ inline float mlp_silu(float z) { return z / (1.0f + expf(-z)); }
 
 #if defined(__CUDACC__)
-// The network in FP32 by one warp (all 32 lanes, warp-uniform): lane l
-// computes neurons l and l + 32 of each layer from the parameters P in
-// global memory; hbuf holds a layer's 64 outputs (per-warp shared memory).
-__device__ inline float mlp_forward_warp(const float* __restrict__ P, const float x[MLP_IN], float* hbuf) {
-  const int l = threadIdx.x & 31;
-  float z0 = __ldg(P + MLP_B1 + l), z1 = __ldg(P + MLP_B1 + l + 32);
-  for (int k = 0; k < MLP_IN; k++) {
-    z0 += x[k] * __ldg(P + MLP_W1 + k * MLP_H + l);
-    z1 += x[k] * __ldg(P + MLP_W1 + k * MLP_H + l + 32);
+// The network on the tensor cores by one warp, for one problem at a time
+// inside the latency-bound interface loop.  Each layer is a row of 16 x 16
+// BF16 tiles times the weights, D = A B + C with
+// mma.sync.m16n8k16.row.col.f32.bf16.bf16.f32: the problem is row 0 of A
+// (rows 1-15 zero), C starts at the bias, FP32 accumulation.  In this shape
+// row 0 of D sits in lanes 0-3 (columns 8t + 2l, 8t + 2l + 1 of n-tile t),
+// exactly where the next layer's A fragments need it (k-step s takes n-tiles
+// 2s and 2s + 1), so the activations never leave their lanes.  The last
+// layer (64 -> 1) is an FP32 dot product over lanes 0-3.  B fragments come
+// pre-arranged per lane (MLP_FRAG_WORDS words, k_mlp_frag_pack): for layer L,
+// k-step s, n-tile t, lane l the two words at ((MLP_FRAG_OFF[L] + 8 s + t) 32
+// + l) 2 hold W[16 s + 2 (l & 3) + {0, 1}][8 t + (l >> 2)] and the same rows
+// + 8, BF16 pairs with the lower k in the low half.
+constexpr int MLP_FRAG_TILES = 8 + 32 + 32;           // (k-step, n-tile) pairs of the three layers
+constexpr int MLP_FRAG_WORDS = MLP_FRAG_TILES * 64;   // 32 lanes x 2 words each
+
+__device__ __forceinline__ uint32_t mlp_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mlp_mma(float c[4], uint32_t a0, uint32_t a2, uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(0u), "r"(a2), "r"(0u), "r"(b.x), "r"(b.y));
+}
+
+// the network's output for the warp's problem x (all lanes hold the same x);
+// every lane returns it
+__device__ inline float mlp_forward_warp_tc(const uint32_t* __restrict__ frag, const float* __restrict__ P,
+                                            const float x[MLP_IN]) {
+  const int lane = threadIdx.x & 31;
+  const int tig = lane & 3;
+  const bool row0 = lane < 4;
+  const uint2* F = reinterpret_cast<const uint2*>(frag) + lane;
+  float h[8][2];   // row 0 of the layer's output: columns 8 t + 2 tig + {0, 1} (lanes 0-3)
+  // layer 1: K = 10 features padded to 16
+  uint32_t a0 = 0u, a2 = 0u;
+  if (row0) {
+    a0 = mlp_bf16x2(x[2 * tig], x[2 * tig + 1]);
+    a2 = tig == 0 ? mlp_bf16x2(x[8], x[9]) : 0u;
   }
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    float c[4] = {row0 ? __ldg(P + MLP_B1 + 8 * t + 2 * tig) : 0.0f,
+                  row0 ? __ldg(P + MLP_B1 + 8 * t + 2 * tig + 1) : 0.0f, 0.0f, 0.0f};
+    mlp_mma(c, a0, a2, __ldg(F + 32 * t));
+    h[t][0] = c[0];
+    h[t][1] = c[1];
+  }
+  // layers 2 and 3: K = 64 in four k-steps
+#pragma unroll
   for (int layer = 0; layer < 2; layer++) {
-    __syncwarp();
-    hbuf[l] = mlp_silu(z0);
-    hbuf[l + 32] = mlp_silu(z1);
-    __syncwarp();
-    const float* W = P + (layer == 0 ? MLP_W2 : MLP_W3);
+    uint32_t A0[4], A2[4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      A0[s] = row0 ? mlp_bf16x2(mlp_silu(h[2 * s][0]), mlp_silu(h[2 * s][1])) : 0u;
+      A2[s] = row0 ? mlp_bf16x2(mlp_silu(h[2 * s + 1][0]), mlp_silu(h[2 * s + 1][1])) : 0u;
+    }
     const float* b = P + (layer == 0 ? MLP_B2 : MLP_B3);
-    z0 = __ldg(b + l);
-    z1 = __ldg(b + l + 32);
-    for (int k = 0; k < MLP_H; k++) {
-      const float h = hbuf[k];
-      z0 += h * __ldg(W + k * MLP_H + l);
-      z1 += h * __ldg(W + k * MLP_H + l + 32);
+    const uint2* FL = F + 32 * (8 + 32 * layer);
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      float c[4] = {row0 ? __ldg(b + 8 * t + 2 * tig) : 0.0f, row0 ? __ldg(b + 8 * t + 2 * tig + 1) : 0.0f, 0.0f,
+                    0.0f};
+#pragma unroll
+      for (int s = 0; s < 4; s++) mlp_mma(c, A0[s], A2[s], __ldg(FL + 32 * (8 * s + t)));
+      h[t][0] = c[0];
+      h[t][1] = c[1];
     }
   }
-  float y = mlp_silu(z0) * __ldg(P + MLP_W4 + l) + mlp_silu(z1) * __ldg(P + MLP_W4 + l + 32);
-  for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
-  return y + __ldg(P + MLP_B4);
+  // output layer in FP32 over row 0's 64 activations (lanes 0-3)
+  float y = 0.0f;
+#pragma unroll
+  for (int t = 0; t < 8; t++)
+    y += mlp_silu(h[t][0]) * __ldg(P + MLP_W4 + 8 * t + 2 * tig) +
+         mlp_silu(h[t][1]) * __ldg(P + MLP_W4 + 8 * t + 2 * tig + 1);
+  y += __shfl_xor_sync(0xffffffffu, y, 1);
+  y += __shfl_xor_sync(0xffffffffu, y, 2);
+  return __shfl_sync(0xffffffffu, y, 0) + __ldg(P + MLP_B4);
 }
+
+// B fragments of the three layers from the FP32 parameters (one word per thread)
+__global__ void k_mlp_frag_pack(const float* __restrict__ P, uint32_t* __restrict__ frag);
 #endif
 
 // counter-based generator (splitmix64 finaliser): uniform in [0, 1)

@@ -105,6 +105,9 @@ __global__ void k_noalloc_init(DevTime* D, unsigned int* counters, double t, int
   D->n_ifc = 0;
   D->n_rounds = 0;
   D->newton_iters = 0ull;
+  D->ifc_iters = 0ull;
+  D->ifc_gated = 0;
+  D->ifc_solves_total = D->ifc_iters_total = D->ifc_gated_total = 0ull;
   int full[4] = {P.g, P.g + P.Ny, P.g, P.g + P.Nx};
   for (int q = 0; q < 8; q++) D->rc[q] = full[q & 3];
   for (int q = 0; q < 64; q++) counters[q] = 0u;

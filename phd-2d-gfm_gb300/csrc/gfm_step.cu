@@ -222,6 +222,9 @@ __global__ void k_end_step(DevTime* D) {
   if (D->active) {
     D->t += D->dt;
     D->numsteps += 1;
+    D->ifc_solves_total += (unsigned long long)D->n_ifc;
+    D->ifc_iters_total += D->ifc_iters;
+    D->ifc_gated_total += (unsigned long long)D->ifc_gated;
   }
 }
 
@@ -716,6 +719,7 @@ struct IfcArgs {
   DevTime* D;
   int slip;             // GFM_base::use_slip_BCs
   const float* mlp;     // learned-proposal network (gfm_mlp.cuh), or null
+  const uint32_t* mlp_frag;   // its B fragments for the warp-level tensor-core path
   float* cap_X;         // gated problems appended here (features, target), or null
   float* cap_Y;
   int* cap_count;
@@ -977,7 +981,7 @@ struct PairStar { double p, u, rho_own; bool trivial; };
 // the warp in FP32 on the actual states; with a capture buffer, such problems
 // are recorded (features and the solved p* relative to the two-shock guess).
 __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const Gas& kL, const Gas& kR, const V4& Uown,
-                                                  uint32_t* status, int* iters, const IfcArgs& a, float* hbuf,
+                                                  uint32_t* status, int* iters, const IfcArgs& a,
                                                   int* proposed) {
   // cons_to_prims_phys with its three quotients by rho (rho u, rho v, E) in
   // one: lane kc of each group of four divides component kc + 1 (E twice)
@@ -1035,7 +1039,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
     gated = c_gt(ratio, 0.0) && c_gt(fabs(gfm_log(ratio)), MLP_GATE);
     if (gated) mlp_features_f(rhoL, uL, pbL, kL.g, kL.pinf, rhoR, uR, pbR, kR.g, kR.pinf, x);
     if (gated && a.mlp) {
-      const float y = fminf(fmaxf(mlp_forward_warp(a.mlp, x, hbuf), -20.0f), 20.0f);
+      const float y = fminf(fmaxf(mlp_forward_warp_tc(a.mlp_frag, a.mlp, x), -20.0f), 20.0f);
       p0 = (pts + pinf_min) * gfm_exp((double)y) - pinf_min;
       *proposed += 1;
     }
@@ -1258,8 +1262,6 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
   const int lane = threadIdx.x & 31;
   const bool isR = (lane >> 4) == 1;
   const Gas k = isR ? P.gas2 : P.gas1;
-  __shared__ float s_h[8][MLP_H];   // per-warp layer outputs of the learned proposal
-  float* hbuf = s_h[(threadIdx.x >> 5) & 7];
   uint32_t st = 0;
   int iters = 0, gated = 0;
   for (;;) {
@@ -1277,7 +1279,7 @@ __global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
       continue;
     }
     int it = 0, gt = 0;
-    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, cell.Us, &st, &it, a, hbuf, &gt);
+    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, cell.Us, &st, &it, a, &gt);
     if (lane == 0) { iters += it; gated += gt; }
     if (c_isnan(m.p)) st |= ST_NAN;
     if (lane == 16 * cell.sr) {
@@ -1572,7 +1574,7 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       const V4 Us = prims_to_cons(k.g, k.pinf, V4{own[0], un, 0.0, c_lt(1e-6, own[3]) ? own[3] : 1e-6}, &okp);
       if (!okp) st |= ST_UNPHYSICAL;
       int it = 0, gt = 0;
-      const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it, a, nullptr, &gt);
+      const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it, a, &gt);
       if (lane == 0) iters += it;
       if (c_isnan(m.p)) st |= ST_NAN;
       const double orho = xside(m.rho_own), otx = xside(tx), oty = xside(ty);
@@ -2141,8 +2143,12 @@ void launch_cfl_ogfm(gfm_ctx* ctx, double CFL, double T, bool ogfm, unsigned int
 }
 
 // the learned proposal and the capture of training problems (both off by default)
-static void set_learning(gfm_ctx* ctx, IfcArgs& ia) {
+// the learned proposal and the capture of the interface loop launched on
+// stream s (the network's fragments are packed on s just before it)
+static void set_learning(gfm_ctx* ctx, IfcArgs& ia, cudaStream_t s) {
   ia.mlp = ctx->mlp ? mlp_params(ctx->mlp) : nullptr;
+  ia.mlp_frag = ctx->mlp ? mlp_frag(ctx->mlp) : nullptr;
+  if (ctx->mlp) launch_mlp_frag_pack(ctx->mlp, s);
   ia.cap_X = ctx->cap_X; ia.cap_Y = ctx->cap_Y; ia.cap_count = ctx->cap_count; ia.cap = ctx->cap;
 }
 
@@ -2201,7 +2207,7 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.spin_limit = ctx->ifc_spin_limit > 0 ? ctx->ifc_spin_limit : IFC_SPIN_LIMIT;
   ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
-  set_learning(ctx, ia);
+  set_learning(ctx, ia, s);
   ia.probe_ij = nullptr; ia.probe_w = nullptr;
   if (variant == GFM_RIEMANN) {
     k_ifc_probes<<<152, 256, 0, s>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
@@ -2425,7 +2431,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.spin_limit = ctx->ifc_spin_limit > 0 ? ctx->ifc_spin_limit : IFC_SPIN_LIMIT;
   ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
-  set_learning(ctx, ia);
+  set_learning(ctx, ia, ctx->s_chain);
   ia.probe_ij = nullptr; ia.probe_w = nullptr;
   if (variant == GFM_RIEMANN) {
     k_ifc_probes<<<16, 256, 0, ctx->s_chain>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
@@ -2597,7 +2603,7 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.spin_limit = ctx->ifc_spin_limit > 0 ? ctx->ifc_spin_limit : IFC_SPIN_LIMIT;
   ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
-  ia.mlp = nullptr; ia.cap_X = nullptr; ia.cap_Y = nullptr; ia.cap_count = nullptr; ia.cap = 0;
+  ia.mlp = nullptr; ia.mlp_frag = nullptr; ia.cap_X = nullptr; ia.cap_Y = nullptr; ia.cap_count = nullptr; ia.cap = 0;
   ia.probe_ij = nullptr; ia.probe_w = nullptr;
   if (og) k_vof_chain<VOF_OGFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
   else k_vof_chain<VOF_GFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);

@@ -116,6 +116,8 @@ def lib():
         "gfm_capture_interface_problems": [P, V, V, I, V],
         "gfm_get_interface_stats": [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                     ctypes.POINTER(ctypes.c_int64)],
+        "gfm_get_interface_totals": [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                     ctypes.POINTER(ctypes.c_int64)],
         "gfm_case_init_shock_bubble": [V, ctypes.POINTER(GridDesc), pd, pd, pd],
         "gfm_get_device_status": [P, ctypes.POINTER(ctypes.c_uint32)],
         "gfm_clear_device_status": [P],
@@ -376,6 +378,14 @@ class Context:
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         _check(lib().gfm_get_interface_stats(self._p, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
                "gfm_get_interface_stats")
+        return {"solves": a.value, "newton_iters": b.value, "proposed": c.value}
+
+    def interface_totals(self):
+        """Interface solves, their Newton iterations and the solves started
+        from the learned proposal, summed since the last upload / set_time."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().gfm_get_interface_totals(self._p, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "gfm_get_interface_totals")
         return {"solves": a.value, "newton_iters": b.value, "proposed": c.value}
 
     def fluid_mass(self, interiorsign):

@@ -117,6 +117,25 @@ def test_tensor_core_inference_matches_fp32():
     assert np.corrcoef(b, ref)[0, 1] > 0.999
 
 
+def test_warp_tensor_core_inference_matches_fp32():
+    """The interface loop's path: one warp per problem, BF16 mma.sync tiles,
+    FP32 accumulation (gfm_mlp_infer with tensor_cores = 2)."""
+    m = g.MLP(seed=11)
+    n = 777
+    X = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+    Y = torch.empty(n, dtype=torch.float32, device="cuda")
+    g.mlp_generate(13, n, X.data_ptr(), Y.data_ptr())
+    ow = torch.zeros(n, dtype=torch.float32, device="cuda")
+    m.infer(X.data_ptr(), n, ow.data_ptr(), tensor_cores=2)
+    torch.cuda.synchronize()
+    w = ow.cpu().numpy()
+    ref, _ = forward(m.params(), X.cpu().numpy().astype(np.float64))
+    m.close()
+    scale = np.max(np.abs(ref)) + 1.0
+    assert np.max(np.abs(w - ref)) <= 0.03 * scale, np.max(np.abs(w - ref))   # BF16 operands, FP32 accumulation
+    assert np.corrcoef(w, ref)[0, 1] > 0.999
+
+
 def stiffened_cons(g_, pinf, rho, u, p):
     E = (p + g_ * pinf) / (g_ - 1.0) + 0.5 * rho * u * u
     return np.stack([rho, rho * u, np.zeros_like(rho), E], 1)
