@@ -696,8 +696,21 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def relaunch_command(argv, gpus, port):
+    """The command that runs this benchmark as `gpus` ranks, one per GPU, when
+    --gpus N > 1 is asked outside a distributed launch (the same command line
+    as a distributed launch of the benchmark)."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(gpus),
+            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + list(argv)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: independent replicas with a barrier and the
+        # max over ranks (rank 0 prints the line)
+        port = 29500 + os.getpid() % 2000
+        sys.exit(subprocess.call(relaunch_command(sys.argv[1:], args.gpus, port)))
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch64":

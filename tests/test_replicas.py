@@ -42,3 +42,17 @@ def test_two_replicas_max_over_ranks():
     for rank, slowest, value in res:
         assert slowest == 125.0
         assert value == pytest.approx(400000 * 10 * 2 / 0.125)
+
+
+def test_gpus_flag_relaunches_one_rank_per_gpu():
+    """bench.py --gpus N outside a distributed launch runs itself under
+    torch.distributed.run with N ranks on 127.0.0.1."""
+    sys.path.insert(0, ROOT)
+    import bench
+    cmd = bench.relaunch_command(["--gpus", "4", "--steps", "10"], 4, 29511)
+    i = cmd.index("torch.distributed.run")
+    assert cmd[i - 1] == "-m"
+    assert cmd[cmd.index("--nproc-per-node") + 1] == "4"
+    assert cmd[cmd.index("--master-addr") + 1] == "127.0.0.1"
+    assert cmd[cmd.index("--master-port") + 1] == "29511"
+    assert cmd[-4:] == ["--gpus", "4", "--steps", "10"] and cmd[-5].endswith("bench.py")
