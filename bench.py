@@ -586,6 +586,15 @@ def batched_learned_block(args):
     outp = [ctx.download() for ctx in bp.instances]
     learned = timed(bl, True)
     outl = [ctx.download() for ctx in bl.instances]
+    # the project's autotuner: flux tile shape per grid-size class and the
+    # schedule (per-instance streams, or one persistent flux launch over all
+    # instances per step), timed on the batch's state; then the tuned run
+    for ctx, st in zip(bp.instances, start):
+        ctx.upload(st[0], st[1], st[2], t=st[3], numsteps=st[4])
+    tuning = bp.autotune(m, steps=16)
+    tuned = timed(bp, True)
+    outt = [ctx.download() for ctx in bp.instances]
+    tuned_identical = all(np.array_equal(a, b) for a3, b3 in zip(outt, outp) for a, b in zip(a3, b3))
     rel = 0.0
     identical = True
     for (d, *_), a3, b3 in zip(cases, outl, outp):
@@ -600,6 +609,8 @@ def batched_learned_block(args):
     return {"workload": "batch64_shock_bubble_riemannGFM", "instances": len(spec), "cells": cells, "steps": K,
             "warmup": args.warmup, "seed": BATCH_SEED, "weights": weights,
             "plain_sequential": seq, "batched_plain": plain, "batched_learned": learned,
+            "autotune": tuning, "batched_tuned": tuned, "tuned_bit_identical_to_plain": tuned_identical,
+            "batched_tuned_over_plain_sequential": tuned["value"] / seq["value"],
             "batched_learned_over_plain_sequential": learned["value"] / seq["value"],
             "batched_plain_over_plain_sequential": plain["value"] / seq["value"],
             "max_rel_l1_learned_vs_plain": rel, "learned_bit_identical_to_plain": identical,

@@ -212,6 +212,16 @@ gfm_status_t gfm_set_newton_limit(gfm_ctx* ctx, int max_iterations);
  * the default).  The step's results are not valid after a withheld entry. */
 gfm_status_t gfm_set_interface_wait(gfm_ctx* ctx, int64_t spin_limit, int withheld_entry);
 
+/* Tile shape of the context's flux update: 32 x 8 cells (the default), 16 x 16
+ * or 64 x 4 per CTA.  Results are identical for every shape (each face flux is
+ * formed once and each cell sums its faces in the reference's order); the
+ * time differs with the grid.  The overlapped ghost fill's passes always use
+ * 32 x 8.  gfm_batch_autotune chooses it per grid-size class. */
+#define GFM_FLUX_TILE_32x8 0
+#define GFM_FLUX_TILE_16x16 1
+#define GFM_FLUX_TILE_64x4 2
+gfm_status_t gfm_set_flux_tile(gfm_ctx* ctx, int shape);
+
 /* number of kernels this library has launched since it was loaded */
 int64_t gfm_launch_count(void);
 
@@ -275,6 +285,25 @@ gfm_status_t gfm_batch_set_stream(gfm_batch* b, void* cuda_stream);
 gfm_status_t gfm_step_batched_graph(gfm_batch* b, const gfm_method_desc* m, int nsteps);
 gfm_status_t gfm_step_batched_sequential(gfm_batch* b, const gfm_method_desc* m, int nsteps);
 gfm_status_t gfm_batch_synchronize(gfm_batch* b);
+/* Schedule of a batched step (both give each instance the results of
+ * stepping it alone):
+ *   GFM_BATCH_STREAMS  (default) each instance's whole step on its own
+ *                      stream, the instances side by side
+ *   GFM_BATCH_PHASED   every instance up to its flux update, then one
+ *                      persistent flux launch per tile shape over the tiles of
+ *                      all instances (CTAs pull instance / fluid / tile work
+ *                      items, the largest instances first), then every
+ *                      instance's commit
+ * gfm_batch_autotune times, on the batch's own current state (restored
+ * afterwards), the flux tile shapes of each grid-size class (padded cells
+ * below 2^17, below 2^19, larger; on the class's largest instance) and then
+ * the two schedules over `steps` steps (rounded up to a multiple of 8), keeps
+ * the fastest, and writes a JSON report of the times into report (report_len
+ * bytes, may be NULL). */
+#define GFM_BATCH_STREAMS 0
+#define GFM_BATCH_PHASED 1
+gfm_status_t gfm_batch_set_schedule(gfm_batch* b, int schedule);
+gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int steps, char* report, int report_len);
 
 /* Learned star-pressure proposal (no counterpart in the reference): a
  * multilayer perceptron 10 -> 64 -> 64 -> 64 -> 1 (SiLU) maps a two-material

@@ -160,6 +160,9 @@ __global__ void k_rc_empty(GridP P, DevTime* D) {
 }
 
 gfm_status_t gfm::validate_method(gfm_ctx* ctx, const gfm_method_desc* m) { return check_method(ctx, m); }
+static_assert(GFM_FLUX_TILE_32x8 == FLUX_SHAPE_32x8 && GFM_FLUX_TILE_16x16 == FLUX_SHAPE_16x16 &&
+                  GFM_FLUX_TILE_64x4 == FLUX_SHAPE_64x4,
+              "tile shape codes");
 double* gfm::mass_scratch(gfm_ctx* ctx) { return extra(ctx).mass_part; }
 gfm_status_t gfm::launch_status() { return last_error(); }
 
@@ -717,6 +720,49 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
   return r;
 }
 
+// The one-stream step of run_steps split around its flux update, for a
+// batch's phased schedule (every instance's front, one flux launch over all
+// instances, every instance's back): the same launches in the same order on
+// the context's stream as a step of run_steps without overlap.  The method
+// has been checked (check_method) by the caller.
+gfm_status_t gfm::step_front(gfm_ctx* ctx, const gfm_method_desc* m) {
+  ctx->ifc_opp = reinterpret_cast<int*>(extra(ctx).counters + 1);
+  if (ctx->two_fluid) ctx->itm = m->itm;
+  const bool vof = ctx->two_fluid && m->itm == GFM_ITM_VOF;
+  const bool ogfm = ctx->two_fluid && (m->gfm == GFM_OGFM || m->gfm == GFM_OGFM_VOF);
+  if (ctx->two_fluid && !vof) {
+    ctx->cfl_counter = extra(ctx).counters;
+    launch_step_begin(ctx, m->CFL, m->T, ogfm);
+  } else {
+    ctx->cfl_counter = nullptr;
+    launch_cfl_impl(ctx, m->CFL, m->T, ogfm, extra(ctx).counters);
+  }
+  if (ctx->two_fluid) {
+    if (vof) launch_ghost_fill_vof(ctx, m);
+    else launch_ghost_fill(ctx, m);
+    cudaEventRecord(ctx->ev_ls_fork, ctx->stream);
+    cudaStreamWaitEvent(ctx->s_ls, ctx->ev_ls_fork, 0);
+    if (vof) launch_vof_update(ctx, ctx->s_ls);
+    else launch_level_set(ctx, m, ctx->s_ls, 3);
+    cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
+  }
+  ctx->cfl_counter = nullptr;
+  return last_error();
+}
+
+gfm_status_t gfm::step_back(gfm_ctx* ctx, const gfm_method_desc* m) {
+  (void)m;
+  if (ctx->two_fluid) {
+    cudaStreamWaitEvent(ctx->stream, ctx->ev_ls_done, 0);
+    launch_commit(ctx, 3, true);
+  } else {
+    launch_commit(ctx, 1, true);
+  }
+  launch_end_step(ctx);
+  ctx->steps_done_host++;
+  return last_error();
+}
+
 extern "C" {
 
 gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps) {
@@ -765,6 +811,12 @@ gfm_status_t gfm_get_interface_totals(gfm_ctx* ctx, int64_t* n_solves, int64_t* 
   if (n_solves) *n_solves = (int64_t)ctx->h_dtime->ifc_solves_total;
   if (newton_iters) *newton_iters = (int64_t)ctx->h_dtime->ifc_iters_total;
   if (n_proposed) *n_proposed = (int64_t)ctx->h_dtime->ifc_gated_total;
+  return GFM_OK;
+}
+
+gfm_status_t gfm_set_flux_tile(gfm_ctx* ctx, int shape) {
+  if (!ctx || shape < GFM_FLUX_TILE_32x8 || shape > GFM_FLUX_TILE_64x4) return GFM_ERR_ARG;
+  ctx->flux_shape = shape;
   return GFM_OK;
 }
 

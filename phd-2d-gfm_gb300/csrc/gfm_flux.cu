@@ -20,28 +20,33 @@
 //   phase 4  per cell: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn, the
 //            accumulation order of the reference's face loop (:290-292).
 #include "gfm_internal.cuh"
+#include <cstring>
 #include <mutex>
 
 namespace gfm {
 
-constexpr int TX = FLUX_TX;
-constexpr int TY = FLUX_TY;
 constexpr int NT = 256;
-constexpr int WR = TY + 4;   // primitive region rows   (i0-2 .. i0+TY+1)
-constexpr int WC = TX + 4;   // primitive region columns (j0-2 .. j0+TX+1)
-constexpr int SR = TY + 2;   // face-state cells rows    (i0-1 .. i0+TY)
-constexpr int SC = TX + 2;   // face-state cells columns (j0-1 .. j0+TX)
-constexpr int NXF = TY * (TX + 1);
-constexpr int NYF = (TY + 1) * TX;
 
-struct FluxSmem {
-  double w[4][WR][WC];          // primitives (MUSCL) or conserved (Godunov)
-  double irho[WR][WC];          // MUSCL: 1/rho of the conversion, reused by the cell's face states
-  double fs[4][4][SR][SC];      // [face L,R,B,T][component][r][c]
-  double fx[4][TY][TX + 1];
-  double fy[4][TY + 1][TX];
-  double qd[6][NXF + NYF];      // queued faces: uR, pR, utL, utR, irhoL, irhoR (rhoL, uL, pL, rhoR sit in the flux slot)
-  unsigned short qid[NXF + NYF];
+// Tile shape TX x TY: the shared-memory regions of one tile.  The default
+// 32 x 8 (FLUX_TX x FLUX_TY) is the one the overlapped schedule's tile
+// marking assumes; 16 x 16 and 64 x 4 are the autotuner's alternatives.
+template <int TX, int TY>
+struct FluxShape {
+  static constexpr int WR = TY + 4;   // primitive region rows   (i0-2 .. i0+TY+1)
+  static constexpr int WC = TX + 4;   // primitive region columns (j0-2 .. j0+TX+1)
+  static constexpr int SR = TY + 2;   // face-state cells rows    (i0-1 .. i0+TY)
+  static constexpr int SC = TX + 2;   // face-state cells columns (j0-1 .. j0+TX)
+  static constexpr int NXF = TY * (TX + 1);
+  static constexpr int NYF = (TY + 1) * TX;
+  struct Smem {
+    double w[4][WR][WC];          // primitives (MUSCL) or conserved (Godunov)
+    double irho[WR][WC];          // MUSCL: 1/rho of the conversion, reused by the cell's face states
+    double fs[4][4][SR][SC];      // [face L,R,B,T][component][r][c]
+    double fx[4][TY][TX + 1];
+    double fy[4][TY + 1][TX];
+    double qd[6][NXF + NYF];      // queued faces: uR, pR, utL, utR, irhoL, irhoR (rhoL, uL, pL, rhoR sit in the flux slot)
+    unsigned short qid[NXF + NYF];
+  };
 };
 
 struct FluxArgs {
@@ -55,13 +60,16 @@ struct FluxArgs {
   int tiles;              // TILES_ALL, TILES_FAR or TILES_NEAR
 };
 
-__device__ __forceinline__ V4 sW(const FluxSmem& s, int r, int c) {
+template <class S>
+__device__ __forceinline__ V4 sW(const S& s, int r, int c) {
   return V4{s.w[0][r][c], s.w[1][r][c], s.w[2][r][c], s.w[3][r][c]};
 }
-__device__ __forceinline__ V4 sFS(const FluxSmem& s, int f, int r, int c) {
+template <class S>
+__device__ __forceinline__ V4 sFS(const S& s, int f, int r, int c) {
   return V4{s.fs[f][0][r][c], s.fs[f][1][r][c], s.fs[f][2][r][c], s.fs[f][3][r][c]};
 }
-__device__ __forceinline__ void putFS(FluxSmem& s, int f, int r, int c, const V4& v) {
+template <class S>
+__device__ __forceinline__ void putFS(S& s, int f, int r, int c, const V4& v) {
   s.fs[f][0][r][c] = v.a; s.fs[f][1][r][c] = v.b; s.fs[f][2][r][c] = v.c; s.fs[f][3][r][c] = v.d;
 }
 __device__ __forceinline__ V4 v4sub(const V4& x, const V4& y) { return V4{x.a - y.a, x.b - y.b, x.c - y.c, x.d - y.d}; }
@@ -136,21 +144,25 @@ __device__ __forceinline__ V4 muscl_face_flux(bool xdir, V4 Sr, V4 Sl, const V4&
   return pure_rs_flux(xdir, gas, UL, UR, st, iters);
 }
 
-template <bool MUSCL>
-__global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FluxSmem& s = *reinterpret_cast<FluxSmem*>(smem_raw);
+// One tile (bx, by) of fluid slot bz of the grid a, whose tile rows are gx
+// tiles wide, by the whole CTA (NT threads); the CTA's dynamic shared memory
+// holds the tile's Smem.
+template <bool MUSCL, int TX, int TY>
+__device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int bz, int gx, unsigned char* smem_raw) {
+  using Sh = FluxShape<TX, TY>;
+  constexpr int WR = Sh::WR, WC = Sh::WC, SR = Sh::SR, SC = Sh::SC, NXF = Sh::NXF, NYF = Sh::NYF;
+  typename Sh::Smem& s = *reinterpret_cast<typename Sh::Smem*>(smem_raw);
   __shared__ V4 s_uniform_flux[2];
   __shared__ int s_nq, s_nt;   // queued faces with waves and without (phase 3)
   const GridP& P = a.P;
-  const int fluid = a.fluid_base + blockIdx.z;
-  const double* __restrict__ U = a.U[blockIdx.z];
-  double* __restrict__ Unew = a.Unew[blockIdx.z];
+  const int fluid = a.fluid_base + bz;
+  const double* __restrict__ U = a.U[bz];
+  double* __restrict__ Unew = a.Unew[bz];
   const Gas& gas = fluid == 0 ? P.gas1 : P.gas2;
   const double gam = gas.g;
   const double pinf = gas.pinf;
-  const int i0 = P.g + blockIdx.y * TY;
-  const int j0 = P.g + blockIdx.x * TX;
+  const int i0 = P.g + by * TY;
+  const int j0 = P.g + bx * TX;
   const int tid = threadIdx.x;
   const bool active = a.dtime->active != 0;
   const int* rc = &a.dtime->rc[4 * fluid];
@@ -158,7 +170,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
 
   if (!active) return;   // the step after t reaches T changes nothing
   if (a.tiles != TILES_ALL) {
-    const bool near = a.tile_near[blockIdx.y * gridDim.x + blockIdx.x] != 0;
+    const bool near = a.tile_near[by * gx + bx] != 0;
     if ((a.tiles == TILES_NEAR) != near) return;   // the other pass owns this tile
   }
   // tile outside the realcells box: its cells keep their values
@@ -326,18 +338,82 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
   }
 }
 
-static size_t flux_smem() { return sizeof(FluxSmem); }
+template <bool MUSCL, int TX, int TY>
+__global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  flux_tile<MUSCL, TX, TY>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, smem_raw);
+}
+
+// The flux update of many grids in one persistent launch (a batch's phased
+// schedule): each CTA takes (instance, fluid, tile) work items in list order
+// from a counter -- the list holds the costliest instances first, so the
+// uneven grids finish together -- copies the instance's arguments into
+// shared memory and runs the tile.  The last CTA to finish resets the
+// counters for the next launch (stream-ordered, so a replayed graph finds
+// them at zero).  Item: instance << 24 | fluid slot << 23 | tile.
+template <bool MUSCL, int TX, int TY>
+__global__ void __launch_bounds__(NT, 2) k_flux_batch(const FluxArgs* __restrict__ args,
+                                                       const uint32_t* __restrict__ items, int n_items,
+                                                       unsigned int* counters) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ FluxArgs s_args;
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(&counters[0], 1u);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const uint32_t w = items[it];
+    const int inst = (int)(w >> 24), bz = (int)((w >> 23) & 1u), tile = (int)(w & 0x7fffffu);
+    {
+      const int* src = reinterpret_cast<const int*>(args + inst);
+      int* dst = reinterpret_cast<int*>(&s_args);
+      for (int q = threadIdx.x; q < (int)(sizeof(FluxArgs) / sizeof(int)); q += NT) dst[q] = src[q];
+    }
+    __syncthreads();
+    const int gx = (s_args.P.Nx + TX - 1) / TX;
+    flux_tile<MUSCL, TX, TY>(s_args, tile % gx, tile / gx, bz, gx, smem_raw);
+    __syncthreads();   // the next item reuses the shared memory
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&counters[1], 1u) == gridDim.x - 1) {
+      counters[0] = 0u;
+      counters[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+template <int TX, int TY>
+static size_t flux_smem() { return sizeof(typename FluxShape<TX, TY>::Smem); }
+
+// the tile shapes a flux update can take (FLUX_SHAPE_*)
+template <bool MUSCL>
+static void set_flux_attributes() {
+  cudaFuncSetAttribute(k_flux_update<MUSCL, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<32, 8>());
+  cudaFuncSetAttribute(k_flux_update<MUSCL, 16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)flux_smem<16, 16>());
+  cudaFuncSetAttribute(k_flux_update<MUSCL, 64, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<64, 4>());
+  cudaFuncSetAttribute(k_flux_batch<MUSCL, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<32, 8>());
+  cudaFuncSetAttribute(k_flux_batch<MUSCL, 16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)flux_smem<16, 16>());
+  cudaFuncSetAttribute(k_flux_batch<MUSCL, 64, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<64, 4>());
+}
 
 // Kernel attributes, set once per process before any launch (and so before
 // any stream capture).
 void prepare_kernels() {
   static std::once_flag once;
   std::call_once(once, [] {
-    cudaFuncSetAttribute(k_flux_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem());
-    cudaFuncSetAttribute(k_flux_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem());
+    set_flux_attributes<true>();
+    set_flux_attributes<false>();
   });
   prepare_step_kernels();
 }
+
+int flux_tile_w(int shape) { return shape == FLUX_SHAPE_16x16 ? 16 : (shape == FLUX_SHAPE_64x4 ? 64 : 32); }
+int flux_tile_h(int shape) { return shape == FLUX_SHAPE_16x16 ? 16 : (shape == FLUX_SHAPE_64x4 ? 4 : 8); }
 
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
   launch_fs_update_sel(ctx, fs, fluid_mask, TILES_ALL, ctx->stream);
@@ -359,15 +435,86 @@ void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaS
     a.Unew[nz] = ctx->Unew[f];
     nz++;
   }
-  dim3 grid((P.Nx + TX - 1) / TX, (P.Ny + TY - 1) / TY, nz);
-  size_t sm = flux_smem();
   prepare_kernels();
-  if (fs == GFM_FS_MUSCL)
-    k_flux_update<true><<<grid, NT, sm, stream>>>(a);
-  else
-    k_flux_update<false><<<grid, NT, sm, stream>>>(a);
+  // the overlapped schedule's passes use the tile grid its marking assumes
+  const int shape = tiles == TILES_ALL ? ctx->flux_shape : FLUX_SHAPE_32x8;
+  const int tw = flux_tile_w(shape), th = flux_tile_h(shape);
+  dim3 grid((P.Nx + tw - 1) / tw, (P.Ny + th - 1) / th, nz);
+  const bool mu = fs == GFM_FS_MUSCL;
+  if (shape == FLUX_SHAPE_16x16) {
+    if (mu) k_flux_update<true, 16, 16><<<grid, NT, flux_smem<16, 16>(), stream>>>(a);
+    else k_flux_update<false, 16, 16><<<grid, NT, flux_smem<16, 16>(), stream>>>(a);
+  } else if (shape == FLUX_SHAPE_64x4) {
+    if (mu) k_flux_update<true, 64, 4><<<grid, NT, flux_smem<64, 4>(), stream>>>(a);
+    else k_flux_update<false, 64, 4><<<grid, NT, flux_smem<64, 4>(), stream>>>(a);
+  } else {
+    if (mu) k_flux_update<true, 32, 8><<<grid, NT, flux_smem<32, 8>(), stream>>>(a);
+    else k_flux_update<false, 32, 8><<<grid, NT, flux_smem<32, 8>(), stream>>>(a);
+  }
   counted();
   // the new values are in Unew; launch_commit copies them (with the BCs) to U
+}
+
+// The arguments of one instance's flux update of both fluids (the work
+// items of k_flux_batch carry the fluid slot).
+void flux_batch_args(const gfm_ctx* ctx, void* out) {
+  FluxArgs a;
+  memset(&a, 0, sizeof(a));
+  a.P = ctx->P;
+  a.dtime = ctx->dtime;
+  a.dtime_w = ctx->dtime;
+  a.tile_near = nullptr;
+  a.tiles = TILES_ALL;
+  a.fluid_base = 0;
+  const int nf = ctx->two_fluid ? 2 : 1;
+  for (int f = 0; f < nf; f++) {
+    a.U[f] = ctx->U[f];
+    a.Unew[f] = ctx->Unew[f];
+  }
+  memcpy(out, &a, sizeof(a));
+}
+size_t flux_batch_args_size() { return sizeof(FluxArgs); }
+
+void launch_flux_batch(int fs, int shape, const void* args, const uint32_t* items, int n_items,
+                       unsigned int* counters, int ctas, cudaStream_t stream) {
+  prepare_kernels();
+  const bool mu = fs == GFM_FS_MUSCL;
+  const FluxArgs* A = static_cast<const FluxArgs*>(args);
+  if (shape == FLUX_SHAPE_16x16) {
+    if (mu) k_flux_batch<true, 16, 16><<<ctas, NT, flux_smem<16, 16>(), stream>>>(A, items, n_items, counters);
+    else k_flux_batch<false, 16, 16><<<ctas, NT, flux_smem<16, 16>(), stream>>>(A, items, n_items, counters);
+  } else if (shape == FLUX_SHAPE_64x4) {
+    if (mu) k_flux_batch<true, 64, 4><<<ctas, NT, flux_smem<64, 4>(), stream>>>(A, items, n_items, counters);
+    else k_flux_batch<false, 64, 4><<<ctas, NT, flux_smem<64, 4>(), stream>>>(A, items, n_items, counters);
+  } else {
+    if (mu) k_flux_batch<true, 32, 8><<<ctas, NT, flux_smem<32, 8>(), stream>>>(A, items, n_items, counters);
+    else k_flux_batch<false, 32, 8><<<ctas, NT, flux_smem<32, 8>(), stream>>>(A, items, n_items, counters);
+  }
+  counted();
+}
+
+// resident CTAs per SM of the batched flux kernel of a shape
+int flux_batch_occupancy(int fs, int shape) {
+  prepare_kernels();
+  int per = 0;
+  const bool mu = fs == GFM_FS_MUSCL;
+  const void* k;
+  size_t sm;
+  if (shape == FLUX_SHAPE_16x16) {
+    k = mu ? (const void*)k_flux_batch<true, 16, 16> : (const void*)k_flux_batch<false, 16, 16>;
+    sm = flux_smem<16, 16>();
+  } else if (shape == FLUX_SHAPE_64x4) {
+    k = mu ? (const void*)k_flux_batch<true, 64, 4> : (const void*)k_flux_batch<false, 64, 4>;
+    sm = flux_smem<64, 4>();
+  } else {
+    k = mu ? (const void*)k_flux_batch<true, 32, 8> : (const void*)k_flux_batch<false, 32, 8>;
+    sm = flux_smem<32, 8>();
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, sm) != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return per;
 }
 
 }  // namespace gfm

@@ -86,6 +86,7 @@ struct gfm_ctx {
   int itm;           // interface tracker of the last method used (GFM_ITM_*)
   int* ifc_opp;      // real GFM: opposite cell
   long long ifc_spin_limit;  // polls before an interface-loop wait gives up (0: the default)
+  int flux_shape;    // tile shape of the flux update (FLUX_SHAPE_*; the overlapped passes use 32 x 8)
   int ifc_withhold;  // test hook: 1 + the interface-list entry left unsolved (0: none)
   gfm::DevTime* dtime;
   gfm::DevTime* h_dtime;  // pinned host mirror
@@ -175,6 +176,18 @@ inline int flux_tiles_y(const GridP& P) { return (P.Ny + FLUX_TY - 1) / FLUX_TY;
 
 // tile selection of the flux update
 enum { TILES_ALL = 0, TILES_FAR = 1, TILES_NEAR = 2 };
+// tile shapes of the flux update (gfm_ctx::flux_shape)
+enum { FLUX_SHAPE_32x8 = 0, FLUX_SHAPE_16x16 = 1, FLUX_SHAPE_64x4 = 2, FLUX_SHAPES = 3 };
+int flux_tile_w(int shape);
+int flux_tile_h(int shape);
+// the persistent flux update of a batch (k_flux_batch): per-instance
+// arguments (flux_batch_args_size() bytes each, filled by flux_batch_args),
+// work items instance << 24 | fluid slot << 23 | tile, two counters at zero
+void flux_batch_args(const gfm_ctx* ctx, void* out);
+size_t flux_batch_args_size();
+void launch_flux_batch(int fs, int shape, const void* args, const uint32_t* items, int n_items,
+                       unsigned int* counters, int ctas, cudaStream_t stream);
+int flux_batch_occupancy(int fs, int shape);
 
 // kernel launch helpers (defined in the .cu files)
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask);
@@ -198,6 +211,9 @@ const uint32_t* mlp_frag(const struct gfm_mlp* m);  // its B fragments for mlp_f
 void launch_mlp_frag_pack(const struct gfm_mlp* m, cudaStream_t s);   // refresh them from the parameters
 // nsteps iterations of the time loop on ctx's stream (gfm_step, gfm_step_timed)
 gfm_status_t run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, double* phase_ms);
+// one-stream step split around the flux update (a batch's phased schedule)
+gfm_status_t step_front(gfm_ctx* ctx, const gfm_method_desc* m);
+gfm_status_t step_back(gfm_ctx* ctx, const gfm_method_desc* m);
 gfm_status_t validate_method(gfm_ctx* ctx, const gfm_method_desc* m);
 double* mass_scratch(gfm_ctx* ctx);   // 256 + 1 doubles of the mass reduction
 gfm_status_t launch_status();   // GFM_ERR_CUDA (and a message) if a launch failed

@@ -96,6 +96,9 @@ def lib():
         "gfm_step": [P, ctypes.POINTER(MethodDesc), I],
         "gfm_step_timed": [P, ctypes.POINTER(MethodDesc), I, pd],
         "gfm_set_overlap": [P, I],
+        "gfm_set_flux_tile": [P, I],
+        "gfm_batch_set_schedule": [P, I],
+        "gfm_batch_autotune": [P, ctypes.POINTER(MethodDesc), I, ctypes.c_char_p, I],
         "gfm_set_newton_limit": [P, I],
         "gfm_set_interface_wait": [P, ctypes.c_int64, I],
         "gfm_fp64_peak": [pd, V],
@@ -345,6 +348,12 @@ class Context:
         _check(rc, "gfm_set_overlap")
         return True
 
+    def set_flux_tile(self, shape):
+        """Tile shape of the flux update: "32x8" (default), "16x16" or "64x4"
+        (results are identical)."""
+        code = {"32x8": 0, "16x16": 1, "64x4": 2}[shape]
+        _check(lib().gfm_set_flux_tile(self._p, code), "gfm_set_flux_tile")
+
     def set_newton_limit(self, max_iterations):
         """Newton iteration limit of the exact Riemann solves (default 60);
         a solve that reaches it sets GFM_ST_NEWTON_NO_CONVERGE."""
@@ -423,6 +432,21 @@ class Batch:
 
     def synchronize(self):
         _check(lib().gfm_batch_synchronize(self._p), "gfm_batch_synchronize")
+
+    def set_schedule(self, schedule):
+        """"streams" (each instance's step on its own stream, the default) or
+        "phased" (one persistent flux launch over all instances per step)."""
+        _check(lib().gfm_batch_set_schedule(self._p, {"streams": 0, "phased": 1}[schedule]),
+               "gfm_batch_set_schedule")
+
+    def autotune(self, m, steps=16):
+        """Times the flux tile shapes per grid-size class and the two
+        schedules on the batch's current state (restored afterwards), keeps
+        the fastest; returns the report."""
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        _check(lib().gfm_batch_autotune(self._p, ctypes.byref(m), int(steps), buf, len(buf)), "gfm_batch_autotune")
+        return json.loads(buf.value.decode())
 
     def close(self):
         for c in getattr(self, "instances", []):

@@ -95,3 +95,100 @@ def test_batch_vof_graph_matches_single():
         single.close()
         for a, c in zip(outs[k], S):
             assert np.array_equal(a, c), "VOF instance %d differs from its single run" % k
+
+
+@pytest.mark.parametrize("shape", ["32x8", "16x16", "64x4"])
+def test_flux_tile_shapes_match_oracle(shape):
+    """Every tile shape of the flux update gives the oracle's bits (each face
+    flux is formed once and each cell sums its faces in the reference's
+    order, whatever the tiling)."""
+    desc, T = g.case_params("twofluid", "shock_bubble", 80, 32)
+    U1, U2, phi = g.case_init("twofluid", "shock_bubble", desc)
+    for fs in ("MUSCL", "Godunov"):
+        m = g.method(fs=fs, gfm="riemannGFM", CFL=0.6, T=T)
+        ctx = g.Context(desc, two_fluid=True)
+        ctx.set_overlap("off")
+        ctx.set_flux_tile(shape)
+        ctx.upload(U1, U2, phi)
+        ctx.step(m, 12)
+        G = ctx.download()
+        st = ctx.status()
+        ctx.close()
+        ref = orc.twofluid_run(desc, m, U1, U2, phi, 12)
+        assert st == 0
+        assert np.array_equal(G[0], ref["U1"]) and np.array_equal(G[1], ref["U2"]) and np.array_equal(G[2], ref["phi"])
+    d1, T1 = g.case_params("onefluid", "circularexplosion", 72, 40)
+    U, _, _ = g.case_init("onefluid", "circularexplosion", d1)
+    m1 = g.method(fs="MUSCL", CFL=0.8, T=T1)
+    c1 = g.Context(d1, two_fluid=False)
+    c1.set_flux_tile(shape)
+    c1.upload(U)
+    c1.step(m1, 15)
+    G1, _, _ = c1.download()
+    c1.close()
+    R, _, _, _ = orc.onefluid_run(d1, m1, U, 15)
+    assert np.array_equal(G1, R)
+
+
+@pytest.mark.parametrize("reinit_every,nsteps", [(1, 12), (3, 21)])
+def test_phased_batch_matches_single(reinit_every, nsteps):
+    """The phased schedule (every instance up to its flux update, one
+    persistent flux launch per tile shape over all instances, every
+    instance's commit), recorded into a graph for 8 steps and issued directly
+    for the rest, with mixed tile shapes: each instance ends bit-identical to
+    the same instance stepped alone."""
+    cases = members()
+    m = g.method(gfm="riemannGFM", CFL=0.6, T=1.0, reinit_every=reinit_every)
+    b = g.Batch([c[0] for c in cases], two_fluid=True)
+    b.set_schedule("phased")
+    for ctx, shape, (d, T, U1, U2, phi) in zip(b.instances, ["16x16", "64x4", "32x8"], cases):
+        ctx.set_flux_tile(shape)
+        ctx.upload(U1, U2, phi)
+    b.step(m, nsteps, graph=True)
+    b.synchronize()
+    outs = [ctx.download() for ctx in b.instances]
+    stats = [ctx.status() for ctx in b.instances]
+    times = [ctx.time()[:2] for ctx in b.instances]
+    b.close()
+    for k, (d, T, U1, U2, phi) in enumerate(cases):
+        single = g.Context(d, two_fluid=True)
+        single.upload(U1, U2, phi)
+        single.step(m, nsteps)
+        S = single.download()
+        ts = single.time()[:2]
+        single.close()
+        assert stats[k] == 0 and times[k] == ts
+        for a, c in zip(outs[k], S):
+            assert np.array_equal(a, c), "instance %d differs from its single run" % k
+
+
+def test_autotune_keeps_the_state_and_the_results():
+    """gfm_batch_autotune times tile shapes per size class and the two
+    schedules on the batch's state, restores it, and keeps the fastest: the
+    run continues bit-identically to an untuned one."""
+    cases = members()
+    m = g.method(gfm="riemannGFM", CFL=0.6, T=1.0)
+    b = g.Batch([c[0] for c in cases], two_fluid=True)
+    for ctx, (d, T, U1, U2, phi) in zip(b.instances, cases):
+        ctx.upload(U1, U2, phi)
+    b.step(m, 3, graph=False)
+    report = b.autotune(m, steps=8)
+    b.step(m, 9, graph=True)
+    b.synchronize()
+    outs = [ctx.download() for ctx in b.instances]
+    times = [ctx.time()[:2] for ctx in b.instances]
+    b.close()
+    assert report["schedule"] in ("streams", "phased") and report["steps"] == 8
+    assert len(report["classes"]) >= 1
+    for c in report["classes"]:
+        assert c["tile"] in ("32x8", "16x16", "64x4") and min(c["ms_per_step"].values()) > 0
+    for k, (d, T, U1, U2, phi) in enumerate(cases):
+        single = g.Context(d, two_fluid=True)
+        single.upload(U1, U2, phi)
+        single.step(m, 12)
+        S = single.download()
+        ts = single.time()[:2]
+        single.close()
+        assert times[k] == ts
+        for a, c in zip(outs[k], S):
+            assert np.array_equal(a, c), "instance %d differs after tuning" % k
