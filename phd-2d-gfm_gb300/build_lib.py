@@ -29,7 +29,7 @@ ORACLE_LIBDIR = os.path.join(ORACLE, "lib", MACHINE)
 CU_SOURCES = ["gfm_flux.cu", "gfm_step.cu", "gfm_api.cu", "gfm_noalloc.cu", "gfm_batch.cu", "gfm_mlp.cu",
               "gfm_output.cu", "gfm_cases_dev.cu"]
 CPP_SOURCES = ["gfm_cases.cpp", "gfm_classes.cpp"]
-HEADERS = ["gfm_math.cuh", "gfm_internal.cuh", "gfm_tables.h", "gfm_mlp.cuh", "gfm_cases.cuh"]
+HEADERS = ["gfm_math.cuh", "gfm_xfp64.cuh", "gfm_internal.cuh", "gfm_tables.h", "gfm_mlp.cuh", "gfm_cases.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off"]

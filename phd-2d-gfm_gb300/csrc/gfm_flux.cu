@@ -19,6 +19,18 @@
 //            idle lanes and no warp runs both kinds.
 //   phase 4  per cell: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn, the
 //            accumulation order of the reference's face loop (:290-292).
+//
+// Built with GFM_FLUX_INT_MUL defined, the kernel's products (mulx) are
+// formed in integer arithmetic (xmul, gfm_xfp64.cuh: the same bits) instead
+// of on the FP64 pipe.  Off by default: measured on the 1000 x 400
+// shock-bubble, the launch takes 2.19 ms that way against 1.69 ms with FP64
+// multiplies -- each integer product costs about 77 issue cycles of the
+// integer pipes, which this kernel already loads, against the 64-cycle FP64
+// slot it frees, and its 4 warps per sub-partition do not hide the 208-cycle
+// latency.
+#ifdef GFM_FLUX_INT_MUL
+#define GFM_INT_MUL 1
+#endif
 #include "gfm_internal.cuh"
 #include <cstring>
 #include <mutex>
@@ -77,13 +89,15 @@ __device__ __forceinline__ V4 v4sub(const V4& x, const V4& y) { return V4{x.a - 
 // (s A(W)) d, quasilinear_form_A (headers/euler_misc.hpp:149-163), non-zero
 // terms; irho = 1/rho and rcc = rho c c are the matrix entries A(1,3), A(3,1).
 __device__ __forceinline__ V4 A_times(double s, const V4& W, double irho, double rcc, const V4& d) {
-  double su = s * W.b;
-  return V4{su * d.a + (s * W.a) * d.b, su * d.b + (s * irho) * d.d, su * d.c, (s * rcc) * d.b + su * d.d};
+  double su = mulx(s, W.b);
+  return V4{mulx(su, d.a) + mulx(mulx(s, W.a), d.b), mulx(su, d.b) + mulx(mulx(s, irho), d.d), mulx(su, d.c),
+            mulx(mulx(s, rcc), d.b) + mulx(su, d.d)};
 }
 // (s B(W)) d, quasilinear_form_B (headers/euler_misc.hpp:166-180)
 __device__ __forceinline__ V4 B_times(double s, const V4& W, double irho, double rcc, const V4& d) {
-  double sv = s * W.c;
-  return V4{sv * d.a + (s * W.a) * d.c, sv * d.b, sv * d.c + (s * irho) * d.d, (s * rcc) * d.c + sv * d.d};
+  double sv = mulx(s, W.c);
+  return V4{mulx(sv, d.a) + mulx(mulx(s, W.a), d.c), mulx(sv, d.b), mulx(sv, d.c) + mulx(mulx(s, irho), d.d),
+            mulx(mulx(s, rcc), d.c) + mulx(sv, d.d)};
 }
 
 // Phase 2 for one cell: minmod slopes (FS_MUSCL.cpp:189-196), boundary
@@ -97,10 +111,12 @@ __device__ __forceinline__ void cell_face_states(const V4& W, double irho_W, con
   V4 dyL = v4sub(W, Ws), dyR = v4sub(Wn, W);
   V4 sxv = V4{minmod(dxL.a, dxR.a), minmod(dxL.b, dxR.b), minmod(dxL.c, dxR.c), minmod(dxL.d, dxR.d)};
   V4 syv = V4{minmod(dyL.a, dyR.a), minmod(dyL.b, dyR.b), minmod(dyL.c, dyR.c), minmod(dyL.d, dyR.d)};
-  V4 L = V4{W.a - 0.5 * sxv.a, W.b - 0.5 * sxv.b, W.c - 0.5 * sxv.c, W.d - 0.5 * sxv.d};
-  V4 R = V4{W.a + 0.5 * sxv.a, W.b + 0.5 * sxv.b, W.c + 0.5 * sxv.c, W.d + 0.5 * sxv.d};
-  V4 B = V4{W.a - 0.5 * syv.a, W.b - 0.5 * syv.b, W.c - 0.5 * syv.c, W.d - 0.5 * syv.d};
-  V4 T = V4{W.a + 0.5 * syv.a, W.b + 0.5 * syv.b, W.c + 0.5 * syv.c, W.d + 0.5 * syv.d};
+  const V4 hx = V4{mulx(0.5, sxv.a), mulx(0.5, sxv.b), mulx(0.5, sxv.c), mulx(0.5, sxv.d)};
+  const V4 hy = V4{mulx(0.5, syv.a), mulx(0.5, syv.b), mulx(0.5, syv.c), mulx(0.5, syv.d)};
+  V4 L = V4{W.a - hx.a, W.b - hx.b, W.c - hx.c, W.d - hx.d};
+  V4 R = V4{W.a + hx.a, W.b + hx.b, W.c + hx.c, W.d + hx.d};
+  V4 B = V4{W.a - hy.a, W.b - hy.b, W.c - hy.c, W.d - hy.d};
+  V4 T = V4{W.a + hy.a, W.b + hy.b, W.c + hy.c, W.d + hy.d};
   if (!is_physical_primitives_fast(gam, pinf, L) || !is_physical_primitives_fast(gam, pinf, R)) { L = W; R = W; }
   if (!is_physical_primitives_fast(gam, pinf, B) || !is_physical_primitives_fast(gam, pinf, T)) { B = W; T = W; }
   // 1/rho from the cell's conversion (the correctly rounded quotient, as
@@ -108,7 +124,7 @@ __device__ __forceinline__ void cell_face_states(const V4& W, double irho_W, con
   Recip Rr;
   Rr.b = W.a; Rr.y = irho_W; Rr.fast = mid_range(W.a);
   double cs = eos_soundspeed_r(gam, pinf, W.d, Rr);
-  double irho = Rr.y, rcc = W.a * cs * cs;   // irho = 1.0 / W.a
+  double irho = Rr.y, rcc = mulx(mulx(W.a, cs), cs);   // irho = 1.0 / W.a
   V4 X = A_times(sx, W, irho, rcc, v4sub(L, R));
   V4 Y = B_times(sy, W, irho, rcc, v4sub(B, T));
   out[0] = V4{(L.a + X.a) + Y.a, (L.b + X.b) + Y.b, (L.c + X.c) + Y.c, (L.d + X.d) + Y.d};
@@ -319,9 +335,9 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
         double fe = uniform ? ux[q] : s.fx[q][r][c + 1];
         double fs_ = uniform ? uy[q] : s.fy[q][r][c];
         double fn = uniform ? uy[q] : s.fy[q][r + 1][c];
-        double v = o[q] + (dtodx * fw + dtody * fs_);
-        v = v - dtodx * fe;
-        v = v - dtody * fn;
+        double v = o[q] + (mulx(dtodx, fw) + mulx(dtody, fs_));
+        v = v - mulx(dtodx, fe);
+        v = v - mulx(dtody, fn);
         o[q] = v;
       }
       u = V4{o[0], o[1], o[2], o[3]};

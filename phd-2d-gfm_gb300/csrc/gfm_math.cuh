@@ -25,6 +25,7 @@
 #include <string.h>
 #include <math.h>
 #include "gfm_tables.h"
+#include "gfm_xfp64.cuh"
 
 #if defined(__CUDACC__)
 #define GFM_HD __host__ __device__ __forceinline__
@@ -33,6 +34,43 @@
 #endif
 
 namespace gfm {
+
+// The products of the functions below.  In the device code of a translation
+// unit compiled with GFM_INT_MUL defined (the throughput-bound flux update)
+// they are formed on the integer pipes (xmul, gfm_xfp64.cuh: the same bits
+// as the FP64 multiply, for a third of the FP64 pipe's work); everywhere else,
+// the host included, they are the FP64 multiply itself.
+#if defined(__CUDA_ARCH__) && defined(GFM_INT_MUL)
+GFM_HD double mulx(double a, double b) { return xmul(a, b); }
+#else
+GFM_HD double mulx(double a, double b) { return a * b; }
+#endif
+
+// The quotients and square roots of the functions below.  In device code
+// they are formed in integer arithmetic (xdiv, xsqrt: the correctly rounded
+// result, so the same bits as the FP64 division and square root), which
+// takes none of the FP64 pipe's time: 2.4 (division) and 3.1 (square root)
+// times the FP64 operations' throughput on GB300, where the FP64 pipe bounds
+// every full-grid kernel here.  GFM_FP64_DIV selects the FP64 operations
+// everywhere; the host always uses them.
+// The functions that divide or take roots carry the choice as their template
+// argument ID (true: integer arithmetic); the latency-bound interface loop,
+// where a dependent integer quotient (about 510 cycles) saves little over the
+// FP64 one (560) and its longer code costs more, instantiates them with false.
+template <bool ID = true>
+GFM_HD double divx(double a, double b) {
+#if defined(__CUDA_ARCH__) && !defined(GFM_FP64_DIV)
+  if (ID) return xdiv(a, b);
+#endif
+  return a / b;
+}
+template <bool ID = true>
+GFM_HD double sqrtx(double x) {
+#if defined(__CUDA_ARCH__) && !defined(GFM_FP64_DIV)
+  if (ID) return xsqrt(x);
+#endif
+  return sqrt(x);
+}
 
 // ---------------------------------------------------------------------------
 // Status bits written by kernels (never __trap or assert on the device).
@@ -206,21 +244,22 @@ GFM_HD bool mid_range(double x) {   // 2^-500 <= |x| < 2^500 (exponent field 523
   const int e = (int)((as_bits(x) >> 52) & 0x7ff);
   return e >= 523 && e < 1523;
 }
+template <bool ID = true>
 GFM_HD Recip recip(double b) {
   Recip r;
   r.b = b;
-  r.y = 1.0 / b;
+  r.y = divx<ID>(1.0, b);
   r.fast = mid_range(b);
   return r;
 }
 GFM_HD double i_rdiv(double a, const Recip& R) {
   if (R.fast && mid_range(a)) {
-    const double q = a * R.y;
+    const double q = mulx(a, R.y);
     const double rem = fma(-R.b, q, a);
     return fma(rem, R.y, q);
   }
   if (R.fast && (as_bits(a) & GFM_MAG_BITS) == 0) return a * R.y;   // signed zero
-  return a / R.b;
+  return divx(a, R.b);
 }
 #if defined(__CUDA_ARCH__)
 GFM_HD double rdiv(double a, const Recip& R) { return i_rdiv(a, R); }
@@ -259,7 +298,7 @@ GFM_HD double gfm_exp(double x) {
   p = fma(p, r, 0x1.5555555555555p-5);
   p = fma(p, r, 0x1.5555555555555p-3);
   p = fma(p, r, 0.5);
-  const double q = fma(r * r, p, r);
+  const double q = fma(mulx(r, r), p, r);
   const double tj = tab_exp2(k & 63);
   const double y = fma(tj, q, tj);
   const int m = k >> 6;   // floor(n / 64)
@@ -302,13 +341,13 @@ GFM_HD double gfm_log(double x) {
     fbits = 0x3ff0000000000000LL + ((int64_t)j << 45);
   }
   const double f = from_bits(mbits) - from_bits(fbits);
-  const double r = f * tab_invf(j + 32);
+  const double r = mulx(f, tab_invf(j + 32));
   double a = fma(r, 0x1.2492492492492p-3, -0x1.5555555555555p-3);
   a = fma(a, r, 0x1.999999999999ap-3);
   a = fma(a, r, -0.25);
   a = fma(a, r, 0x1.5555555555555p-2);
   a = fma(a, r, -0.5);
-  const double p = (r * r) * a;
+  const double p = mulx(mulx(r, r), a);
   const double ed = (double)e;
   const double hi = fma(ed, GFM_LN2_HI, tab_logf(j + 32));   // exact product
   const double lo = fma(ed, GFM_LN2_LO, p);
@@ -318,7 +357,7 @@ GFM_HD double gfm_log(double x) {
 // pow for x >= 0 (all uses have a positive base): exp(y log x); pow(1,y) == 1.
 GFM_HD double gfm_pow(double x, double y) {
   if ((as_bits(x) & GFM_MAG_BITS) == 0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : gfm_inf());
-  return gfm_exp(y * gfm_log(x));
+  return gfm_exp(mulx(y, gfm_log(x)));
 }
 
 // asin on [-0.5, 0.5] by its Taylor series (28 terms), in Horner form in x^2.
@@ -330,9 +369,10 @@ GFM_HD double gfm_asin_small(double x) {
 }
 
 // acos on [-1, 1]: series for |x| <= 0.5, half-angle reduction otherwise.
+template <bool ID = true>
 GFM_HD double gfm_acos(double x) {
-  if (x > 0.5) return 2.0 * gfm_asin_small(sqrt((1.0 - x) * 0.5));
-  if (x < -0.5) return GFM_PI - 2.0 * gfm_asin_small(sqrt((1.0 + x) * 0.5));
+  if (x > 0.5) return 2.0 * gfm_asin_small(sqrtx<ID>((1.0 - x) * 0.5));
+  if (x < -0.5) return GFM_PI - 2.0 * gfm_asin_small(sqrtx<ID>((1.0 + x) * 0.5));
   return GFM_PI_2 - gfm_asin_small(x);
 }
 
@@ -340,20 +380,24 @@ GFM_HD double gfm_acos(double x) {
 // Stiffened-gas EOS: p = (g-1) rho e - g pinf
 // ---------------------------------------------------------------------------
 GFM_HD double eos_pressure(double g, double pinf, double e, double rho) {
-  return (g - 1.0) * rho * e - g * pinf;
+  return mulx(mulx(g - 1.0, rho), e) - mulx(g, pinf);
 }
+template <bool ID = true>
 GFM_HD double eos_specific_ie(double g, double pinf, double p, double rho) {
-  return (p + g * pinf) / ((g - 1.0) * rho);
+  return divx<ID>(p + mulx(g, pinf), mulx(g - 1.0, rho));
 }
+template <bool ID = true>
 GFM_HD double eos_soundspeed(double g, double pinf, double p, double rho) {
-  return sqrt(g * (p + pinf) / rho);
+  return sqrtx<ID>(divx<ID>(g * (p + pinf), rho));
 }
 // the same with a reciprocal of rho at hand
+template <bool ID = true>
 GFM_HD double eos_soundspeed_r(double g, double pinf, double p, const Recip& R) {
-  return sqrt(rdiv(g * (p + pinf), R));
+  return sqrtx<ID>(rdiv(mulx(g, p + pinf), R));
 }
+template <bool ID = true>
 GFM_HD double eos_isentropic_extrapolation(double g, double pinf, double rho1, double p1, double p2) {
-  return rho1 * gfm_pow((p2 + pinf) / (p1 + pinf), 1.0 / g);
+  return rho1 * gfm_pow(divx<ID>(p2 + pinf, p1 + pinf), divx<ID>(1.0, g));
 }
 
 // ---------------------------------------------------------------------------
@@ -363,63 +407,69 @@ GFM_HD double eos_isentropic_extrapolation(double g, double pinf, double rho1, d
 struct V4 { double a, b, c, d; };
 
 // euler_misc.hpp:23-29
+template <bool ID = true>
 GFM_HD double misc_specific_ie(const V4& U) {
   double rho = U.a;
-  const Recip R = recip(rho);
+  const Recip R = recip<ID>(rho);
   double u = rdiv(U.b, R);
   double v = rdiv(U.c, R);
-  return rdiv(U.d, R) - 0.5 * (u * u + v * v);
+  return rdiv(U.d, R) - mulx(0.5, mulx(u, u) + mulx(v, v));
 }
 // euler_misc.hpp:32-41
+template <bool ID = true>
 GFM_HD bool is_physical_state(const V4& U) {
   double rho = U.a;
-  const Recip R = recip(rho);
+  const Recip R = recip<ID>(rho);
   double u = rdiv(U.b, R);
   double v = rdiv(U.c, R);
-  double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
+  double e = rdiv(U.d, R) - mulx(0.5, mulx(u, u) + mulx(v, v));
   return c_ge0(rho) && c_ge0(e);
 }
 // is_physical_state without its three divisions when the state is plainly
 // physical: rho > 0, E > 0 and 2 E rho >= (1 + 2^-40) ((rho u)^2 + (rho v)^2)
 // with 2 E rho a normal number well inside the range put e = E/rho -
 // (u^2 + v^2)/2 above zero by far more than the rounding of either form.
+template <bool ID = true>
 GFM_HD bool is_physical_state_fast(const V4& U) {
   if (c_gt0(U.a) && c_gt0(U.d)) {
-    const double lhs = 2.0 * (U.d * U.a);
-    const double rhs = (U.b * U.b + U.c * U.c) * (1.0 + 0x1p-40);
+    const double lhs = mulx(2.0, mulx(U.d, U.a));
+    const double rhs = mulx(mulx(U.b, U.b) + mulx(U.c, U.c), 1.0 + 0x1p-40);
     const int el = (int)(as_bits(lhs) >> 52);
     if (el > 200 && el < 2047 && c_le(rhs, lhs)) return true;
   }
-  return is_physical_state(U);
+  return is_physical_state<ID>(U);
 }
 // euler_misc.hpp:44-49
+template <bool ID = true>
 GFM_HD bool is_physical_primitives(double g, double pinf, const V4& W) {
-  double e = eos_specific_ie(g, pinf, W.d, W.a);
+  double e = eos_specific_ie<ID>(g, pinf, W.d, W.a);
   return c_ge0(e) && c_ge0(W.a);
 }
 // the same test with e's sign taken from its numerator and denominator
 GFM_HD bool is_physical_primitives_fast(double g, double pinf, const V4& W) {
-  return quotient_ge0(W.d + g * pinf, (g - 1.0) * W.a) && c_ge0(W.a);
+  return quotient_ge0(W.d + mulx(g, pinf), mulx(g - 1.0, W.a)) && c_ge0(W.a);
 }
 // euler_misc.hpp:52-67
+template <bool ID = true>
 GFM_HD V4 cons_to_prims(double g, double pinf, const V4& U) {
   double rho = U.a;
-  const Recip R = recip(rho);
+  const Recip R = recip<ID>(rho);
   double u = rdiv(U.b, R);
   double v = rdiv(U.c, R);
-  double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
+  double e = rdiv(U.d, R) - mulx(0.5, mulx(u, u) + mulx(v, v));
   double p = eos_pressure(g, pinf, e, rho);
   return V4{rho, u, v, p};
 }
 // conserved_to_primitives together with is_physical_state of the same state:
 // both compute u, v and e with the same operations, done here once.
+template <bool ID = true>
 GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys, Recip* Rout = nullptr) {
   double rho = U.a;
-  const Recip R = recip(rho);
+  const Recip R = recip<ID>(rho);
   if (Rout) *Rout = R;
   double u = rdiv(U.b, R);
   double v = rdiv(U.c, R);
-  double e = rdiv(U.d, R) - 0.5 * (u * u + v * v);
+  double e = rdiv(U.d, R) - mulx(0.5, mulx(u, u) + mulx(v, v));
   *phys = c_ge0(rho) && c_ge0(e);
   double p = eos_pressure(g, pinf, e, rho);
   return V4{rho, u, v, p};
@@ -428,22 +478,25 @@ GFM_HD V4 cons_to_prims_phys(double g, double pinf, const V4& U, bool* phys, Rec
 // (by is_physical_primitives of the same state)
 GFM_HD V4 prims_to_cons_e(const V4& W, double e) {
   double rho = W.a, u = W.b, v = W.c;
-  return V4{rho, rho * u, rho * v, rho * e + 0.5 * rho * (u * u + v * v)};
+  return V4{rho, mulx(rho, u), mulx(rho, v), mulx(rho, e) + mulx(mulx(0.5, rho), mulx(u, u) + mulx(v, v))};
 }
 
 // euler_misc.hpp:70-86
+template <bool ID = true>
 GFM_HD V4 flux_primitive_var(double g, double pinf, const V4& W) {
   double rho = W.a, u = W.b, v = W.c, p = W.d;
-  double e = eos_specific_ie(g, pinf, p, rho);
-  double E = rho * e + 0.5 * rho * (u * u + v * v);
-  return V4{rho * u, rho * u * u + p, rho * u * v, u * (E + p)};
+  double e = eos_specific_ie<ID>(g, pinf, p, rho);
+  double E = mulx(rho, e) + mulx(mulx(0.5, rho), mulx(u, u) + mulx(v, v));
+  const double ru = mulx(rho, u);
+  return V4{ru, mulx(ru, u) + p, mulx(ru, v), mulx(u, E + p)};
 }
 // euler_misc.hpp:89-108 (the asserts become a returned flag)
+template <bool ID = true>
 GFM_HD V4 prims_to_cons(double g, double pinf, const V4& W, bool* ok) {
   double rho = W.a, u = W.b, v = W.c, p = W.d;
-  double e = eos_specific_ie(g, pinf, p, rho);
+  double e = eos_specific_ie<ID>(g, pinf, p, rho);
   if (ok) *ok = c_ge0(rho) && c_ge0(e);
-  return V4{rho, rho * u, rho * v, rho * e + 0.5 * rho * (u * u + v * v)};
+  return V4{rho, mulx(rho, u), mulx(rho, v), mulx(rho, e) + mulx(mulx(0.5, rho), mulx(u, u) + mulx(v, v))};
 }
 
 // ---------------------------------------------------------------------------
@@ -513,29 +566,31 @@ GFM_HD RSSide rs_side_r(double rho, double irho, double u, double p, const Gas& 
 }
 // Two divisions and one square root per side (1/rho, 1/pb, c); A = G5/rho and
 // 1/(rho c) = c / (g pb) follow by multiplication.
+template <bool ID = true>
 GFM_HD void rs_side_consts(RSSide& s, const Gas& k) {
-  double irho = s.has_irho ? s.irho : 1.0 / s.rho;
-  s.ipb = 1.0 / s.pb;
-  s.c = sqrt(k.g * s.pb * irho);
-  s.AK = k.G5 * irho;
-  s.BK = k.G6 * s.pb;
-  s.G4c = k.G4 * s.c;
-  s.irc = s.c * s.ipb * k.IG;
+  double irho = s.has_irho ? s.irho : divx<ID>(1.0, s.rho);
+  s.ipb = divx<ID>(1.0, s.pb);
+  s.c = sqrtx<ID>(mulx(mulx(k.g, s.pb), irho));
+  s.AK = mulx(k.G5, irho);
+  s.BK = mulx(k.G6, s.pb);
+  s.G4c = mulx(k.G4, s.c);
+  s.irc = mulx(mulx(s.c, s.ipb), k.IG);
 }
 
 // Toro's PREFUN: pressure function f_K and its derivative at pressure p.
+template <bool ID = true>
 GFM_HD void rs_prefun(const RSSide& K, const Gas& k, double p, double* f, double* fd) {
   double pb = p + k.pinf;
   if (c_gt(p, K.p)) {  // shock
-    double r = 1.0 / (pb + K.BK);
-    double qrt = sqrt(K.AK * r);
-    *f = (p - K.p) * qrt;
-    *fd = (1.0 - 0.5 * ((p - K.p) * r)) * qrt;
+    double r = divx<ID>(1.0, pb + K.BK);
+    double qrt = sqrtx<ID>(mulx(K.AK, r));
+    *f = mulx(p - K.p, qrt);
+    *fd = mulx(1.0 - mulx(0.5, mulx(p - K.p, r)), qrt);
   } else {        // rarefaction
-    double prat = pb * K.ipb;
+    double prat = mulx(pb, K.ipb);
     double pw = gfm_pow(prat, k.G1);
-    *f = K.G4c * (pw - 1.0);
-    *fd = K.irc * (pw / prat);
+    *f = mulx(K.G4c, pw - 1.0);
+    *fd = mulx(K.irc, divx<ID>(pw, prat));
   }
 }
 
@@ -543,22 +598,23 @@ GFM_HD void rs_prefun(const RSSide& K, const Gas& k, double p, double* f, double
 // pw/prat of the rarefaction) issued as one: when lanes of a warp take
 // different branches the division runs once for all of them.  Every value
 // comes from the same operations as in rs_prefun.
+template <bool ID = true>
 GFM_HD void rs_prefun_merged(const RSSide& K, const Gas& k, double p, double* f, double* fd) {
   const double pb = p + k.pinf;
   const bool shock = c_gt(p, K.p);
   double pw = 0.0, prat = 1.0;
   if (!shock) {
-    prat = pb * K.ipb;
+    prat = mulx(pb, K.ipb);
     pw = gfm_pow(prat, k.G1);
   }
-  const double q = (shock ? 1.0 : pw) / (shock ? pb + K.BK : prat);
+  const double q = divx<ID>(shock ? 1.0 : pw, shock ? pb + K.BK : prat);
   if (shock) {
-    const double qrt = sqrt(K.AK * q);
-    *f = (p - K.p) * qrt;
-    *fd = (1.0 - 0.5 * ((p - K.p) * q)) * qrt;
+    const double qrt = sqrtx<ID>(mulx(K.AK, q));
+    *f = mulx(p - K.p, qrt);
+    *fd = mulx(1.0 - mulx(0.5, mulx(p - K.p, q)), qrt);
   } else {
-    *f = K.G4c * (pw - 1.0);
-    *fd = K.irc * q;
+    *f = mulx(K.G4c, pw - 1.0);
+    *fd = mulx(K.irc, q);
   }
 }
 
@@ -572,6 +628,7 @@ struct RSStar {
 
 // Newton-Raphson on p* (Toro's STARPU) from the initial guess p0, then u*
 // from the last pressure-function evaluation taken to p* along its tangent.
+template <bool ID = true>
 GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, double p0) {
   RSStar s;
   s.status = ST_OK;
@@ -579,7 +636,7 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   if (c_le(L.G4c + R.G4c, udiff)) s.status |= ST_VACUUM;
   double pinf_min = c_lt(kL.pinf, kR.pinf) ? kL.pinf : kR.pinf;
   double pbmin = c_lt(L.pb, R.pb) ? L.pb : R.pb;
-  double pfl = 1e-6 * pbmin - pinf_min;
+  double pfl = mulx(1e-6, pbmin) - pinf_min;
   double pold = c_gt(p0, pfl) ? p0 : pfl;
   double fL = 0.0, fLd = 0.0, fR = 0.0, fRd = 0.0;
   double p = pold, dp = 0.0;
@@ -594,14 +651,14 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   const Gas kA = rfirst ? kR : kL, kB = rfirst ? kL : kR;
   for (;;) {
     double fA, fAd, fB, fBd;
-    rs_prefun_merged(A, kA, pold, &fA, &fAd);   // lanes of a warp may take different branches
-    rs_prefun_merged(B, kB, pold, &fB, &fBd);
+    rs_prefun_merged<ID>(A, kA, pold, &fA, &fAd);   // lanes of a warp may take different branches
+    rs_prefun_merged<ID>(B, kB, pold, &fB, &fBd);
     fL = rfirst ? fB : fA; fLd = rfirst ? fBd : fAd;
     fR = rfirst ? fA : fB; fRd = rfirst ? fAd : fBd;
-    p = pold - (fL + fR + udiff) / (fLd + fRd);
+    p = pold - divx<ID>(fL + fR + udiff, fLd + fRd);
     if (c_lt(p, pfl)) p = pfl;
     it++;
-    bool conv = c_le(2.0 * fabs(p - pold), GFM_RS_TOL * (p + pold + 2.0 * pinf_min));
+    bool conv = c_le(mulx(2.0, fabs(p - pold)), mulx(GFM_RS_TOL, p + pold + mulx(2.0, pinf_min)));
     dp = p - pold;
     pold = p;
     if (conv) break;
@@ -610,26 +667,28 @@ GFM_HD RSStar rs_star(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   s.p = p;
   // the pressure functions carried from the last evaluation point to p along
   // their tangents, so u* keeps the accuracy of p*
-  s.u = 0.5 * (L.u + R.u + (fR + fRd * dp) - (fL + fLd * dp));
+  s.u = mulx(0.5, L.u + R.u + (fR + mulx(fRd, dp)) - (fL + mulx(fLd, dp)));
   s.iters = it;
   return s;
 }
 
 // PVRS guess (Toro eq. 4.47)
 GFM_HD double rs_guess_pvrs(const RSSide& L, const RSSide& R) {
-  return 0.5 * (L.p + R.p) - 0.125 * (R.u - L.u) * (L.rho + R.rho) * (L.c + R.c);
+  return mulx(0.5, L.p + R.p) - mulx(mulx(mulx(0.125, R.u - L.u), L.rho + R.rho), L.c + R.c);
 }
 
 // Two-shock guess (TSRS, Toro eq. 9.42) with the shock constants taken at pg;
 // used by the mixed (two-material) solve, whose data hold strong waves.
+template <bool ID = true>
 GFM_HD double rs_guess_tsrs(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, double pg) {
-  const double gL = sqrt(L.AK / (pg + kL.pinf + L.BK));
-  const double gR = sqrt(R.AK / (pg + kR.pinf + R.BK));
-  return (gL * L.p + gR * R.p - (R.u - L.u)) / (gL + gR);
+  const double gL = sqrtx<ID>(divx<ID>(L.AK, pg + kL.pinf + L.BK));
+  const double gR = sqrtx<ID>(divx<ID>(R.AK, pg + kR.pinf + R.BK));
+  return divx<ID>(gL * L.p + gR * R.p - (R.u - L.u), gL + gR);
 }
 
 // Whole solve.  When u and p agree on both sides the data hold at most a
 // contact and the exact answer p* = p, u* = u is returned without iterating.
+template <bool ID = true>
 GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR, bool two_shock = false) {
   if (c_eq(L.u, R.u) && c_eq(L.p, R.p)) {
     RSStar s;
@@ -640,25 +699,26 @@ GFM_HD RSStar rs_solve(RSSide& L, const Gas& kL, RSSide& R, const Gas& kR, bool 
     s.trivial = true;
     return s;
   }
-  rs_side_consts(L, kL);
-  rs_side_consts(R, kR);
+  rs_side_consts<ID>(L, kL);
+  rs_side_consts<ID>(R, kR);
   double p0 = rs_guess_pvrs(L, R);
   if (two_shock) {   // at max(PVRS, the Newton floor of rs_star)
     const double pinf_min = c_lt(kL.pinf, kR.pinf) ? kL.pinf : kR.pinf;
     const double pbmin = c_lt(L.pb, R.pb) ? L.pb : R.pb;
     const double pfl = 1e-6 * pbmin - pinf_min;
-    p0 = rs_guess_tsrs(L, kL, R, kR, c_gt(p0, pfl) ? p0 : pfl);
+    p0 = rs_guess_tsrs<ID>(L, kL, R, kR, c_gt(p0, pfl) ? p0 : pfl);
   }
-  RSStar s = rs_star(L, kL, R, kR, p0);
+  RSStar s = rs_star<ID>(L, kL, R, kR, p0);
   s.trivial = false;
   return s;
 }
 
 // Star density behind the K wave (shock or rarefaction).
+template <bool ID = true>
 GFM_HD double rs_rho_star(const RSSide& K, const Gas& k, double pstar) {
-  double pr = (pstar + k.pinf) * K.ipb;
-  if (c_gt(pstar, K.p)) return K.rho * ((pr + k.G6) / (pr * k.G6 + 1.0));
-  return K.rho * gfm_pow(pr, k.IG);
+  double pr = mulx(pstar + k.pinf, K.ipb);
+  if (c_gt(pstar, K.p)) return mulx(K.rho, divx<ID>(pr + k.G6, mulx(pr, k.G6) + 1.0));
+  return mulx(K.rho, gfm_pow(pr, k.IG));
 }
 
 // Toro's SAMPLE at speed S; returns (rho, u, p).
@@ -671,6 +731,7 @@ GFM_HD double rs_rho_star(const RSSide& K, const Gas& k, double pstar) {
 // IEEE operation), and a rarefaction's star density shares the logarithm of
 // (p* + pinf)/(p_K + pinf) with the tail speed (gfm_pow is exp(y log x)).
 struct RS1D { double rho, u, p; };
+template <bool ID = true>
 GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, const RSStar& st,
                       double S) {
   RS1D w;
@@ -687,13 +748,13 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   const double G6 = left ? kL.G6 : kR.G6, G7 = left ? kL.G7 : kR.G7, IG = left ? kL.IG : kR.IG;
   // left: rarefaction when p* <= p_L; right: shock when p* > p_R
   const bool shock = left ? !c_le(st.p, L.p) : c_gt(st.p, R.p);
-  const double pr = (st.p + pinf) * Kipb;
+  const double pr = mulx(st.p + pinf, Kipb);
   if (shock) {
-    const double q = Kc * sqrt(G2 * pr + G1);
+    const double q = mulx(Kc, sqrtx<ID>(mulx(G2, pr) + G1));
     const double sK = Ku + (left ? -q : q);   // shock speed
     if (left ? c_le(S, sK) : c_ge(S, sK)) { w.rho = Krho; w.u = Ku; w.p = Kp; return w; }
     // rs_rho_star behind the K wave
-    w.rho = c_gt(st.p, Kp) ? Krho * ((pr + G6) / (pr * G6 + 1.0)) : Krho * gfm_pow(pr, IG);
+    w.rho = c_gt(st.p, Kp) ? mulx(Krho, divx<ID>(pr + G6, mulx(pr, G6) + 1.0)) : mulx(Krho, gfm_pow(pr, IG));
     w.u = st.u; w.p = st.p;
     return w;
   }
@@ -701,21 +762,21 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   if (left ? c_le(S, hK) : c_ge(S, hK)) { w.rho = Krho; w.u = Ku; w.p = Kp; return w; }
   const bool zero = (as_bits(pr) & GFM_MAG_BITS) == 0;
   const double lpr = zero ? 0.0 : gfm_log(pr);
-  const double cm = Kc * (zero ? gfm_pow(pr, G1) : gfm_exp(G1 * lpr));
+  const double cm = mulx(Kc, zero ? gfm_pow(pr, G1) : gfm_exp(mulx(G1, lpr)));
   const double tK = st.u + (left ? -cm : cm);   // rarefaction tail
   if (left ? c_gt(S, tK) : c_le(S, tK)) {
     // rs_rho_star of a rarefaction (p* <= p_K here, or NaN on the right)
-    w.rho = Krho * (zero ? gfm_pow(pr, IG) : gfm_exp(IG * lpr));
+    w.rho = mulx(Krho, zero ? gfm_pow(pr, IG) : gfm_exp(mulx(IG, lpr)));
     w.u = st.u; w.p = st.p;
     return w;
   }
   // inside the fan
-  const double t = G7 * (Ku - S);
-  const double c = G5 * (Kc + (left ? t : -t));
-  const double cr = c / Kc;
-  w.rho = Krho * gfm_pow(cr, G4);
-  w.u = G5 * ((left ? Kc : -Kc) + G7 * Ku + S);
-  w.p = Kpb * gfm_pow(cr, G3) - pinf;
+  const double t = mulx(G7, Ku - S);
+  const double c = mulx(G5, Kc + (left ? t : -t));
+  const double cr = divx<ID>(c, Kc);
+  w.rho = mulx(Krho, gfm_pow(cr, G4));
+  w.u = mulx(G5, (left ? Kc : -Kc) + mulx(G7, Ku) + S);
+  w.p = mulx(Kpb, gfm_pow(cr, G3)) - pinf;
   return w;
 }
 
@@ -730,12 +791,13 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
 // irhoL, irhoR: the conversions' reciprocals 1/rho, which the solve reuses
 struct FaceData { double rhoL, uL, pL, rhoR, uR, pR, utL, utR, irhoL, irhoR; };
 
+template <bool ID = true>
 GFM_HD bool rs_face_front(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status,
                           FaceData& d) {
   bool okL, okR;
   Recip RL, RR;
-  V4 Lp = cons_to_prims_phys(k.g, k.pinf, UL, &okL, &RL);
-  V4 Rp = cons_to_prims_phys(k.g, k.pinf, UR, &okR, &RR);
+  V4 Lp = cons_to_prims_phys<ID>(k.g, k.pinf, UL, &okL, &RL);
+  V4 Rp = cons_to_prims_phys<ID>(k.g, k.pinf, UR, &okR, &RR);
   if (!okL || !okR) *status |= ST_UNPHYSICAL;
   d.rhoL = Lp.a; d.uL = paralleltox ? Lp.b : Lp.c; d.pL = Lp.d;
   d.rhoR = Rp.a; d.uR = paralleltox ? Rp.b : Rp.c; d.pR = Rp.d;
@@ -745,42 +807,45 @@ GFM_HD bool rs_face_front(bool paralleltox, const Gas& k, const V4& UL, const V4
   return c_eq(d.uL, d.uR) && c_eq(d.pL, d.pR);
 }
 
+template <bool ID = true>
 GFM_HD V4 rs_face_finish(bool paralleltox, const Gas& k, const FaceData& d, uint32_t* status, int* iters) {
   RSSide L = rs_side_r(d.rhoL, d.irhoL, d.uL, d.pL, k);
   RSSide R = rs_side_r(d.rhoR, d.irhoR, d.uR, d.pR, k);
-  RSStar st = rs_solve(L, k, R, k);
+  RSStar st = rs_solve<ID>(L, k, R, k);
   *status |= st.status;
   *iters += st.iters;
-  RS1D w = rs_sample(L, k, R, k, st, 0.0);
+  RS1D w = rs_sample<ID>(L, k, R, k, st, 0.0);
   double ut = c_le0(st.u) ? d.utR : d.utL;
-  V4 f = flux_primitive_var(k.g, k.pinf, V4{w.rho, w.u, ut, w.p});
+  V4 f = flux_primitive_var<ID>(k.g, k.pinf, V4{w.rho, w.u, ut, w.p});
   if (!paralleltox) { double t = f.b; f.b = f.c; f.c = t; }
   return f;
 }
 
+template <bool ID = true>
 GFM_HD V4 pure_rs_flux(bool paralleltox, const Gas& k, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
   FaceData d;
-  rs_face_front(paralleltox, k, UL, UR, status, d);
-  return rs_face_finish(paralleltox, k, d, status, iters);
+  rs_face_front<ID>(paralleltox, k, UL, UR, status, d);
+  return rs_face_finish<ID>(paralleltox, k, d, status, iters);
 }
 
 // mixed_RS_exact::solve_mixed_RP (sourcecode/mixed_RS_exact.cpp:8-48).
 struct MixedStar { double p_star, u_star, rho_star_L, rho_star_R; };
+template <bool ID = true>
 GFM_HD MixedStar mixed_rs(const Gas& kL, const Gas& kR, const V4& UL, const V4& UR, uint32_t* status, int* iters) {
   bool okL, okR;
-  V4 Lp = cons_to_prims_phys(kL.g, kL.pinf, UL, &okL);
-  V4 Rp = cons_to_prims_phys(kR.g, kR.pinf, UR, &okR);
+  V4 Lp = cons_to_prims_phys<ID>(kL.g, kL.pinf, UL, &okL);
+  V4 Rp = cons_to_prims_phys<ID>(kR.g, kR.pinf, UR, &okR);
   if (!okL || !okR) *status |= ST_UNPHYSICAL;
   RSSide L = rs_side(Lp.a, Lp.b, Lp.d, kL);
   RSSide R = rs_side(Rp.a, Rp.b, Rp.d, kR);
-  RSStar st = rs_solve(L, kL, R, kR, true);
+  RSStar st = rs_solve<ID>(L, kL, R, kR, true);
   *status |= st.status;
   *iters += st.iters;
   MixedStar m;
   m.p_star = st.p;
   m.u_star = st.u;
-  m.rho_star_L = st.trivial ? L.rho : rs_rho_star(L, kL, st.p);
-  m.rho_star_R = st.trivial ? R.rho : rs_rho_star(R, kR, st.p);
+  m.rho_star_L = st.trivial ? L.rho : rs_rho_star<ID>(L, kL, st.p);
+  m.rho_star_R = st.trivial ? R.rho : rs_rho_star<ID>(R, kR, st.p);
   if (c_isnan(m.p_star)) *status |= ST_NAN;
   return m;
 }

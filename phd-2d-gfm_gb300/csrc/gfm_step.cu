@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(CHUNK_T) k_prims(PrimArgs a) {
     }
     // raw gradient, its norm, and the unit normal with the reference's
     // fallback (sourcecode/GFM_riemann.cpp:58-68), once per step
-    double nn = sqrt(gx * gx + gy * gy);
+    double nn = sqrtx(gx * gx + gy * gy);
     double ux = 1.0, uy = 0.0;
     if (!c_lt(nn, 1e-12)) {
       const Recip rn = recip(nn);
@@ -859,7 +859,7 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
         for (int yinc = -1; yinc <= 1; yinc++) {
           double dp = dpk[(xinc + 1) * 3 + (yinc + 1)];
           if (dp < -2.0 || dp < dbest - 1e-6) continue;
-          double ang = gfm_acos(dp);
+          double ang = gfm_acos<false>(dp);
           if (ang < mindiff) { iopp = i + yinc; jopp = j + xinc; mindiff = ang; }
         }
       if (iopp == -1000) { st |= ST_BAD_ARGUMENT; iopp = i; jopp = j; }
@@ -901,10 +901,10 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
     V4 Lp = V4{ip1.a, u1n, 0.0, (1e-6 < ip1.d) ? ip1.d : 1e-6};
     V4 Rp = V4{ip2.a, u2n, 0.0, (1e-6 < ip2.d) ? ip2.d : 1e-6};
     bool ok1 = true, ok2 = true;
-    V4 Ls = prims_to_cons(P.g1, P.p1, Lp, &ok1);
-    V4 Rs = prims_to_cons(P.g2, P.p2, Rp, &ok2);
+    V4 Ls = prims_to_cons<false>(P.g1, P.p1, Lp, &ok1);
+    V4 Rs = prims_to_cons<false>(P.g2, P.p2, Rp, &ok2);
     if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
-    MixedStar m = mixed_rs(P.gas1, P.gas2, Ls, Rs, &st, &iters);
+    MixedStar m = mixed_rs<false>(P.gas1, P.gas2, Ls, Rs, &st, &iters);
     double snx = m.u_star * nx, sny = m.u_star * ny;
     if (MODE == IFC_MODIFIED) {
       double u1x, u1y, u2x, u2y;
@@ -912,10 +912,10 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
       else if (lsval <= 0.0) { u1x = snx + t1x; u1y = sny + t1y; u2x = snx + t1x; u2y = sny + t1y; }
       else { u1x = snx + t2x; u1y = sny + t2y; u2x = snx + t2x; u2y = sny + t2y; }
       if (lsval <= 0.0) {
-        o[0] = eos_isentropic_extrapolation(P.g1, P.p1, m.rho_star_L, m.p_star, load4(a.W1, P, c).d);
+        o[0] = eos_isentropic_extrapolation<false>(P.g1, P.p1, m.rho_star_L, m.p_star, load4(a.W1, P, c).d);
         o[1] = m.rho_star_R; o[2] = u2x; o[3] = u2y; o[4] = m.p_star;
       } else {
-        o[0] = eos_isentropic_extrapolation(P.g2, P.p2, m.rho_star_R, m.p_star, load4(a.W2, P, c).d);
+        o[0] = eos_isentropic_extrapolation<false>(P.g2, P.p2, m.rho_star_R, m.p_star, load4(a.W2, P, c).d);
         o[1] = m.rho_star_L; o[2] = u1x; o[3] = u1y; o[4] = m.p_star;
       }
       o[5] = snx; o[6] = sny;
@@ -986,7 +986,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   // cons_to_prims_phys with its three quotients by rho (rho u, rho v, E) in
   // one: lane kc of each group of four divides component kc + 1 (E twice)
   const int lane = threadIdx.x & 31, grp = lane & ~3, kq = lane & 3;
-  const Recip Rr = recip(Uown.a);
+  const Recip Rr = recip<false>(Uown.a);
   const double qv = rdiv(kq == 0 ? Uown.b : (kq == 1 ? Uown.c : Uown.d), Rr);
   const double uq = __shfl_sync(FULL_MASK, qv, grp), vq = __shfl_sync(FULL_MASK, qv, grp + 1);
   const double eq = __shfl_sync(FULL_MASK, qv, grp + 2) - 0.5 * (uq * uq + vq * vq);
@@ -1006,10 +1006,10 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   {
     // rs_side_consts with its two reciprocals (1/rho, 1/pb) in one division:
     // even lanes divide by rho, odd lanes by pb, and exchange
-    const double y = 1.0 / ((lane & 1) ? S.pb : S.rho);
+    const double y = divx<false>(1.0, (lane & 1) ? S.pb : S.rho);
     const double irho = __shfl_sync(FULL_MASK, y, lane & ~1), ipb = __shfl_sync(FULL_MASK, y, lane | 1);
     S.ipb = ipb;
-    S.c = sqrt(k.g * S.pb * irho);
+    S.c = sqrtx<false>(k.g * S.pb * irho);
     S.AK = k.G5 * irho;
     S.BK = k.G6 * S.pb;
     S.G4c = k.G4 * S.c;
@@ -1027,15 +1027,15 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   const double pbmin = c_lt(pbL, pbR) ? pbL : pbR;
   const double pfl = 1e-6 * pbmin - pinf_min;
   const double pg = c_gt(ppv, pfl) ? ppv : pfl;
-  const double gown = sqrt(S.AK / (pg + k.pinf + S.BK));
+  const double gown = sqrtx<false>(divx<false>(S.AK, pg + k.pinf + S.BK));
   const double goth = xside(gown);
   const double gL = isR ? goth : gown, gR = isR ? gown : goth;
-  const double pts = (gL * pL + gR * pR - (uR - uL)) / (gL + gR);
+  const double pts = divx<false>(gL * pL + gR * pR - (uR - uL), gL + gR);
   double p0 = pts;
   bool gated = false;
   float x[MLP_IN];
   if (a.mlp || a.cap_X) {   // warp-uniform: both halves hold the same values
-    const double ratio = (pts + pinf_min) / (pg + pinf_min);
+    const double ratio = divx<false>(pts + pinf_min, pg + pinf_min);
     gated = c_gt(ratio, 0.0) && c_gt(fabs(gfm_log(ratio)), MLP_GATE);
     if (gated) mlp_features_f(rhoL, uL, pbL, kL.g, kL.pinf, rhoR, uR, pbR, kR.g, kR.pinf, x);
     if (gated && a.mlp) {
@@ -1058,7 +1058,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
     fR = isR ? f : of;
     fLd = isR ? ofd : fd;
     fRd = isR ? fd : ofd;
-    p = pold - (fL + fR + udiff) / (fLd + fRd);
+    p = pold - divx<false>(fL + fR + udiff, fLd + fRd);
     if (c_lt(p, pfl)) p = pfl;
     it++;
     bool conv = c_le(2.0 * fabs(p - pold), GFM_RS_TOL * (p + pold + 2.0 * pinf_min));
@@ -1069,7 +1069,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   }
   r.p = p;
   r.u = 0.5 * (uL + uR + (fR + fRd * dp) - (fL + fLd * dp));
-  r.rho_own = rs_rho_star(S, k, p);
+  r.rho_own = rs_rho_star<false>(S, k, p);
   *iters += it;
   if (gated && a.cap_X && (threadIdx.x & 31) == 0 && it < kL.maxit && !c_le(G4cL + G4cR, udiff)) {
     const double y = gfm_log((p + pinf_min) / (pts + pinf_min));
@@ -1196,7 +1196,7 @@ __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k,
     const bool elig = lane < 9 && !(dp < -2.0 || dp < dbest - 1e-6);
     long long key = 0x7ff0000000000000LL;   // +inf: not a candidate
     if (elig) {
-      const double ang = gfm_acos(dp);
+      const double ang = gfm_acos<false>(dp);
       if (ang == ang) key = as_bits(ang);   // angles are >= +0: bits order as values
     }
     int bl = (key == 0x7ff0000000000000LL) ? 32 : lane;
@@ -1249,7 +1249,7 @@ __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k,
   cell.tx = ib - un * nx;
   cell.ty = ic - un * ny;
   bool okp = true;
-  cell.Us = prims_to_cons(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
+  cell.Us = prims_to_cons<false>(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
   if (!okp) st |= ST_UNPHYSICAL;
   return true;
 }
@@ -1341,22 +1341,22 @@ __device__ double vof_area(double b, double c1, double c2) {
   if (b <= 0.0) return 0.0;
   const double s = m1 + m2;
   if (b >= s) return 1.0;
-  if (m1 == 0.0) return b / m2;
+  if (m1 == 0.0) return divx(b, m2);
   const double d = (2.0 * m1) * m2;
-  if (b < m1) return (b * b) / d;
-  if (b <= m2) return (b - 0.5 * m1) / m2;
+  if (b < m1) return divx(b * b, d);
+  if (b <= m2) return divx(b - 0.5 * m1, m2);
   const double r = s - b;
-  return 1.0 - (r * r) / d;
+  return 1.0 - divx(r * r, d);
 }
 
 // the line constant with vof_area(b, m1, m2) = z (0 < z < 1, m1 <= m2, m2 > 0)
 __device__ double vof_line_constant(double z, double m1, double m2) {
   if (m1 == 0.0) return z * m2;
-  const double v1 = m1 / (2.0 * m2);
+  const double v1 = divx(m1, 2.0 * m2);
   const double d = (2.0 * m1) * m2;
-  if (z < v1) return sqrt(d * z);
+  if (z < v1) return sqrtx(d * z);
   if (z <= 1.0 - v1) return z * m2 + 0.5 * m1;
-  return (m1 + m2) - sqrt(d * (1.0 - z));
+  return (m1 + m2) - sqrtx(d * (1.0 - z));
 }
 
 // PLIC reconstruction of the mixed cell c: in the unit cell with the axes
@@ -1368,10 +1368,10 @@ __device__ VofPlic vof_reconstruct(const GridP& P, const double* z, int64_t c) {
   const int64_t w = P.pitch;
   const double gx = ((z[c - w + 1] + 2.0 * z[c + 1]) + z[c + w + 1]) - ((z[c - w - 1] + 2.0 * z[c - 1]) + z[c + w - 1]);
   const double gy = ((z[c + w - 1] + 2.0 * z[c + w]) + z[c + w + 1]) - ((z[c - w - 1] + 2.0 * z[c - w]) + z[c - w + 1]);
-  const double mx = -gx / P.dx, my = -gy / P.dy;
-  const double nn = sqrt(mx * mx + my * my);
+  const double mx = divx(-gx, P.dx), my = divx(-gy, P.dy);
+  const double nn = sqrtx(mx * mx + my * my);
   VofPlic r;
-  if (nn > 0.0) { r.nx = mx / nn; r.ny = my / nn; }
+  if (nn > 0.0) { r.nx = divx(mx, nn); r.ny = divx(my, nn); }
   else { r.nx = 1.0; r.ny = 0.0; }
   r.a = fabs(r.nx) * P.dx;
   r.b = fabs(r.ny) * P.dy;
@@ -1452,9 +1452,9 @@ __global__ void __launch_bounds__(CHUNK_T) k_vof_prims(VofPrimArgs a) {
       // midpoint of the PLIC segment
       const double m1 = vlo(r.a, r.b), m2 = vhi(r.a, r.b), be = r.beta;
       double u1, w1v, u2, w2v;
-      if (be < m1) { u1 = be / m1; w1v = 0.0; u2 = 0.0; w2v = be / m2; }
-      else if (be <= m2) { u1 = 0.0; w1v = be / m2; u2 = 1.0; w2v = (be - m1) / m2; }
-      else { u1 = 1.0; w1v = (be - m1) / m2; u2 = (be - m2) / m1; w2v = 1.0; }
+      if (be < m1) { u1 = divx(be, m1); w1v = 0.0; u2 = 0.0; w2v = divx(be, m2); }
+      else if (be <= m2) { u1 = 0.0; w1v = divx(be, m2); u2 = 1.0; w2v = divx(be - m1, m2); }
+      else { u1 = 1.0; w1v = divx(be - m1, m2); u2 = divx(be - m2, m1); w2v = 1.0; }
       const double um = 0.5 * (u1 + u2), wm = 0.5 * (w1v + w2v);
       const bool swapped = r.b < r.a;
       const double xr = swapped ? wm : um, er = swapped ? um : wm;
@@ -1571,7 +1571,7 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       const double un = own[1] * nx + own[2] * ny;
       const double tx = own[1] - un * nx, ty = own[2] - un * ny;
       bool okp = true;
-      const V4 Us = prims_to_cons(k.g, k.pinf, V4{own[0], un, 0.0, c_lt(1e-6, own[3]) ? own[3] : 1e-6}, &okp);
+      const V4 Us = prims_to_cons<false>(k.g, k.pinf, V4{own[0], un, 0.0, c_lt(1e-6, own[3]) ? own[3] : 1e-6}, &okp);
       if (!okp) st |= ST_UNPHYSICAL;
       int it = 0, gt = 0;
       const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it, a, &gt);
@@ -1589,10 +1589,10 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       m1v[0] = rhoL; m1v[1] = u1x; m1v[2] = u1y; m1v[3] = m.p;
       m2v[0] = rhoR; m2v[1] = u2x; m2v[2] = u2y; m2v[3] = m.p;
       if (zc > 0.5) {
-        o1[0] = eos_isentropic_extrapolation(P.g1, P.p1, rhoL, m.p, w1.d); o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
+        o1[0] = eos_isentropic_extrapolation<false>(P.g1, P.p1, rhoL, m.p, w1.d); o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
         for (int e = 0; e < 4; e++) o2[e] = m2v[e];
       } else {
-        o2[0] = eos_isentropic_extrapolation(P.g2, P.p2, rhoR, m.p, w2.d); o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
+        o2[0] = eos_isentropic_extrapolation<false>(P.g2, P.p2, rhoR, m.p, w2.d); o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
         for (int e = 0; e < 4; e++) o1[e] = m1v[e];
       }
     } else {
@@ -1601,10 +1601,10 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       for (int e = 0; e < 4; e++) { m1v[e] = s0[e]; m2v[e] = s1[e]; }
       if (zc > 0.5) {
         o1[0] = w1.a; o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
-        o2[0] = eos_isentropic_extrapolation(P.g2, P.p2, m2v[0], m2v[3], w1.d); o2[1] = w1.b; o2[2] = w1.c; o2[3] = w1.d;
+        o2[0] = eos_isentropic_extrapolation<false>(P.g2, P.p2, m2v[0], m2v[3], w1.d); o2[1] = w1.b; o2[2] = w1.c; o2[3] = w1.d;
       } else {
         o2[0] = w2.a; o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
-        o1[0] = eos_isentropic_extrapolation(P.g1, P.p1, m1v[0], m1v[3], w2.d); o1[1] = w2.b; o1[2] = w2.c; o1[3] = w2.d;
+        o1[0] = eos_isentropic_extrapolation<false>(P.g1, P.p1, m1v[0], m1v[3], w2.d); o1[1] = w2.b; o1[2] = w2.c; o1[3] = w2.d;
       }
     }
     if (lane == 0) {
@@ -1656,12 +1656,12 @@ __device__ V4 vof_invdist_average(const VofGhostArgs& a, int i, int j, int f) {
       const double tx = P.x0 + ((double)(j + xinc - P.g) + 0.5) * P.dx;
       const double ty = P.y0 + ((double)(i + yinc - P.g) + 0.5) * P.dy;
       const double ddx = tx - ccx, ddy = ty - ccy;
-      const double w = 1.0 / sqrt(ddx * ddx + ddy * ddy);
+      const double w = divx(1.0, sqrtx(ddx * ddx + ddy * ddy));
       sw += w;
       const double* r = a.mrp + (int64_t)a.ifc_map[c2] * 8 + 4 * f;
       sum = V4{sum.a + w * r[0], sum.b + w * r[1], sum.c + w * r[2], sum.d + w * r[3]};
     }
-  return V4{sum.a / sw, sum.b / sw, sum.c / sw, sum.d / sw};
+  return V4{divx(sum.a, sw), divx(sum.b, sw), divx(sum.c, sw), divx(sum.d, sw)};
 }
 
 template <int MODE>
@@ -2010,7 +2010,7 @@ __global__ void __launch_bounds__(256) k_ls_stage(GridP P, const double* X, cons
     else if (STAGE == 2) r = 0.75 * phi[c] + 0.25 * (X[c] + dt * L);
     else r = (1.0 / 3.0) * phi[c] + (2.0 / 3.0) * (X[c] + dt * L);
     out[cidx(P, i, j)] = r;
-    if (sign) S[cidx(P, i, j)] = r / sqrt(r * r + h * h);
+    if (sign) S[cidx(P, i, j)] = divx(r, sqrtx(r * r + h * h));
   }
 }
 
@@ -2056,7 +2056,7 @@ __global__ void __launch_bounds__(256) k_reinit_iter(GridP P, const double* cur,
     const double mx = c_lt(fabs_bits(x1), fabs_bits(x2)) ? x2 : x1;
     const double my = c_lt(fabs_bits(y1), fabs_bits(y2)) ? y2 : y1;
     const double gx = mx * mx, gy = my * my;
-    double G = sqrt(gx + gy) - 1.0;
+    double G = sqrtx(gx + gy) - 1.0;
     out[cidx(P, i, j)] = f - dtau * sg * G;
   }
 }
