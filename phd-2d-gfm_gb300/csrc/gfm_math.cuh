@@ -36,10 +36,10 @@
 namespace gfm {
 
 // The products of the functions below.  In the device code of a translation
-// unit compiled with GFM_INT_MUL defined (the throughput-bound flux update)
-// they are formed on the integer pipes (xmul, gfm_xfp64.cuh: the same bits
-// as the FP64 multiply, for a third of the FP64 pipe's work); everywhere else,
-// the host included, they are the FP64 multiply itself.
+// unit compiled with GFM_INT_MUL defined (the flux update built with
+// GFM_FLUX_INT_MUL) they are formed on the integer pipes (xmul,
+// gfm_xfp64.cuh: the same bits as the FP64 multiply); everywhere else, the
+// host included, they are the FP64 multiply itself.
 #if defined(__CUDA_ARCH__) && defined(GFM_INT_MUL)
 GFM_HD double mulx(double a, double b) { return xmul(a, b); }
 #else
