@@ -619,9 +619,11 @@ def batched_learned_block(args):
 
 
 def run_batch(args):
-    """64 independent shock-bubble instances: K steps of all of them through
-    the recorded step graph (instances side by side), and the same K steps one
-    instance after another (the unbatched path), from the same state."""
+    """64 independent shock-bubble instances: K steps of all of them one
+    instance after another (the unbatched path), through the recorded step
+    graph with the default schedule, and -- the line's value -- through the
+    graph after gfm_batch_autotune has chosen the schedule and the flux tile
+    shape per grid-size class, each from the same state."""
     import ctypes
     import numpy as np
     import torch
@@ -658,6 +660,13 @@ def run_batch(args):
         return e0.elapsed_time(e1), L.gfm_launch_count() - l0, clk.summary()
 
     ms_seq, launches_seq, clk_seq = timed(False)
+    ms_streams, launches_streams, clk_streams = timed(True)
+    # the project's autotuner (tile shape per grid-size class, schedule),
+    # timed on the state after the warm-up and restored; then the tuned run
+    for ctx, st in zip(b.instances, start):
+        ctx.upload(st[0], st[1], st[2], t=st[3], numsteps=st[4])
+    tuning = b.autotune(m, steps=16)
+    L.gfm_batch_set_stream(b._p, ctypes.c_void_p(stream.cuda_stream))
     ms_graph, launches, clk = timed(True)
     stats = [ctx.status() for ctx in b.instances]
     value = cells * args.steps / (ms_graph * 1e-3)
@@ -697,10 +706,16 @@ def run_batch(args):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "batch64_shock_bubble_riemannGFM", "instances": len(spec), "cells": cells,
                        "seed": BATCH_SEED, "sides": "128..1024 step 64, aspect U[1,3]", "CFL": 0.6,
-                       "p_star_guess": "plain (PVRS / TSRS)", "schedule": "recorded CUDA graph, 8 steps per replay",
+                       "p_star_guess": "plain (PVRS / TSRS)",
+                       "schedule": "recorded CUDA graph, 8 steps per replay; %s schedule and tile shapes per size "
+                                   "class from gfm_batch_autotune" % tuning["schedule"],
                        "l2": "inputs larger than L2 (%.1f GB of state)" % (cells * 9 * 8 / 1e9)},
             "plain_sequential": {"value": plain, "ms_per_step": ms_seq / args.steps, "gpu_launches": launches_seq,
                                  "clocks": clk_seq},
+            "batched_streams_untuned": {"value": cells * args.steps / (ms_streams * 1e-3),
+                                        "ms_per_step": ms_streams / args.steps, "gpu_launches": launches_streams,
+                                        "clocks": clk_streams},
+            "autotune": tuning,
             "batched_over_plain": value / plain,
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
             "device_status_nonzero": int(sum(1 for x in stats if x))}

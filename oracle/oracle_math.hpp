@@ -4,11 +4,15 @@
 // Scalar arithmetic of the oracle, written independently of the CUDA kernels
 // from the same specification (same operations in the same order, so a
 // -ffp-contract=off build agrees bit for bit with --fmad=false kernels):
-//   * Tang's table-driven exp and log (ACM TOMS 15(2) 1989, 16(4) 1990), pow
-//     as exp(y log x), and acos by the asin Taylor series with half-angle
-//     reduction, polynomials in Horner form with fused multiply-adds (std::fma
-//     is correctly rounded, like the GPU's).  The table data come from the
-//     generated gfm_tables.h.
+//   * Tang's table-driven exp and log (ACM TOMS 15(2) 1989, 16(4) 1990) and
+//     acos by the asin Taylor series with half-angle reduction, polynomials in
+//     Horner form with fused multiply-adds (std::fma is correctly rounded,
+//     like the GPU's); pow as 2^(y log2 x) in 32/64/128-bit fixed point (two
+//     table reductions of log2 to |r| < 2^-12.97 and the series of ln(1 + r)
+//     to r^4 in Q75, the exact 128-bit product y log2 x, exp2 by 2^(j/64)
+//     and 2^(k/4096) tables and the series of 2^g - 1 to g^4, one rounding),
+//     written here with the compiler's 128-bit integers.  The table data come from the generated
+//     gfm_tables.h.
 //   * the stiffened-gas EOS that the reference takes from its absent
 //     PhD-Common dependency (call sites headers/euler_misc.hpp:46,59,77,96).
 //   * exact_rs_stiffenedgas, the absent exact solver called at
@@ -30,6 +34,12 @@ static const double EXP2T[64] = GFM_EXP2_TABLE;
 static const double LOGFT[97] = GFM_LOGF_TABLE;
 static const double INVFT[97] = GFM_INVF_TABLE;
 static const double ASINC[28] = GFM_ASIN_COEFFS;
+static const uint32_t XLOG1_RI[49] = GFM_XLOG1_RI;
+static const int64_t XLOG1_T[49] = GFM_XLOG1_T;
+static const uint32_t XLOG2_RI[97] = GFM_XLOG2_RI;
+static const int64_t XLOG2_T[97] = GFM_XLOG2_T;
+static const uint64_t XEXP1_E[64] = GFM_XEXP1_E;
+static const uint64_t XEXP2_E[64] = GFM_XEXP2_E;
 
 inline int64_t bits_of(double x) { int64_t b; std::memcpy(&b, &x, 8); return b; }
 inline double double_of(int64_t b) { double x; std::memcpy(&x, &b, 8); return x; }
@@ -104,9 +114,93 @@ inline double log(double x) {
   return hi + (r + lo);
 }
 
+// log2 x * 2^62 for a positive finite x, as a 128-bit integer
+inline __int128 log2_q62(double x) {
+  const uint64_t b = (uint64_t)bits_of(x);
+  int be = (int)(b >> 52);
+  uint64_t sig = b & 0x000fffffffffffffULL;
+  if (be == 0) {                       // subnormal
+    int s = 0;
+    while (!(sig & (1ULL << 52))) { sig <<= 1; s++; }
+    be = 1 - s;
+  } else {
+    sig |= 1ULL << 52;
+  }
+  // m = sig / 2^52 in [1, 2); taken to [0.75, 1.5) with the exponent
+  const bool halve = sig >= (3ULL << 51);
+  const int64_t m53 = (int64_t)(halve ? sig : sig << 1);   // m 2^53
+  const int expo = be - 1023 + (halve ? 1 : 0);
+  const int j = (int)((m53 - (1LL << 53) + (1LL << 46)) >> 47);         // round(64 (m - 1))
+  const unsigned __int128 P1 = (unsigned __int128)(uint64_t)m53 * XLOG1_RI[j + 16];   // m R1 2^69
+  const int k = (int)((P1 + ((unsigned __int128)1 << 56)) >> 57) - 4096;  // round(4096 (m R1 - 1))
+  const unsigned __int128 P2 = P1 * XLOG2_RI[k + 48];                     // m R1 R2 2^93
+  const int64_t r75 = (int64_t)(uint64_t)(P2 >> 18);                      // (m R1 R2 - 1) 2^75, mod 2^64
+  // ln(1 + r) = r - r^2/2 + r^3/3 - r^4/4, Q75; r^3/3 and r^4/4 from the
+  // leading 32 bits of r 2^43 and r^2 2^56
+  const int64_t r2_86 = (int64_t)(((__int128)r75 * r75) >> 64);
+  const int32_t r2_56 = (int32_t)(r2_86 >> 30);
+  const int32_t r_43 = (int32_t)(r75 >> 32);
+  const int32_t r_43_third = (int32_t)(((int64_t)r_43 * 0x55555556LL) >> 32);
+  const int64_t ln1p = r75 - (r2_86 >> 12) + (((int64_t)r2_56 * r_43_third) >> 24) -
+                       (((int64_t)r2_56 * r2_56) >> 39);
+  const int64_t log2_1p = (int64_t)(((__int128)ln1p * GFM_XLOG_INVLN2) >> 75);   // Q62
+  return (__int128)expo * ((__int128)1 << 62) + XLOG1_T[j + 16] + XLOG2_T[k + 48] + log2_1p;
+}
+
+// 2^(t 2^-64) for a 128-bit t with |t| < 2^75
+inline double exp2_q64(__int128 t) {
+  const int64_t n = (int64_t)(t >> 64);
+  const uint64_t f = (uint64_t)t;
+  const int j = (int)(f >> 58), k = (int)((f >> 52) & 63);
+  const uint64_t g76 = (f & 0x000fffffffffffffULL) << 12;                // (f 2^-64 - j/64 - k/4096) 2^76
+  const uint64_t u = (uint64_t)(((unsigned __int128)g76 * GFM_XEXP_LN2) >> 64);   // g ln2, Q76
+  const uint64_t u2 = (uint64_t)(((unsigned __int128)u * u) >> 64);     // Q88
+  const uint32_t u_44 = (uint32_t)(u >> 32), u2_56 = (uint32_t)(u2 >> 32);
+  const uint32_t u_sixth = (uint32_t)(((uint64_t)u_44 * 0x2aaaaaabULL) >> 32);
+  const uint32_t u2_24th = (uint32_t)(((uint64_t)u2_56 * 0x0aaaaaabULL) >> 32);
+  const uint64_t q = (u + (u2 >> 13) + (((uint64_t)u_sixth * u2_56) >> 24) + (((uint64_t)u2_24th * u2_56) >> 36)) >> 12;
+  const uint64_t E = XEXP1_E[j] + (uint64_t)(((unsigned __int128)XEXP1_E[j] * XEXP2_E[k]) >> 64);   // Q63
+  const uint64_t R = E + (uint64_t)(((unsigned __int128)E * q) >> 64);
+  uint64_t mant = R >> 11;
+  const uint64_t rem = R & 0x7ff;
+  if (rem > 0x400 || (rem == 0x400 && (mant & 1))) mant++;
+  const int64_t bexp = n + 1023;
+  if (bexp >= 1 && bexp <= 2046) return double_of((int64_t)(((uint64_t)(bexp - 1) << 52) + mant));
+  if (bexp > 2046) return HUGE_VAL;
+  if (bexp < -60) return 0.0;
+  const double s = double_of((int64_t)(((uint64_t)(bexp + 599) << 52) + mant));
+  return s * double_of((int64_t)((uint64_t)423 << 52));   // 2^-600
+}
+
+// x^y = 2^(y log2 x) for a positive finite x and a finite y
+inline double pow_fixed(double x, double y) {
+  const __int128 L = log2_q62(x);
+  if (y == 0.0 || L == 0) return 1.0;
+  const uint64_t yb = (uint64_t)bits_of(y);
+  int ey = (int)((yb >> 52) & 0x7ff);
+  uint64_t my = yb & 0x000fffffffffffffULL;
+  if (ey == 0) ey = 1; else my |= 1ULL << 52;
+  const unsigned __int128 mag = (unsigned __int128)(L < 0 ? -L : L) * my;   // |y| |L| 2^(1075 - ey + 62)
+  int nbits = 0;
+  for (unsigned __int128 v = mag; v; v >>= 1) nbits++;
+  const bool neg = (L < 0) != ((yb >> 63) != 0);
+  const int sh = ey - 1073;                                // |T| 2^64 = mag 2^sh
+  if (nbits + sh > 75) return neg ? 0.0 : HUGE_VAL;
+  unsigned __int128 t = sh >= 0 ? (mag << sh) : (-sh >= 128 ? 0 : (mag >> -sh));
+  const __int128 T = neg ? -(__int128)t : (__int128)t;
+  return exp2_q64(T);
+}
+
 inline double pow(double x, double y) {
-  if (x == 0.0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : HUGE_VAL);
-  return omath::exp(y * omath::log(x));
+  if (y == 0.0) return 1.0;
+  if (std::isnan(x) || std::isnan(y) || x < 0.0) return NAN;
+  if (x == 0.0) return (y > 0.0) ? 0.0 : HUGE_VAL;
+  if (std::isinf(x)) return (y > 0.0) ? HUGE_VAL : 0.0;
+  if (std::isinf(y)) {
+    if (x == 1.0) return 1.0;
+    return ((x > 1.0) == (y > 0.0)) ? HUGE_VAL : 0.0;
+  }
+  return pow_fixed(x, y);
 }
 
 inline double asin_series(double x) {

@@ -17,7 +17,7 @@ using namespace gfm;
 std::atomic<long long> gfm::g_launches{0};
 
 // ---------------------------------------------------------------------------
-// SM partitions for the overlapped ghost fill: an 8-SM green context for the
+// SM partitions for the overlapped ghost fill: a 16-SM green context for the
 // interface chain and one for the remaining SMs, with one stream each,
 // created once per device.  The driver entry points are fetched through the
 // runtime, so the library does not link libcuda.  Without green-context
@@ -28,7 +28,7 @@ std::atomic<long long> gfm::g_launches{0};
 
 namespace {
 std::mutex g_green_mutex;
-struct GreenPair { bool init; bool ok; cudaStream_t chain, far; };
+struct GreenPair { bool init; bool ok; int chain_sms; cudaStream_t chain, far; };
 GreenPair g_green[64];
 
 template <typename F>
@@ -42,7 +42,7 @@ bool entry(const char* name, F* fn, unsigned version = 12040) {
   return true;
 }
 
-bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far) {
+bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms_out) {
   PFN_cuDeviceGet_v2000 pDeviceGet;
   PFN_cuDeviceGetDevResource_v12040 pGetRes;
   PFN_cuDevSmResourceSplitByCount_v12040 pSplit;
@@ -58,9 +58,18 @@ bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far) {
   CUdevResource res, grp[1], rem;
   if (pGetRes(d, &res, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return false;
   unsigned nb = 1;
-  // 8 SMs for the chain: measured on the 1000x400 shock-bubble against 16,
-  // 24 and 32 (2.66 against 2.71, 2.79 and 2.89 ms per step)
-  if (pSplit(grp, &nb, &res, &rem, 0, 8) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
+  // 16 SMs for the chain: measured on the 1000x400 shock-bubble against 8
+  // and 24 (steps 5-25: 240.2 against 228.5 and 242.3 M cell-updates/s;
+  // steps 3-303: 201.9, 198.4, 201.1 M; the whole run: 180.0, 178.7, 178.0 M
+  // -- the far field grows along the run and wants the SMs back);
+  // GFM_CHAIN_SMS (environment, a multiple of 8 up to 64) overrides it
+  unsigned chain_sms = 16;
+  if (const char* e = getenv("GFM_CHAIN_SMS")) {
+    const int v = atoi(e);
+    if (v >= 8 && v <= 64 && v % 8 == 0) chain_sms = (unsigned)v;
+  }
+  if (pSplit(grp, &nb, &res, &rem, 0, chain_sms) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
+  *chain_sms_out = (int)grp[0].sm.smCount;
   CUdevResourceDesc d1, d2;
   if (pDesc(&d1, grp, 1) != CUDA_SUCCESS || pDesc(&d2, &rem, 1) != CUDA_SUCCESS) return false;
   CUgreenCtx g1, g2;
@@ -75,13 +84,14 @@ bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far) {
 }
 }  // namespace
 
-bool gfm::green_streams(int dev, cudaStream_t* chain, cudaStream_t* far) {
+bool gfm::green_streams(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms) {
   if (dev < 0 || dev >= 64) return false;
   std::lock_guard<std::mutex> lk(g_green_mutex);
   GreenPair& g = g_green[dev];
   if (!g.init) {
     g.init = true;
-    g.ok = make_green(dev, &g.chain, &g.far);
+    g.chain_sms = 16;
+    g.ok = make_green(dev, &g.chain, &g.far, &g.chain_sms);
     if (!g.ok) {
       cudaGetLastError();
       g.ok = cudaStreamCreateWithFlags(&g.chain, cudaStreamNonBlocking) == cudaSuccess &&
@@ -90,6 +100,7 @@ bool gfm::green_streams(int dev, cudaStream_t* chain, cudaStream_t* far) {
   }
   *chain = g.chain;
   *far = g.far;
+  *chain_sms = g.chain_sms;
   return g.ok;
 }
 
@@ -225,7 +236,8 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur) != cudaSuccess || sms < 1)
       sms = 152;
     ctx->num_sms = sms;
-    ctx->far_sms = sms > 16 ? sms - 8 : sms;   // the far partition of the overlapped ghost fill
+    ctx->chain_sms = 16;
+    ctx->far_sms = sms > 32 ? sms - 16 : sms;   // the far partition of the overlapped ghost fill
   }
   CtxExtra& X = extra(ctx);
   alloc((void**)&X.counters, 64);
@@ -291,7 +303,8 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_lists, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_done, cudaEventDisableTiming);
-    if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far) ? 1 : 0;
+    if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far, &ctx->chain_sms) ? 1 : 0;
+    if (ctx->overlap_ok && ctx->num_sms > ctx->chain_sms + 8) ctx->far_sms = ctx->num_sms - ctx->chain_sms;
     ctx->overlap = ctx->overlap_ok ? GFM_OVERLAP_AUTO : GFM_OVERLAP_OFF;
   }
   if (e == cudaSuccess) prepare_kernels();   // kernel attributes and occupancies, before any capture

@@ -74,6 +74,7 @@ struct gfm_ctx {
   int chunk;         // cells per CTA of the chunked kernels (k_prims, k_vof_prims, k_compact)
   int num_sms;       // SMs of the device, and of the far partition of the overlapped ghost fill
   int far_sms;
+  int chain_sms;   // SMs of the overlapped ghost fill's chain partition
   double* stage;     // packed (unpitched) copy of the whole state: 4, 4 and 1 planes of nr x nc
                      // (gfm_upload_state / gfm_download_state)
   // per-interface work arrays (capacity = Nx*Ny)
@@ -192,7 +193,7 @@ int flux_batch_occupancy(int fs, int shape);
 // kernel launch helpers (defined in the .cu files)
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask);
 void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaStream_t stream);
-bool green_streams(int device, cudaStream_t* chain, cudaStream_t* far);
+bool green_streams(int device, cudaStream_t* chain, cudaStream_t* far, int* chain_sms);
 void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_bcs(gfm_ctx* ctx, int fluid_mask);
 void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);

@@ -146,6 +146,29 @@ GFM_HD double tab_asin(int j) {
 #endif
 }
 
+// tables of the fixed-point pow (gen_tables.py)
+#if defined(__CUDACC__)
+__device__ static const uint32_t d_xlog1_ri[49] = GFM_XLOG1_RI;
+__device__ static const int64_t d_xlog1_t[49] = GFM_XLOG1_T;
+__device__ static const uint32_t d_xlog2_ri[97] = GFM_XLOG2_RI;
+__device__ static const int64_t d_xlog2_t[97] = GFM_XLOG2_T;
+__device__ static const uint64_t d_xexp1_e[64] = GFM_XEXP1_E;
+__device__ static const uint64_t d_xexp2_e[64] = GFM_XEXP2_E;
+#endif
+static const uint32_t h_xlog1_ri[49] = GFM_XLOG1_RI;
+static const int64_t h_xlog1_t[49] = GFM_XLOG1_T;
+static const uint32_t h_xlog2_ri[97] = GFM_XLOG2_RI;
+static const int64_t h_xlog2_t[97] = GFM_XLOG2_T;
+static const uint64_t h_xexp1_e[64] = GFM_XEXP1_E;
+static const uint64_t h_xexp2_e[64] = GFM_XEXP2_E;
+#if defined(__CUDA_ARCH__)
+#define GFM_XTAB(name, j) __ldg(&d_##name[j])
+#define GFM_XTAB64(type, name, j) ((type)__ldg((const unsigned long long*)&d_##name[j]))
+#else
+#define GFM_XTAB(name, j) (h_##name[j])
+#define GFM_XTAB64(type, name, j) (h_##name[j])
+#endif
+
 GFM_HD double gfm_inf() { return from_bits(0x7ff0000000000000LL); }
 GFM_HD double gfm_nan() { return from_bits(0x7ff8000000000000LL); }
 
@@ -354,10 +377,168 @@ GFM_HD double gfm_log(double x) {
   return hi + (r + lo);
 }
 
-// pow for x >= 0 (all uses have a positive base): exp(y log x); pow(1,y) == 1.
+// ---------------------------------------------------------------------------
+// pow in fixed point on the integer pipes.  A dependent chain of FP64
+// instructions costs 64 cycles each on GB300, and exp(y log x) in FP64 is
+// about 25 of them; here x^y = 2^(y log2 x) is formed in 32-, 64- and
+// 128-bit integer arithmetic with few dependent 64-bit products, and rounded
+// once:
+//   log2 x = e + log2 m, m in [0.75, 1.5).  Two table reductions:
+//   j = round(64 (m - 1)) picks R1 = RI1_j / 2^16 ~ 1/(1 + j/64), then
+//   k = round(4096 (m R1 - 1)) picks R2 = RI2_k / 2^24, so that
+//   m R1 R2 = 1 + r exactly (|r| < 2^-12.97, formed in integers as r 2^75);
+//   ln(1 + r) = r - r^2/2 + r^3/3 - r^4/4 (r^2 from a 64-bit product, the
+//   two small terms in 32-bit), times 1/ln2, plus log2(1/R1) + log2(1/R2)
+//   (tables), all in Q62.
+//   T = y log2 x exactly as a 128-bit product of y's significand and
+//   (e 2^62 + log2 m 2^62), scaled to T 2^64 = n 2^64 + f.
+//   2^T = 2^n 2^(j/64) 2^(k/4096) 2^g, g < 2^-12: the first two factors
+//   from tables (Q63, and 2^(k/4096) - 1 in Q64), 2^g - 1 = u + u^2/2 +
+//   u^3/6 + u^4/24 with u = g ln2 (u and u^2 from 64-bit products, the
+//   small terms in 32-bit), rounded to nearest even.
+// The result is within about 2^-57 of x^y (relative; 0.51 ulp for the
+// exponents of the Riemann solver); the same integer operations on the host
+// and the device give the same bits.  Tables: gen_tables.py (mpmath).
+// ---------------------------------------------------------------------------
+struct XLog2 { int e; int64_t f; };   // log2 x = e + f 2^-62
+
+// high 32 bits of 32 x 32-bit products (signed: floor of the product / 2^32)
+GFM_HD int32_t xfp_smulhi32(int32_t a, int32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __mulhi(a, b);
+#else
+  return (int32_t)(((int64_t)a * b) >> 32);
+#endif
+}
+GFM_HD uint32_t xfp_umulhi32(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+// log2 of a positive finite x
+GFM_HD XLog2 xlog2_fixed(double x) {
+  const uint64_t b = (uint64_t)as_bits(x);
+  int ex = (int)(b >> 52);
+  uint64_t M = b & 0x000fffffffffffffull;
+  if (ex == 0) {   // subnormal: normalise the significand
+    const int sh = (int)xfp_clz64(M) - 11;
+    M <<= sh;
+    ex = 1 - sh;
+  } else {
+    M |= 1ull << 52;
+  }
+  const int h = (int)((M >> 51) & 1u);            // m >= 1.5: halve it
+  const uint64_t mq = h ? M : (M << 1);           // m 2^53, m in [0.75, 1.5)
+  const int j = (int)(((int64_t)mq - (1ll << 53) + (1ll << 46)) >> 47);   // -16..32
+  const uint64_t R1 = (uint64_t)GFM_XTAB(xlog1_ri, j + 16);
+  const uint64_t p1l = mq * R1, p1h = xfp_mulhi(mq, R1);                   // m R1 2^69
+  const uint64_t t = p1l + (1ull << 56);
+  const int k = (int)((int64_t)(((p1h + (t < p1l ? 1u : 0u)) << 7) | (t >> 57)) - 4096);   // -48..48
+  const uint64_t R2 = (uint64_t)GFM_XTAB(xlog2_ri, k + 48);
+  const uint64_t p2l = p1l * R2, p2h = xfp_mulhi(p1l, R2) + p1h * R2;     // m R1 R2 2^93
+  const int64_t rho = (int64_t)((p2h << 46) | (p2l >> 18));               // r 2^75
+  const int64_t s2 = xfp_smulhi(rho, rho);                                 // r^2 2^86
+  const int32_t a2 = (int32_t)(s2 >> 30);                                  // r^2 2^56
+  const int32_t a1 = (int32_t)(rho >> 32);                                 // r 2^43
+  const int32_t a1d3 = xfp_smulhi32(a1, 0x55555556);                       // r/3 2^43
+  const int64_t ln1p = rho - (s2 >> 12) + (((int64_t)a2 * a1d3) >> 24) - (((int64_t)a2 * a2) >> 39);   // Q75
+  XLog2 L;
+  L.e = ex - 1023 + h;
+  L.f = GFM_XTAB64(int64_t, xlog1_t, j + 16) + GFM_XTAB64(int64_t, xlog2_t, k + 48) +
+        (xfp_smulhi(ln1p, GFM_XLOG_INVLN2) >> 11);
+  return L;
+}
+
+// 2^(n + f 2^-64), n an integer and f in Q64
+GFM_HD double xexp2_fixed(int64_t n, uint64_t f) {
+  const int j = (int)(f >> 58), k = (int)((f >> 52) & 63u);
+  const uint64_t g76 = (f & 0x000fffffffffffffull) << 12;                 // g 2^76
+  const uint64_t u = xfp_mulhi(g76, GFM_XEXP_LN2);                         // g ln2, Q76
+  const uint64_t u2 = xfp_mulhi(u, u);                                     // Q88
+  const uint32_t b1 = (uint32_t)(u >> 32), b2 = (uint32_t)(u2 >> 32);      // Q44, Q56
+  const uint32_t b1d6 = xfp_umulhi32(b1, 0x2aaaaaabu);                     // u/6
+  const uint32_t b2d24 = xfp_umulhi32(b2, 0x0aaaaaabu);                    // u^2/24
+  const uint64_t q = (u + (u2 >> 13) + (((uint64_t)b1d6 * b2) >> 24) + (((uint64_t)b2d24 * b2) >> 36)) >> 12;   // 2^g - 1, Q64
+  const uint64_t E1 = GFM_XTAB64(uint64_t, xexp1_e, j);
+  const uint64_t E = E1 + xfp_mulhi(E1, GFM_XTAB64(uint64_t, xexp2_e, k));  // 2^(j/64 + k/4096), Q63
+  const uint64_t R = E + xfp_mulhi(E, q);                                   // 2^(f 2^-64), Q63
+  uint64_t mant = R >> 11;
+  const uint32_t rem = (uint32_t)R & 0x7ffu;
+  mant += (rem > 0x400u || (rem == 0x400u && (mant & 1u) != 0u)) ? 1u : 0u;   // [2^52, 2^53]
+  const int64_t be = n + 1023;
+  if (be >= 1 && be <= 2046) return from_bits((int64_t)(((uint64_t)(be - 1) << 52) + mant));
+  if (be > 2046) return gfm_inf();
+  if (be < -60) return 0.0;
+  // below the normal range: the rounded significand scaled by 2^(n + 600),
+  // exactly, then by 2^-600 with one more rounding
+  const double s = from_bits((int64_t)(((uint64_t)(be + 599) << 52) + mant));
+  return s * from_bits((int64_t)((uint64_t)(1023 - 600) << 52));
+}
+
+// 2^(y log2 x) for log2 x = L of a positive finite x and a finite y
+GFM_HD double xpow_fixed(const XLog2& L, double y) {
+  const uint64_t yb = (uint64_t)as_bits(y);
+  int ey = (int)((yb >> 52) & 0x7ffu);
+  uint64_t My = yb & 0x000fffffffffffffull;
+  if (ey == 0) ey = 1;   // subnormal y (or zero: a zero product below)
+  else My |= 1ull << 52;
+  // Lambda = e 2^62 + f, signed 128-bit (lh, ll), then its magnitude
+  uint64_t ll = (uint64_t)(int64_t)L.e << 62;
+  int64_t lh = (int64_t)L.e >> 2;
+  const uint64_t s1 = ll + (uint64_t)L.f;
+  lh += (L.f < 0 ? -1 : 0) + (s1 < ll ? 1 : 0);
+  ll = s1;
+  const bool lneg = lh < 0;
+  if (lneg) {
+    ll = ~ll + 1u;
+    lh = (int64_t)(~(uint64_t)lh + (ll == 0u ? 1u : 0u));
+  }
+  // Pi = My |Lambda| < 2^126; |T| 2^64 = Pi 2^(ey - 1073)
+  uint64_t pl = My * ll;
+  uint64_t ph = xfp_mulhi(My, ll) + My * (uint64_t)lh;
+  if ((pl | ph) == 0u) return 1.0;
+  const int bits = ph ? 128 - (int)xfp_clz64(ph) : 64 - (int)xfp_clz64(pl);
+  const int sh = ey - 1073;
+  const bool neg = lneg != ((yb >> 63) != 0u);
+  if (bits + sh > 75) return neg ? 0.0 : gfm_inf();   // |T| >= 2^11
+  if (sh > 0) {
+    if (sh >= 64) { ph = pl << (sh - 64); pl = 0u; }
+    else { ph = (ph << sh) | (pl >> (64 - sh)); pl <<= sh; }
+  } else if (sh < 0) {
+    const int k = -sh;
+    if (k >= 128) { pl = 0u; ph = 0u; }
+    else if (k >= 64) { pl = ph >> (k - 64); ph = 0u; }
+    else { pl = (pl >> k) | (ph << (64 - k)); ph >>= k; }
+  }
+  if (neg) {
+    pl = ~pl + 1u;
+    ph = ~ph + (pl == 0u ? 1u : 0u);
+  }
+  return xexp2_fixed((int64_t)ph, pl);   // n = floor(T), f = T - n in Q64
+}
+
+// x^y for x >= 0 (every use has a positive base; a negative or NaN base
+// gives NaN): 1 for y = 0; 0 or inf for x = 0 and x = inf by y's sign; x = 1
+// gives 1 exactly.
+GFM_HD bool xpow_plain(double x) {   // positive and finite: the fixed-point path
+  const int64_t b = as_bits(x);
+  return b > 0 && b < GFM_INF_BITS;
+}
 GFM_HD double gfm_pow(double x, double y) {
-  if ((as_bits(x) & GFM_MAG_BITS) == 0) return (y > 0.0) ? 0.0 : ((y == 0.0) ? 1.0 : gfm_inf());
-  return gfm_exp(mulx(y, gfm_log(x)));
+  const int64_t xb = as_bits(x), yb = as_bits(y);
+  const int64_t xm = xb & GFM_MAG_BITS, ym = yb & GFM_MAG_BITS;
+  if (ym == 0) return 1.0;
+  if (xm > GFM_INF_BITS || ym > GFM_INF_BITS || (xb < 0 && xm != 0)) return gfm_nan();
+  if (xm == 0) return yb > 0 ? 0.0 : gfm_inf();
+  if (xm == GFM_INF_BITS) return yb > 0 ? gfm_inf() : 0.0;
+  if (ym == GFM_INF_BITS) {
+    if (xb == 0x3ff0000000000000LL) return 1.0;
+    return ((xb > 0x3ff0000000000000LL) == (yb > 0)) ? gfm_inf() : 0.0;
+  }
+  return xpow_fixed(xlog2_fixed(x), y);
 }
 
 // asin on [-0.5, 0.5] by its Taylor series (28 terms), in Horner form in x^2.
@@ -728,8 +909,9 @@ GFM_HD double rs_rho_star(const RSSide& K, const Gas& k, double pstar) {
 // from the side: a warp whose lanes sample different sides issues the FP64
 // work once, not once per side.  Every value comes from the same operations
 // as Toro's four branches (a - b is formed as a + (-b), which is the same
-// IEEE operation), and a rarefaction's star density shares the logarithm of
-// (p* + pinf)/(p_K + pinf) with the tail speed (gfm_pow is exp(y log x)).
+// IEEE operation), and a rarefaction's star density shares the fixed-point
+// log2 of (p* + pinf)/(p_K + pinf) with the tail speed (the same values as
+// two gfm_pow calls).
 struct RS1D { double rho, u, p; };
 template <bool ID = true>
 GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas& kR, const RSStar& st,
@@ -760,13 +942,14 @@ GFM_HD RS1D rs_sample(const RSSide& L, const Gas& kL, const RSSide& R, const Gas
   }
   const double hK = Ku + (left ? -Kc : Kc);   // rarefaction head
   if (left ? c_le(S, hK) : c_ge(S, hK)) { w.rho = Krho; w.u = Ku; w.p = Kp; return w; }
-  const bool zero = (as_bits(pr) & GFM_MAG_BITS) == 0;
-  const double lpr = zero ? 0.0 : gfm_log(pr);
-  const double cm = mulx(Kc, zero ? gfm_pow(pr, G1) : gfm_exp(mulx(G1, lpr)));
+  const bool plain = xpow_plain(pr);
+  XLog2 lpr;
+  if (plain) lpr = xlog2_fixed(pr);
+  const double cm = mulx(Kc, plain ? xpow_fixed(lpr, G1) : gfm_pow(pr, G1));
   const double tK = st.u + (left ? -cm : cm);   // rarefaction tail
   if (left ? c_gt(S, tK) : c_le(S, tK)) {
     // rs_rho_star of a rarefaction (p* <= p_K here, or NaN on the right)
-    w.rho = mulx(Krho, zero ? gfm_pow(pr, IG) : gfm_exp(mulx(IG, lpr)));
+    w.rho = mulx(Krho, plain ? xpow_fixed(lpr, IG) : gfm_pow(pr, IG));
     w.u = st.u; w.p = st.p;
     return w;
   }

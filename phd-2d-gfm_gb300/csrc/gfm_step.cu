@@ -509,8 +509,8 @@ constexpr int NEAR_RADIUS = 6;
 constexpr int BAND_CLASSES = NEAR_RADIUS + 1;
 // CTAs of the listed sweeps after the loop: the band holds a few thousand to
 // about ten thousand cells, about one per thread of 40 CTAs of 256 threads
-// (one wave on the loop's own 8 SMs, which these kernels share with the
-// level set while the far field's flux update fills the other SMs)
+// (within one wave on the loop's own 16 SMs, which these kernels share with
+// the level set while the far field's flux update fills the other SMs)
 constexpr int NEAR_CTAS = 40;
 
 struct ExtrapArgs {
@@ -803,6 +803,16 @@ __device__ V4 ifc_bilinear(const IfcArgs& a, int f, double x, double y, int64_t 
             w00 * g00.d + w01 * g01.d + w10 * g10.d + w11 * g11.d};
 }
 
+// The interface loops are latency-bound chains of dependent cells: they form
+// their quotients and roots with the FP64 operations (CHAIN_ID false), whose
+// dependent latency is about that of the integer forms while their code is
+// shorter.
+#ifndef GFM_CHAIN_INT_DIV
+constexpr bool CHAIN_ID = false;
+#else
+constexpr bool CHAIN_ID = true;
+#endif
+
 template <int MODE>
 __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
   const GridP& P = a.P;
@@ -859,7 +869,7 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
         for (int yinc = -1; yinc <= 1; yinc++) {
           double dp = dpk[(xinc + 1) * 3 + (yinc + 1)];
           if (dp < -2.0 || dp < dbest - 1e-6) continue;
-          double ang = gfm_acos<false>(dp);
+          double ang = gfm_acos<CHAIN_ID>(dp);
           if (ang < mindiff) { iopp = i + yinc; jopp = j + xinc; mindiff = ang; }
         }
       if (iopp == -1000) { st |= ST_BAD_ARGUMENT; iopp = i; jopp = j; }
@@ -901,10 +911,10 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
     V4 Lp = V4{ip1.a, u1n, 0.0, (1e-6 < ip1.d) ? ip1.d : 1e-6};
     V4 Rp = V4{ip2.a, u2n, 0.0, (1e-6 < ip2.d) ? ip2.d : 1e-6};
     bool ok1 = true, ok2 = true;
-    V4 Ls = prims_to_cons<false>(P.g1, P.p1, Lp, &ok1);
-    V4 Rs = prims_to_cons<false>(P.g2, P.p2, Rp, &ok2);
+    V4 Ls = prims_to_cons<CHAIN_ID>(P.g1, P.p1, Lp, &ok1);
+    V4 Rs = prims_to_cons<CHAIN_ID>(P.g2, P.p2, Rp, &ok2);
     if (!ok1 || !ok2) st |= ST_UNPHYSICAL;
-    MixedStar m = mixed_rs<false>(P.gas1, P.gas2, Ls, Rs, &st, &iters);
+    MixedStar m = mixed_rs<CHAIN_ID>(P.gas1, P.gas2, Ls, Rs, &st, &iters);
     double snx = m.u_star * nx, sny = m.u_star * ny;
     if (MODE == IFC_MODIFIED) {
       double u1x, u1y, u2x, u2y;
@@ -912,10 +922,10 @@ __global__ void __launch_bounds__(128) k_interface(IfcArgs a) {
       else if (lsval <= 0.0) { u1x = snx + t1x; u1y = sny + t1y; u2x = snx + t1x; u2y = sny + t1y; }
       else { u1x = snx + t2x; u1y = sny + t2y; u2x = snx + t2x; u2y = sny + t2y; }
       if (lsval <= 0.0) {
-        o[0] = eos_isentropic_extrapolation<false>(P.g1, P.p1, m.rho_star_L, m.p_star, load4(a.W1, P, c).d);
+        o[0] = eos_isentropic_extrapolation<CHAIN_ID>(P.g1, P.p1, m.rho_star_L, m.p_star, load4(a.W1, P, c).d);
         o[1] = m.rho_star_R; o[2] = u2x; o[3] = u2y; o[4] = m.p_star;
       } else {
-        o[0] = eos_isentropic_extrapolation<false>(P.g2, P.p2, m.rho_star_R, m.p_star, load4(a.W2, P, c).d);
+        o[0] = eos_isentropic_extrapolation<CHAIN_ID>(P.g2, P.p2, m.rho_star_R, m.p_star, load4(a.W2, P, c).d);
         o[1] = m.rho_star_L; o[2] = u1x; o[3] = u1y; o[4] = m.p_star;
       }
       o[5] = snx; o[6] = sny;
@@ -986,7 +996,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   // cons_to_prims_phys with its three quotients by rho (rho u, rho v, E) in
   // one: lane kc of each group of four divides component kc + 1 (E twice)
   const int lane = threadIdx.x & 31, grp = lane & ~3, kq = lane & 3;
-  const Recip Rr = recip<false>(Uown.a);
+  const Recip Rr = recip<CHAIN_ID>(Uown.a);
   const double qv = rdiv(kq == 0 ? Uown.b : (kq == 1 ? Uown.c : Uown.d), Rr);
   const double uq = __shfl_sync(FULL_MASK, qv, grp), vq = __shfl_sync(FULL_MASK, qv, grp + 1);
   const double eq = __shfl_sync(FULL_MASK, qv, grp + 2) - 0.5 * (uq * uq + vq * vq);
@@ -1006,10 +1016,10 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   {
     // rs_side_consts with its two reciprocals (1/rho, 1/pb) in one division:
     // even lanes divide by rho, odd lanes by pb, and exchange
-    const double y = divx<false>(1.0, (lane & 1) ? S.pb : S.rho);
+    const double y = divx<CHAIN_ID>(1.0, (lane & 1) ? S.pb : S.rho);
     const double irho = __shfl_sync(FULL_MASK, y, lane & ~1), ipb = __shfl_sync(FULL_MASK, y, lane | 1);
     S.ipb = ipb;
-    S.c = sqrtx<false>(k.g * S.pb * irho);
+    S.c = sqrtx<CHAIN_ID>(k.g * S.pb * irho);
     S.AK = k.G5 * irho;
     S.BK = k.G6 * S.pb;
     S.G4c = k.G4 * S.c;
@@ -1027,15 +1037,15 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   const double pbmin = c_lt(pbL, pbR) ? pbL : pbR;
   const double pfl = 1e-6 * pbmin - pinf_min;
   const double pg = c_gt(ppv, pfl) ? ppv : pfl;
-  const double gown = sqrtx<false>(divx<false>(S.AK, pg + k.pinf + S.BK));
+  const double gown = sqrtx<CHAIN_ID>(divx<CHAIN_ID>(S.AK, pg + k.pinf + S.BK));
   const double goth = xside(gown);
   const double gL = isR ? goth : gown, gR = isR ? gown : goth;
-  const double pts = divx<false>(gL * pL + gR * pR - (uR - uL), gL + gR);
+  const double pts = divx<CHAIN_ID>(gL * pL + gR * pR - (uR - uL), gL + gR);
   double p0 = pts;
   bool gated = false;
   float x[MLP_IN];
   if (a.mlp || a.cap_X) {   // warp-uniform: both halves hold the same values
-    const double ratio = divx<false>(pts + pinf_min, pg + pinf_min);
+    const double ratio = divx<CHAIN_ID>(pts + pinf_min, pg + pinf_min);
     gated = c_gt(ratio, 0.0) && c_gt(fabs(gfm_log(ratio)), MLP_GATE);
     if (gated) mlp_features_f(rhoL, uL, pbL, kL.g, kL.pinf, rhoR, uR, pbR, kR.g, kR.pinf, x);
     if (gated && a.mlp) {
@@ -1058,7 +1068,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
     fR = isR ? f : of;
     fLd = isR ? ofd : fd;
     fRd = isR ? fd : ofd;
-    p = pold - divx<false>(fL + fR + udiff, fLd + fRd);
+    p = pold - divx<CHAIN_ID>(fL + fR + udiff, fLd + fRd);
     if (c_lt(p, pfl)) p = pfl;
     it++;
     bool conv = c_le(2.0 * fabs(p - pold), GFM_RS_TOL * (p + pold + 2.0 * pinf_min));
@@ -1069,7 +1079,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   }
   r.p = p;
   r.u = 0.5 * (uL + uR + (fR + fRd * dp) - (fL + fLd * dp));
-  r.rho_own = rs_rho_star<false>(S, k, p);
+  r.rho_own = rs_rho_star<CHAIN_ID>(S, k, p);
   *iters += it;
   if (gated && a.cap_X && (threadIdx.x & 31) == 0 && it < kL.maxit && !c_le(G4cL + G4cR, udiff)) {
     const double y = gfm_log((p + pinf_min) / (pts + pinf_min));
@@ -1196,7 +1206,7 @@ __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k,
     const bool elig = lane < 9 && !(dp < -2.0 || dp < dbest - 1e-6);
     long long key = 0x7ff0000000000000LL;   // +inf: not a candidate
     if (elig) {
-      const double ang = gfm_acos<false>(dp);
+      const double ang = gfm_acos<CHAIN_ID>(dp);
       if (ang == ang) key = as_bits(ang);   // angles are >= +0: bits order as values
     }
     int bl = (key == 0x7ff0000000000000LL) ? 32 : lane;
@@ -1249,13 +1259,21 @@ __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k,
   cell.tx = ib - un * nx;
   cell.ty = ic - un * ny;
   bool okp = true;
-  cell.Us = prims_to_cons<false>(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
+  cell.Us = prims_to_cons<CHAIN_ID>(k.g, k.pinf, V4{ia, un, 0.0, c_lt(1e-6, id) ? id : 1e-6}, &okp);
   if (!okp) st |= ST_UNPHYSICAL;
   return true;
 }
 
+// CTAs of k_interface_warp resident per SM that the register allocation
+// must allow: the overlapped schedule launches two CTAs of 8 warps per SM of
+// its chain partition, and two resident per SM (128 registers, a few
+// spilled) ran the shock-bubble's chain 13% faster than one (212 registers,
+// no spills) on an 8-SM partition
+#ifndef GFM_CHAIN_MIN_CTAS
+#define GFM_CHAIN_MIN_CTAS 2
+#endif
 template <int MODE>
-__global__ void __launch_bounds__(256) k_interface_warp(IfcArgs a) {
+__global__ void __launch_bounds__(256, GFM_CHAIN_MIN_CTAS) k_interface_warp(IfcArgs a) {
   const GridP& P = a.P;
   if (!a.D->active) return;
   const int n = a.D->n_ifc;
@@ -1571,7 +1589,7 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       const double un = own[1] * nx + own[2] * ny;
       const double tx = own[1] - un * nx, ty = own[2] - un * ny;
       bool okp = true;
-      const V4 Us = prims_to_cons<false>(k.g, k.pinf, V4{own[0], un, 0.0, c_lt(1e-6, own[3]) ? own[3] : 1e-6}, &okp);
+      const V4 Us = prims_to_cons<CHAIN_ID>(k.g, k.pinf, V4{own[0], un, 0.0, c_lt(1e-6, own[3]) ? own[3] : 1e-6}, &okp);
       if (!okp) st |= ST_UNPHYSICAL;
       int it = 0, gt = 0;
       const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, Us, &st, &it, a, &gt);
@@ -1589,10 +1607,10 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       m1v[0] = rhoL; m1v[1] = u1x; m1v[2] = u1y; m1v[3] = m.p;
       m2v[0] = rhoR; m2v[1] = u2x; m2v[2] = u2y; m2v[3] = m.p;
       if (zc > 0.5) {
-        o1[0] = eos_isentropic_extrapolation<false>(P.g1, P.p1, rhoL, m.p, w1.d); o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
+        o1[0] = eos_isentropic_extrapolation<CHAIN_ID>(P.g1, P.p1, rhoL, m.p, w1.d); o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
         for (int e = 0; e < 4; e++) o2[e] = m2v[e];
       } else {
-        o2[0] = eos_isentropic_extrapolation<false>(P.g2, P.p2, rhoR, m.p, w2.d); o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
+        o2[0] = eos_isentropic_extrapolation<CHAIN_ID>(P.g2, P.p2, rhoR, m.p, w2.d); o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
         for (int e = 0; e < 4; e++) o1[e] = m1v[e];
       }
     } else {
@@ -1601,10 +1619,10 @@ __global__ void __launch_bounds__(256) k_vof_chain(IfcArgs a, double* mrp) {
       for (int e = 0; e < 4; e++) { m1v[e] = s0[e]; m2v[e] = s1[e]; }
       if (zc > 0.5) {
         o1[0] = w1.a; o1[1] = w1.b; o1[2] = w1.c; o1[3] = w1.d;
-        o2[0] = eos_isentropic_extrapolation<false>(P.g2, P.p2, m2v[0], m2v[3], w1.d); o2[1] = w1.b; o2[2] = w1.c; o2[3] = w1.d;
+        o2[0] = eos_isentropic_extrapolation<CHAIN_ID>(P.g2, P.p2, m2v[0], m2v[3], w1.d); o2[1] = w1.b; o2[2] = w1.c; o2[3] = w1.d;
       } else {
         o2[0] = w2.a; o2[1] = w2.b; o2[2] = w2.c; o2[3] = w2.d;
-        o1[0] = eos_isentropic_extrapolation<false>(P.g1, P.p1, m1v[0], m1v[3], w2.d); o1[1] = w2.b; o1[2] = w2.c; o1[3] = w2.d;
+        o1[0] = eos_isentropic_extrapolation<CHAIN_ID>(P.g1, P.p1, m1v[0], m1v[3], w2.d); o1[1] = w2.b; o1[2] = w2.c; o1[3] = w2.d;
       }
     }
     if (lane == 0) {
@@ -2437,7 +2455,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     k_ifc_probes<<<16, 256, 0, ctx->s_chain>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
     ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w;
   }
-  const int chain_ctas = 16;   // 8 warps each on the 8-SM partition: 4 chain warps per SM sub-partition
+  const int chain_ctas = 2 * ctx->chain_sms;   // 8 warps each, two per SM: 4 chain warps per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   counted();

@@ -65,6 +65,14 @@ XFP_HD uint64_t xfp_mulhi(uint64_t a, uint64_t b) {
   return (uint64_t)(((unsigned __int128)a * b) >> 64);
 #endif
 }
+// high 64 bits of the signed 128-bit product (floor of the product / 2^64)
+XFP_HD int64_t xfp_smulhi(int64_t a, int64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __mul64hi(a, b);
+#else
+  return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
 
 // Seeds of the Newton-Raphson iterations below: 1/f and 1/sqrt(f) for a
 // float f in [2^22, 2^24), to about 2^-22 relative (the hardware's

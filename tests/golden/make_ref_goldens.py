@@ -101,17 +101,30 @@ def main():
         d = md.digest(desc, r["U1"], None, None, None, r["t"], r["numsteps"])
         d["spec"] = {"sim": "onefluid", "case": case, "Nx": nx, "Ny": ny, "fs": fs, "steps": 25, "CFL": 0.8}
         out["cases"].append(d)
-    # the step at which the reference's assert stops the coarse shock-bubble
+    # the step at which the reference's assert stops the coarse shock-bubble:
+    # the first step count whose run raises it (bisection over 1..3000)
     desc, T = g.case_params("twofluid", "shock_bubble", 100, 40)
     U1, U2, phi = g.case_init("twofluid", "shock_bubble", desc)
     m = g.method(fs="MUSCL", gfm="riemannGFM", itm="LS5", CFL=0.6, T=T)
-    try:
-        rb.twofluid_state(desc, m, U1, U2, phi, 672)
-        raise SystemExit("expected the reference to stop at step 672")
-    except RuntimeError as e:
-        assert "GFM_riemann.cpp:37" in str(e)
+
+    def aborts(n):
+        try:
+            rb.twofluid_state(desc, m, U1, U2, phi, n)
+            return False
+        except RuntimeError as e:
+            assert "GFM_riemann.cpp:37" in str(e), str(e)
+            return True
+    lo, hi = 0, 3000
+    if not aborts(hi):
+        raise SystemExit("expected the reference to stop the coarse shock-bubble within %d steps" % hi)
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        if aborts(mid):
+            hi = mid
+        else:
+            lo = mid
     out["reference_abort"] = {"case": "shock_bubble", "Nx": 100, "Ny": 40, "gfm": "riemannGFM", "fs": "MUSCL",
-                              "itm": "LS5", "CFL": 0.6, "clean_steps": 671, "abort_step": 672,
+                              "itm": "LS5", "CFL": 0.6, "clean_steps": lo, "abort_step": hi,
                               "assert": "sourcecode/GFM_riemann.cpp:37 is_physical_state(grid1[i][j])"}
     json.dump(out, open(OUT, "w"), indent=1, sort_keys=True)
     print(len(out["cases"]), "cases ->", OUT)

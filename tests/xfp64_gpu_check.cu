@@ -4,11 +4,16 @@
 // argument's) significand with random low bits, exponent parity and
 // dividend, then random bit patterns and near squares.  The device seeds are
 // the hardware's approximate reciprocal and reciprocal square root, which
-// the host check (xfp64_check.cpp) does not exercise.  Prints "ok <count>" or
-// the first mismatches.  Built and run by tests/test_xfp64.py.
+// the host check (xfp64_check.cpp) does not exercise.  Then the fixed-point
+// gfm_pow (gfm_math.cuh) on the device against the same function compiled
+// for the host, bit for bit, on the argument ranges of the Riemann solver and
+// beyond.  Prints "ok <count>" or the first mismatches.  Built and run by
+// tests/test_xfp64.py.
 #include <cstdio>
 #include <cstdint>
-#include "../phd-2d-gfm_gb300/csrc/gfm_xfp64.cuh"
+#include <cstring>
+#include <vector>
+#include "../phd-2d-gfm_gb300/csrc/gfm_math.cuh"
 
 using namespace gfm;
 
@@ -50,6 +55,34 @@ __global__ void check(int mode, uint64_t n, unsigned long long* bad, double* fir
   }
 }
 
+// pow case k: (x, y) from the same generator on both sides
+__host__ __device__ void pow_case(uint64_t k, double& x, double& y) {
+  uint64_t a = k * 0x9e3779b97f4a7c15ull + 12345u;
+  a ^= a >> 31; a *= 0xbf58476d1ce4e5b9ull; a ^= a >> 29;
+  uint64_t b = a * 0x94d049bb133111ebull; b ^= b >> 32;
+  // only exact integer work and correctly rounded IEEE operations, so the
+  // host and the device build the same arguments
+  const double u = (double)(a >> 11) * 0x1p-53, v = (double)(b >> 11) * 0x1p-53;
+  const uint64_t frac = a & 0x000fffffffffffffull;
+  uint64_t xb;
+  switch (k % 5) {
+    case 0: xb = frac | ((uint64_t)(1023 - 15 + (b % 31)) << 52); memcpy(&x, &xb, 8);   // pressure ratios
+            y = (v - 0.5) * 16.0; break;
+    case 1: x = 1.0 + (u - 0.5) * 1e-3; y = (v - 0.5) * 20.0; break;                    // near 1
+    case 2: xb = a & 0x7fffffffffffffffull; memcpy(&x, &xb, 8); y = (v - 0.5) * 4.0; break;   // any positive double
+    case 3: x = u * 100.0; y = 1.0 / (1.09 + v * 5.0); break;                           // 1/gamma
+    default: xb = frac | ((uint64_t)(23 + (b % 2001)) << 52); memcpy(&x, &xb, 8);       // extreme bases
+             y = v * 2.0 - 1.0; break;
+  }
+}
+__global__ void pow_dev(uint64_t n, double* out) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double x, y;
+  pow_case(k, x, y);
+  out[k] = gfm::gfm_pow(x, y);
+}
+
 int main() {
   unsigned long long* bad;
   double* first;
@@ -62,6 +95,28 @@ int main() {
     check<<<(unsigned)((n + 255) / 256), 256>>>(mode, n, bad, first);
     total += 3 * n;
   }
+  // fixed-point pow: device against host
+  const uint64_t np = 1ull << 22;
+  double* d_pow;
+  if (cudaMalloc(&d_pow, np * 8) != cudaSuccess) return 2;
+  pow_dev<<<(unsigned)(np / 256), 256>>>(np, d_pow);
+  std::vector<double> hp(np);
+  if (cudaMemcpy(hp.data(), d_pow, np * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
+  uint64_t pow_bad = 0;
+  for (uint64_t k = 0; k < np; k++) {
+    double x, y;
+    pow_case(k, x, y);
+    const double want = gfm::gfm_pow(x, y);
+    if (memcmp(&want, &hp[k], 8) != 0 && !(want != want && hp[k] != hp[k])) {
+      if (pow_bad < 4) printf("pow(%a, %a): host %a device %a\n", x, y, want, hp[k]);
+      pow_bad++;
+    }
+  }
+  if (pow_bad) {
+    printf("pow mismatches %llu\n", (unsigned long long)pow_bad);
+    return 1;
+  }
+  total += np;
   unsigned long long h_bad = 0;
   double h_first[16];
   if (cudaMemcpy(&h_bad, bad, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
