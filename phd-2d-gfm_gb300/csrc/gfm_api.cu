@@ -677,9 +677,7 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
         // writes of phi (copy, reinitialisation) wait for the ghost fill's
         // last read of phi.
         cudaStreamWaitEvent(ctx->s_ls, ctx->ev_chain, 0);
-        launch_level_set(ctx, m, ctx->s_ls, 1);
-        cudaStreamWaitEvent(ctx->s_ls, ctx->ev_phi_free, 0);
-        launch_level_set(ctx, m, ctx->s_ls, 2);
+        launch_level_set(ctx, m, ctx->s_ls, 3, ctx->ev_phi_free);
         cudaEventRecord(ctx->ev_ls_done, ctx->s_ls);
         launch_fs_update_sel(ctx, m->fs, 3, TILES_NEAR, ctx->s_near);
         cudaEventRecord(ctx->ev_near, ctx->s_near);

@@ -201,7 +201,8 @@ void launch_cfl(gfm_ctx* ctx, double CFL, double T);
 void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m);
 // the step's level set: parts 1 the advection stages, 2 phi := the result
 // (or the reinitialisation from it), 3 both
-void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts);
+void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts,
+                      cudaEvent_t phi_free = nullptr);
 void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_vof_update(gfm_ctx* ctx, cudaStream_t s);
 void launch_end_step(gfm_ctx* ctx);

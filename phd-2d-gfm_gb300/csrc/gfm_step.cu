@@ -2531,7 +2531,7 @@ static int ls_reinit_every(const gfm_ctx* ctx, const gfm_method_desc* m) {
   return ((ctx->steps_done_host + 1) % m->reinit_every == 0) ? 0 : -1;
 }
 
-void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts) {
+void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, int parts, cudaEvent_t phi_free) {
   const GridP& P = ctx->P;
   const int64_t n = padded_cells(P);
   const int every = ls_reinit_every(ctx, m);
@@ -2551,21 +2551,28 @@ void launch_level_set(gfm_ctx* ctx, const gfm_method_desc* m, cudaStream_t s, in
     }
   }
   if (parts & 2) {
+    // The advected field is in phi_a.  Only the last write lands in phi, after
+    // phi_free (the ghost fill's last read of phi) when given: the
+    // reinitialisation's earlier iterations alternate between phi_b (free
+    // once the stages have run) and phi_a.
     const int cblocks = wave_blocks((const void*)k_copy_plane, 256, ctx->num_sms, n);
-    // phi := phi_a on the steps without a reinitialisation
-    if (every < 0) {
-      k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0, 0); counted();
-    } else if (every > 1) {
-      k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, every, 1); counted();
+    const int iters = every >= 0 ? m->reinit_iters : 0;
+    const int blocks = wave_blocks((const void*)k_reinit_iter, 256, ctx->num_sms, n);
+    const double* src = ctx->phi_a;
+    for (int it = 0; it + 1 < iters; it++) {
+      double* dst = (it & 1) ? ctx->phi_a : ctx->phi_b;
+      k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime, ev); counted();
+      src = dst;
     }
-    if (every >= 0) {
-      const int blocks = wave_blocks((const void*)k_reinit_iter, 256, ctx->num_sms, n);
-      for (int it = 0; it < m->reinit_iters; it++) {
-        const double* src = (it & 1) ? ctx->phi : ctx->phi_a;
-        double* dst = (it & 1) ? ctx->phi_a : ctx->phi;
-        k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, dst, ctx->dtime, ev); counted();
-      }
-      if (!(m->reinit_iters & 1)) {
+    if (phi_free) cudaStreamWaitEvent(s, phi_free, 0);
+    if (every < 0) {              // no reinitialisation: phi := phi_a
+      k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, 0, 0); counted();
+    } else {
+      // phi := phi_a on the steps that skip the reinitialisation
+      if (every > 1) { k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, every, 1); counted(); }
+      if (iters > 0) {
+        k_reinit_iter<<<blocks, 256, 0, s>>>(P, src, ctx->phi0, ctx->phi, ctx->dtime, ev); counted();
+      } else {
         k_copy_plane<<<cblocks, 256, 0, s>>>(P, ctx->phi_a, ctx->phi, ctx->dtime, ev, 0); counted();
       }
     }
