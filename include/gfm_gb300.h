@@ -464,9 +464,10 @@ gfm_status_t gfm_case_init_shock_bubble_device(gfm_ctx* ctx, const gfm_bubble_pa
  * GFM_NOALLOC_MAX_CELLS padded cells ((Nx+2 numGC)(Ny+2 numGC)); larger
  * grids are rejected with GFM_ERR_ARG.  It works in the CUDA context current
  * on the calling thread; the first call in each context (once per device
- * with the runtime's primary context) looks up the array's device address
- * and should come before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race. */
+ * with the runtime's primary context) looks up the array's device address.
+ * Every call waits for its own work on the stream (it reads t, numsteps and
+ * the status back), so no call can be recorded into a graph.  All calls
+ * share the array: calls that overlap on the GPU race. */
 #define GFM_NOALLOC_MAX_CELLS 524272
 gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* grid, const gfm_method_desc* m, double* U, int nsteps,
                                        double* t, int* numsteps, uint32_t* status, void* cuda_stream);
