@@ -447,7 +447,10 @@ def run_reference(args):
         wall = time.perf_counter() - t0
     total_steps = sum(d for d, _ in res)
     cells = desc.Nx * desc.Ny
-    value = cells * total_steps / wall
+    # the processes step side by side: their aggregate rate is the cell-updates
+    # over the longest process's own stepping time (the state's transfer to
+    # the processes and their start are not the reference's work)
+    value = cells * total_steps / max(max(el for _, el in res), 1e-9)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, total_steps / cores),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -455,8 +458,9 @@ def run_reference(args):
             "config": {"workload": W["workload"], "Nx": desc.Nx, "Ny": desc.Ny, "GFM": W["GFM"], "FS": W["FS"],
                        "ITM": W["ITM"], "CFL": W["CFL"], "parallelism": "%d independent CPU runs" % cores},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d independent oracle runs x up to %d steps from step %d, %.0f s budget"
-                                       % (cores, args.steps, args.warmup, budget)},
+                             "sample": "%d independent oracle runs x up to %d steps from step %d, %.0f s budget; "
+                                       "rate over the longest run's own stepping time" % (cores, args.steps, args.warmup,
+                                                                                          budget)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
