@@ -120,8 +120,8 @@ inline __int128 log2_q62(double x) {
   int be = (int)(b >> 52);
   uint64_t sig = b & 0x000fffffffffffffULL;
   if (be == 0) {                       // subnormal
-    int s = 0;
-    while (!(sig & (1ULL << 52))) { sig <<= 1; s++; }
+    const int s = __builtin_clzll(sig) - 11;
+    sig <<= s;
     be = 1 - s;
   } else {
     sig |= 1ULL << 52;
@@ -181,8 +181,8 @@ inline double pow_fixed(double x, double y) {
   uint64_t my = yb & 0x000fffffffffffffULL;
   if (ey == 0) ey = 1; else my |= 1ULL << 52;
   const unsigned __int128 mag = (unsigned __int128)(L < 0 ? -L : L) * my;   // |y| |L| 2^(1075 - ey + 62)
-  int nbits = 0;
-  for (unsigned __int128 v = mag; v; v >>= 1) nbits++;
+  const uint64_t mag_hi = (uint64_t)(mag >> 64), mag_lo = (uint64_t)mag;
+  const int nbits = mag_hi ? 128 - __builtin_clzll(mag_hi) : (mag_lo ? 64 - __builtin_clzll(mag_lo) : 0);
   const bool neg = (L < 0) != ((yb >> 63) != 0);
   const int sh = ey - 1073;                                // |T| 2^64 = mag 2^sh
   if (nbits + sh > 75) return neg ? 0.0 : HUGE_VAL;
