@@ -39,6 +39,15 @@ constexpr int MLP_B4 = MLP_W4 + MLP_H;
 constexpr int MLP_NPARAM = MLP_B4 + 1;   // 9089
 
 constexpr double MLP_GATE = 1e-2;
+// The gate |gfm_log(ratio)| > MLP_GATE as two comparisons, without the
+// logarithm: MLP_GATE_HI is the least double whose gfm_log exceeds 1e-2 and
+// MLP_GATE_LO the greatest double whose gfm_log is below -1e-2 (gfm_log is
+// monotone there; tests/gate_check.cpp checks both against gfm_log).
+constexpr double MLP_GATE_HI = 0x1.0292a5d2f2227p+0;   // 1.0100501670841682
+constexpr double MLP_GATE_LO = 0x1.fae7cfd2b9cfdp-1;   // 0.9900498337491680
+GFM_HD bool mlp_gated(double ratio) {
+  return c_le(MLP_GATE_HI, ratio) || (c_gt0(ratio) && c_le(ratio, MLP_GATE_LO));
+}
 
 // Guesses and features of one Riemann problem given its sides (rho, u, p)
 // and gases; the PVRS guess is floored as rs_star floors its start.
@@ -58,7 +67,7 @@ GFM_HD GuessInfo rs_guess_info(const RSSide& L, const Gas& kL, const RSSide& R, 
   g.ppv_f = c_gt(ppv, pfl) ? ppv : pfl;
   g.pts = rs_guess_tsrs(L, kL, R, kR, g.ppv_f);
   const double ratio = (g.pts + g.qmin) / (g.ppv_f + g.qmin);
-  g.gated = c_gt(ratio, 0.0) && c_gt(fabs(gfm_log(ratio)), MLP_GATE);
+  g.gated = mlp_gated(ratio);
   return g;
 }
 
@@ -90,7 +99,7 @@ GFM_HD double mlp_apply(const GuessInfo& g, float y) {
   return (g.pts + g.qmin) * gfm_exp((double)yc) - g.qmin;
 }
 
-__host__ __device__ inline float mlp_silu(float z) { return z / (1.0f + expf(-z)); }
+GFM_HD float mlp_silu(float z) { return z / (1.0f + expf(-z)); }
 
 #if defined(__CUDACC__)
 // The network on the tensor cores by one warp, for one problem at a time
@@ -182,13 +191,13 @@ __global__ void k_mlp_frag_pack(const float* __restrict__ P, uint32_t* __restric
 #endif
 
 // counter-based generator (splitmix64 finaliser): uniform in [0, 1)
-__host__ __device__ inline uint64_t mlp_mix(uint64_t z) {
+GFM_HD uint64_t mlp_mix(uint64_t z) {
   z += 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
 }
-__host__ __device__ inline double mlp_uniform(uint64_t seed, uint64_t k) {
+GFM_HD double mlp_uniform(uint64_t seed, uint64_t k) {
   return (double)(mlp_mix(seed ^ mlp_mix(k)) >> 11) * 0x1p-53;
 }
 

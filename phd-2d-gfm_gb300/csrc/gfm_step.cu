@@ -1046,7 +1046,7 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   float x[MLP_IN];
   if (a.mlp || a.cap_X) {   // warp-uniform: both halves hold the same values
     const double ratio = divx<CHAIN_ID>(pts + pinf_min, pg + pinf_min);
-    gated = c_gt(ratio, 0.0) && c_gt(fabs(gfm_log(ratio)), MLP_GATE);
+    gated = mlp_gated(ratio);
     if (gated) mlp_features_f(rhoL, uL, pbL, kL.g, kL.pinf, rhoR, uR, pbR, kR.g, kR.pinf, x);
     if (gated && a.mlp) {
       const float y = fminf(fmaxf(mlp_forward_warp_tc(a.mlp_frag, a.mlp, x), -20.0f), 20.0f);

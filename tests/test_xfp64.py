@@ -64,6 +64,19 @@ def test_fixed_point_pow_accuracy(tmp_path):
     assert worst < 0.51, worst
 
 
+def test_learned_gate_comparisons_match_the_logarithm(tmp_path):
+    """The learned proposal's gate, two comparisons against thresholds, decides
+    as |log(ratio)| > 1e-2 did for every ratio checked."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "gate_check")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(HERE, "gate_check.cpp"), "-o", exe],
+                   check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0 and out.stdout.startswith("ok"), out.stdout + out.stderr
+
+
 @pytest.mark.gpu
 def test_integer_division_and_root_match_the_gpu(tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
