@@ -237,6 +237,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
       sms = 152;
     ctx->num_sms = sms;
     ctx->chain_sms = 16;
+    ctx->chain_ctas = 32;
     ctx->far_sms = sms > 32 ? sms - 16 : sms;   // the far partition of the overlapped ghost fill
   }
   CtxExtra& X = extra(ctx);
@@ -305,6 +306,13 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_done, cudaEventDisableTiming);
     if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far, &ctx->chain_sms) ? 1 : 0;
     if (ctx->overlap_ok && ctx->num_sms > ctx->chain_sms + 8) ctx->far_sms = ctx->num_sms - ctx->chain_sms;
+    // two CTAs of the interface loop per chain SM (4 warps per sub-partition);
+    // GFM_CHAIN_CTAS_PER_SM (environment, 1 or 2) overrides it
+    ctx->chain_ctas = 2 * ctx->chain_sms;
+    if (const char* env = getenv("GFM_CHAIN_CTAS_PER_SM")) {
+      const int v = atoi(env);
+      if (v == 1 || v == 2) ctx->chain_ctas = v * ctx->chain_sms;
+    }
     ctx->overlap = ctx->overlap_ok ? GFM_OVERLAP_AUTO : GFM_OVERLAP_OFF;
   }
   if (e == cudaSuccess) prepare_kernels();   // kernel attributes and occupancies, before any capture

@@ -75,6 +75,7 @@ struct gfm_ctx {
   int num_sms;       // SMs of the device, and of the far partition of the overlapped ghost fill
   int far_sms;
   int chain_sms;   // SMs of the overlapped ghost fill's chain partition
+  int chain_ctas;  // CTAs of the interface loop (8 warps each) on that partition
   double* stage;     // packed (unpitched) copy of the whole state: 4, 4 and 1 planes of nr x nc
                      // (gfm_upload_state / gfm_download_state)
   // per-interface work arrays (capacity = Nx*Ny)

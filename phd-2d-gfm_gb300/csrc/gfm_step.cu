@@ -2455,7 +2455,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     k_ifc_probes<<<16, 256, 0, ctx->s_chain>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
     ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w;
   }
-  const int chain_ctas = 2 * ctx->chain_sms;   // 8 warps each, two per SM: 4 chain warps per SM sub-partition
+  const int chain_ctas = ctx->chain_ctas;   // 8 warps each
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   else k_interface_warp<IFC_REAL><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
   counted();
