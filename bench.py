@@ -51,7 +51,8 @@ UNIT = "cell-updates/s"
 FLUX_BYTES_PER_CELL = 128   # flux update, both fluids: 32 B read + 32 B write of U each
 STEP_BYTES_PER_CELL = 144   # whole step: the flux update's 128 B plus phi read and write
 NPHASES = 9
-PHASE_NAMES = ["cfl", "ghost_fill", "flux_update", "level_set", "bcs", "interface_loop", "far_partition",
+PHASE_NAMES = ["cfl", "ghost_fill", "flux_update", "commit_bcs_and_level_set_join", "end_step", "interface_loop",
+               "far_partition",
                "near_extrapolation", "far_flux_update"]
 
 

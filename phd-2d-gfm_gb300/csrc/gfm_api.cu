@@ -700,15 +700,17 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
         launch_fs_update(ctx, m->fs, 3);
         mark(3);
       }
+      // U := new values + apply_BCs_euler, beside the level set's tail (which
+      // reads phi and the velocity field, never U)
+      launch_commit(ctx, 3, true);
       cudaStreamWaitEvent(ctx->stream, ctx->ev_ls_done, 0);
       mark(4);
-      launch_commit(ctx, 3, true);   // U := new values + apply_BCs_euler
     } else {
       mark(2);
       launch_fs_update(ctx, m->fs, 1);
       mark(3);
-      mark(4);
       launch_commit(ctx, 1, true);
+      mark(4);
     }
     launch_end_step(ctx);
     mark(5);
@@ -772,8 +774,8 @@ gfm_status_t gfm::step_front(gfm_ctx* ctx, const gfm_method_desc* m) {
 gfm_status_t gfm::step_back(gfm_ctx* ctx, const gfm_method_desc* m) {
   (void)m;
   if (ctx->two_fluid) {
+    launch_commit(ctx, 3, true);   // beside the level set's tail, which never reads U
     cudaStreamWaitEvent(ctx->stream, ctx->ev_ls_done, 0);
-    launch_commit(ctx, 3, true);
   } else {
     launch_commit(ctx, 1, true);
   }
