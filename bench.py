@@ -292,6 +292,14 @@ def run_gfm(args):
                      "achieved_gflops": round(fl / (flux_ms_prof * 1e-3) / 1e9, 1),
                      "frac": round(fl / (flux_ms_prof * 1e-3) / 1e9 / fp64_peak.value, 4),
                      "pipe_active_frac_ncu": prof.get("fp64_pipe_active_frac")})
+        if "fp64_lane_instructions_per_cell" in prof:
+            # an FP64 add or multiply holds the pipe as long as a fused
+            # multiply-add: the pipe's share is the lane-instruction rate over
+            # the peak's (the FMA loop's flop rate / 2)
+            li = prof["fp64_lane_instructions_per_cell"] * cells / (flux_ms_prof * 1e-3) / 1e9
+            fp64.update({"lane_instructions_per_cell": prof["fp64_lane_instructions_per_cell"],
+                         "achieved_g_lane_inst": round(li, 1), "peak_g_lane_inst": round(fp64_peak.value / 2, 1),
+                         "pipe_frac": round(li / (fp64_peak.value / 2), 4)})
     if "fp64_flops_per_cell_step" in step_prof and step_ms_prof:
         # the whole step's FP64 work (ncu, all kernels of one step) over that
         # step's time measured here
