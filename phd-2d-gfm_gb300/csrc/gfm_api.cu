@@ -267,6 +267,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->ifc_mrp, sizeof(double) * 8 * cap);
     alloc((void**)&ctx->probe_ij, sizeof(int) * 4 * cap);
     alloc((void**)&ctx->probe_w, sizeof(double) * 8 * cap);
+    alloc((void**)&ctx->probe_dep, sizeof(int) * 8 * cap);
     // chunks of at least 2048 cells (the count array's size), enough of them
     // for one CTA per SM on large grids (the chunked kernels run one CTA per SM)
     const int sms = ctx->num_sms;
@@ -338,7 +339,7 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   cudaFree(ctx->nrm); cudaFree(ctx->vel); cudaFree(ctx->vel_t);
   cudaFree(ctx->mask); cudaFree(ctx->ifc_map); cudaFree(ctx->ifc_list); cudaFree(ctx->ifc_done);
   cudaFree(ctx->ifc_out); cudaFree(ctx->ifc_mrp); cudaFree(ctx->chunk_count);
-  cudaFree(ctx->probe_ij); cudaFree(ctx->probe_w);
+  cudaFree(ctx->probe_ij); cudaFree(ctx->probe_w); cudaFree(ctx->probe_dep);
   for (int b = 0; b < 5; b++)
     for (int f = 0; f < 2; f++) cudaFree(ctx->SF[b][f]);
   cudaFree(ctx->near_cell); cudaFree(ctx->band_cls); cudaFree(ctx->tile_near);

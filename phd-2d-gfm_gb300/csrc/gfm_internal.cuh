@@ -85,6 +85,7 @@ struct gfm_ctx {
   double* ifc_mrp;   // 8 per mixed cell of the VOF loop: MRPsoln1, MRPsoln2
   int* probe_ij;     // Riemann GFM: per interfacial cell and side, the bilinear probe's cell (i0, j0)
   double* probe_w;   // and its 4 weights
+  int* probe_dep;    // and per bilinear corner the list entry whose published value it reads, or -1
   int itm;           // interface tracker of the last method used (GFM_ITM_*)
   int* ifc_opp;      // real GFM: opposite cell
   long long ifc_spin_limit;  // polls before an interface-loop wait gives up (0: the default)

@@ -728,6 +728,9 @@ struct IfcArgs {
   // per list entry and side, the bilinear cell (i0, j0) and the 4 weights
   const int* probe_ij;
   const double* probe_w;
+  // and per list entry, side and bilinear corner the list entry whose
+  // published value that corner reads, or -1 (the corner reads the grid)
+  const int* probe_dep;
   long long spin_limit;   // polls of a completion flag before a wait gives up
   int withhold;           // test hook: this list entry is never solved or published (-1: none)
 };
@@ -753,6 +756,46 @@ __device__ __forceinline__ bool ifc_wait(const IfcArgs& a, int p) {
     if (spins > 512) __nanosleep(64);
   }
   return v == 1;
+}
+
+// Published values of k_interface_warp's cells.  Each of a cell's four
+// values that dependants read (out[0..3]: its real fluid's star density,
+// velocity and pressure) starts the step as IFC_PENDING (k_ifc_reset) and is
+// written once, by one 64-bit store, so a dependant polls the value it needs
+// itself: any other bit pattern is the final value (aligned 64-bit accesses
+// are single-copy atomic).  A cell that gave up publishes IFC_FAILED.  Both
+// are signalling NaNs, which no FP64 operation returns; a published value
+// with either pattern (only a NaN copied from the input grids could have
+// one) is published as the quiet NaN instead.
+constexpr unsigned long long IFC_PENDING = 0x7ff00000c0ffee00ull;
+constexpr unsigned long long IFC_FAILED = 0x7ff00000badbad00ull;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(double* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void ifc_publish(double* p, double v) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  if (b == IFC_PENDING || b == IFC_FAILED) b = 0x7fffffffffffffffull;
+  st_relaxed_u64(p, b);
+}
+// value kc of list entry p once it is published; false when the entry gave
+// up or the polls ran out
+__device__ __forceinline__ bool ifc_poll(const IfcArgs& a, int p, int kc, double& v) {
+  const double* w = a.out + (int64_t)p * IFC_OUT + kc;
+  long long spins = 0;
+  unsigned long long x;
+  while ((x = ld_relaxed_u64(w)) == IFC_PENDING) {
+    if (++spins > a.spin_limit) return false;
+    if (spins > 512) __nanosleep(64);
+  }
+  if (x == IFC_FAILED) return false;
+  v = __longlong_as_double((long long)x);
+  return true;
 }
 
 __device__ __forceinline__ V4 ifc_out4(const IfcArgs& a, int p) {
@@ -963,15 +1006,16 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 
 __device__ __forceinline__ double xside(double x) { return __shfl_xor_sync(FULL_MASK, x, 16); }
 
-// component kc of ifc_read
+// component kc of ifc_read for k_interface_warp, whose cells publish their
+// values for polling (ifc_poll)
 __device__ __forceinline__ double ifc_read1(const IfcArgs& a, int f, int i, int j, int kc, int64_t lin, bool& ok) {
   const GridP& P = a.P;
   int64_t c = cidx(P, i, j);
   int64_t l2 = (int64_t)i * P.nc + j;
   if (a.mask[c] && ((a.phi[c] <= 0.0) == (f == 0)) && l2 < lin) {
-    int p = a.ifc_map[c];
-    if (!ifc_wait(a, p)) { ok = false; return 0.0; }
-    return __ldcg(a.out + (int64_t)p * IFC_OUT + kc);
+    double v = 0.0;
+    if (!ifc_poll(a, a.ifc_map[c], kc, v)) ok = false;
+    return v;
   }
   return (f == 0 ? a.W1 : a.W2)[c + kc * P.plane];
 }
@@ -1138,8 +1182,11 @@ __device__ __forceinline__ void ifc_probe(const IfcArgs& a, int64_t c, int i, in
 
 // The probes of every interfacial cell ahead of the interface loop: they
 // depend on phi and its normals only, so computing them here in parallel
-// takes their FP64 instructions off the loop's dependency chain.
-__global__ void __launch_bounds__(256) k_ifc_probes(IfcArgs a, int* probe_ij, double* probe_w) {
+// takes their FP64 instructions off the loop's dependency chain.  So does
+// the test of each bilinear corner (ifc_read1's: an earlier interfacial cell
+// whose real fluid is the probed one), which depends on the mask, phi and
+// the list only: probe_dep holds the list entry the corner waits for, or -1.
+__global__ void __launch_bounds__(256) k_ifc_probes(IfcArgs a, int* probe_ij, double* probe_w, int* probe_dep) {
   const GridP& P = a.P;
   if (!a.D->active) return;
   const int n = a.D->n_ifc;
@@ -1156,10 +1203,15 @@ __global__ void __launch_bounds__(256) k_ifc_probes(IfcArgs a, int* probe_ij, do
     probe_ij[4 * (int64_t)t + 2 * s] = i0;
     probe_ij[4 * (int64_t)t + 2 * s + 1] = j0;
     double* w = probe_w + 8 * (int64_t)t + 4 * s;
+    int* dep = probe_dep + 8 * (int64_t)t + 4 * s;
     for (int e = 0; e < 4; e++) {
       const double fa = (e & 1) ? wa : 1.0 - wa;
       const double fb = (e & 2) ? wb : 1.0 - wb;
       w[e] = fa * fb;
+      const int ci = i0 + (e >> 1), cj = j0 + (e & 1);
+      const int64_t cc = cidx(P, ci, cj);
+      const int64_t l2 = (int64_t)ci * P.nc + cj;
+      dep[e] = (a.mask[cc] && ((a.phi[cc] <= 0.0) == (s == 0)) && l2 < lin) ? a.ifc_map[cc] : -1;
     }
   }
 }
@@ -1227,19 +1279,26 @@ __device__ __forceinline__ bool ifc_front(const IfcArgs& a, int t, const Gas& k,
     // get_interpolated_mixedRPstates (sourcecode/GFM_base.cpp:4-33); the
     // probe geometry depends on phi only and comes from k_ifc_probes when set
     int i0, j0;
-    double w;
+    double w, g;
     if (a.probe_ij) {
       i0 = __ldg(a.probe_ij + 4 * (int64_t)t + 2 * s);
       j0 = __ldg(a.probe_ij + 4 * (int64_t)t + 2 * s + 1);
       w = __ldg(a.probe_w + 8 * (int64_t)t + 4 * s + q);
+      const int dep = __ldg(a.probe_dep + 8 * (int64_t)t + 4 * s + q);
+      if (dep >= 0) {
+        g = 0.0;
+        if (!ifc_poll(a, dep, kc, g)) ok = false;
+      } else {
+        g = (s == 0 ? a.W1 : a.W2)[cidx(P, i0 + (q >> 1), j0 + (q & 1)) + kc * P.plane];
+      }
     } else {
       double wa, wb;
       ifc_probe(a, c, i, j, lsval, nx, ny, isR, i0, j0, wa, wb);
       const double fa = (q & 1) ? wa : 1.0 - wa;
       const double fb = (q & 2) ? wb : 1.0 - wb;
       w = fa * fb;
+      g = ifc_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
     }
-    const double g = ifc_read1(a, s, i0 + (q >> 1), j0 + (q & 1), kc, lin, ok);
     const double pr = w * g;
     const double p1 = __shfl_down_sync(FULL_MASK, pr, 4);
     const double p2 = __shfl_down_sync(FULL_MASK, pr, 8);
@@ -1291,9 +1350,7 @@ __global__ void __launch_bounds__(256, GFM_CHAIN_MIN_CTAS) k_interface_warp(IfcA
     IfcCell cell;
     if (!ifc_front<MODE>(a, t, k, st, cell)) {
       st |= ST_SCHEDULE_LIMIT;
-      if (lane == 0) {
-        st_release(a.done + t, 2);
-      }
+      if (lane < 4) st_relaxed_u64(a.out + (int64_t)t * IFC_OUT + lane, IFC_FAILED);
       continue;
     }
     int it = 0, gt = 0;
@@ -1303,9 +1360,11 @@ __global__ void __launch_bounds__(256, GFM_CHAIN_MIN_CTAS) k_interface_warp(IfcA
     if (lane == 16 * cell.sr) {
       double* o = a.out + (int64_t)t * IFC_OUT;
       const double snx = m.u * cell.nx, sny = m.u * cell.ny;
-      o[0] = m.rho_own; o[1] = snx + cell.tx; o[2] = sny + cell.ty; o[3] = m.p;
-      o[4] = snx; o[5] = sny;
-      st_release(a.done + t, 1);
+      o[4] = snx; o[5] = sny;   // read after the loop only
+      ifc_publish(o + 3, m.p);
+      ifc_publish(o, m.rho_own);
+      ifc_publish(o + 1, snx + cell.tx);
+      ifc_publish(o + 2, sny + cell.ty);
     }
   }
   uint32_t wst = __reduce_or_sync(FULL_MASK, st);
@@ -1770,11 +1829,17 @@ __global__ void __launch_bounds__(256) k_vof_sweep(GridP P, const double* z, con
 }
 
 // Reset of the per-step interface bookkeeping.
-__global__ void k_ifc_reset(int* done, int cap, unsigned int* ticket, const DevTime* D) {
+// Completion flags and (out, for k_interface_warp) published values of the
+// interface loop set to pending
+__global__ void k_ifc_reset(int* done, double* out, int cap, unsigned int* ticket, const DevTime* D) {
   if (!D->active) return;
   int n = D->n_ifc;
   if (n > cap) n = cap;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) done[k] = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    done[k] = 0;
+    if (out)
+      for (int q = 0; q < 4; q++) out[(int64_t)k * IFC_OUT + q] = __longlong_as_double((long long)IFC_PENDING);
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) *ticket = 0u;
 }
 
@@ -2213,7 +2278,9 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (variant != GFM_REAL) run_extrap(ctx, 2, false);
   // 3. interface loop
   int cap = P.Nx * P.Ny;
-  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime); counted();
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, ctx->ifc_out, cap, (unsigned int*)(ctx->ifc_opp),
+                                                     ctx->dtime);
+  counted();
   IfcArgs ia;
   ia.P = P;
   ia.W1 = ctx->W[0]; ia.W2 = ctx->W[1];
@@ -2226,10 +2293,10 @@ void launch_ghost_fill(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia, s);
-  ia.probe_ij = nullptr; ia.probe_w = nullptr;
+  ia.probe_ij = nullptr; ia.probe_w = nullptr; ia.probe_dep = nullptr;
   if (variant == GFM_RIEMANN) {
-    k_ifc_probes<<<152, 256, 0, s>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
-    ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w;
+    k_ifc_probes<<<152, 256, 0, s>>>(ia, ctx->probe_ij, ctx->probe_w, ctx->probe_dep); counted();
+    ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w; ia.probe_dep = ctx->probe_dep;
   }
   int iblocks = 152;   // 4 warps per CTA: one chain warp per SM sub-partition
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<iblocks, 128, 0, s>>>(ia);
@@ -2435,7 +2502,8 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
 
   // chain partition: the interface loop
   cudaStreamWaitEvent(ctx->s_chain, ctx->ev_fork, 0);
-  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, ctx->s_chain>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp),
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, ctx->s_chain>>>(ctx->ifc_done, ctx->ifc_out, cap,
+                                                               (unsigned int*)(ctx->ifc_opp),
                                                                ctx->dtime);
   counted();
   IfcArgs ia;
@@ -2450,10 +2518,10 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
   set_learning(ctx, ia, ctx->s_chain);
-  ia.probe_ij = nullptr; ia.probe_w = nullptr;
+  ia.probe_ij = nullptr; ia.probe_w = nullptr; ia.probe_dep = nullptr;
   if (variant == GFM_RIEMANN) {
-    k_ifc_probes<<<16, 256, 0, ctx->s_chain>>>(ia, ctx->probe_ij, ctx->probe_w); counted();
-    ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w;
+    k_ifc_probes<<<16, 256, 0, ctx->s_chain>>>(ia, ctx->probe_ij, ctx->probe_w, ctx->probe_dep); counted();
+    ia.probe_ij = ctx->probe_ij; ia.probe_w = ctx->probe_w; ia.probe_dep = ctx->probe_dep;
   }
   const int chain_ctas = ctx->chain_ctas;   // 8 warps each
   if (variant == GFM_RIEMANN) k_interface_warp<IFC_RIEMANN><<<chain_ctas, 256, 0, ctx->s_chain>>>(ia);
@@ -2610,7 +2678,8 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   k_compact<<<ctx->n_chunks, CHUNK_T, 0, s>>>(P, ctx->mask, ctx->chunk_count, ctx->n_chunks, ctx->chunk, ctx->ifc_list,
                                               ctx->ifc_map, ctx->dtime); counted();
   const int cap = P.nr * P.nc;
-  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, cap, (unsigned int*)(ctx->ifc_opp), ctx->dtime);
+  k_ifc_reset<<<grid_blocks(cap, 256), 256, 0, s>>>(ctx->ifc_done, nullptr, cap, (unsigned int*)(ctx->ifc_opp),
+                                                     ctx->dtime);
   counted();
   // the real cells flagged 1 or 2 by the loop: within the ring of a mixed cell
   cudaMemsetAsync(ctx->near_cell, 0, (size_t)P.plane, s);
@@ -2629,7 +2698,7 @@ void launch_ghost_fill_vof(gfm_ctx* ctx, const gfm_method_desc* m) {
   ia.withhold = ctx->ifc_withhold - 1;
   ia.slip = m->use_slip_BCs;
   ia.mlp = nullptr; ia.mlp_frag = nullptr; ia.cap_X = nullptr; ia.cap_Y = nullptr; ia.cap_count = nullptr; ia.cap = 0;
-  ia.probe_ij = nullptr; ia.probe_w = nullptr;
+  ia.probe_ij = nullptr; ia.probe_w = nullptr; ia.probe_dep = nullptr;
   if (og) k_vof_chain<VOF_OGFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
   else k_vof_chain<VOF_GFM><<<152, 128, 0, s>>>(ia, ctx->ifc_mrp);
   counted();
