@@ -17,7 +17,7 @@ using namespace gfm;
 std::atomic<long long> gfm::g_launches{0};
 
 // ---------------------------------------------------------------------------
-// SM partitions for the overlapped ghost fill: a 16-SM green context for the
+// SM partitions for the overlapped ghost fill: an 8-SM green context for the
 // interface chain and one for the remaining SMs, with one stream each,
 // created once per device.  The driver entry points are fetched through the
 // runtime, so the library does not link libcuda.  Without green-context
@@ -58,12 +58,12 @@ bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms_
   CUdevResource res, grp[1], rem;
   if (pGetRes(d, &res, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return false;
   unsigned nb = 1;
-  // 16 SMs for the chain: measured on the 1000x400 shock-bubble against 8
-  // and 24 (steps 5-25: 240.2 against 228.5 and 242.3 M cell-updates/s;
-  // steps 3-303: 201.9, 198.4, 201.1 M; the whole run: 180.0, 178.7, 178.0 M
-  // -- the far field grows along the run and wants the SMs back);
+  // 8 SMs for the chain: measured on the 1000x400 shock-bubble's whole run
+  // (2000 steps) against 16, three runs each: 2.127-2.131 against
+  // 2.135-2.140 ms per step (24 and 32 SMs were slower still); with 8 SMs the
+  // chain and the far field take about as long (1.45 and 1.52 ms per step).
   // GFM_CHAIN_SMS (environment, a multiple of 8 up to 64) overrides it
-  unsigned chain_sms = 16;
+  unsigned chain_sms = 8;
   if (const char* e = getenv("GFM_CHAIN_SMS")) {
     const int v = atoi(e);
     if (v >= 8 && v <= 64 && v % 8 == 0) chain_sms = (unsigned)v;
@@ -90,7 +90,7 @@ bool gfm::green_streams(int dev, cudaStream_t* chain, cudaStream_t* far, int* ch
   GreenPair& g = g_green[dev];
   if (!g.init) {
     g.init = true;
-    g.chain_sms = 16;
+    g.chain_sms = 8;
     g.ok = make_green(dev, &g.chain, &g.far, &g.chain_sms);
     if (!g.ok) {
       cudaGetLastError();
@@ -236,9 +236,9 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur) != cudaSuccess || sms < 1)
       sms = 152;
     ctx->num_sms = sms;
-    ctx->chain_sms = 16;
-    ctx->chain_ctas = 32;
-    ctx->far_sms = sms > 32 ? sms - 16 : sms;   // the far partition of the overlapped ghost fill
+    ctx->chain_sms = 8;
+    ctx->chain_ctas = 16;
+    ctx->far_sms = sms > 16 ? sms - 8 : sms;   // the far partition of the overlapped ghost fill
   }
   CtxExtra& X = extra(ctx);
   alloc((void**)&X.counters, 64);

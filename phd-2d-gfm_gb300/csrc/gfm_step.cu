@@ -509,8 +509,8 @@ constexpr int NEAR_RADIUS = 6;
 constexpr int BAND_CLASSES = NEAR_RADIUS + 1;
 // CTAs of the listed sweeps after the loop: the band holds a few thousand to
 // about ten thousand cells, about one per thread of 40 CTAs of 256 threads
-// (within one wave on the loop's own 16 SMs, which these kernels share with
-// the level set while the far field's flux update fills the other SMs)
+// (they share the loop's own SMs with the level set while the far field's
+// flux update fills the other SMs; 20, 80 or 152 CTAs measured within 0.5%)
 constexpr int NEAR_CTAS = 40;
 
 struct ExtrapArgs {
