@@ -1030,13 +1030,17 @@ struct PairStar { double p, u, rho_own; bool trivial; };
 // density of the lane's side.  The Newton loop is warp-uniform: both halves
 // compute the same pressure iterates.
 //
+// star_side >= 0: rho_own is that side's star density on every lane (the
+// caller publishes only it), evaluated once for the warp, so the two halves
+// do not take the shock's and the rarefaction's branch one after the other.
+//
 // With a network (a.mlp), problems whose two-shock guess moved far from PVRS
 // (the gate of gfm_mlp.cuh) start from the network's proposal, evaluated by
 // the warp in FP32 on the actual states; with a capture buffer, such problems
 // are recorded (features and the solved p* relative to the two-shock guess).
 __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const Gas& kL, const Gas& kR, const V4& Uown,
                                                   uint32_t* status, int* iters, const IfcArgs& a,
-                                                  int* proposed) {
+                                                  int* proposed, int star_side = -1) {
   // cons_to_prims_phys with its three quotients by rho (rho u, rho v, E) in
   // one: lane kc of each group of four divides component kc + 1 (E twice)
   const int lane = threadIdx.x & 31, grp = lane & ~3, kq = lane & 3;
@@ -1123,7 +1127,16 @@ __device__ __forceinline__ PairStar mixed_rs_pair(bool isR, const Gas& k, const 
   }
   r.p = p;
   r.u = 0.5 * (uL + uR + (fR + fRd * dp) - (fL + fLd * dp));
-  r.rho_own = rs_rho_star<CHAIN_ID>(S, k, p);
+  if (star_side < 0) {
+    r.rho_own = rs_rho_star<CHAIN_ID>(S, k, p);
+  } else {
+    // rs_rho_star reads the side's rho, p and 1/pb
+    RSSide K = S;
+    K.rho = __shfl_sync(FULL_MASK, S.rho, 16 * star_side);
+    K.p = __shfl_sync(FULL_MASK, S.p, 16 * star_side);
+    K.ipb = __shfl_sync(FULL_MASK, S.ipb, 16 * star_side);
+    r.rho_own = rs_rho_star<CHAIN_ID>(K, star_side ? kR : kL, p);
+  }
   *iters += it;
   if (gated && a.cap_X && (threadIdx.x & 31) == 0 && it < kL.maxit && !c_le(G4cL + G4cR, udiff)) {
     const double y = gfm_log((p + pinf_min) / (pts + pinf_min));
@@ -1354,7 +1367,7 @@ __global__ void __launch_bounds__(256, GFM_CHAIN_MIN_CTAS) k_interface_warp(IfcA
       continue;
     }
     int it = 0, gt = 0;
-    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, cell.Us, &st, &it, a, &gt);
+    const PairStar m = mixed_rs_pair(isR, k, P.gas1, P.gas2, cell.Us, &st, &it, a, &gt, cell.sr);
     if (lane == 0) { iters += it; gated += gt; }
     if (c_isnan(m.p)) st |= ST_NAN;
     if (lane == 16 * cell.sr) {
