@@ -28,8 +28,8 @@ std::atomic<long long> gfm::g_launches{0};
 
 namespace {
 std::mutex g_green_mutex;
-struct GreenPair { bool init; bool ok; int chain_sms; cudaStream_t chain, far; };
-GreenPair g_green[64];
+struct GreenSet { bool init; bool ok; GreenParts parts; };
+GreenSet g_green[64];
 
 template <typename F>
 bool entry(const char* name, F* fn, unsigned version = 12040) {
@@ -42,7 +42,8 @@ bool entry(const char* name, F* fn, unsigned version = 12040) {
   return true;
 }
 
-bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms_out) {
+// one (chain, far) pair of green-context streams: chain_req SMs and the rest
+bool make_green(int dev, unsigned chain_req, cudaStream_t* chain, cudaStream_t* far, int* chain_sms_out) {
   PFN_cuDeviceGet_v2000 pDeviceGet;
   PFN_cuDeviceGetDevResource_v12040 pGetRes;
   PFN_cuDevSmResourceSplitByCount_v12040 pSplit;
@@ -58,17 +59,7 @@ bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms_
   CUdevResource res, grp[1], rem;
   if (pGetRes(d, &res, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return false;
   unsigned nb = 1;
-  // 8 SMs for the chain: measured on the 1000x400 shock-bubble's whole run
-  // (2000 steps) against 16, three runs each: 2.127-2.131 against
-  // 2.135-2.140 ms per step (24 and 32 SMs were slower still); with 8 SMs the
-  // chain and the far field take about as long (1.45 and 1.52 ms per step).
-  // GFM_CHAIN_SMS (environment, a multiple of 8 up to 64) overrides it
-  unsigned chain_sms = 8;
-  if (const char* e = getenv("GFM_CHAIN_SMS")) {
-    const int v = atoi(e);
-    if (v >= 8 && v <= 64 && v % 8 == 0) chain_sms = (unsigned)v;
-  }
-  if (pSplit(grp, &nb, &res, &rem, 0, chain_sms) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
+  if (pSplit(grp, &nb, &res, &rem, 0, chain_req) != CUDA_SUCCESS || nb != 1 || rem.sm.smCount == 0) return false;
   *chain_sms_out = (int)grp[0].sm.smCount;
   CUdevResourceDesc d1, d2;
   if (pDesc(&d1, grp, 1) != CUDA_SUCCESS || pDesc(&d2, &rem, 1) != CUDA_SUCCESS) return false;
@@ -84,23 +75,39 @@ bool make_green(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms_
 }
 }  // namespace
 
-bool gfm::green_streams(int dev, cudaStream_t* chain, cudaStream_t* far, int* chain_sms) {
+// Two partitions, chain 8 and 16 SMs: on the 1000x400 shock-bubble 16 SMs
+// give the shorter step early in the run (steps 5-25: 1.538 against 1.607 ms;
+// the chain is the longer path while the far field's tiles are uniform) and
+// 8 SMs later (the whole run: 2.127-2.131 against 2.135-2.140 ms); contexts
+// choose between them step by step (choose_partition).  GFM_CHAIN_SMS
+// (environment, a multiple of 8 up to 64) fixes one partition instead.
+bool gfm::green_streams(int dev, GreenParts* parts) {
   if (dev < 0 || dev >= 64) return false;
   std::lock_guard<std::mutex> lk(g_green_mutex);
-  GreenPair& g = g_green[dev];
+  GreenSet& g = g_green[dev];
   if (!g.init) {
     g.init = true;
-    g.chain_sms = 8;
-    g.ok = make_green(dev, &g.chain, &g.far, &g.chain_sms);
-    if (!g.ok) {
+    GreenParts& q = g.parts;
+    unsigned req[2] = {8, 16};
+    q.n = 2;
+    if (const char* e = getenv("GFM_CHAIN_SMS")) {
+      const int v = atoi(e);
+      if (v >= 8 && v <= 64 && v % 8 == 0) { req[0] = (unsigned)v; q.n = 1; }
+    }
+    g.ok = true;
+    for (int k = 0; k < q.n && g.ok; k++) {
+      q.chain_sms[k] = (int)req[k];
+      g.ok = make_green(dev, req[k], &q.chain[k], &q.far[k], &q.chain_sms[k]);
+    }
+    if (!g.ok) {   // no green contexts: one pair of ordinary streams
       cudaGetLastError();
-      g.ok = cudaStreamCreateWithFlags(&g.chain, cudaStreamNonBlocking) == cudaSuccess &&
-             cudaStreamCreateWithFlags(&g.far, cudaStreamNonBlocking) == cudaSuccess;
+      q.n = 1;
+      q.chain_sms[0] = (int)req[0];
+      g.ok = cudaStreamCreateWithFlags(&q.chain[0], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&q.far[0], cudaStreamNonBlocking) == cudaSuccess;
     }
   }
-  *chain = g.chain;
-  *far = g.far;
-  *chain_sms = g.chain_sms;
+  *parts = g.parts;
   return g.ok;
 }
 
@@ -109,6 +116,16 @@ namespace {
 struct CtxExtra {
   unsigned int* counters;   // [0] CFL last-block counter, [1] interface ticket
   double* mass_part;        // 256 partial sums + 1 result
+  // timed steps of the overlapped ghost fill, for choose_partition: a ring
+  // of event triples (fork, near sweeps done, far flux done)
+  cudaEvent_t pev[8][3];
+  bool pev_made;
+  bool pev_pending[8];
+  int pev_part[8];
+  int pev_next;
+  bool meas_ok;             // the latest finished measurement
+  float meas_chain, meas_far;
+  int meas_part;
 };
 
 // the extra buffers live right after the context allocation
@@ -124,6 +141,75 @@ CtxExtra& extra(gfm_ctx* ctx) { return *reinterpret_cast<CtxExtra*>(ctx + 1); }
   } while (0)
 
 bool valid_bc(int b) { return b == GFM_BC_TRANSMISSIVE || b == GFM_BC_REFLECTIVE || b == GFM_BC_PERIODIC; }
+
+// The streams, SM counts and interface-loop grid of partition k.
+void use_partition(gfm_ctx* ctx, int k) {
+  ctx->part = k;
+  ctx->s_chain = ctx->part_chain[k];
+  ctx->s_far = ctx->part_far[k];
+  ctx->chain_sms = ctx->part_sms[k];
+  ctx->chain_ctas = ctx->chain_ctas_per_sm * ctx->chain_sms;
+  ctx->far_sms = ctx->num_sms > ctx->chain_sms + 8 ? ctx->num_sms - ctx->chain_sms : ctx->num_sms;
+}
+
+// The partition of the next overlapped step, from the latest finished
+// measurement of an earlier step: its chain path (fork to the end of the
+// near-field sweeps) and far path (fork to the end of the far tiles' flux
+// update), carried to the other partition with factors measured on the
+// shock-bubble (twice the chain SMs: the chain path x 0.965; the far path
+// in proportion to its SMs), and the partition with the shorter longer path
+// taken (by at least 1% to switch).  Results are the same on every
+// partition; a step while the stream is being captured is neither measured
+// nor switched.  Each step measured takes the next slot of a ring of event
+// triples; a slot whose step has not finished when its turn comes again is
+// overwritten.
+void choose_partition(gfm_ctx* ctx) {
+  ctx->part_ev[0] = ctx->part_ev[1] = ctx->part_ev[2] = nullptr;
+  CtxExtra& X = extra(ctx);
+  if (ctx->n_parts < 2 || !X.pev_made) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+  // an unfinished event answers "not ready", which must not reach the next
+  // launch check: it is cleared unless an error was already recorded
+  const bool clean = cudaPeekAtLastError() == cudaSuccess;
+  for (int q = 0; q < 8; q++) {   // oldest first
+    const int k = (X.pev_next + q) % 8;
+    if (!X.pev_pending[k]) continue;
+    if (cudaEventQuery(X.pev[k][1]) != cudaSuccess || cudaEventQuery(X.pev[k][2]) != cudaSuccess) {
+      if (clean && cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();
+      break;
+    }
+    float c = 0.0f, f = 0.0f;
+    if (cudaEventElapsedTime(&c, X.pev[k][0], X.pev[k][1]) == cudaSuccess &&
+        cudaEventElapsedTime(&f, X.pev[k][0], X.pev[k][2]) == cudaSuccess) {
+      X.meas_ok = true;
+      X.meas_chain = c;
+      X.meas_far = f;
+      X.meas_part = X.pev_part[k];
+    }
+    X.pev_pending[k] = false;
+  }
+  if (X.meas_ok) {
+    double best = 0.0;
+    int pick = ctx->part;
+    for (int j = 0; j < ctx->n_parts; j++) {
+      const double ratio = (double)ctx->part_sms[j] / (double)ctx->part_sms[X.meas_part];
+      const double chain = X.meas_chain * pow(0.965, log2(ratio));
+      const double far_m = (double)(ctx->num_sms - ctx->part_sms[X.meas_part]);
+      const double far_j = (double)(ctx->num_sms - ctx->part_sms[j]);
+      const double far = X.meas_far * far_m / far_j;
+      double t = chain > far ? chain : far;
+      if (j != ctx->part) t *= 1.01;
+      if (j == 0 || t < best) { best = t; pick = j; }
+    }
+    if (pick != ctx->part) use_partition(ctx, pick);
+  }
+  const int k = X.pev_next;
+  X.pev_next = (k + 1) % 8;
+  X.pev_pending[k] = true;
+  X.pev_part[k] = ctx->part;
+  for (int q = 0; q < 3; q++) ctx->part_ev[q] = X.pev[k][q];
+}
 
 gfm_status_t check_method(const gfm_ctx* ctx, const gfm_method_desc* m) {
   if (!m) return GFM_ERR_ARG;
@@ -239,6 +325,10 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     ctx->chain_sms = 8;
     ctx->chain_ctas = 16;
     ctx->far_sms = sms > 16 ? sms - 8 : sms;   // the far partition of the overlapped ghost fill
+    ctx->n_parts = 0;
+    ctx->part = 0;
+    ctx->chain_ctas_per_sm = 2;
+    ctx->part_ev[0] = ctx->part_ev[1] = ctx->part_ev[2] = nullptr;
   }
   CtxExtra& X = extra(ctx);
   alloc((void**)&X.counters, 64);
@@ -305,14 +395,31 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_lists, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_ls_done, cudaEventDisableTiming);
-    if (e == cudaSuccess) ctx->overlap_ok = green_streams(dev, &ctx->s_chain, &ctx->s_far, &ctx->chain_sms) ? 1 : 0;
-    if (ctx->overlap_ok && ctx->num_sms > ctx->chain_sms + 8) ctx->far_sms = ctx->num_sms - ctx->chain_sms;
+    GreenParts gp;
+    if (e == cudaSuccess && green_streams(dev, &gp)) {
+      ctx->overlap_ok = 1;
+      ctx->n_parts = gp.n;
+      for (int k = 0; k < gp.n; k++) {
+        ctx->part_chain[k] = gp.chain[k];
+        ctx->part_far[k] = gp.far[k];
+        ctx->part_sms[k] = gp.chain_sms[k];
+      }
+    }
     // two CTAs of the interface loop per chain SM (4 warps per sub-partition);
     // GFM_CHAIN_CTAS_PER_SM (environment, 1 or 2) overrides it
-    ctx->chain_ctas = 2 * ctx->chain_sms;
     if (const char* env = getenv("GFM_CHAIN_CTAS_PER_SM")) {
       const int v = atoi(env);
-      if (v == 1 || v == 2) ctx->chain_ctas = v * ctx->chain_sms;
+      if (v == 1 || v == 2) ctx->chain_ctas_per_sm = v;
+    }
+    if (ctx->overlap_ok) {
+      // the larger chain partition first: the chain is the longer path
+      // early in a run, and the measurements decide from there
+      ctx->part = ctx->n_parts - 1;
+      use_partition(ctx, ctx->part);
+      CtxExtra& X2 = extra(ctx);
+      X2.pev_made = true;
+      for (int k = 0; k < 8 && e == cudaSuccess; k++)
+        for (int q = 0; q < 3 && e == cudaSuccess; q++) e = cudaEventCreate(&X2.pev[k][q]);
     }
     ctx->overlap = ctx->overlap_ok ? GFM_OVERLAP_AUTO : GFM_OVERLAP_OFF;
   }
@@ -347,6 +454,13 @@ gfm_status_t gfm_ctx_destroy(gfm_ctx* ctx) {
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_chain) cudaEventDestroy(ctx->ev_chain);
   if (ctx->ev_far) cudaEventDestroy(ctx->ev_far);
+  {
+    CtxExtra& X = extra(ctx);
+    if (X.pev_made)
+      for (int k = 0; k < 8; k++)
+        for (int q = 0; q < 3; q++)
+          if (X.pev[k][q]) cudaEventDestroy(X.pev[k][q]);
+  }
   if (ctx->ev_far_final) cudaEventDestroy(ctx->ev_far_final);
   for (int q = 0; q < 6; q++)
     if (ctx->tev[q]) cudaEventDestroy(ctx->tev[q]);
@@ -680,7 +794,9 @@ gfm_status_t gfm::run_steps(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
       if (overlapped) {
         // ghost fill and flux update interleaved across SM partitions; the
         // flux phase here is the update of the tiles near the interface
+        choose_partition(ctx);
         launch_ghost_fill_overlapped(ctx, m);
+        ctx->part_ev[0] = ctx->part_ev[1] = ctx->part_ev[2] = nullptr;
         // The level set's advection stages read phi and the velocity field,
         // complete once the chain has written its cells' velocities; its
         // writes of phi (copy, reinitialisation) wait for the ghost fill's

@@ -76,6 +76,15 @@ struct gfm_ctx {
   int far_sms;
   int chain_sms;   // SMs of the overlapped ghost fill's chain partition
   int chain_ctas;  // CTAs of the interface loop (8 warps each) on that partition
+  // The partitions the overlapped ghost fill can take (n_parts pairs of chain
+  // and far streams; part: the one in use) and the timing events of this
+  // step's chain and far paths (fork, near sweeps done, far flux done; null
+  // when the step is not measured), from which the next steps choose.
+  int n_parts, part;
+  cudaStream_t part_chain[2], part_far[2];
+  int part_sms[2];
+  int chain_ctas_per_sm;
+  cudaEvent_t part_ev[3];
   double* stage;     // packed (unpitched) copy of the whole state: 4, 4 and 1 planes of nr x nc
                      // (gfm_upload_state / gfm_download_state)
   // per-interface work arrays (capacity = Nx*Ny)
@@ -195,7 +204,14 @@ int flux_batch_occupancy(int fs, int shape);
 // kernel launch helpers (defined in the .cu files)
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask);
 void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaStream_t stream);
-bool green_streams(int device, cudaStream_t* chain, cudaStream_t* far, int* chain_sms);
+// SM partitions of a device for the overlapped ghost fill: n pairs of
+// (chain, far) streams with chain_sms[k] SMs on the chain side
+struct GreenParts {
+  int n;
+  int chain_sms[2];
+  cudaStream_t chain[2], far[2];
+};
+bool green_streams(int device, GreenParts* parts);
 void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m);
 void launch_bcs(gfm_ctx* ctx, int fluid_mask);
 void launch_commit(gfm_ctx* ctx, int fluid_mask, bool bcs);

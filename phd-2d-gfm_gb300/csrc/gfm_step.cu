@@ -2493,6 +2493,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   if (variant == GFM_RIEMANN) run_extrap(ctx, 2, false);
   cudaEventRecord(ctx->ev_fork, s);
   if (ctx->timing) cudaEventRecord(ctx->tev[0], s);
+  if (ctx->part_ev[0]) cudaEventRecord(ctx->part_ev[0], s);
 
   // far partition, first: the band around the interface (distance classes,
   // lists), the near cells and the flux tiles that read them; the interface
@@ -2564,6 +2565,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
   launch_fs_update_sel(ctx, m->fs, 3, TILES_FAR, ctx->s_far);
   cudaEventRecord(ctx->ev_far, ctx->s_far);
   if (ctx->timing) cudaEventRecord(ctx->tev[2], ctx->s_far);
+  if (ctx->part_ev[2]) cudaEventRecord(ctx->part_ev[2], ctx->s_far);
 
   // after the chain, on the highest-priority stream: the true extrapolation
   // (the loop's writes overlaid on the first sweep's reads), conserved grids
@@ -2590,6 +2592,7 @@ void launch_ghost_fill_overlapped(gfm_ctx* ctx, const gfm_method_desc* m) {
     }
   }
   if (ctx->timing) cudaEventRecord(ctx->tev[3], sn);
+  if (ctx->part_ev[1]) cudaEventRecord(ctx->part_ev[1], sn);
   // The near tiles read far cells too: the far cells' conversion is done (the
   // far tiles' flux update writes only its own tiles of Unew).  From here on
   // nothing in the ghost fill reads phi.
