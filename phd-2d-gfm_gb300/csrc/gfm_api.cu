@@ -358,11 +358,11 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     alloc((void**)&ctx->probe_ij, sizeof(int) * 4 * cap);
     alloc((void**)&ctx->probe_w, sizeof(double) * 8 * cap);
     alloc((void**)&ctx->probe_dep, sizeof(int) * 8 * cap);
-    // chunks of at least 2048 cells (the count array's size), enough of them
-    // for one CTA per SM on large grids (the chunked kernels run one CTA per SM)
+    // chunks of at least 2048 cells (the count array's size), one per SM on
+    // large grids (the chunked kernels run one CTA per SM), in whole warps
     const int sms = ctx->num_sms;
     const int64_t ncell = (int64_t)P.nr * P.nc;
-    int64_t chunk = ((ncell + sms - 1) / sms + 511) / 512 * 512;
+    int64_t chunk = ((ncell + sms - 1) / sms + 31) / 32 * 32;
     if (chunk < 2048) chunk = 2048;
     ctx->chunk = (int)chunk;
     ctx->n_chunks = (int)((ncell + chunk - 1) / chunk);

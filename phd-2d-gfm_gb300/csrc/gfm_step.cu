@@ -19,8 +19,8 @@
 namespace gfm {
 
 // Cells per CTA of the chunked full-grid kernels (k_prims, k_vof_prims,
-// k_compact): gfm_ctx::chunk, a multiple of CHUNK_T of at least 2048, sized
-// so that the chunks make one wave of one CTA per SM on large grids.
+// k_compact): gfm_ctx::chunk, a multiple of 32 of at least 2048, sized so
+// that the chunks make one wave of one CTA per SM on large grids.
 constexpr int CHUNK_T = 512;
 
 static int grid_blocks(int64_t n, int per) {
@@ -464,12 +464,13 @@ __global__ void __launch_bounds__(CHUNK_T) k_compact(GridP P, const uint8_t* mas
   const int64_t n = (int64_t)P.nr * P.nc;
   const int64_t base = (int64_t)blockIdx.x * chunk;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // cells base + it*CHUNK_T + tid, in order of it then tid
-  for (int it = 0; it < chunk / CHUNK_T; it++) {
+  // cells base + it*CHUNK_T + tid of the chunk, in order of it then tid
+  const int64_t end = base + chunk < n ? base + chunk : n;
+  for (int it = 0; it < (chunk + CHUNK_T - 1) / CHUNK_T; it++) {
     int64_t lin = base + (int64_t)it * CHUNK_T + threadIdx.x;
     int m = 0;
     int i = 0, j = 0;
-    if (lin < n) {
+    if (lin < end) {
       linear_to_ij(P, lin, i, j);
       m = mask[cidx(P, i, j)];
     }
