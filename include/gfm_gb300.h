@@ -171,8 +171,9 @@ gfm_status_t gfm_step(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps);
 /* gfm_step with CUDA events recorded on the context's stream around each
  * phase; adds the milliseconds of each phase to phase_ms[GFM_NPHASES]:
  * 0 CFL/dt, 1 ghost fill, 2 flux update (both fluids, one launch),
- * 3 level set (the part not hidden: it runs beside the flux update),
- * 4 boundary conditions + end of step; phases 0-4 add up to the step.  With the overlapped schedule (gfm_set_overlap) phase 1 runs up
+ * 3 boundary conditions (the commit of the new values) and the part of the
+ * level set not hidden (it runs beside the flux update and the commit),
+ * 4 end of step; phases 0-4 add up to the step.  With the overlapped schedule (gfm_set_overlap) phase 1 runs up
  * to the flux update of the tiles near the interface and phase 2 is that
  * update; phases 5-8 then time parts that overlap inside phases 1-2:
  * 5 the interface loop, 6 the far-field partition's work, 7 the exact
@@ -184,7 +185,11 @@ gfm_status_t gfm_step_timed(gfm_ctx* ctx, const gfm_method_desc* m, int nsteps, 
 /* Schedule of the ghost fill for the Riemann and real GFM.
  *   GFM_OVERLAP_OFF   every phase on the context's stream in turn
  *   GFM_OVERLAP_ON    the interface loop on a small SM partition while the
- *                     far field is extrapolated and updated on the rest
+ *                     far field is extrapolated and updated on the rest (8 or
+ *                     16 SMs for the loop, chosen step by step from the
+ *                     measured times of earlier steps' loop and far field;
+ *                     GFM_CHAIN_SMS in the environment, a multiple of 8, fixes
+ *                     it)
  *   GFM_OVERLAP_AUTO  (default) ON for the Riemann GFM, whose bilinear probes
  *                     chain interfacial cells many deep, OFF for the real GFM,
  *                     whose cells depend on one opposite cell at most
