@@ -17,9 +17,9 @@ using namespace gfm;
 std::atomic<long long> gfm::g_launches{0};
 
 // ---------------------------------------------------------------------------
-// SM partitions for the overlapped ghost fill: an 8-SM green context for the
-// interface chain and one for the remaining SMs, with one stream each,
-// created once per device.  The driver entry points are fetched through the
+// SM partitions for the overlapped ghost fill: green contexts of 8 and of 16
+// SMs for the interface chain, each with one for the remaining SMs, with one
+// stream each, created once per device.  The driver entry points are fetched through the
 // runtime, so the library does not link libcuda.  Without green-context
 // support two ordinary streams are used (same results, less isolation).
 // ---------------------------------------------------------------------------
@@ -94,11 +94,14 @@ bool gfm::green_streams(int dev, GreenParts* parts) {
       const int v = atoi(e);
       if (v >= 8 && v <= 64 && v % 8 == 0) { req[0] = (unsigned)v; q.n = 1; }
     }
-    g.ok = true;
-    for (int k = 0; k < q.n && g.ok; k++) {
+    int made = 0;
+    for (int k = 0; k < q.n; k++) {
       q.chain_sms[k] = (int)req[k];
-      g.ok = make_green(dev, req[k], &q.chain[k], &q.far[k], &q.chain_sms[k]);
+      if (!make_green(dev, req[k], &q.chain[k], &q.far[k], &q.chain_sms[k])) break;
+      made++;
     }
+    q.n = made;
+    g.ok = made > 0;
     if (!g.ok) {   // no green contexts: one pair of ordinary streams
       cudaGetLastError();
       q.n = 1;
