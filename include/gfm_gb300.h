@@ -217,11 +217,11 @@ gfm_status_t gfm_set_newton_limit(gfm_ctx* ctx, int max_iterations);
  * the default).  The step's results are not valid after a withheld entry. */
 gfm_status_t gfm_set_interface_wait(gfm_ctx* ctx, int64_t spin_limit, int withheld_entry);
 
-/* Tile shape of the context's flux update: 32 x 8 cells (the default), 16 x 16
+/* Tile shape of the context's flux update: 16 x 16 cells (the default), 32 x 8
  * or 64 x 4 per CTA.  Results are identical for every shape (each face flux is
  * formed once and each cell sums its faces in the reference's order); the
  * time differs with the grid.  The overlapped ghost fill's passes always use
- * 32 x 8.  gfm_batch_autotune chooses it per grid-size class. */
+ * 16 x 16.  gfm_batch_autotune chooses it per grid-size class. */
 #define GFM_FLUX_TILE_32x8 0
 #define GFM_FLUX_TILE_16x16 1
 #define GFM_FLUX_TILE_64x4 2

@@ -328,6 +328,7 @@ gfm_status_t gfm_ctx_create(const gfm_grid_desc* d, int two_fluid, gfm_ctx** out
     ctx->chain_sms = 8;
     ctx->chain_ctas = 16;
     ctx->far_sms = sms > 16 ? sms - 8 : sms;   // the far partition of the overlapped ghost fill
+    ctx->flux_shape = FLUX_SHAPE_DEFAULT;
     ctx->n_parts = 0;
     ctx->part = 0;
     ctx->chain_ctas_per_sm = 2;

@@ -21,7 +21,8 @@
 //            items, costliest instances first), then every instance's commit.
 // gfm_batch_autotune times the tile shapes per grid-size class and the two
 // schedules on the batch itself and keeps the fastest, then keeps the chosen
-// shapes only if the whole batch steps faster with them than with 32x8.
+// shapes only if the whole batch steps faster with them than with the
+// default shape.
 #include "gfm_internal.cuh"
 #include <algorithm>
 #include <cstdio>
@@ -464,7 +465,7 @@ gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int step
     cudaEventElapsedTime(&sms_[sc], e0, e1);
   }
   if (r == GFM_OK) b->schedule = sms_[1] < sms_[0] ? GFM_BATCH_PHASED : GFM_BATCH_STREAMS;
-  // 3. the chosen tiles against the default tile (32x8) of every instance,
+  // 3. the chosen tiles against the default tile (16x16) of every instance,
   //    on the whole batch with the chosen schedule: a shape that wins on one
   //    instance stepped alone can lose when the instances share the GPU
   float tms[2] = {0.0f, 0.0f};
@@ -472,12 +473,12 @@ gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int step
   bool differs = false;
   for (int i = 0; i < b->n; i++) {
     chosen[i] = b->inst[i]->flux_shape;
-    differs = differs || chosen[i] != FLUX_SHAPE_32x8;
+    differs = differs || chosen[i] != FLUX_SHAPE_DEFAULT;
   }
   bool keep_chosen = true;
   if (r == GFM_OK && differs) {
     for (int v = 0; v < 2 && r == GFM_OK; v++) {
-      for (int i = 0; i < b->n; i++) b->inst[i]->flux_shape = v == 0 ? chosen[i] : FLUX_SHAPE_32x8;
+      for (int i = 0; i < b->n; i++) b->inst[i]->flux_shape = v == 0 ? chosen[i] : FLUX_SHAPE_DEFAULT;
       for (int i = 0; i < b->n && r == GFM_OK; i++) r = restore(i);
       if (r == GFM_OK) r = gfm_step_batched_graph(b, m, GRAPH_STEPS);   // records the graph (warm-up)
       if (r == GFM_OK && cudaStreamSynchronize(b->main) != cudaSuccess) r = GFM_ERR_CUDA;
@@ -490,7 +491,7 @@ gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int step
       cudaEventElapsedTime(&tms[v], e0, e1);
     }
     keep_chosen = !(tms[1] < tms[0]);
-    for (int i = 0; i < b->n; i++) b->inst[i]->flux_shape = keep_chosen ? chosen[i] : FLUX_SHAPE_32x8;
+    for (int i = 0; i < b->n; i++) b->inst[i]->flux_shape = keep_chosen ? chosen[i] : FLUX_SHAPE_DEFAULT;
   }
   if (r == GFM_OK) {
     for (int i = 0; i < b->n && r == GFM_OK; i++) r = restore(i);
@@ -502,10 +503,10 @@ gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int step
   char buf[384];
   snprintf(buf, sizeof(buf),
            "], \"steps\": %d, \"schedule_ms_per_step\": {\"streams\": %.4f, \"phased\": %.4f}, "
-           "\"schedule\": \"%s\", \"tiles_on_batch_ms_per_step\": {\"chosen\": %.4f, \"32x8\": %.4f}, "
+           "\"schedule\": \"%s\", \"tiles_on_batch_ms_per_step\": {\"chosen\": %.4f, \"default\": %.4f}, "
            "\"tiles\": \"%s\"}",
            steps, sms_[0] / steps, sms_[1] / steps, b->schedule == GFM_BATCH_PHASED ? "phased" : "streams",
-           tms[0] / steps, tms[1] / steps, keep_chosen ? "per class" : "32x8 everywhere");
+           tms[0] / steps, tms[1] / steps, keep_chosen ? "per class" : "default everywhere");
   rep += buf;
   if (report && report_len > 0) {
     strncpy(report, rep.c_str(), (size_t)report_len - 1);

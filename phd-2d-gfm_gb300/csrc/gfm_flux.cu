@@ -40,8 +40,8 @@ namespace gfm {
 constexpr int NT = 256;
 
 // Tile shape TX x TY: the shared-memory regions of one tile.  The default
-// 32 x 8 (FLUX_TX x FLUX_TY) is the one the overlapped schedule's tile
-// marking assumes; 16 x 16 and 64 x 4 are the autotuner's alternatives.
+// 16 x 16 (FLUX_TX x FLUX_TY) is the one the overlapped schedule's tile
+// marking assumes; 32 x 8 and 64 x 4 are the autotuner's alternatives.
 template <int TX, int TY>
 struct FluxShape {
   static constexpr int WR = TY + 4;   // primitive region rows   (i0-2 .. i0+TY+1)
@@ -453,7 +453,7 @@ void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaS
   }
   prepare_kernels();
   // the overlapped schedule's passes use the tile grid its marking assumes
-  const int shape = tiles == TILES_ALL ? ctx->flux_shape : FLUX_SHAPE_32x8;
+  const int shape = tiles == TILES_ALL ? ctx->flux_shape : FLUX_SHAPE_DEFAULT;
   const int tw = flux_tile_w(shape), th = flux_tile_h(shape);
   dim3 grid((P.Nx + tw - 1) / tw, (P.Ny + th - 1) / th, nz);
   const bool mu = fs == GFM_FS_MUSCL;

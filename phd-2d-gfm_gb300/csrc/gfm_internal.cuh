@@ -180,9 +180,13 @@ __device__ __forceinline__ void raise_status(DevTime* dt, uint32_t bits) {
   if (bits) atomicOr(&dt->status, bits);
 }
 
-// flux-update tiles (k_flux_update): TX x TY real cells per CTA, 2-cell halo
-constexpr int FLUX_TX = 32;
-constexpr int FLUX_TY = 8;
+// flux-update tiles (k_flux_update): TX x TY real cells per CTA, 2-cell halo.
+// 16 x 16 is the default shape and the one the overlapped schedule's tile
+// marking uses: on the 1000x400 shock-bubble's whole run 2.060 ms per step
+// against 2.106 with 32 x 8 and 2.400 with 64 x 4 (the far tiles' update 1.244
+// against 1.307 and 1.752 ms).
+constexpr int FLUX_TX = 16;
+constexpr int FLUX_TY = 16;
 inline int flux_tiles_x(const GridP& P) { return (P.Nx + FLUX_TX - 1) / FLUX_TX; }
 inline int flux_tiles_y(const GridP& P) { return (P.Ny + FLUX_TY - 1) / FLUX_TY; }
 
@@ -190,6 +194,7 @@ inline int flux_tiles_y(const GridP& P) { return (P.Ny + FLUX_TY - 1) / FLUX_TY;
 enum { TILES_ALL = 0, TILES_FAR = 1, TILES_NEAR = 2 };
 // tile shapes of the flux update (gfm_ctx::flux_shape)
 enum { FLUX_SHAPE_32x8 = 0, FLUX_SHAPE_16x16 = 1, FLUX_SHAPE_64x4 = 2, FLUX_SHAPES = 3 };
+constexpr int FLUX_SHAPE_DEFAULT = FLUX_SHAPE_16x16;   // FLUX_TX x FLUX_TY
 int flux_tile_w(int shape);
 int flux_tile_h(int shape);
 // the persistent flux update of a batch (k_flux_batch): per-instance

@@ -169,6 +169,7 @@ extern "C" gfm_status_t gfm_onefluid_step_noalloc(const gfm_grid_desc* d, const 
   P.periodic = allper;
   ctx.two_fluid = 0;
   ctx.num_sms = sms;   // grid sizes of the grid-stride kernels, as in gfm_ctx_create
+  ctx.flux_shape = FLUX_SHAPE_DEFAULT;
   ctx.stream = static_cast<cudaStream_t>(stream);
   ctx.U[0] = U;
   unsigned char* b = static_cast<unsigned char*>(base);
