@@ -217,14 +217,16 @@ gfm_status_t gfm_set_newton_limit(gfm_ctx* ctx, int max_iterations);
  * the default).  The step's results are not valid after a withheld entry. */
 gfm_status_t gfm_set_interface_wait(gfm_ctx* ctx, int64_t spin_limit, int withheld_entry);
 
-/* Tile shape of the context's flux update: 16 x 16 cells (the default), 32 x 8
- * or 64 x 4 per CTA.  Results are identical for every shape (each face flux is
- * formed once and each cell sums its faces in the reference's order); the
- * time differs with the grid.  The overlapped ghost fill's passes always use
- * 16 x 16.  gfm_batch_autotune chooses it per grid-size class. */
+/* Tile shape of the context's flux update: 16 x 32 cells (the default, 512
+ * threads per CTA), 16 x 16, 32 x 8 or 64 x 4 (256 threads) per CTA.  Results
+ * are identical for every shape (each face flux is formed once and each cell
+ * sums its faces in the reference's order); the time differs with the grid.
+ * The overlapped ghost fill's passes always use 16 x 32.  gfm_batch_autotune
+ * chooses it per grid-size class. */
 #define GFM_FLUX_TILE_32x8 0
 #define GFM_FLUX_TILE_16x16 1
 #define GFM_FLUX_TILE_64x4 2
+#define GFM_FLUX_TILE_16x32 3
 gfm_status_t gfm_set_flux_tile(gfm_ctx* ctx, int shape);
 
 /* number of kernels this library has launched since it was loaded */

@@ -261,7 +261,7 @@ __global__ void k_rc_empty(GridP P, DevTime* D) {
 
 gfm_status_t gfm::validate_method(gfm_ctx* ctx, const gfm_method_desc* m) { return check_method(ctx, m); }
 static_assert(GFM_FLUX_TILE_32x8 == FLUX_SHAPE_32x8 && GFM_FLUX_TILE_16x16 == FLUX_SHAPE_16x16 &&
-                  GFM_FLUX_TILE_64x4 == FLUX_SHAPE_64x4,
+                  GFM_FLUX_TILE_64x4 == FLUX_SHAPE_64x4 && GFM_FLUX_TILE_16x32 == FLUX_SHAPE_16x32,
               "tile shape codes");
 double* gfm::mass_scratch(gfm_ctx* ctx) { return extra(ctx).mass_part; }
 gfm_status_t gfm::launch_status() { return last_error(); }
@@ -957,7 +957,7 @@ gfm_status_t gfm_get_interface_totals(gfm_ctx* ctx, int64_t* n_solves, int64_t* 
 }
 
 gfm_status_t gfm_set_flux_tile(gfm_ctx* ctx, int shape) {
-  if (!ctx || shape < GFM_FLUX_TILE_32x8 || shape > GFM_FLUX_TILE_64x4) return GFM_ERR_ARG;
+  if (!ctx || shape < GFM_FLUX_TILE_32x8 || shape > GFM_FLUX_TILE_16x32) return GFM_ERR_ARG;
   ctx->flux_shape = shape;
   return GFM_OK;
 }

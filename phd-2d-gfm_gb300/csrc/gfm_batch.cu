@@ -442,10 +442,11 @@ gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int step
     char buf[320];
     snprintf(buf, sizeof(buf),
              "%s{\"max_padded_cells\": %lld, \"probe_instance\": %d, \"probe_cells\": %lld, "
-             "\"ms_per_step\": {\"32x8\": %.4f, \"16x16\": %.4f, \"64x4\": %.4f}, \"tile\": \"%s\"}",
+             "\"ms_per_step\": {\"32x8\": %.4f, \"16x16\": %.4f, \"64x4\": %.4f, \"16x32\": %.4f}, "
+             "\"tile\": \"%s\"}",
              first_class ? "" : ", ", cl == 2 ? -1ll : (long long)bounds[cl], rep_i,
-             (long long)(c->P.Nx) * c->P.Ny, ms[0] / steps, ms[1] / steps, ms[2] / steps,
-             best == 0 ? "32x8" : (best == 1 ? "16x16" : "64x4"));
+             (long long)(c->P.Nx) * c->P.Ny, ms[0] / steps, ms[1] / steps, ms[2] / steps, ms[3] / steps,
+             best == 0 ? "32x8" : (best == 1 ? "16x16" : (best == 2 ? "64x4" : "16x32")));
     rep += buf;
     first_class = false;
   }
@@ -465,7 +466,7 @@ gfm_status_t gfm_batch_autotune(gfm_batch* b, const gfm_method_desc* m, int step
     cudaEventElapsedTime(&sms_[sc], e0, e1);
   }
   if (r == GFM_OK) b->schedule = sms_[1] < sms_[0] ? GFM_BATCH_PHASED : GFM_BATCH_STREAMS;
-  // 3. the chosen tiles against the default tile (16x16) of every instance,
+  // 3. the chosen tiles against the default tile (16x32) of every instance,
   //    on the whole batch with the chosen schedule: a shape that wins on one
   //    instance stepped alone can lose when the instances share the GPU
   float tms[2] = {0.0f, 0.0f};

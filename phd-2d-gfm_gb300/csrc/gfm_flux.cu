@@ -37,13 +37,15 @@
 
 namespace gfm {
 
-constexpr int NT = 256;
-
-// Tile shape TX x TY: the shared-memory regions of one tile.  The default
-// 16 x 16 (FLUX_TX x FLUX_TY) is the one the overlapped schedule's tile
-// marking assumes; 32 x 8 and 64 x 4 are the autotuner's alternatives.
+// Tile shape TX x TY: the shared-memory regions of one tile, and its CTA's
+// threads (NT).  The default 16 x 32 (FLUX_TX x FLUX_TY) is the one the
+// overlapped schedule's tile marking assumes, with 512 threads and one CTA
+// per SM; 16 x 16, 32 x 8 and 64 x 4 (256 threads, two CTAs per SM) are the
+// autotuner's alternatives.
 template <int TX, int TY>
 struct FluxShape {
+  static constexpr int NT = TX * TY >= 512 ? 512 : 256;
+  static constexpr int MIN_CTAS = NT == 512 ? 1 : 2;   // resident per SM (launch bounds)
   static constexpr int WR = TY + 4;   // primitive region rows   (i0-2 .. i0+TY+1)
   static constexpr int WC = TX + 4;   // primitive region columns (j0-2 .. j0+TX+1)
   static constexpr int SR = TY + 2;   // face-state cells rows    (i0-1 .. i0+TY)
@@ -161,7 +163,7 @@ __device__ __forceinline__ V4 muscl_face_flux(bool xdir, V4 Sr, V4 Sl, const V4&
 }
 
 // One tile (bx, by) of fluid slot bz of the grid a, whose tile rows are gx
-// tiles wide, by the whole CTA (NT threads); the CTA's dynamic shared memory
+// tiles wide, by the whole CTA (Sh::NT threads); the CTA's dynamic shared memory
 // holds the tile's Smem.
 template <bool MUSCL, int TX, int TY>
 __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int bz, int gx, unsigned char* smem_raw) {
@@ -192,7 +194,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
   // tile outside the realcells box: its cells keep their values
   const bool tile_live = !(i0 + TY <= imin || i0 >= imax || j0 + TX <= jmin || j0 >= jmax);
   if (!tile_live) {
-    for (int k = tid; k < TX * TY; k += NT) {
+    for (int k = tid; k < TX * TY; k += Sh::NT) {
       int i = i0 + k / TX, j = j0 + k % TX;
       if (i < P.Ny + P.g && j < P.Nx + P.g) {
         int64_t c = cidx(P, i, j);
@@ -214,7 +216,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
   const V4 u00 = load4(U, P, c00);
   if (tid == 0) { s_nq = 0; s_nt = 0; }
   bool same = true;
-  for (int k = tid; k < WR * WC; k += NT) {
+  for (int k = tid; k < WR * WC; k += Sh::NT) {
     int r = k / WC, c = k % WC;
     int i = min(max(i0 - 2 + r, 0), P.nr - 1);
     int j = min(max(j0 - 2 + c, 0), P.nc - 1);
@@ -257,7 +259,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
   } else {
     // phase 2: evolved face states of cells (i0-1 .. i0+TY) x (j0-1 .. j0+TX)
     if (MUSCL) {
-      for (int k = tid; k < SR * SC; k += NT) {
+      for (int k = tid; k < SR * SC; k += Sh::NT) {
         int r = k / SC, c = k % SC;       // cell (i0-1+r, j0-1+c) = w[r+1][c+1]
         V4 fs[4];
         cell_face_states(sW(s, r + 1, c + 1), s.irho[r + 1][c + 1], sW(s, r + 1, c), sW(s, r + 1, c + 2),
@@ -271,7 +273,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
     //   x face (fr, fc): between cells (i0+fr, j0+fc-1) and (i0+fr, j0+fc)
     //   y face (fr, fc): between cells (i0+fr-1, j0+fc) and (i0+fr, j0+fc)
     // Flux slot of face k, component m: fx[m] (flat) + k, or fy[m] + k - NXF.
-    for (int k = tid; k < NXF + NYF; k += NT) {
+    for (int k = tid; k < NXF + NYF; k += Sh::NT) {
       bool xdir = k < NXF;
       int fr, fc;
       if (xdir) { fr = k / (TX + 1); fc = k % (TX + 1); }
@@ -303,7 +305,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
     __syncthreads();
     // phase 3b: the queued faces, those with waves first
     const int nq = s_nq, nt = s_nt;
-    for (int e = tid; e < nq + nt; e += NT) {
+    for (int e = tid; e < nq + nt; e += Sh::NT) {
       const int k = s.qid[e < nq ? e : NXF + NYF - nt + (e - nq)];
       const bool xdir = k < NXF;
       double* slot = xdir ? &s.fx[0][0][0] + k : &s.fy[0][0][0] + (k - NXF);
@@ -320,7 +322,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
 
   // phase 4: U + (dt/dx Fw + dt/dy Fs) - dt/dx Fe - dt/dy Fn
   const V4 ufx = s_uniform_flux[0], ufy = s_uniform_flux[1];
-  for (int k = tid; k < TX * TY; k += NT) {
+  for (int k = tid; k < TX * TY; k += Sh::NT) {
     int r = k / TX, c = k % TX;
     int i = i0 + r, j = j0 + c;
     if (i >= P.Ny + P.g || j >= P.Nx + P.g) continue;
@@ -355,7 +357,7 @@ __device__ __forceinline__ void flux_tile(const FluxArgs& a, int bx, int by, int
 }
 
 template <bool MUSCL, int TX, int TY>
-__global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
+__global__ void __launch_bounds__(FluxShape<TX, TY>::NT, FluxShape<TX, TY>::MIN_CTAS) k_flux_update(FluxArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   flux_tile<MUSCL, TX, TY>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, smem_raw);
 }
@@ -368,7 +370,8 @@ __global__ void __launch_bounds__(NT, 2) k_flux_update(FluxArgs a) {
 // counters for the next launch (stream-ordered, so a replayed graph finds
 // them at zero).  Item: instance << 24 | fluid slot << 23 | tile.
 template <bool MUSCL, int TX, int TY>
-__global__ void __launch_bounds__(NT, 2) k_flux_batch(const FluxArgs* __restrict__ args,
+__global__ void __launch_bounds__(FluxShape<TX, TY>::NT, FluxShape<TX, TY>::MIN_CTAS)
+    k_flux_batch(const FluxArgs* __restrict__ args,
                                                        const uint32_t* __restrict__ items, int n_items,
                                                        unsigned int* counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -384,7 +387,7 @@ __global__ void __launch_bounds__(NT, 2) k_flux_batch(const FluxArgs* __restrict
     {
       const int* src = reinterpret_cast<const int*>(args + inst);
       int* dst = reinterpret_cast<int*>(&s_args);
-      for (int q = threadIdx.x; q < (int)(sizeof(FluxArgs) / sizeof(int)); q += NT) dst[q] = src[q];
+      for (int q = threadIdx.x; q < (int)(sizeof(FluxArgs) / sizeof(int)); q += FluxShape<TX, TY>::NT) dst[q] = src[q];
     }
     __syncthreads();
     const int gx = (s_args.P.Nx + TX - 1) / TX;
@@ -405,16 +408,19 @@ template <int TX, int TY>
 static size_t flux_smem() { return sizeof(typename FluxShape<TX, TY>::Smem); }
 
 // the tile shapes a flux update can take (FLUX_SHAPE_*)
+template <bool MUSCL, int TX, int TY>
+static void set_shape_attributes() {
+  cudaFuncSetAttribute(k_flux_update<MUSCL, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)flux_smem<TX, TY>());
+  cudaFuncSetAttribute(k_flux_batch<MUSCL, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)flux_smem<TX, TY>());
+}
 template <bool MUSCL>
 static void set_flux_attributes() {
-  cudaFuncSetAttribute(k_flux_update<MUSCL, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<32, 8>());
-  cudaFuncSetAttribute(k_flux_update<MUSCL, 16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)flux_smem<16, 16>());
-  cudaFuncSetAttribute(k_flux_update<MUSCL, 64, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<64, 4>());
-  cudaFuncSetAttribute(k_flux_batch<MUSCL, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<32, 8>());
-  cudaFuncSetAttribute(k_flux_batch<MUSCL, 16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)flux_smem<16, 16>());
-  cudaFuncSetAttribute(k_flux_batch<MUSCL, 64, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_smem<64, 4>());
+  set_shape_attributes<MUSCL, 32, 8>();
+  set_shape_attributes<MUSCL, 16, 16>();
+  set_shape_attributes<MUSCL, 64, 4>();
+  set_shape_attributes<MUSCL, 16, 32>();
 }
 
 // Kernel attributes, set once per process before any launch (and so before
@@ -428,8 +434,38 @@ void prepare_kernels() {
   prepare_step_kernels();
 }
 
-int flux_tile_w(int shape) { return shape == FLUX_SHAPE_16x16 ? 16 : (shape == FLUX_SHAPE_64x4 ? 64 : 32); }
-int flux_tile_h(int shape) { return shape == FLUX_SHAPE_16x16 ? 16 : (shape == FLUX_SHAPE_64x4 ? 4 : 8); }
+int flux_tile_w(int shape) {
+  return (shape == FLUX_SHAPE_16x16 || shape == FLUX_SHAPE_16x32) ? 16 : (shape == FLUX_SHAPE_64x4 ? 64 : 32);
+}
+int flux_tile_h(int shape) {
+  return shape == FLUX_SHAPE_16x16 ? 16 : (shape == FLUX_SHAPE_16x32 ? 32 : (shape == FLUX_SHAPE_64x4 ? 4 : 8));
+}
+
+template <int TX, int TY>
+static void update_shape(bool muscl, dim3 grid, const FluxArgs& a, cudaStream_t stream) {
+  constexpr int nt = FluxShape<TX, TY>::NT;
+  if (muscl) k_flux_update<true, TX, TY><<<grid, nt, flux_smem<TX, TY>(), stream>>>(a);
+  else k_flux_update<false, TX, TY><<<grid, nt, flux_smem<TX, TY>(), stream>>>(a);
+}
+template <int TX, int TY>
+static void batch_shape(bool muscl, int ctas, const FluxArgs* A, const uint32_t* items, int n_items,
+                        unsigned int* counters, cudaStream_t stream) {
+  constexpr int nt = FluxShape<TX, TY>::NT;
+  if (muscl) k_flux_batch<true, TX, TY><<<ctas, nt, flux_smem<TX, TY>(), stream>>>(A, items, n_items, counters);
+  else k_flux_batch<false, TX, TY><<<ctas, nt, flux_smem<TX, TY>(), stream>>>(A, items, n_items, counters);
+}
+template <int TX, int TY>
+static int batch_occupancy(bool muscl) {
+  int per = 0;
+  const void* k = muscl ? (const void*)k_flux_batch<true, TX, TY> : (const void*)k_flux_batch<false, TX, TY>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, FluxShape<TX, TY>::NT, flux_smem<TX, TY>()) !=
+          cudaSuccess ||
+      per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return per;
+}
 
 void launch_fs_update(gfm_ctx* ctx, int fs, int fluid_mask) {
   launch_fs_update_sel(ctx, fs, fluid_mask, TILES_ALL, ctx->stream);
@@ -457,16 +493,10 @@ void launch_fs_update_sel(gfm_ctx* ctx, int fs, int fluid_mask, int tiles, cudaS
   const int tw = flux_tile_w(shape), th = flux_tile_h(shape);
   dim3 grid((P.Nx + tw - 1) / tw, (P.Ny + th - 1) / th, nz);
   const bool mu = fs == GFM_FS_MUSCL;
-  if (shape == FLUX_SHAPE_16x16) {
-    if (mu) k_flux_update<true, 16, 16><<<grid, NT, flux_smem<16, 16>(), stream>>>(a);
-    else k_flux_update<false, 16, 16><<<grid, NT, flux_smem<16, 16>(), stream>>>(a);
-  } else if (shape == FLUX_SHAPE_64x4) {
-    if (mu) k_flux_update<true, 64, 4><<<grid, NT, flux_smem<64, 4>(), stream>>>(a);
-    else k_flux_update<false, 64, 4><<<grid, NT, flux_smem<64, 4>(), stream>>>(a);
-  } else {
-    if (mu) k_flux_update<true, 32, 8><<<grid, NT, flux_smem<32, 8>(), stream>>>(a);
-    else k_flux_update<false, 32, 8><<<grid, NT, flux_smem<32, 8>(), stream>>>(a);
-  }
+  if (shape == FLUX_SHAPE_16x32) update_shape<16, 32>(mu, grid, a, stream);
+  else if (shape == FLUX_SHAPE_16x16) update_shape<16, 16>(mu, grid, a, stream);
+  else if (shape == FLUX_SHAPE_64x4) update_shape<64, 4>(mu, grid, a, stream);
+  else update_shape<32, 8>(mu, grid, a, stream);
   counted();
   // the new values are in Unew; launch_commit copies them (with the BCs) to U
 }
@@ -496,41 +526,21 @@ void launch_flux_batch(int fs, int shape, const void* args, const uint32_t* item
   prepare_kernels();
   const bool mu = fs == GFM_FS_MUSCL;
   const FluxArgs* A = static_cast<const FluxArgs*>(args);
-  if (shape == FLUX_SHAPE_16x16) {
-    if (mu) k_flux_batch<true, 16, 16><<<ctas, NT, flux_smem<16, 16>(), stream>>>(A, items, n_items, counters);
-    else k_flux_batch<false, 16, 16><<<ctas, NT, flux_smem<16, 16>(), stream>>>(A, items, n_items, counters);
-  } else if (shape == FLUX_SHAPE_64x4) {
-    if (mu) k_flux_batch<true, 64, 4><<<ctas, NT, flux_smem<64, 4>(), stream>>>(A, items, n_items, counters);
-    else k_flux_batch<false, 64, 4><<<ctas, NT, flux_smem<64, 4>(), stream>>>(A, items, n_items, counters);
-  } else {
-    if (mu) k_flux_batch<true, 32, 8><<<ctas, NT, flux_smem<32, 8>(), stream>>>(A, items, n_items, counters);
-    else k_flux_batch<false, 32, 8><<<ctas, NT, flux_smem<32, 8>(), stream>>>(A, items, n_items, counters);
-  }
+  if (shape == FLUX_SHAPE_16x32) batch_shape<16, 32>(mu, ctas, A, items, n_items, counters, stream);
+  else if (shape == FLUX_SHAPE_16x16) batch_shape<16, 16>(mu, ctas, A, items, n_items, counters, stream);
+  else if (shape == FLUX_SHAPE_64x4) batch_shape<64, 4>(mu, ctas, A, items, n_items, counters, stream);
+  else batch_shape<32, 8>(mu, ctas, A, items, n_items, counters, stream);
   counted();
 }
 
 // resident CTAs per SM of the batched flux kernel of a shape
 int flux_batch_occupancy(int fs, int shape) {
   prepare_kernels();
-  int per = 0;
   const bool mu = fs == GFM_FS_MUSCL;
-  const void* k;
-  size_t sm;
-  if (shape == FLUX_SHAPE_16x16) {
-    k = mu ? (const void*)k_flux_batch<true, 16, 16> : (const void*)k_flux_batch<false, 16, 16>;
-    sm = flux_smem<16, 16>();
-  } else if (shape == FLUX_SHAPE_64x4) {
-    k = mu ? (const void*)k_flux_batch<true, 64, 4> : (const void*)k_flux_batch<false, 64, 4>;
-    sm = flux_smem<64, 4>();
-  } else {
-    k = mu ? (const void*)k_flux_batch<true, 32, 8> : (const void*)k_flux_batch<false, 32, 8>;
-    sm = flux_smem<32, 8>();
-  }
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, sm) != cudaSuccess || per < 1) {
-    cudaGetLastError();
-    per = 1;
-  }
-  return per;
+  if (shape == FLUX_SHAPE_16x32) return batch_occupancy<16, 32>(mu);
+  if (shape == FLUX_SHAPE_16x16) return batch_occupancy<16, 16>(mu);
+  if (shape == FLUX_SHAPE_64x4) return batch_occupancy<64, 4>(mu);
+  return batch_occupancy<32, 8>(mu);
 }
 
 }  // namespace gfm

@@ -98,7 +98,7 @@ struct gfm_ctx {
   int itm;           // interface tracker of the last method used (GFM_ITM_*)
   int* ifc_opp;      // real GFM: opposite cell
   long long ifc_spin_limit;  // polls before an interface-loop wait gives up (0: the default)
-  int flux_shape;    // tile shape of the flux update (FLUX_SHAPE_*; the overlapped passes use 32 x 8)
+  int flux_shape;    // tile shape of the flux update (FLUX_SHAPE_*; the overlapped passes use 16 x 32)
   int ifc_withhold;  // test hook: 1 + the interface-list entry left unsolved (0: none)
   gfm::DevTime* dtime;
   gfm::DevTime* h_dtime;  // pinned host mirror
@@ -181,20 +181,21 @@ __device__ __forceinline__ void raise_status(DevTime* dt, uint32_t bits) {
 }
 
 // flux-update tiles (k_flux_update): TX x TY real cells per CTA, 2-cell halo.
-// 16 x 16 is the default shape and the one the overlapped schedule's tile
-// marking uses: on the 1000x400 shock-bubble's whole run 2.060 ms per step
-// against 2.106 with 32 x 8 and 2.400 with 64 x 4 (the far tiles' update 1.244
-// against 1.307 and 1.752 ms).
+// 16 x 32 (512 threads, one CTA per SM) is the default shape and the one the
+// overlapped schedule's tile marking uses: on the 1000x400 shock-bubble's
+// whole run 2.046 ms per step against 2.064 with 16 x 16, 2.106 with 32 x 8
+// and 2.400 with 64 x 4 (the far tiles' update 1.212 against 1.244, 1.307 and
+// 1.752 ms).
 constexpr int FLUX_TX = 16;
-constexpr int FLUX_TY = 16;
+constexpr int FLUX_TY = 32;
 inline int flux_tiles_x(const GridP& P) { return (P.Nx + FLUX_TX - 1) / FLUX_TX; }
 inline int flux_tiles_y(const GridP& P) { return (P.Ny + FLUX_TY - 1) / FLUX_TY; }
 
 // tile selection of the flux update
 enum { TILES_ALL = 0, TILES_FAR = 1, TILES_NEAR = 2 };
 // tile shapes of the flux update (gfm_ctx::flux_shape)
-enum { FLUX_SHAPE_32x8 = 0, FLUX_SHAPE_16x16 = 1, FLUX_SHAPE_64x4 = 2, FLUX_SHAPES = 3 };
-constexpr int FLUX_SHAPE_DEFAULT = FLUX_SHAPE_16x16;   // FLUX_TX x FLUX_TY
+enum { FLUX_SHAPE_32x8 = 0, FLUX_SHAPE_16x16 = 1, FLUX_SHAPE_64x4 = 2, FLUX_SHAPE_16x32 = 3, FLUX_SHAPES = 4 };
+constexpr int FLUX_SHAPE_DEFAULT = FLUX_SHAPE_16x32;   // FLUX_TX x FLUX_TY
 int flux_tile_w(int shape);
 int flux_tile_h(int shape);
 // the persistent flux update of a batch (k_flux_batch): per-instance

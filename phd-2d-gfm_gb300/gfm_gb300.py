@@ -349,9 +349,9 @@ class Context:
         return True
 
     def set_flux_tile(self, shape):
-        """Tile shape of the flux update: "16x16" (default), "32x8" or "64x4"
+        """Tile shape of the flux update: "16x32" (default), "16x16", "32x8" or "64x4"
         (results are identical)."""
-        code = {"32x8": 0, "16x16": 1, "64x4": 2}[shape]
+        code = {"32x8": 0, "16x16": 1, "64x4": 2, "16x32": 3}[shape]
         _check(lib().gfm_set_flux_tile(self._p, code), "gfm_set_flux_tile")
 
     def set_newton_limit(self, max_iterations):
