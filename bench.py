@@ -613,6 +613,19 @@ def batched_learned_block(args):
     tuning = bp.autotune(m, steps=16)
     tuned = timed(bp, True)
     outt = [ctx.download() for ctx in bp.instances]
+    # the learned batch with the tuner's tiles (each instance takes the tile
+    # of its grid-size class: the class with the smallest bound above its
+    # padded cell count)
+    learned_tuned = None
+    if tuning.get("tiles") == "per class":
+        classes = [(c["max_padded_cells"] if c["max_padded_cells"] > 0 else float("inf"), c["tile"])
+                   for c in tuning.get("classes", [])]
+        for ctx, d in zip(bl.instances, descs):
+            padded = (d.Nx + 2 * d.numGC) * (d.Ny + 2 * d.numGC)
+            fits = [t for bound, t in sorted(classes) if padded < bound]
+            if fits:
+                ctx.set_flux_tile(fits[0])
+        learned_tuned = timed(bl, True)
     tuned_identical = all(np.array_equal(a, b) for a3, b3 in zip(outt, outp) for a, b in zip(a3, b3))
     rel = 0.0
     identical = True
@@ -629,6 +642,9 @@ def batched_learned_block(args):
             "warmup": args.warmup, "seed": BATCH_SEED, "weights": weights,
             "plain_sequential": seq, "batched_plain": plain, "batched_learned": learned,
             "autotune": tuning, "batched_tuned": tuned, "tuned_bit_identical_to_plain": tuned_identical,
+            "batched_learned_tuned": learned_tuned,
+            "batched_learned_tuned_over_plain_sequential": (learned_tuned["value"] / seq["value"]
+                                                            if learned_tuned else None),
             "batched_tuned_over_plain_sequential": tuned["value"] / seq["value"],
             "batched_learned_over_plain_sequential": learned["value"] / seq["value"],
             "batched_plain_over_plain_sequential": plain["value"] / seq["value"],
