@@ -193,6 +193,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def tiles_from_report(tuning, descs):
+    """The flux tile gfm_batch_autotune's report gives each grid: that of its
+    grid-size class, the class with the smallest bound (max_padded_cells, -1:
+    none) above the grid's padded cell count; None where no class fits."""
+    classes = sorted((c["max_padded_cells"] if c["max_padded_cells"] > 0 else float("inf"), c["tile"])
+                     for c in tuning.get("classes", []))
+    out = []
+    for d in descs:
+        padded = (d.Nx + 2 * d.numGC) * (d.Ny + 2 * d.numGC)
+        fits = [t for bound, t in classes if padded < bound]
+        out.append(fits[0] if fits else None)
+    return out
+
+
 def setup(W):
     import gfm_gb300 as g
     desc, T = g.case_params(W["sim"], W["test_case"], W["Nx"], W["Ny"])
@@ -618,13 +632,9 @@ def batched_learned_block(args):
     # padded cell count)
     learned_tuned = None
     if tuning.get("tiles") == "per class":
-        classes = [(c["max_padded_cells"] if c["max_padded_cells"] > 0 else float("inf"), c["tile"])
-                   for c in tuning.get("classes", [])]
-        for ctx, d in zip(bl.instances, descs):
-            padded = (d.Nx + 2 * d.numGC) * (d.Ny + 2 * d.numGC)
-            fits = [t for bound, t in sorted(classes) if padded < bound]
-            if fits:
-                ctx.set_flux_tile(fits[0])
+        for ctx, tile in zip(bl.instances, tiles_from_report(tuning, descs)):
+            if tile:
+                ctx.set_flux_tile(tile)
         learned_tuned = timed(bl, True)
     tuned_identical = all(np.array_equal(a, b) for a3, b3 in zip(outt, outp) for a, b in zip(a3, b3))
     rel = 0.0
